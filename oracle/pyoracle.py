@@ -1,0 +1,285 @@
+"""ctypes front end of the FP64 oracle (oracle/liboracle.so) -- TEST INFRASTRUCTURE.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs import
+this module. It is the checker: nothing in ``annongpu_gb300`` imports it.
+
+``RefHarness`` wraps oracle/_ref/libref.so, the reference's own host code path
+(built by ``make -C oracle ref`` where the reference checkout exists); it is used
+only to (re)generate the golden fixtures under tests/golden/.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+P = ct.c_void_p
+
+
+def _ptr(x):
+    return None if x is None else x.ctypes.data_as(ct.c_void_p)
+
+
+def build_oracle(quiet: bool = True) -> str:
+    so = os.path.join(HERE, "liboracle.so")
+    src = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle.hpp")]
+    if not os.path.exists(so) or any(os.path.getmtime(s) > os.path.getmtime(so) for s in src):
+        subprocess.run(["make", "-C", HERE, "oracle"], check=True,
+                       stdout=subprocess.DEVNULL if quiet else None)
+    return so
+
+
+class OrOp(ct.Structure):
+    _fields_ = [("n", ct.c_uint), ("nw", ct.c_uint), ("a", P), ("b", P), ("coeff", P)]
+
+
+class OrRbm(ct.Structure):
+    _fields_ = [("N", ct.c_uint), ("M", ct.c_uint), ("C", ct.c_uint), ("conn", P), ("a", P), ("b", P),
+                ("W", P), ("fw", P), ("lp_re", ct.c_double), ("lp_im", ct.c_double),
+                ("a_in_log_psi", ct.c_int), ("activation", ct.c_int), ("layout", ct.c_int)]
+
+
+class OrCnn(ct.Structure):
+    _fields_ = [("extent", ct.c_uint * 3), ("num_layers", ct.c_uint), ("channels", P), ("connectivity", P),
+                ("sym_classes", P), ("params", P), ("num_params", ct.c_uint), ("final_factor", ct.c_double),
+                ("lp_re", ct.c_double), ("lp_im", ct.c_double), ("activation", ct.c_int)]
+
+
+def nwords(N):
+    return (N + 63) // 64
+
+
+def conf_words(conf, N):
+    """Python int (or array of words) -> uint64 word array of length nwords(N)."""
+    if isinstance(conf, np.ndarray):
+        return np.ascontiguousarray(conf, dtype=np.uint64).reshape(-1)
+    return np.array([(int(conf) >> (64 * w)) & 0xFFFFFFFFFFFFFFFF for w in range(max(1, nwords(N)))],
+                    dtype=np.uint64)
+
+
+class OpArrays:
+    """Keeps the numpy buffers of an operator alive next to its ctypes struct."""
+
+    def __init__(self, expr, N):
+        nw = max(1, nwords(N))
+        a, b, c = expr.arrays(nw)
+        self.a = np.ascontiguousarray(a)
+        self.b = np.ascontiguousarray(b)
+        self.c = np.ascontiguousarray(c.astype(np.complex128))
+        self.struct = OrOp(len(c), nw, _ptr(self.a), _ptr(self.b), _ptr(self.c))
+
+
+class RbmDesc:
+    """An RBM-family wavefunction for the oracle.
+
+    layout 0: reference PsiRBM, params = W (N x M), scalar final weight.
+    layout 1: reference PsiDeep with one hidden layer, params = [a | b | W(C x M)].
+    """
+
+    def __init__(self, N, M, W, a=None, b=None, fw=None, conn=None, log_prefactor=0j,
+                 a_in_log_psi=True, activation=0, layout=1):
+        self.N, self.M = N, M
+        self.W = np.ascontiguousarray(np.asarray(W, np.complex128).reshape(-1))
+        self.C = self.W.size // M
+        self.a = None if a is None else np.ascontiguousarray(np.asarray(a, np.complex128))
+        self.b = None if b is None else np.ascontiguousarray(np.asarray(b, np.complex128))
+        fw = np.ones(M, np.complex128) if fw is None else np.broadcast_to(np.asarray(fw, np.complex128), (M,))
+        self.fw = np.ascontiguousarray(fw)
+        self.conn = None if conn is None else np.ascontiguousarray(np.asarray(conn, np.uint32).reshape(-1))
+        self.lp = complex(log_prefactor)
+        self.struct = OrRbm(N, M, self.C, _ptr(self.conn), _ptr(self.a), _ptr(self.b), _ptr(self.W),
+                            _ptr(self.fw), self.lp.real, self.lp.imag, int(a_in_log_psi), int(activation),
+                            int(layout))
+
+    @property
+    def num_params(self):
+        return (self.N + self.M + self.C * self.M) if self.struct.layout == 1 else self.C * self.M
+
+    def params(self):
+        if self.struct.layout == 0:
+            return self.W.copy()
+        a = np.zeros(self.N, np.complex128) if self.a is None else self.a
+        b = np.zeros(self.M, np.complex128) if self.b is None else self.b
+        return np.concatenate([a, b, self.W])
+
+
+class CnnDesc:
+    def __init__(self, extent, channels, connectivity, sym_classes, params, final_factor,
+                 log_prefactor=0j, activation=0):
+        self.extent = list(extent)
+        self.channels = np.ascontiguousarray(np.asarray(channels, np.uint32))
+        self.connectivity = np.ascontiguousarray(np.asarray(connectivity, np.uint32).reshape(-1, 3))
+        self.N = int(np.prod(extent))
+        self.sym = np.ascontiguousarray(np.asarray(sym_classes, np.uint32))
+        self.params = np.ascontiguousarray(np.asarray(params, np.complex128))
+        self.lp = complex(log_prefactor)
+        self.struct = OrCnn((ct.c_uint * 3)(*self.extent), len(self.channels), _ptr(self.channels),
+                            _ptr(self.connectivity), _ptr(self.sym), _ptr(self.params), self.params.size,
+                            float(final_factor), self.lp.real, self.lp.imag, int(activation))
+
+    @property
+    def num_params(self):
+        return self.params.size
+
+
+class Oracle:
+    def __init__(self):
+        self.lib = ct.CDLL(build_oracle())
+        L = self.lib
+        L.or_rbm_num_params.restype = ct.c_uint
+        L.or_rbm_mc_reference.restype = ct.c_uint
+        L.or_philox4x32_10.argtypes = [ct.c_uint32, ct.c_uint32, P, P]
+        L.or_rbm_mc_philox.argtypes = [P, P, ct.c_uint, ct.c_uint64, ct.c_uint, ct.c_uint, ct.c_uint,
+                                       ct.c_int, P, ct.c_uint, ct.c_int, ct.c_int, P, P, P, P, P, P, P, P]
+        L.or_rbm_mc_reference.argtypes = [P, P, ct.c_uint, ct.c_uint, ct.c_uint, ct.c_uint,
+                                          P, P, P, P, P, P, P, ct.c_uint, P]
+        L.or_activation.argtypes = [ct.c_double, ct.c_double, ct.c_uint, ct.c_int, P, P]
+
+    # ---- RBM family ----
+    def log_psi(self, psi: RbmDesc, conf):
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_rbm_log_psi(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def O_k(self, psi: RbmDesc, conf):
+        out = np.zeros(psi.num_params, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_rbm_O_k(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out
+
+    def local_energy(self, psi: RbmDesc, expr, conf):
+        op = OpArrays(expr, psi.N)
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_rbm_local_energy(ct.byref(psi.struct), ct.byref(op.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def exact(self, psi: RbmDesc, expr=None, want_S=True):
+        np_ = psi.num_params
+        dim = 1 << psi.N
+        r = dict(
+            E=np.zeros(1, np.complex128), fluct=np.zeros(3), grad=np.zeros(np_, np.complex128),
+            tE=np.zeros(1, np.complex128), tE2=np.zeros(1), tO=np.zeros(np_, np.complex128),
+            tF=np.zeros(np_, np.complex128), tS=np.zeros((np_, np_), np.complex128) if want_S else None,
+            vec=np.zeros(dim, np.complex128), log_vec=np.zeros(dim, np.complex128), norm=np.zeros(1),
+            mean_log_psi=np.zeros(1, np.complex128), O_sum=np.zeros(np_, np.complex128),
+            eloc=np.zeros(dim, np.complex128))
+        op = OpArrays(expr, psi.N) if expr is not None else None
+        self.lib.or_rbm_exact(ct.byref(psi.struct), ct.byref(op.struct) if op else None,
+                              *[_ptr(r[k]) for k in ("E", "fluct", "grad", "tE", "tE2", "tO", "tF", "tS",
+                                                     "vec", "log_vec", "norm", "mean_log_psi", "O_sum",
+                                                     "eloc")])
+        return r
+
+    def mc_reference(self, psi: RbmDesc, expr, num_samples, num_sweeps, num_therm, seed=0, max_props=None):
+        N = psi.N
+        total = num_therm * N + num_samples * num_sweeps * N
+        max_props = total if max_props is None else max_props
+        op = OpArrays(expr, N)
+        r = dict(sconf=np.zeros(num_samples, np.uint64), slp=np.zeros(num_samples, np.complex128),
+                 seloc=np.zeros(num_samples, np.complex128), pconf=np.zeros(max_props, np.uint64),
+                 psite=np.zeros(max_props, np.uint32), pu=np.zeros(max_props), pacc=np.zeros(max_props, np.uint8),
+                 energy=np.zeros(1, np.complex128))
+        n = self.lib.or_rbm_mc_reference(ct.byref(psi.struct), ct.byref(op.struct), num_samples, num_sweeps,
+                                         num_therm, seed, *[_ptr(r[k]) for k in ("sconf", "slp", "seloc", "pconf",
+                                                                                 "psite", "pu", "pacc")],
+                                         max_props, _ptr(r["energy"]))
+        r["num_props"] = n
+        return r
+
+    def philox(self, key, ctr):
+        out = np.zeros(4, np.uint32)
+        c = np.asarray(ctr, np.uint32)
+        self.lib.or_philox4x32_10(key & 0xFFFFFFFF, key >> 32, _ptr(c), _ptr(out))
+        return out
+
+    def mc_philox(self, psi: RbmDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
+                  move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None):
+        N = psi.N
+        nw = max(1, nwords(N))
+        op = OpArrays(expr, N) if expr is not None else None
+        conf = np.zeros(n_chains * nw, np.uint64) if conf is None else np.ascontiguousarray(conf, np.uint64).copy()
+        counter = np.zeros(n_chains, np.uint64) if counter is None else np.ascontiguousarray(counter,
+                                                                                            np.uint64).copy()
+        ns = samples_per_chain * n_chains
+        bonds_a = None if bonds is None else np.ascontiguousarray(np.asarray(bonds, np.uint32).reshape(-1))
+        r = dict(sconf=np.zeros(ns * nw, np.uint64), slp=np.zeros(ns, np.complex128),
+                 seloc=np.zeros(ns, np.complex128), acc=np.zeros(1, np.uint64), rej=np.zeros(1, np.uint64),
+                 tie=np.zeros(1))
+        self.lib.or_rbm_mc_philox(ct.byref(psi.struct), ct.byref(op.struct) if op else None, n_chains, seed,
+                                  samples_per_chain, num_sweeps, num_therm, move_kind, _ptr(bonds_a),
+                                  0 if bonds_a is None else bonds_a.size // 2, int(init), n_up,
+                                  _ptr(conf), _ptr(counter), _ptr(r["sconf"]), _ptr(r["slp"]),
+                                  _ptr(r["seloc"]), _ptr(r["acc"]), _ptr(r["rej"]), _ptr(r["tie"]))
+        r["conf"] = conf
+        r["counter"] = counter
+        return r
+
+    # ---- CNN ----
+    def cnn_log_psi(self, psi: CnnDesc, conf):
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_cnn_log_psi(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def cnn_O_k(self, psi: CnnDesc, conf):
+        out = np.zeros(psi.num_params, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_cnn_O_k(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out
+
+    def cnn_local_energy(self, psi: CnnDesc, expr, conf):
+        op = OpArrays(expr, psi.N)
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_cnn_local_energy(ct.byref(psi.struct), ct.byref(op.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def cnn_exact(self, psi: CnnDesc, expr, want_S=False):
+        np_ = psi.num_params
+        r = dict(E=np.zeros(1, np.complex128), norm=np.zeros(1), tE=np.zeros(1, np.complex128), tE2=np.zeros(1),
+                 tO=np.zeros(np_, np.complex128), tF=np.zeros(np_, np.complex128),
+                 tS=np.zeros((np_, np_), np.complex128) if want_S else None)
+        op = OpArrays(expr, psi.N)
+        self.lib.or_cnn_exact(ct.byref(psi.struct), ct.byref(op.struct),
+                              *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
+        return r
+
+    def pauli_apply(self, a, b, conf, N):
+        nw = max(1, nwords(N))
+        aw, bw, cw = conf_words(a, N), conf_words(b, N), conf_words(conf, N)
+        f = np.zeros(1, np.complex128)
+        out = np.zeros(nw, np.uint64)
+        self.lib.or_pauli_apply(_ptr(aw), _ptr(bw), nw, _ptr(cw), _ptr(f), _ptr(out))
+        return f[0], out
+
+    def activation(self, z, layer=0, exact=False):
+        f = np.zeros(1, np.complex128)
+        df = np.zeros(1, np.complex128)
+        self.lib.or_activation(z.real, z.imag, layer, int(exact), _ptr(f), _ptr(df))
+        return f[0], df[0]
+
+
+class RefHarness:
+    """The reference's own host path (oracle/_ref/libref.so). Fixture generation only."""
+
+    def __init__(self, path=None):
+        path = path or os.path.join(HERE, "_ref", "libref.so")
+        self.lib = ct.CDLL(path)
+        self.lib.ref_deep_mc.restype = ct.c_uint
+        self.lib.ref_rbm_mc.restype = ct.c_uint
+        U, D = ct.c_uint, ct.c_double
+        self.lib.ref_deep_log_psi_s.argtypes = [U, U, U, P, P, P, P, ct.c_uint64, P]
+        self.lib.ref_deep_O_k.argtypes = [U, U, U, P, P, P, P, ct.c_uint64, P]
+        self.lib.ref_rbm_log_psi_s.argtypes = [U, U, P, P, P, ct.c_uint64, P]
+        self.lib.ref_rbm_O_k.argtypes = [U, U, P, P, P, ct.c_uint64, P]
+        self.lib.ref_cnn_log_psi_s.argtypes = [P, U, P, P, P, P, U, D, P, ct.c_uint64, P]
+        self.lib.ref_cnn_O_k.argtypes = [P, U, P, P, P, P, U, D, P, ct.c_uint64, P]
+        self.lib.ref_cnn_exact_energy.argtypes = [P, U, P, P, P, P, U, D, P, P, P, P, U, P, P]
+        self.lib.ref_activation.argtypes = [D, D, U, P, P]
+        self.lib.ref_pauli_apply.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64, U, P, P]

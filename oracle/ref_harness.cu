@@ -1,0 +1,413 @@
+// Harness around the reference implementation's own CPU (host) code path.
+//
+// TEST INFRASTRUCTURE ONLY. Built by oracle/Makefile into oracle/_ref/ from the
+// reference sources where they lie (never copied into this repository); used
+// only to generate the golden fixtures under tests/golden/ and to pin the FP64
+// restatement in oracle/oracle.cpp. Nothing in the product links or loads it.
+//
+// Every computation below runs the reference's templates with gpu=false:
+//   * Operator / PauliString::apply / local_energy  include/operator/Operator.hpp:36-121
+//   * PsiDeep (1 hidden layer, ENABLE_NETWORK_BASES) include/quantum_state/PsiDeep.hpp:138-445
+//   * PsiRBM kernel                                 include/quantum_state/PsiRBM.hpp:69-176
+//   * PsiCNN kernel                                 include/quantum_state/PsiCNN.hpp:97-266
+//   * MonteCarlo_t::kernel_foreach / mc_update       include/ensembles/MonteCarlo.hpp:55-177
+//   * ExactSummation_t::kernel_foreach               include/ensembles/ExactSummation.hpp:33-72
+//   * ExpectationValue / TDVP / PsiVector / PsiOkVector / PsiNorm bodies
+//     (source/network_functions/*.cu.template, with the "//! begin template"
+//     instantiation blocks stripped at build time by oracle/Makefile).
+// The only harness-side logic is construction (the reference's constructors for
+// these types exist only behind its Python binding) and a logging update policy
+// that records every Metropolis proposal.
+
+#include "bases.hpp"
+#include "operators.hpp"
+#include "quantum_states.hpp"
+#include "ensembles.hpp"
+#include "network_functions/ExpectationValue.hpp"
+#include "network_functions/TDVP.hpp"
+#include "network_functions/PsiVector.hpp"
+#include "network_functions/PsiNorm.hpp"
+#include "network_functions/PsiOkVector.hpp"
+
+#include <vector>
+#include <cstdint>
+#include <cstring>
+#include <set>
+
+namespace ann_on_gpu {
+
+// A Pauli-sum expression as the three arrays that cross the reference's
+// Operator constructor (source/operator/Operator.cpp:26-36).
+struct HarnessExpr {
+    const uint64_t* a;
+    const uint64_t* b;
+    const double* coeff;  // interleaved re, im
+    unsigned int n;
+};
+
+template<>
+template<>
+StandartOperator<PauliString>::StandartOperator(const HarnessExpr& expr, const bool gpu)
+    : gpu(gpu), coefficients(expr.n, gpu), quantum_strings(expr.n, gpu) {
+    for(auto i = 0u; i < expr.n; i++) {
+        this->coefficients[i] = complex_t(expr.coeff[2 * i], expr.coeff[2 * i + 1]);
+        this->quantum_strings[i] = PauliString(expr.a[i], expr.b[i]);
+    }
+    this->kernel().num_strings = expr.n;
+    this->kernel().coefficients = this->coefficients.data();
+    this->kernel().quantum_strings = this->quantum_strings.data();
+}
+
+// PsiRBM: the reference's host constructor exists only under __PYTHONCC__
+// (PsiRBM.hpp:225-243); this shim fills the same kernel fields.
+struct HarnessRBM : public kernel::PsiRBM_t<complex_t, false> {
+    using Kernel = kernel::PsiRBM_t<complex_t, false>;
+    Array<complex_t> W_store;
+    bool gpu;
+
+    HarnessRBM(unsigned N_, unsigned M_, const double* W, const double* fw, const double* lp)
+        : W_store(N_ * M_, false), gpu(false) {
+        this->N = N_; this->num_sites = N_; this->M = M_; this->num_params = N_ * M_;
+        for(auto k = 0u; k < N_ * M_; k++) this->W_store[k] = complex_t(W[2 * k], W[2 * k + 1]);
+        this->final_weight = complex_t(fw[0], fw[1]);
+        this->log_prefactor = complex_t(lp[0], lp[1]);
+        this->kernel().W = this->W_store.data();
+    }
+    HarnessRBM(const HarnessRBM& o) : Kernel(o), W_store(o.W_store), gpu(false) {
+        this->kernel().W = this->W_store.data();
+    }
+    Kernel& kernel() { return *this; }
+    const Kernel& kernel() const { return *this; }
+};
+
+// PsiCNN: same situation (PsiCNN.hpp:347-373 is __PYTHONCC__-only); the layout
+// assignment mirrors PsiCNN_t::init_kernel (source/quantum_state/PsiCNN.cpp:9-55).
+struct HarnessCNN : public kernel::PsiCNN_t<3u, complex_t> {
+    using Kernel = kernel::PsiCNN_t<3u, complex_t>;
+    Array<complex_t> params;
+    Array<complex_t> angles;
+    bool gpu;
+    unsigned extent_[3];
+    std::vector<unsigned> channels_, connectivity_, classes_;
+
+    HarnessCNN(const unsigned* extent, unsigned num_layers, const unsigned* num_channels,
+               const unsigned* connectivity, const unsigned* sym_classes,
+               const double* p, unsigned num_params_, double final_factor_, const double* lp)
+        : params(num_params_, false), angles(false), gpu(false) {
+        for(int d = 0; d < 3; d++) extent_[d] = extent[d];
+        unsigned N_ = extent[0] * extent[1] * extent[2];
+        channels_.assign(num_channels, num_channels + num_layers);
+        connectivity_.assign(connectivity, connectivity + 3 * num_layers);
+        classes_.assign(sym_classes, sym_classes + N_);
+        for(auto k = 0u; k < num_params_; k++) this->params[k] = complex_t(p[2 * k], p[2 * k + 1]);
+        this->N = N_; this->num_sites = N_;
+        this->final_factor = final_factor_;
+        this->log_prefactor = complex_t(lp[0], lp[1]);
+        this->num_symmetry_classes = std::set<unsigned>(classes_.begin(), classes_.end()).size();
+        this->init();
+    }
+    HarnessCNN(const HarnessCNN& o)
+        : Kernel(o), params(o.params), angles(o.angles), gpu(false),
+          channels_(o.channels_), connectivity_(o.connectivity_), classes_(o.classes_) {
+        for(int d = 0; d < 3; d++) extent_[d] = o.extent_[d];
+        this->init();
+    }
+    void init() {
+        this->num_layers = channels_.size();
+        this->num_params = this->params.size();
+        this->num_angles = 0u;
+        unsigned off = 0u;
+        for(int d = 0; d < 3; d++) this->convolve.extent[d] = extent_[d];
+        for(auto i = 0u; i < this->N; i++) this->convolve.symmetry_classes[i] = classes_[i];
+        for(auto l = 0u; l < this->num_layers; l++) {
+            auto& layer = this->layers[l];
+            layer.num_channels = channels_[l];
+            layer.num_channel_links = layer.num_channels * (l > 0 ? this->layers[l - 1].num_channels : 1u);
+            layer.connectivity_vol = 1u;
+            for(int d = 0; d < 3; d++) {
+                layer.connectivity[d] = connectivity_[3 * l + d];
+                layer.connectivity_vol *= layer.connectivity[d];
+            }
+            for(auto cl = 0u; cl < layer.num_channel_links; cl++) {
+                layer.channel_links[cl].begin_params = off;
+                layer.channel_links[cl].weights = this->params.data() + off;
+                off += this->num_symmetry_classes * layer.connectivity_vol;
+            }
+            this->num_angles += layer.num_channels * this->N;
+        }
+        if(this->angles.size() < this->num_angles) this->angles.resize(this->num_angles);
+        unsigned aoff = 0u;
+        for(auto l = 0u; l < this->num_layers; l++)
+            for(auto c = 0u; c < this->layers[l].num_channels; c++) {
+                this->layers[l].channels[c].angles = this->angles.data() + aoff;
+                aoff += this->N;
+            }
+    }
+    void init_gradient(unsigned num_steps) {
+        this->angles.resize(num_steps * this->num_angles);
+        unsigned aoff = 0u;
+        for(auto l = 0u; l < this->num_layers; l++)
+            for(auto c = 0u; c < this->layers[l].num_channels; c++) {
+                this->layers[l].channels[c].angles = this->angles.data() + aoff;
+                aoff += this->N;
+            }
+    }
+    Kernel& kernel() { return *this; }
+    const Kernel& kernel() const { return *this; }
+};
+
+// Update policy that defers to the reference's single-flip policy
+// (include/ensembles/policies/Update_Policy.hpp:20-33) and logs each
+// proposal: the configuration it starts from and the flipped site.
+std::vector<uint64_t> g_log_conf;
+std::vector<uint32_t> g_log_site;
+
+struct LoggingPolicyKernel {
+    template<typename Psi_t>
+    HDINLINE void operator()(Spins& next_spins, const Spins& spins, const Psi_t& psi, void* rng_state) const {
+        const auto site = random_uint32(rng_state) % psi.num_sites;
+        next_spins = spins.flip(site);
+#ifndef __CUDA_ARCH__
+        g_log_conf.push_back(spins.configuration());
+        g_log_site.push_back(site);
+#endif
+    }
+    LoggingPolicyKernel& kernel() { return *this; }
+};
+struct LoggingPolicy : public LoggingPolicyKernel {
+    using kernel_t = LoggingPolicyKernel;
+};
+
+}  // namespace ann_on_gpu
+
+// Reference bodies (stripped of their explicit-instantiation blocks).
+#include "ExpectationValue.cu"
+#include "TDVP.cu"
+#include "PsiVector.cu"
+#include "PsiNorm.cu"
+#include "PsiOkVector.cu"
+#include "ensembles/MonteCarlo.cu"
+
+using namespace ann_on_gpu;
+
+using LoggingMC = MonteCarlo_t<Spins, Init_Policy<Spins>, LoggingPolicy>;
+
+namespace {
+
+struct DeepDesc {
+    unsigned N, M, C;
+    const unsigned* conn;     // C x M, entry (i, j) at i*M + j; may be null (identity, C == N)
+    const double* params;     // [a(N) | b(M) | W(C*M)] interleaved complex
+    const double* final_w;    // M complex
+    const double* log_pref;   // 1 complex
+};
+
+PsiDeep make_deep(const DeepDesc& d) {
+    PsiDeep psi(d.N, d.M, false);
+    auto& layer0 = *psi.layers.begin();
+    auto& layer1 = *std::next(psi.layers.begin());
+    if(d.C != d.N) {
+        layer1.lhs_connectivity = d.C;
+        layer1.lhs_connections.resize(d.C * d.M);
+        layer1.lhs_weights.resize(d.C * d.M);
+    }
+    if(d.conn) {
+        for(auto k = 0u; k < d.C * d.M; k++) layer1.lhs_connections[k] = d.conn[k];
+    }
+    // the input layer's rhs (site -> hidden unit) lists follow the connections
+    // (PsiDeep.cu:213-242); set_params only refreshes their weights.
+    auto rhs = psi.compile_rhs_connections_and_weights(d.N, d.M, d.C, layer1.lhs_connections, layer1.lhs_weights);
+    layer0.rhs_connections = std::move(rhs.first);
+    layer0.rhs_weights = std::move(rhs.second);
+    psi.init_kernel();
+    const auto np = d.N + d.M + d.C * d.M;
+    Array<complex_t> p(np, false);
+    for(auto k = 0u; k < np; k++) p[k] = complex_t(d.params[2 * k], d.params[2 * k + 1]);
+    for(auto j = 0u; j < d.M; j++) psi.final_weights[j] = complex_t(d.final_w[2 * j], d.final_w[2 * j + 1]);
+    psi.log_prefactor = complex_t(d.log_pref[0], d.log_pref[1]);
+    psi.set_params(p);
+    return psi;
+}
+
+void put(double* out, const complex_t& z) { out[0] = z.real(); out[1] = z.imag(); }
+void put(double* out, const std::complex<double>& z) { out[0] = z.real(); out[1] = z.imag(); }
+
+template<typename Psi>
+void psi_log_psi_s(Psi& psi, uint64_t conf, double* out) {
+    put(out, log_psi_s(psi, Spins(conf, psi.num_sites)));
+}
+
+template<typename Psi>
+void psi_O_k(Psi& psi, uint64_t conf, double* out) {
+    auto r = ann_on_gpu::psi_O_k(psi, Spins(conf, psi.num_sites));
+    for(auto k = 0u; k < r.size(); k++) put(out + 2 * k, r[k]);
+}
+
+// Exact-summation quantities: <A> (unnormalised weights), fluctuation, gradient,
+// TDVP E/E2/O/F/S, psi vector, norm, <log psi>.
+template<typename Psi>
+void exact_all(Psi& psi, const HarnessExpr& expr, double* E, double* fluct, double* grad,
+               double* tdvp_E, double* tdvp_E2, double* tdvp_O, double* tdvp_F, double* tdvp_S,
+               double* vec, double* norm, double* mean_log_psi, double* O_sum) {
+    Operator op(expr, false);
+    ExactSummationSpins es(psi.num_sites, false);
+    ExpectationValue ev(false);
+    put(E, ev(op, psi, es));
+    auto fl = ev.fluctuation(op, psi, es);
+    fluct[0] = fl.first; put(fluct + 1, fl.second);
+    auto g = ev.gradient(op, psi, es);
+    for(auto k = 0u; k < psi.num_params; k++) put(grad + 2 * k, g.first[k]);
+    TDVP tdvp(psi.num_params, false);
+    tdvp.eval(op, psi, es, false_t());
+    put(tdvp_E, tdvp.E_local.front());
+    tdvp_E2[0] = tdvp.E2_local.front();
+    for(auto k = 0u; k < psi.num_params; k++) {
+        put(tdvp_O + 2 * k, tdvp.O_k_ar[k]);
+        put(tdvp_F + 2 * k, tdvp.F_vector[k]);
+    }
+    for(auto k = 0u; k < psi.num_params * psi.num_params; k++) put(tdvp_S + 2 * k, tdvp.S_matrix[k]);
+    auto v = psi_vector(psi, es);
+    for(auto k = 0u; k < v.size(); k++) put(vec + 2 * k, v[k]);
+    norm[0] = psi_norm(psi, es);
+    put(mean_log_psi, log_psi(psi, es));
+    auto os = psi_O_k_vector(psi, es);
+    for(auto k = 0u; k < os.size(); k++) put(O_sum + 2 * k, os[k]);
+}
+
+// One Markov chain on the host path (the host path always runs chain 0,
+// MonteCarlo.hpp:69-71), recording every sample the functor sees and every
+// proposal the update policy makes.
+template<typename Psi>
+unsigned mc_trace(Psi& psi, const HarnessExpr& expr, unsigned num_samples, unsigned num_sweeps,
+                  unsigned num_therm, uint64_t* sample_conf, double* sample_log_psi, double* sample_eloc,
+                  uint64_t* prop_conf, uint32_t* prop_site, unsigned max_props, double* mc_energy) {
+    Operator op(expr, false);
+    auto op_kernel = op.kernel();
+    auto psi_kernel = psi.kernel();
+    LoggingMC mc(num_samples, num_sweeps, num_therm, 1u, LoggingPolicy(), false);
+    g_log_conf.clear();
+    g_log_site.clear();
+    mc.foreach(psi, [=] __host__ __device__ (const unsigned index, const Spins& conf, const complex_t& lp,
+                        typename Psi::Payload& payload, const double) {
+        complex_t eloc;
+        op_kernel.local_energy(eloc, psi_kernel, conf, lp, payload);
+        sample_conf[index] = conf.configuration();
+        sample_log_psi[2 * index] = lp.real();
+        sample_log_psi[2 * index + 1] = lp.imag();
+        sample_eloc[2 * index] = eloc.real();
+        sample_eloc[2 * index + 1] = eloc.imag();
+    });
+    const unsigned n = g_log_site.size();
+    for(auto i = 0u; i < n && i < max_props; i++) {
+        prop_conf[i] = g_log_conf[i];
+        prop_site[i] = g_log_site[i];
+    }
+    // ExpectationValue through the reference's own MonteCarloSpins (1 chain).
+    MonteCarloSpins mcs(num_samples, num_sweeps, num_therm, 1u, Update_Policy<Spins>(), false);
+    ExpectationValue ev(false);
+    put(mc_energy, ev(op, psi, mcs));
+    return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- PsiDeep (1 hidden layer) ----
+void ref_deep_log_psi_s(unsigned N, unsigned M, unsigned C, const unsigned* conn, const double* params,
+                        const double* fw, const double* lp, uint64_t conf, double* out) {
+    auto psi = make_deep({N, M, C, conn, params, fw, lp});
+    psi_log_psi_s(psi, conf, out);
+}
+void ref_deep_O_k(unsigned N, unsigned M, unsigned C, const unsigned* conn, const double* params,
+                  const double* fw, const double* lp, uint64_t conf, double* out) {
+    auto psi = make_deep({N, M, C, conn, params, fw, lp});
+    psi_O_k(psi, conf, out);
+}
+void ref_deep_exact(unsigned N, unsigned M, unsigned C, const unsigned* conn, const double* params,
+                    const double* fw, const double* lp,
+                    const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                    double* E, double* fluct, double* grad, double* tE, double* tE2, double* tO,
+                    double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
+    auto psi = make_deep({N, M, C, conn, params, fw, lp});
+    exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
+}
+unsigned ref_deep_mc(unsigned N, unsigned M, unsigned C, const unsigned* conn, const double* params,
+                     const double* fw, const double* lp,
+                     const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                     unsigned num_samples, unsigned num_sweeps, unsigned num_therm,
+                     uint64_t* sconf, double* slp, double* seloc, uint64_t* pconf, uint32_t* psite,
+                     unsigned max_props, double* mc_energy) {
+    auto psi = make_deep({N, M, C, conn, params, fw, lp});
+    return mc_trace(psi, {a, b, coeff, n_strings}, num_samples, num_sweeps, num_therm,
+                    sconf, slp, seloc, pconf, psite, max_props, mc_energy);
+}
+
+// ---- PsiRBM (no biases) ----
+void ref_rbm_log_psi_s(unsigned N, unsigned M, const double* W, const double* fw, const double* lp,
+                       uint64_t conf, double* out) {
+    HarnessRBM psi(N, M, W, fw, lp);
+    psi_log_psi_s(psi, conf, out);
+}
+void ref_rbm_O_k(unsigned N, unsigned M, const double* W, const double* fw, const double* lp,
+                 uint64_t conf, double* out) {
+    HarnessRBM psi(N, M, W, fw, lp);
+    psi_O_k(psi, conf, out);
+}
+void ref_rbm_exact(unsigned N, unsigned M, const double* W, const double* fw, const double* lp,
+                   const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                   double* E, double* fluct, double* grad, double* tE, double* tE2, double* tO,
+                   double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
+    HarnessRBM psi(N, M, W, fw, lp);
+    exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
+}
+unsigned ref_rbm_mc(unsigned N, unsigned M, const double* W, const double* fw, const double* lp,
+                    const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                    unsigned num_samples, unsigned num_sweeps, unsigned num_therm,
+                    uint64_t* sconf, double* slp, double* seloc, uint64_t* pconf, uint32_t* psite,
+                    unsigned max_props, double* mc_energy) {
+    HarnessRBM psi(N, M, W, fw, lp);
+    return mc_trace(psi, {a, b, coeff, n_strings}, num_samples, num_sweeps, num_therm,
+                    sconf, slp, seloc, pconf, psite, max_props, mc_energy);
+}
+
+// ---- PsiCNN ----
+void ref_cnn_log_psi_s(const unsigned* extent, unsigned L, const unsigned* ch, const unsigned* conn,
+                       const unsigned* cls, const double* p, unsigned np, double ff, const double* lp,
+                       uint64_t conf, double* out) {
+    HarnessCNN psi(extent, L, ch, conn, cls, p, np, ff, lp);
+    psi_log_psi_s(psi, conf, out);
+}
+void ref_cnn_O_k(const unsigned* extent, unsigned L, const unsigned* ch, const unsigned* conn,
+                 const unsigned* cls, const double* p, unsigned np, double ff, const double* lp,
+                 uint64_t conf, double* out) {
+    HarnessCNN psi(extent, L, ch, conn, cls, p, np, ff, lp);
+    psi.init_gradient(1u);
+    psi_O_k(psi, conf, out);
+}
+void ref_cnn_exact_energy(const unsigned* extent, unsigned L, const unsigned* ch, const unsigned* conn,
+                          const unsigned* cls, const double* p, unsigned np, double ff, const double* lp,
+                          const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                          double* E, double* norm) {
+    HarnessCNN psi(extent, L, ch, conn, cls, p, np, ff, lp);
+    Operator op(HarnessExpr{a, b, coeff, n_strings}, false);
+    ExactSummationSpins es(psi.num_sites, false);
+    ExpectationValue ev(false);
+    put(E, ev(op, psi, es));
+    norm[0] = psi_norm(psi, es);
+}
+
+// ---- activation ----
+void ref_activation(double re, double im, unsigned layer, double* out, double* dout) {
+    put(out, my_logcosh(complex_t(re, im), layer));
+    put(dout, my_tanh(complex_t(re, im), layer));
+}
+
+// ---- Pauli string application (PauliString.hpp:242-254) ----
+void ref_pauli_apply(uint64_t a, uint64_t b, uint64_t conf, unsigned N, double* factor, uint64_t* out_conf) {
+    auto me = PauliString(a, b).apply(Spins(conf, N));
+    put(factor, me.coefficient);
+    out_conf[0] = me.vector.configuration();
+}
+
+}  // extern "C"

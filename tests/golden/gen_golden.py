@@ -1,0 +1,226 @@
+"""Generate the golden fixtures in this directory from the reference's own host code.
+
+Runs the reference implementation's CPU path (oracle/_ref/libref.so, built by
+``make -C oracle ref`` from the reference checkout) on small seeded cases and
+stores inputs and outputs as .npz files. The fixtures pin the FP64 oracle
+(oracle/oracle.cpp) and, through it, the CUDA path. The reference checkout is
+needed only to regenerate them:
+
+    make -C oracle ref && python tests/golden/gen_golden.py
+"""
+
+import ctypes as ct
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from annongpu_gb300.expression import sigma_x, sigma_y, sigma_z, transverse_field_ising_1d  # noqa: E402
+from pyoracle import RefHarness  # noqa: E402
+
+
+def P(x):
+    return x.ctypes.data_as(ct.c_void_p)
+
+
+def cplx(rng, shape, scale):
+    return (scale * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))).astype(np.complex128)
+
+
+def mixed_hamiltonian(N):
+    """TFIM plus strings with one, two and three sigma_y factors (phase coverage)."""
+    H = transverse_field_ising_1d(N, h=0.9, J=1.1)
+    H = H + 0.3 * sigma_y(1) * sigma_y(2) + 0.2 * sigma_x(0) * sigma_z(3)
+    H = H + 0.15 * sigma_y(4) + 0.05 * sigma_y(0) * sigma_y(2) * sigma_y(5) + 0.1 * sigma_z(2)
+    return H
+
+
+def op_arrays(H):
+    a, b, c = H.arrays(1)
+    return (np.ascontiguousarray(a[:, 0]), np.ascontiguousarray(b[:, 0]),
+            np.ascontiguousarray(c.astype(np.complex128)), len(c))
+
+
+def exact_outputs(np_, N):
+    dim = 1 << N
+    return dict(E=np.zeros(1, np.complex128), fluct=np.zeros(3), grad=np.zeros(np_, np.complex128),
+                tE=np.zeros(1, np.complex128), tE2=np.zeros(1), tO=np.zeros(np_, np.complex128),
+                tF=np.zeros(np_, np.complex128), tS=np.zeros((np_, np_), np.complex128),
+                vec=np.zeros(dim, np.complex128), norm=np.zeros(1), mlp=np.zeros(1, np.complex128),
+                O_sum=np.zeros(np_, np.complex128))
+
+
+KEYS = ("E", "fluct", "grad", "tE", "tE2", "tO", "tF", "tS", "vec", "norm", "mlp", "O_sum")
+
+
+def mc_outputs(num_samples, total_props):
+    return dict(sconf=np.zeros(num_samples, np.uint64), slp=np.zeros(num_samples, np.complex128),
+                seloc=np.zeros(num_samples, np.complex128), pconf=np.zeros(total_props, np.uint64),
+                psite=np.zeros(total_props, np.uint32), mc_energy=np.zeros(1, np.complex128))
+
+
+def gen_rbm(ref, rng):
+    N, M = 8, 8
+    W = cplx(rng, (N, M), 0.15)
+    fw = np.array([0.8 + 0.3j])
+    lp = np.array([0.1 - 0.2j])
+    H = mixed_hamiltonian(N)
+    a, b, c, n = op_arrays(H)
+    confs = rng.integers(0, 1 << N, 12).astype(np.uint64)
+    out = {"N": N, "M": M, "W": W, "fw": fw, "lp": lp, "op_a": a, "op_b": b, "op_c": c, "confs": confs}
+    lps, oks = [], []
+    for s in confs:
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_rbm_log_psi_s(N, M, P(W), P(fw), P(lp), int(s), P(r))
+        lps.append(r[0])
+        o = np.zeros(N * M, np.complex128)
+        ref.lib.ref_rbm_O_k(N, M, P(W), P(fw), P(lp), int(s), P(o))
+        oks.append(o)
+    out["log_psi"] = np.array(lps)
+    out["O_k"] = np.array(oks)
+    ex = exact_outputs(N * M, N)
+    ref.lib.ref_rbm_exact(N, M, P(W), P(fw), P(lp), P(a), P(b), P(c), n, *[P(ex[k]) for k in KEYS])
+    out.update({"ex_" + k: v for k, v in ex.items()})
+    ns, sw, th = 40, 2, 3
+    total = th * N + ns * sw * N
+    mc = mc_outputs(ns, total)
+    nprop = ref.lib.ref_rbm_mc(N, M, P(W), P(fw), P(lp), P(a), P(b), P(c), n, ns, sw, th,
+                               *[P(mc[k]) for k in ("sconf", "slp", "seloc", "pconf", "psite")], total,
+                               P(mc["mc_energy"]))
+    assert nprop == total, (nprop, total)
+    out.update({"mc_" + k: v for k, v in mc.items()})
+    out["mc_params"] = np.array([ns, sw, th])
+    np.savez_compressed(os.path.join(HERE, "rbm_n8_m8.npz"), **out)
+
+
+def gen_deep(ref, rng, name, N, M, C, conn, with_S=True, mc=True, confs_n=12):
+    np_ = N + M + C * M
+    params = np.concatenate([cplx(rng, N, 0.05), cplx(rng, M, 0.05), cplx(rng, C * M, 0.12)])
+    fw = (1.0 + cplx(rng, M, 0.1)).astype(np.complex128)
+    lp = np.array([-0.05 + 0.3j])
+    H = mixed_hamiltonian(N) if N >= 6 else transverse_field_ising_1d(N)
+    a, b, c, n = op_arrays(H)
+    connp = None if conn is None else np.ascontiguousarray(conn.astype(np.uint32).reshape(-1))
+    cp = P(connp) if connp is not None else None
+    confs = rng.integers(0, 1 << N, confs_n).astype(np.uint64)
+    out = {"N": N, "M": M, "C": C, "params": params, "fw": fw, "lp": lp, "op_a": a, "op_b": b, "op_c": c,
+           "confs": confs}
+    if connp is not None:
+        out["conn"] = connp
+    lps, oks = [], []
+    for s in confs:
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_deep_log_psi_s(N, M, C, cp, P(params), P(fw), P(lp), int(s), P(r))
+        lps.append(r[0])
+        o = np.zeros(np_, np.complex128)
+        ref.lib.ref_deep_O_k(N, M, C, cp, P(params), P(fw), P(lp), int(s), P(o))
+        oks.append(o)
+    out["log_psi"] = np.array(lps)
+    out["O_k"] = np.array(oks)
+    ex = exact_outputs(np_, N)
+    ref.lib.ref_deep_exact(N, M, C, cp, P(params), P(fw), P(lp), P(a), P(b), P(c), n, *[P(ex[k]) for k in KEYS])
+    if not with_S:
+        # keep the fixture small: a checksum and a strided sample of S
+        S = ex.pop("tS")
+        out["ex_tS_trace"] = np.array([np.trace(S)])
+        out["ex_tS_fro"] = np.array([np.linalg.norm(S)])
+        idx = np.arange(0, np_ * np_, 97)
+        out["ex_tS_idx"] = idx
+        out["ex_tS_sample"] = S.reshape(-1)[idx]
+        ex.pop("vec")
+    out.update({"ex_" + k: v for k, v in ex.items()})
+    if mc:
+        ns, sw, th = 30, 1, 4
+        total = th * N + ns * sw * N
+        m = mc_outputs(ns, total)
+        nprop = ref.lib.ref_deep_mc(N, M, C, cp, P(params), P(fw), P(lp), P(a), P(b), P(c), n, ns, sw, th,
+                                    *[P(m[k]) for k in ("sconf", "slp", "seloc", "pconf", "psite")], total,
+                                    P(m["mc_energy"]))
+        assert nprop == total
+        out.update({"mc_" + k: v for k, v in m.items()})
+        out["mc_params"] = np.array([ns, sw, th])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def gen_cnn(ref, rng):
+    extent = np.array([1, 4, 4], np.uint32)
+    channels = np.array([2, 2], np.uint32)
+    connectivity = np.array([[1, 3, 3], [1, 2, 2]], np.uint32)
+    N = 16
+    classes = np.zeros(N, np.uint32)
+    classes[N // 2:] = 1  # two symmetry classes
+    ncls = 2
+    np_ = (2 * 1 * ncls * 9) + (2 * 2 * ncls * 4)
+    params = cplx(rng, np_, 0.15)
+    ff = 0.7
+    lp = np.array([0.02 + 0.01j])
+    H = transverse_field_ising_1d(N, h=0.8) + 0.2 * sigma_y(3) * sigma_y(7)
+    a, b, c, n = op_arrays(H)
+    confs = rng.integers(0, 1 << N, 10).astype(np.uint64)
+    lps, oks = [], []
+    for s in confs:
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_cnn_log_psi_s(P(extent), 2, P(channels), P(connectivity), P(classes), P(params), np_, ff,
+                                  P(lp), int(s), P(r))
+        lps.append(r[0])
+        o = np.zeros(np_, np.complex128)
+        ref.lib.ref_cnn_O_k(P(extent), 2, P(channels), P(connectivity), P(classes), P(params), np_, ff,
+                            P(lp), int(s), P(o))
+        oks.append(o)
+    E = np.zeros(1, np.complex128)
+    norm = np.zeros(1)
+    ref.lib.ref_cnn_exact_energy(P(extent), 2, P(channels), P(connectivity), P(classes), P(params), np_, ff, P(lp),
+                                 P(a), P(b), P(c), n, P(E), P(norm))
+    np.savez_compressed(os.path.join(HERE, "cnn_4x4.npz"), extent=extent, channels=channels,
+                        connectivity=connectivity, classes=classes, params=params, ff=np.array([ff]), lp=lp,
+                        op_a=a, op_b=b, op_c=c, confs=confs, log_psi=np.array(lps), O_k=np.array(oks),
+                        ex_E=E, ex_norm=norm)
+
+
+def gen_kats(ref, rng):
+    zs = cplx(rng, 24, 0.6)
+    f = np.zeros((2, 24), np.complex128)
+    df = np.zeros((2, 24), np.complex128)
+    for layer in (0, 1):
+        for k, z in enumerate(zs):
+            o1 = np.zeros(1, np.complex128)
+            o2 = np.zeros(1, np.complex128)
+            ref.lib.ref_activation(z.real, z.imag, layer, P(o1), P(o2))
+            f[layer, k], df[layer, k] = o1[0], o2[0]
+    N = 12
+    na = 64
+    pa = rng.integers(0, 1 << N, na).astype(np.uint64)
+    pb = rng.integers(0, 1 << N, na).astype(np.uint64)
+    pc = rng.integers(0, 1 << N, na).astype(np.uint64)
+    fac = np.zeros(na, np.complex128)
+    oc = np.zeros(na, np.uint64)
+    for k in range(na):
+        o1 = np.zeros(1, np.complex128)
+        o2 = np.zeros(1, np.uint64)
+        ref.lib.ref_pauli_apply(int(pa[k]), int(pb[k]), int(pc[k]), N, P(o1), P(o2))
+        fac[k], oc[k] = o1[0], o2[0]
+    np.savez_compressed(os.path.join(HERE, "kats.npz"), z=zs, f=f, df=df, pauli_N=np.array([N]), pauli_a=pa,
+                        pauli_b=pb, pauli_conf=pc, pauli_factor=fac, pauli_out=oc)
+
+
+def main():
+    ref = RefHarness()
+    rng = np.random.default_rng(20261203)
+    gen_kats(ref, rng)
+    gen_rbm(ref, rng)
+    gen_deep(ref, rng, "deep_n8_m8", 8, 8, 8, None)
+    n, m, c = 6, 12, 3
+    conn = np.array([[(j * 1 + i) % n for j in range(m)] for i in range(c)])
+    gen_deep(ref, rng, "deep_n6_m12_c3", n, m, c, conn)
+    gen_deep(ref, rng, "deep_n16_m16", 16, 16, 16, None, with_S=False, mc=False, confs_n=6)
+    gen_cnn(ref, rng)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,139 @@
+"""Pins the FP64 oracle (oracle/oracle.cpp) against fixtures produced by the
+reference's own host code path (tests/golden/gen_golden.py)."""
+
+import os
+
+import numpy as np
+import pytest
+
+from pyoracle import CnnDesc, RbmDesc
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name)))
+
+
+class _Expr:
+    """Operator arrays straight from a fixture."""
+
+    def __init__(self, a, b, c):
+        self.a, self.b, self.c = a, b, c
+
+    def arrays(self, nw):
+        return self.a.reshape(-1, 1), self.b.reshape(-1, 1), self.c
+
+
+def rbm_from(g):
+    return RbmDesc(int(g["N"]), int(g["M"]), g["W"], fw=np.full(int(g["M"]), g["fw"][0]),
+                   log_prefactor=g["lp"][0], layout=0, a_in_log_psi=False)
+
+
+def deep_from(g):
+    N, M, C = int(g["N"]), int(g["M"]), int(g["C"])
+    p = g["params"]
+    return RbmDesc(N, M, p[N + M:], a=p[:N], b=p[N:N + M], fw=g["fw"], conn=g.get("conn"),
+                   log_prefactor=g["lp"][0], layout=1, a_in_log_psi=False)
+
+
+def close(x, y, rtol=1e-10, atol=1e-12):
+    np.testing.assert_allclose(np.asarray(x), np.asarray(y), rtol=rtol, atol=atol)
+
+
+def test_activation_kats(oracle):
+    g = load("kats.npz")
+    for layer in (0, 1):
+        for k, z in enumerate(g["z"]):
+            f, df = oracle.activation(z, layer)
+            close(f, g["f"][layer, k], rtol=1e-14)
+            close(df, g["df"][layer, k], rtol=1e-14)
+
+
+def test_pauli_apply_kats(oracle):
+    g = load("kats.npz")
+    N = int(g["pauli_N"][0])
+    for k in range(len(g["pauli_a"])):
+        f, out = oracle.pauli_apply(int(g["pauli_a"][k]), int(g["pauli_b"][k]), int(g["pauli_conf"][k]), N)
+        assert f == g["pauli_factor"][k]
+        assert int(out[0]) == int(g["pauli_out"][k])
+
+
+@pytest.mark.parametrize("name", ["rbm_n8_m8.npz", "deep_n8_m8.npz", "deep_n6_m12_c3.npz", "deep_n16_m16.npz"])
+def test_log_psi_and_O_k(oracle, name):
+    g = load(name)
+    psi = rbm_from(g) if name.startswith("rbm") else deep_from(g)
+    for k, s in enumerate(g["confs"]):
+        close(oracle.log_psi(psi, int(s)), g["log_psi"][k])
+        close(oracle.O_k(psi, int(s)), g["O_k"][k])
+
+
+@pytest.mark.parametrize("name", ["rbm_n8_m8.npz", "deep_n8_m8.npz", "deep_n6_m12_c3.npz", "deep_n16_m16.npz"])
+def test_exact_summation(oracle, name):
+    g = load(name)
+    psi = rbm_from(g) if name.startswith("rbm") else deep_from(g)
+    expr = _Expr(g["op_a"], g["op_b"], g["op_c"])
+    want_S = "ex_tS" in g
+    r = oracle.exact(psi, expr, want_S=True)
+    close(r["E"][0], g["ex_E"][0])
+    close(r["fluct"], g["ex_fluct"], rtol=1e-9)
+    close(r["grad"], g["ex_grad"], rtol=1e-9, atol=1e-10)
+    close(r["tE"][0], g["ex_tE"][0])
+    close(r["tE2"][0], g["ex_tE2"][0])
+    close(r["tO"], g["ex_tO"])
+    close(r["tF"], g["ex_tF"], rtol=1e-9, atol=1e-10)
+    if want_S:
+        close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-10)
+        close(r["vec"], g["ex_vec"])
+    else:
+        S = r["tS"]
+        close(np.trace(S), g["ex_tS_trace"][0], rtol=1e-9)
+        close(np.linalg.norm(S), g["ex_tS_fro"][0], rtol=1e-9)
+        close(S.reshape(-1)[g["ex_tS_idx"]], g["ex_tS_sample"], rtol=1e-8, atol=1e-10)
+    close(r["norm"][0], g["ex_norm"][0])
+    close(r["mean_log_psi"][0], g["ex_mlp"][0])
+    close(r["O_sum"], g["ex_O_sum"], rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["rbm_n8_m8.npz", "deep_n8_m8.npz", "deep_n6_m12_c3.npz"])
+def test_mc_trace_bit_exact(oracle, name):
+    """The oracle's restatement of the host Monte Carlo, fed the same mt19937 stream,
+    visits exactly the reference's configurations, proposal by proposal."""
+    g = load(name)
+    psi = rbm_from(g) if name.startswith("rbm") else deep_from(g)
+    expr = _Expr(g["op_a"], g["op_b"], g["op_c"])
+    ns, sw, th = (int(x) for x in g["mc_params"])
+    r = oracle.mc_reference(psi, expr, ns, sw, th, seed=0)
+    assert r["num_props"] == len(g["mc_psite"])
+    np.testing.assert_array_equal(r["psite"], g["mc_psite"])
+    np.testing.assert_array_equal(r["pconf"], g["mc_pconf"])
+    np.testing.assert_array_equal(r["sconf"], g["mc_sconf"])
+    close(r["slp"], g["mc_slp"])
+    close(r["seloc"], g["mc_seloc"], rtol=1e-9, atol=1e-11)
+    close(r["energy"][0], g["mc_mc_energy"][0], rtol=1e-9)
+
+
+def test_cnn(oracle):
+    g = load("cnn_4x4.npz")
+    psi = CnnDesc(g["extent"], g["channels"], g["connectivity"], g["classes"], g["params"], g["ff"][0],
+                  log_prefactor=g["lp"][0])
+    for k, s in enumerate(g["confs"]):
+        close(oracle.cnn_log_psi(psi, int(s)), g["log_psi"][k])
+        close(oracle.cnn_O_k(psi, int(s)), g["O_k"][k], rtol=1e-9, atol=1e-12)
+    r = oracle.cnn_exact(psi, _Expr(g["op_a"], g["op_b"], g["op_c"]))
+    close(r["E"][0], g["ex_E"][0], rtol=1e-9)
+    close(r["norm"][0], g["ex_norm"][0])
+
+
+def test_expression_matrix_matches_exact_energy(oracle):
+    """The dense builder of annongpu_gb300.expression reproduces the exact-summation
+    energy: sum_s |psi(s)|^2 E_loc(s) == psi^H H psi."""
+    from annongpu_gb300.expression import sigma_x, sigma_y, sigma_z, transverse_field_ising_1d
+    g = load("deep_n8_m8.npz")
+    psi = deep_from(g)
+    N = psi.N
+    H = transverse_field_ising_1d(N, 0.9, 1.1) + 0.3 * sigma_y(1) * sigma_y(2) + 0.2 * sigma_x(0) * sigma_z(3)
+    H = H + 0.15 * sigma_y(4) + 0.05 * sigma_y(0) * sigma_y(2) * sigma_y(5) + 0.1 * sigma_z(2)
+    r = oracle.exact(psi, H, want_S=False)
+    v = r["vec"]
+    close(np.vdot(v, H.matrix(N) @ v), r["E"][0], rtol=1e-10)
