@@ -1,0 +1,20 @@
+"""GB300-native VMC inner loop with the pyANNonGPU interface.
+
+    import annongpu_gb300 as pyANNonGPU
+
+exposes PsiRBM, PsiDeep, Operator, Spins, MonteCarloSpins / MonteCarloLoop,
+ExactSummationSpins, ExpectationValue, TDVP and the free functions of the
+reference's _pyANNonGPU module, backed by libannongpu.so (CUDA, sm_103a).
+"""
+
+from .expression import (PauliExpression, heisenberg_j1j2_2d, identity, sigma_x, sigma_y, sigma_z,  # noqa: F401
+                         square_lattice_bonds, transverse_field_ising_1d, transverse_field_ising_2d)
+from .json_numpy import NumpyDecoder, NumpyEncoder  # noqa: F401
+from .api import (ExactSummationSpins, ExpectationValue, MonteCarloLoop, MonteCarloSpins, Operator,  # noqa: F401
+                  PsiDeep, PsiRBM, Spins, TDVP, activation_function, apply_operator, log_psi, log_psi_batch,
+                  log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
+                  stop_profiling)
+from .builders import new_RBM, new_deep_neural_network  # noqa: F401
+from ._lib import AnnError, launch_count  # noqa: F401
+
+__version__ = "1.0.0"

@@ -1,0 +1,696 @@
+"""The pyANNonGPU-compatible Python surface over the C ABI (include/annongpu.h).
+
+Names, argument order and return shapes follow the reference's pybind11 module
+_pyANNonGPU (pyANNonGPU/main.cpp.template:65-541) and the monkeypatched helpers
+of pyANNonGPU/{PsiRBM,PsiDeep,PsiCNN}.py, so the reference's user code and tests
+run unchanged for the VMC path. Every computation runs in libannongpu.so on the
+GPU; the `gpu` arguments are kept for signature compatibility (there is no CPU
+path to select).
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import json
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import call, cbuf, c128, ptr, stream_ptr
+from .expression import PauliExpression
+from .json_numpy import NumpyDecoder, NumpyEncoder
+
+_ACT = {"poly": L.ACT_POLY, "logcosh": L.ACT_LOGCOSH, 0: L.ACT_POLY, 1: L.ACT_LOGCOSH}
+_PREC = {"fp32": L.PREC_FP32, "fp64": L.PREC_FP64, "complex64": L.PREC_FP32, "complex128": L.PREC_FP64}
+
+
+def _conf_words(conf, num_words: int) -> np.ndarray:
+    if isinstance(conf, Spins):
+        conf = conf.configuration
+    conf = int(conf)
+    return np.array([(conf >> (64 * w)) & 0xFFFFFFFFFFFFFFFF for w in range(num_words)], np.uint64)
+
+
+class _Handle:
+    _destroy = None
+
+    def __init__(self):
+        self._h = ct.c_void_p()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and self._destroy:
+            try:
+                getattr(L.lib, self._destroy)(h)
+            except Exception:
+                pass
+            self._h = ct.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+
+# ----------------------------------------------------------------------------------
+# Spins (include/basis/Spins.h:273-403; binding main.cpp.template:340-344)
+class Spins:
+    def __init__(self, configuration: int, num_spins: int):
+        configuration = int(configuration)
+        if num_spins < 128:
+            configuration &= (1 << num_spins) - 1
+        self.configuration = configuration
+        self.num_spins = num_spins
+
+    @staticmethod
+    def enumerate(index: int) -> "Spins":
+        return Spins(int(index), 128)
+
+    def roll(self, shift: int, N: int) -> "Spins":
+        c = self.configuration & ((1 << N) - 1)
+        shift %= N
+        return Spins(((c << shift) | (c >> (N - shift))) & ((1 << N) - 1), N)
+
+    def array(self, num_spins: int) -> np.ndarray:
+        return np.array([1.0 if (self.configuration >> i) & 1 else -1.0 for i in range(num_spins)])
+
+    def __int__(self):
+        return self.configuration
+
+    def __eq__(self, other):
+        return isinstance(other, Spins) and other.configuration == self.configuration
+
+    def __hash__(self):
+        return hash(self.configuration)
+
+    def __repr__(self):
+        return f"Spins({self.configuration:#x})"
+
+
+# ----------------------------------------------------------------------------------
+class _Psi(_Handle):
+    _destroy = "ann_psi_destroy"
+
+    def _init_common(self, gpu):
+        self.gpu = bool(gpu)
+        n = ct.c_uint()
+        call("ann_psi_num_params", self._h, ct.byref(n))
+        self._num_params = n.value
+
+    @property
+    def num_params(self) -> int:
+        return self._num_params
+
+    @property
+    def params(self) -> np.ndarray:
+        out = cbuf(self._num_params)
+        call("ann_psi_get_params", self._h, ptr(out))
+        return out
+
+    @params.setter
+    def params(self, value):
+        v = c128(value).reshape(-1)
+        if v.size != self._num_params:
+            raise ValueError(f"expected {self._num_params} parameters, got {v.size}")
+        call("ann_psi_set_params", self._h, ptr(v))
+
+    def set_params_async(self, host_params, stream):
+        """Copies parameters (complex128, ideally pinned host memory) on `stream`;
+        `host_params` may be a numpy array or a torch CPU tensor of float64 pairs."""
+        if hasattr(host_params, "data_ptr"):
+            p = ct.c_void_p(host_params.data_ptr())
+        else:
+            self._pending = c128(host_params)
+            p = ptr(self._pending)
+        call("ann_psi_set_params_async", self._h, p, stream_ptr(stream))
+
+    @property
+    def log_prefactor(self) -> complex:
+        out = np.zeros(2)
+        call("ann_psi_get_log_prefactor", self._h, ptr(out))
+        return complex(out[0], out[1])
+
+    @log_prefactor.setter
+    def log_prefactor(self, value):
+        value = complex(value)
+        call("ann_psi_set_log_prefactor", self._h, value.real, value.imag)
+
+    @property
+    def symmetric(self) -> bool:
+        return False
+
+    def copy(self):
+        other = object.__new__(type(self))
+        _Handle.__init__(other)
+        call("ann_psi_copy", self._h, ct.byref(other._h))
+        other.__dict__.update({k: v for k, v in self.__dict__.items() if k != "_h"})
+        return other
+
+    def __pos__(self):
+        return self.copy()
+
+    # PsiDeep.py:47-57 / PsiRBM.py:39-49 / PsiCNN.py:47-57
+    def _vector(self, exact_summation):
+        return psi_vector(self, exact_summation)
+
+    def vector(self, exact_summation):
+        return self._vector(exact_summation)
+
+    def norm(self, exact_summation) -> float:
+        out = np.zeros(1)
+        call("ann_psi_norm", self._h, exact_summation.handle, None, ptr(out))
+        return float(out[0])
+
+    def normalize(self, exact_summation):
+        self.log_prefactor -= np.log(self.norm(exact_summation))
+
+    def calibrate(self, ensemble):
+        if type(ensemble).__name__.startswith("ExactSummation"):
+            self.normalize(ensemble)
+            self.log_prefactor -= 1j * log_psi(self, ensemble).imag
+        else:
+            self.log_prefactor = 0
+            self.log_prefactor -= log_psi(self, ensemble)
+
+    def _device_params(self) -> int:
+        p = ct.c_void_p()
+        call("ann_psi_params_device", self._h, ct.byref(p))
+        return p.value
+
+
+def _make_rbm(obj, N, M, C, conn, params, fw, log_prefactor, layout, a_in_log_psi, activation, precision, gpu):
+    params = c128(params).reshape(-1)
+    fw = c128(np.broadcast_to(np.asarray(fw, np.complex128), (M,)))
+    conn_a = None if conn is None else np.ascontiguousarray(np.asarray(conn, np.uint32).reshape(-1))
+    lp = complex(log_prefactor)
+    d = L.RbmDesc(N, M, C, ptr(conn_a), ptr(params), ptr(fw), (ct.c_double * 2)(lp.real, lp.imag), layout,
+                  int(bool(a_in_log_psi)), _ACT[activation], _PREC[precision])
+    _Handle.__init__(obj)
+    call("ann_psi_create_rbm", ct.byref(d), ct.byref(obj._h))
+    obj._init_common(gpu)
+
+
+class PsiRBM(_Psi):
+    """Restricted Boltzmann machine (include/quantum_state/PsiRBM.hpp:41-262).
+
+    Reference form: ``PsiRBM(W, final_weight, log_prefactor, gpu)`` with
+    log psi = log_prefactor + final_weight * sum_j f(sum_i W_ij s_i) and params = W.
+    Optional visible/hidden biases ``a``, ``b`` switch to params = [a | b | W] with
+    log psi += a.s (the standard complex RBM).
+    """
+
+    def __init__(self, W, final_weight=1.0, log_prefactor=0.0, gpu=True, *, a=None, b=None,
+                 activation="poly", precision="fp32", a_in_log_psi=True):
+        W = c128(W)
+        N, M = W.shape
+        self.N, self.M = N, M
+        self.num_sites = N
+        self.final_weight = complex(final_weight)
+        self.activation = activation
+        self.precision = precision
+        self._biased = a is not None or b is not None
+        if self._biased:
+            a = np.zeros(N, np.complex128) if a is None else c128(a)
+            b = np.zeros(M, np.complex128) if b is None else c128(b)
+            params = np.concatenate([a, b, W.reshape(-1)])
+            layout = L.LAYOUT_DEEP
+        else:
+            params = W.reshape(-1)
+            layout = L.LAYOUT_RBM
+        _make_rbm(self, N, M, N, None, params, self.final_weight, log_prefactor, layout, a_in_log_psi,
+                  activation, precision, gpu)
+
+    @property
+    def W(self) -> np.ndarray:
+        p = self.params
+        off = self.N + self.M if self._biased else 0
+        return p[off:].reshape(self.N, self.M)
+
+    @property
+    def a(self):
+        return self.params[:self.N] if self._biased else np.zeros(self.N, np.complex128)
+
+    @property
+    def b(self):
+        return self.params[self.N:self.N + self.M] if self._biased else np.zeros(self.M, np.complex128)
+
+    # PsiRBM.py:7-36
+    def to_json(self):
+        obj = dict(type="PsiRBM", W=self.W, final_weight=self.final_weight,
+                   log_prefactor_re=self.log_prefactor.real, log_prefactor_im=self.log_prefactor.imag)
+        if self._biased:
+            obj.update(a=self.a, b=self.b)
+        return json.loads(json.dumps(obj, cls=NumpyEncoder, default=_json_default))
+
+    @staticmethod
+    def from_json(json_obj, gpu=True):
+        obj = json.loads(json.dumps(json_obj, cls=NumpyEncoder), cls=NumpyDecoder)
+        fw = obj["final_weight"]
+        if isinstance(fw, dict):
+            fw = complex(fw["re"], fw["im"])
+        return PsiRBM(obj["W"], fw, obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu,
+                      a=obj.get("a"), b=obj.get("b"))
+
+
+def _json_default(o):
+    if isinstance(o, complex):
+        return {"re": o.real, "im": o.imag}
+    raise TypeError(type(o))
+
+
+class PsiDeep(_Psi):
+    """Feed-forward network with sparse connectivity (include/quantum_state/PsiDeep.hpp:70-471),
+    one hidden layer: theta_j = b_j + sum_c W[c,j] s[connections[c,j]],
+    log psi = log_prefactor + (a.s) + sum_j final_weights_j f(theta_j), params = [a | b | W].
+
+    ``a_in_log_psi=False`` reproduces the reference exactly, whose log psi omits a.s
+    (PsiDeep.hpp:260-264) while its O_k still reports s for the a entries.
+    """
+
+    def __init__(self, num_sites, a, b, connections, W, final_weights, log_prefactor=0.0, gpu=True, *,
+                 a_in_log_psi=True, activation="poly", precision="fp32"):
+        if isinstance(b, np.ndarray) and b.ndim == 1:
+            b, connections, W = [b], [connections], [W]
+        if len(W) != 1:
+            raise NotImplementedError("this build supports PsiDeep with one hidden layer")
+        a = c128(a)
+        b0 = c128(b[0])
+        W0 = c128(W[0])
+        conn0 = np.asarray(connections[0], np.uint32)
+        C, M = W0.shape
+        N = a.size
+        self.num_sites = int(num_sites)
+        self.N = N
+        self.N_i = 0
+        self.N_j = 0
+        self._M, self._C = M, C
+        self._connections = [conn0.copy()]
+        self._final_weights = c128(final_weights).reshape(-1)
+        self.activation = activation
+        self.precision = precision
+        self.a_in_log_psi = a_in_log_psi
+        params = np.concatenate([a, b0, W0.reshape(-1)])
+        _make_rbm(self, N, M, C, conn0, params, self._final_weights, log_prefactor, L.LAYOUT_DEEP, a_in_log_psi,
+                  activation, precision, gpu)
+
+    @property
+    def a(self):
+        return self.params[:self.N]
+
+    input_weights = a
+
+    @property
+    def b(self):
+        return [self.params[self.N:self.N + self._M]]
+
+    @property
+    def W(self):
+        return [self.params[self.N + self._M:].reshape(self._C, self._M)]
+
+    @property
+    def connections(self):
+        return [c.copy() for c in self._connections]
+
+    @property
+    def final_weights(self):
+        return self._final_weights.copy()
+
+    @property
+    def first_layer_params_slice(self):
+        return slice(self.N, self.N + self.W[0].size + self.b[0].size)
+
+    # PsiDeep.py:7-44
+    def to_json(self):
+        obj = dict(type="PsiDeep", num_sites=self.num_sites, a=self.a, b=self.b, connections=self.connections,
+                   W=self.W, final_weights=self.final_weights, log_prefactor_re=self.log_prefactor.real,
+                   log_prefactor_im=self.log_prefactor.imag)
+        return json.loads(json.dumps(obj, cls=NumpyEncoder))
+
+    @staticmethod
+    def from_json(json_obj, gpu=True):
+        obj = json.loads(json.dumps(json_obj, cls=NumpyEncoder), cls=NumpyDecoder)
+        return PsiDeep(obj["num_sites"], obj["a"], obj["b"], obj["connections"], obj["W"], obj["final_weights"],
+                       obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu)
+
+
+# ----------------------------------------------------------------------------------
+class Operator(_Handle):
+    """Sum of Pauli strings (include/operator/Operator.hpp:26-214)."""
+
+    _destroy = "ann_op_destroy"
+
+    def __init__(self, expr, gpu=True):
+        _Handle.__init__(self)
+        if not isinstance(expr, PauliExpression):
+            expr = PauliExpression({(int(a), int(b)): c for (a, b), c in expr})
+        self.expr = expr
+        self.gpu = bool(gpu)
+        a, b, c = expr.arrays(2)
+        a = np.ascontiguousarray(a)
+        b = np.ascontiguousarray(b)
+        c = c128(c)
+        call("ann_op_create_pauli", len(c), 2, ptr(a), ptr(b), ptr(c), ct.byref(self._h))
+        self.num_strings = len(c)
+
+
+# ----------------------------------------------------------------------------------
+class ExactSummationSpins(_Handle):
+    """All 2^N configurations, weight |psi(s)|^2 unnormalised (include/ensembles/ExactSummation.hpp:33-72)."""
+
+    _destroy = "ann_ens_destroy"
+
+    def __init__(self, num_sites, gpu=True):
+        _Handle.__init__(self)
+        self.num_sites = int(num_sites)
+        self.gpu = bool(gpu)
+        call("ann_ens_create_exact", self.num_sites, ct.byref(self._h))
+
+    @property
+    def num_steps(self) -> int:
+        return 1 << self.num_sites
+
+
+_MOVES = {"single_flip": L.MOVE_FLIP, "flip": L.MOVE_FLIP, "exchange": L.MOVE_EXCHANGE_BONDS,
+          "exchange_bonds": L.MOVE_EXCHANGE_BONDS, "exchange_pairs": L.MOVE_EXCHANGE_PAIRS}
+
+
+class MonteCarloSpins(_Handle):
+    """Metropolis chains (include/ensembles/MonteCarlo.hpp:28-259).
+
+    ``MonteCarloSpins(num_samples, num_sweeps, num_thermalization_sweeps, num_markov_chains, gpu)``
+    as in the reference; ``MonteCarloSpins(other)`` copies. Extensions (keyword-only):
+    ``move`` ("single_flip", "exchange" over ``bonds``, "exchange_pairs"), ``n_up``
+    (fixed-magnetisation initial configurations), ``seed`` (Philox key) and
+    ``persistent`` (chains continue across calls instead of being re-drawn and
+    re-thermalised each call as the reference does, MonteCarlo.hpp:79, 89-93).
+    """
+
+    _destroy = "ann_ens_destroy"
+
+    def __init__(self, num_samples, num_sweeps=None, num_thermalization_sweeps=None, num_markov_chains=None,
+                 gpu=True, *, move="single_flip", bonds=None, n_up=None, seed=0, persistent=False):
+        _Handle.__init__(self)
+        if isinstance(num_samples, MonteCarloSpins):
+            other = num_samples
+            call("ann_ens_copy", other._h, ct.byref(self._h))
+            self.__dict__.update({k: v for k, v in other.__dict__.items() if k != "_h"})
+            return
+        self.num_samples = int(num_samples)
+        self.num_sweeps = int(num_sweeps)
+        self.num_thermalization_sweeps = int(num_thermalization_sweeps)
+        self.num_markov_chains = int(num_markov_chains)
+        self.gpu = bool(gpu)
+        self.move = move
+        self._bonds = None if bonds is None else np.ascontiguousarray(np.asarray(bonds, np.uint32).reshape(-1, 2))
+        d = L.McDesc(self.num_samples, self.num_sweeps, self.num_thermalization_sweeps, self.num_markov_chains,
+                     _MOVES[move], ptr(self._bonds), 0 if self._bonds is None else len(self._bonds),
+                     -1 if n_up is None else int(n_up), int(seed) & 0xFFFFFFFFFFFFFFFF, int(bool(persistent)))
+        call("ann_ens_create_mc", ct.byref(d), ct.byref(self._h))
+
+    @property
+    def num_steps(self) -> int:
+        return self.num_samples
+
+    @property
+    def acceptance_rate(self) -> float:
+        out = np.zeros(1)
+        call("ann_ens_acceptance_rate", self._h, ptr(out))
+        return float(out[0])
+
+    def get_chains(self):
+        conf = np.zeros((self.num_markov_chains, 2), np.uint64)
+        ctr = np.zeros(self.num_markov_chains, np.uint64)
+        call("ann_ens_get_chains", self._h, ptr(conf), ptr(ctr))
+        return conf, ctr
+
+    def set_chains(self, conf, counter):
+        conf = np.ascontiguousarray(np.asarray(conf, np.uint64).reshape(self.num_markov_chains, -1))
+        if conf.shape[1] == 1:
+            conf = np.concatenate([conf, np.zeros_like(conf)], axis=1)
+        ctr = np.ascontiguousarray(np.asarray(counter, np.uint64))
+        call("ann_ens_set_chains", self._h, ptr(conf), ptr(ctr))
+
+    def set_tape(self, init_conf, sites, u):
+        """Replays recorded proposals: init_conf (chains,), sites/u (chains, len)."""
+        if sites is None:
+            call("ann_ens_set_tape", self._h, None, None, None, 0)
+            return
+        init = np.zeros((self.num_markov_chains, 2), np.uint64)
+        init[:, 0] = np.asarray(init_conf, np.uint64).reshape(-1)
+        s = np.ascontiguousarray(np.asarray(sites, np.uint32).reshape(self.num_markov_chains, -1))
+        uu = np.ascontiguousarray(np.asarray(u, np.float64).reshape(self.num_markov_chains, -1))
+        self._tape = (init, s, uu)
+        call("ann_ens_set_tape", self._h, ptr(init), ptr(s), ptr(uu), s.shape[1])
+
+    def samples(self):
+        """(configurations (num_steps, 2) uint64, log psi, local energy) of the last call."""
+        n = (self.num_samples // self.num_markov_chains) * self.num_markov_chains
+        conf = np.zeros((n, 2), np.uint64)
+        lp = cbuf(n)
+        el = cbuf(n)
+        call("ann_ens_get_samples", self._h, ptr(conf), ptr(lp), ptr(el))
+        return conf, lp, el
+
+
+MonteCarloLoop = MonteCarloSpins
+
+
+# ----------------------------------------------------------------------------------
+class ExpectationValue:
+    """source/network_functions/ExpectationValue.cu.template"""
+
+    def __init__(self, gpu=True, stream=None):
+        self.gpu = bool(gpu)
+        self.stream = stream
+
+    def __call__(self, operator, psi, ensemble):
+        if isinstance(operator, (list, tuple)):
+            hs = (ct.c_void_p * len(operator))(*[o.handle.value for o in operator])
+            out = cbuf(len(operator))
+            call("ann_expectation_list", hs, len(operator), psi.handle, ensemble.handle, stream_ptr(self.stream),
+                 ptr(out))
+            return out
+        out = np.zeros(2)
+        call("ann_expectation", operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream), ptr(out))
+        return complex(out[0], out[1])
+
+    def fluctuation(self, operator, psi, ensemble):
+        out = np.zeros(3)
+        call("ann_fluctuation", operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream), ptr(out))
+        return float(out[0]), complex(out[1], out[2])
+
+    def gradient(self, operator, psi, ensemble):
+        g = cbuf(psi.num_params)
+        v = np.zeros(2)
+        call("ann_gradient", operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream), ptr(g), ptr(v))
+        return g, complex(v[0], v[1])
+
+    gradient_with_noise = gradient  # bound to gradient in the reference (main.cpp.template:428)
+
+    def exp_sigma_z(self, operator, psi, ensemble):
+        out = np.zeros(2)
+        call("ann_exp_sigma_z", operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream), ptr(out))
+        return complex(out[0], out[1])
+
+
+_S_MODES = {"fp32": L.S_FP32, "plain": L.S_FP32, "bf16": L.S_BF16, "bf16_split": L.S_BF16_SPLIT}
+
+
+class TDVP(_Handle):
+    """S matrix, F vector and energy moments (include/network_functions/TDVP.hpp,
+    source/network_functions/TDVP.cu.template), plus the GPU SR solve this build adds."""
+
+    _destroy = "ann_tdvp_destroy"
+
+    def __init__(self, num_params, gpu=True, *, s_mode="fp32", stream=None):
+        _Handle.__init__(self)
+        self.num_params = int(num_params)
+        self.gpu = bool(gpu)
+        self.threshold = -1e6
+        self.stream = stream
+        call("ann_tdvp_create", self.num_params, ct.byref(self._h))
+        self.s_mode = s_mode
+
+    @property
+    def s_mode(self):
+        return self._s_mode
+
+    @s_mode.setter
+    def s_mode(self, mode):
+        call("ann_tdvp_set_s_mode", self._h, _S_MODES[mode])
+        self._s_mode = mode
+
+    def eval(self, operator, psi, ensemble):
+        call("ann_tdvp_eval", self._h, operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream))
+
+    def eval_F(self, operator, psi, ensemble):
+        call("ann_tdvp_eval_F", self._h, operator.handle, psi.handle, ensemble.handle, stream_ptr(self.stream))
+
+    @property
+    def S_matrix(self):
+        out = cbuf(self.num_params * self.num_params)
+        call("ann_tdvp_get_S", self._h, ptr(out))
+        return out.reshape(self.num_params, self.num_params)
+
+    @property
+    def F_vector(self):
+        out = cbuf(self.num_params)
+        call("ann_tdvp_get_F", self._h, ptr(out))
+        return out
+
+    @property
+    def O_k_vector(self):
+        out = cbuf(self.num_params)
+        call("ann_tdvp_get_O", self._h, ptr(out))
+        return out
+
+    def _energy(self):
+        E = np.zeros(2)
+        E2 = np.zeros(1)
+        call("ann_tdvp_get_energy", self._h, ptr(E), ptr(E2))
+        return complex(E[0], E[1]), float(E2[0])
+
+    @property
+    def E_local(self):
+        return self._energy()[0]
+
+    @property
+    def var_H(self):
+        E, E2 = self._energy()
+        return E2 - abs(E) ** 2
+
+    @property
+    def total_weight(self):
+        out = np.zeros(1)
+        call("ann_tdvp_get_total_weight", self._h, ptr(out))
+        return float(out[0])
+
+    @property
+    def O_k_samples(self):
+        n = ct.c_uint()
+        out = None
+        # rows of the last eval
+        out = cbuf(self._rows() * self.num_params)
+        call("ann_tdvp_get_O_samples", self._h, ptr(out))
+        return out
+
+    def _rows(self):
+        return self._last_rows
+
+    def S_dot_vector(self, vec, ensemble=None):
+        v = c128(vec)
+        out = cbuf(self.num_params)
+        call("ann_tdvp_S_dot_vector", self._h, ptr(v), stream_ptr(self.stream), ptr(out))
+        return out
+
+    def solve(self, diag_shift, return_info=False):
+        """delta = (S + diag_shift I)^{-1} F by FP64 Cholesky on the GPU (+1 refinement step)."""
+        delta = cbuf(self.num_params)
+        info = np.zeros(2)
+        call("ann_tdvp_solve", self._h, float(diag_shift), stream_ptr(self.stream), ptr(delta), ptr(info))
+        return (delta, info) if return_info else delta
+
+    def update(self, psi, lr):
+        call("ann_sr_update", self._h, psi.handle, float(lr), stream_ptr(self.stream))
+
+    def sr_step(self, operator, psi, ensemble, diag_shift, lr):
+        """One stochastic-reconfiguration step: eval, solve, params -= lr * delta (all on the device)."""
+        call("ann_sr_step", self._h, operator.handle, psi.handle, ensemble.handle, float(diag_shift), float(lr),
+             stream_ptr(self.stream))
+
+    def capture_sr_step(self, operator, psi, ensemble, diag_shift, lr, stream):
+        call("ann_sr_graph_capture", self._h, operator.handle, psi.handle, ensemble.handle, float(diag_shift),
+             float(lr), stream_ptr(stream))
+
+    def launch_sr_step(self, stream):
+        call("ann_sr_graph_launch", self._h, stream_ptr(stream))
+
+
+def _track_rows(fn):
+    def wrapped(self, operator, psi, ensemble):
+        fn(self, operator, psi, ensemble)
+        self._last_rows = ensemble.num_steps if isinstance(ensemble, ExactSummationSpins) else \
+            (ensemble.num_samples // ensemble.num_markov_chains) * ensemble.num_markov_chains
+    return wrapped
+
+
+TDVP.eval = _track_rows(TDVP.eval)
+TDVP.eval_F = _track_rows(TDVP.eval_F)
+
+
+# ----------------------------------------------------------------------------------
+# free functions (main.cpp.template:495-540)
+def _nwords(psi):
+    return 2 if psi.N > 64 else 1
+
+
+def log_psi_s(psi, spins) -> complex:
+    w = _conf_words(spins, _nwords(psi))
+    out = np.zeros(2)
+    call("ann_log_psi_s", psi.handle, ptr(w), ptr(out))
+    return complex(out[0], out[1])
+
+
+def log_psi_batch(psi, confs) -> np.ndarray:
+    confs = list(confs)
+    nw = _nwords(psi)
+    arr = np.ascontiguousarray(np.concatenate([_conf_words(c, nw) for c in confs]) if confs else
+                               np.zeros(0, np.uint64))
+    out = cbuf(len(confs))
+    call("ann_log_psi_batch", psi.handle, ptr(arr), len(confs), None, ptr(out))
+    return out
+
+
+def psi_O_k(psi, spins) -> np.ndarray:
+    w = _conf_words(spins, _nwords(psi))
+    out = cbuf(psi.num_params)
+    call("ann_psi_O_k", psi.handle, ptr(w), ptr(out))
+    return out
+
+
+def psi_O_k_vector(psi, ensemble) -> np.ndarray:
+    out = cbuf(psi.num_params)
+    call("ann_psi_O_k_vector", psi.handle, ensemble.handle, None, ptr(out))
+    return out
+
+
+def log_psi(psi, ensemble) -> complex:
+    out = np.zeros(2)
+    call("ann_log_psi", psi.handle, ensemble.handle, None, ptr(out))
+    return complex(out[0], out[1])
+
+
+def psi_vector(psi, ensemble) -> np.ndarray:
+    out = cbuf(ensemble.num_steps)
+    call("ann_psi_vector", psi.handle, ensemble.handle, None, ptr(out))
+    return out
+
+
+def log_psi_vector(psi, ensemble) -> np.ndarray:
+    out = cbuf(ensemble.num_steps)
+    call("ann_log_psi_vector", psi.handle, ensemble.handle, None, ptr(out))
+    return out
+
+
+def apply_operator(psi, operator, ensemble) -> np.ndarray:
+    out = cbuf(ensemble.num_steps)
+    call("ann_apply_operator", psi.handle, operator.handle, ensemble.handle, None, ptr(out))
+    return out
+
+
+def activation_function(z, layer=0, activation="poly") -> complex:
+    z = complex(z)
+    out = np.zeros(2)
+    call("ann_activation_function", z.real, z.imag, int(layer), _ACT[activation], ptr(out))
+    return complex(out[0], out[1])
+
+
+def setDevice(device: int):
+    call("ann_set_device", int(device))
+
+
+def start_profiling():
+    call("ann_profiler_start")
+
+
+def stop_profiling():
+    call("ann_profiler_stop")

@@ -1,0 +1,186 @@
+// Device-side building blocks shared by every kernel of the VMC inner loop:
+// complex arithmetic, spin/Pauli bit algebra, activations, Philox4x32-10 and
+// warp reductions. sm_103a only.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ann {
+
+constexpr int kMaxWords = 2;  // spin configurations up to 128 sites (two 64-bit words)
+
+// ---------------------------------------------------------------------------------
+// complex numbers (interleaved re, im; 8 B for float, 16 B for double)
+template<typename T>
+struct alignas(2 * sizeof(T)) cplx {
+    T re, im;
+};
+
+template<typename T> __host__ __device__ __forceinline__ cplx<T> mk(T r, T i) { return {r, i}; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return {a.re - b.re, a.im - b.im}; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T> operator-(cplx<T> a) { return {-a.re, -a.im}; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cplx<T> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template<typename T> __host__ __device__ __forceinline__ cplx<T> operator*(T s, cplx<T> a) { return {s * a.re, s * a.im}; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T>& operator+=(cplx<T>& a, cplx<T> b) { a.re += b.re; a.im += b.im; return a; }
+template<typename T> __host__ __device__ __forceinline__ cplx<T> conj(cplx<T> a) { return {a.re, -a.im}; }
+template<typename T> __host__ __device__ __forceinline__ T norm2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
+template<typename D, typename S> __host__ __device__ __forceinline__ cplx<D> cvt(cplx<S> a) { return {(D)a.re, (D)a.im}; }
+
+__device__ __forceinline__ float fexp(float x) { return expf(x); }
+__device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ void fsincos(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void fsincos(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ float flog1p(float x) { return log1pf(x); }
+__device__ __forceinline__ double flog1p(double x) { return log1p(x); }
+__device__ __forceinline__ float flog(float x) { return logf(x); }
+__device__ __forceinline__ double flog(double x) { return log(x); }
+__device__ __forceinline__ float fatan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double fatan2(double y, double x) { return atan2(y, x); }
+
+template<typename T>
+__device__ __forceinline__ cplx<T> cexp(cplx<T> z) {
+    T s, c;
+    fsincos(z.im, &s, &c);
+    const T e = fexp(z.re);
+    return {e * c, e * s};
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> clog(cplx<T> z) {
+    return {T(0.5) * flog(norm2(z)), fatan2(z.im, z.re)};
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> cdiv(cplx<T> a, cplx<T> b) {
+    const T d = T(1) / norm2(b);
+    return {(a.re * b.re + a.im * b.im) * d, (a.im * b.re - a.re * b.im) * d};
+}
+
+// ---------------------------------------------------------------------------------
+// activations. Reference polynomial forms (include/quantum_state/psi_functions.hpp:
+// my_logcosh :40-48, my_tanh :102-116); "exact" = log cosh / tanh.
+enum Activation : int { kPoly = 0, kLogCosh = 1 };
+
+template<typename T>
+__device__ __forceinline__ cplx<T> poly_f(cplx<T> z, int layer) {
+    const cplx<T> z2 = z * z, z4 = z2 * z2;
+    if(layer == 0) return T(0.5) * z2 - T(1.0 / 12.0) * z4 + T(1.0 / 45.0) * (z4 * z2);
+    return z - T(1.0 / 3.0) * (z2 * z) + T(2.0 / 15.0) * (z4 * z);
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> poly_df(cplx<T> z, int layer) {
+    const cplx<T> z2 = z * z, z4 = z2 * z2;
+    if(layer == 0) return z - T(1.0 / 3.0) * (z2 * z) + T(2.0 / 15.0) * (z4 * z);
+    return mk<T>(T(1), T(0)) - z2 + T(2.0 / 3.0) * z4;
+}
+// log cosh z = w + log(1 + e^{-2w}) - log 2 with w = +-z, Re w >= 0 (cosh is even)
+template<typename T>
+__device__ __forceinline__ cplx<T> logcosh(cplx<T> z) {
+    const cplx<T> w = z.re >= T(0) ? z : -z;
+    const cplx<T> e = cexp(T(-2) * w);
+    const cplx<T> l = clog(mk<T>(T(1) + e.re, e.im));
+    return {w.re + l.re - T(0.69314718055994530942), w.im + l.im};
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> ctanh(cplx<T> z) {
+    // tanh z = (1 - e^{-2w}) / (1 + e^{-2w}) * sign, w = +-z with Re w >= 0
+    const bool neg = z.re < T(0);
+    const cplx<T> w = neg ? -z : z;
+    const cplx<T> e = cexp(T(-2) * w);
+    const cplx<T> r = cdiv(mk<T>(T(1) - e.re, -e.im), mk<T>(T(1) + e.re, e.im));
+    return neg ? -r : r;
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> act_f(cplx<T> z, int act, int layer) {
+    return act == kPoly ? poly_f(z, layer) : logcosh(z);
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> act_df(cplx<T> z, int act, int layer) {
+    return act == kPoly ? poly_df(z, layer) : ctanh(z);
+}
+
+// ---------------------------------------------------------------------------------
+// spin configurations: bit i = 1 <-> sigma^z_i = +1 (include/basis/Spins.h:104-118)
+template<int NW>
+struct Conf {
+    uint64_t w[NW];
+};
+template<int NW>
+__device__ __forceinline__ int spin_bit(const Conf<NW>& s, unsigned i) {
+    return (int)((s.w[i >> 6] >> (i & 63u)) & 1u);
+}
+template<int NW>
+__device__ __forceinline__ void flip(Conf<NW>& s, unsigned i) {
+    s.w[i >> 6] ^= (uint64_t)1 << (i & 63u);
+}
+
+// ---------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as
+// 1, 2, 3", SC'11). Counter-based: every (key, counter) gives 4 independent words.
+struct u32x4 {
+    uint32_t x, y, z, w;
+};
+__host__ __device__ __forceinline__ u32x4 philox4x32_10(uint32_t k0, uint32_t k1, u32x4 c) {
+#pragma unroll
+    for(int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        c = u32x4{(uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t r, uint32_t n) {
+    return (uint32_t)(((uint64_t)r * n) >> 32);
+}
+__host__ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
+    return (double)((((uint64_t)hi << 32) | lo) >> 11) * 0x1.0p-53;
+}
+
+// ---------------------------------------------------------------------------------
+// warp reductions (xor butterflies leave the bit-identical sum in every lane)
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template<typename T>
+__device__ __forceinline__ cplx<T> warp_sum(cplx<T> v) {
+    return {warp_sum(v.re), warp_sum(v.im)};
+}
+
+// Pauli-sum operator grouped by flip mask. A string's matrix element on |s> is
+// coeff * (-i)^{n_y} * (-1)^{popcount(~s & (Z|Y))} and it maps s -> s ^ (X|Y)
+// (include/basis/PauliString.hpp:193-208, 242-254). Strings with no flips form
+// the diagonal part; the others are grouped by their flip mask so one psi ratio
+// serves the whole group.
+struct OpDev {
+    unsigned nw;
+    unsigned n_diag;
+    const uint64_t* diag_mask;    // [n_diag][nw]: sites with Z (the sign mask)
+    const double* diag_coeff;     // [n_diag][2]
+    unsigned n_groups;
+    const unsigned* grp_site_begin;  // [n_groups + 1] into grp_sites
+    const uint16_t* grp_sites;       // flipped sites of each group
+    const unsigned* grp_str_begin;   // [n_groups + 1] into str_*
+    const uint64_t* str_mask;        // [n_str][nw]: sites with Z or Y
+    const double* str_coeff;         // [n_str][2]: coeff * (-i)^{n_y}
+};
+
+// device status word bits (returned to the host as C-ABI status)
+enum StatusBits : unsigned {
+    kStatusNonFinite = 1u,    // NaN / Inf in log psi, E_loc or S
+    kStatusNotPosDef = 2u,    // Cholesky pivot <= 0
+    kStatusTimeout = 4u,      // a bounded device-side wait gave up
+    kStatusBadInput = 8u,     // an index or size outside the checked bounds
+};
+
+}  // namespace ann

@@ -1,0 +1,200 @@
+// Host-side objects behind the C ABI handles, and the launchers each .cu file provides.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "annongpu.h"
+#include "ann_common.cuh"
+
+namespace ann {
+
+using zd = std::complex<double>;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define ANN_CUDA(x) ::ann::cuda_check((x), #x)
+void count_launch(unsigned n = 1);
+void check_launch(const char* what);
+
+// device allocation that only grows
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf();
+    void ensure(size_t n);
+    void free_();
+    template<typename X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+void upload(DevBuf& b, const void* src, size_t bytes);
+
+// ---------------------------------------------------------------------------------
+struct CnnLayerHost {
+    unsigned channels, prev_channels, vol, conn[3], param_offset;
+};
+
+struct ann_psi_impl {
+    int kind = 0;       // 0 RBM family, 1 CNN
+    int precision = 0;  // 0 fp32, 1 fp64
+    int act = 0;
+    unsigned N = 0, NW = 1, Np = 0;
+    zd lp{0.0, 0.0};
+    DevBuf params;      // FP64 master copy (Np complex128)
+    // RBM family
+    unsigned M = 0, Mpad = 0, C = 0, U = 1;
+    int layout = 0, a_in = 1;
+    std::vector<unsigned> conn;
+    std::vector<zd> fw;
+    DevBuf Wd, a, b, fwd, connd;
+    // CNN
+    unsigned extent[3] = {1, 1, 1};
+    std::vector<CnnLayerHost> layers;
+    std::vector<unsigned> sym;
+    unsigned ncls = 1;
+    double final_factor = 1.0;
+    DevBuf cnn_w, cnn_meta;  // kernel-precision weights; packed metadata
+    size_t elem_bytes() const { return precision ? 16 : 8; }
+};
+
+struct ann_op_impl {
+    unsigned n_strings = 0, nw = 2, max_site = 0;
+    std::vector<uint64_t> a, b;   // n x nw
+    std::vector<zd> coeff;
+    // grouped device form
+    unsigned n_diag = 0, n_groups = 0;
+    DevBuf diag_mask, diag_coeff, grp_site_begin, grp_sites, grp_str_begin, str_mask, str_coeff;
+    OpDev view() const;
+};
+
+// per-call sample rows written by the sampling / enumeration kernels
+struct Rows {
+    size_t n = 0;
+    DevBuf conf, log_psi, eloc, weight;
+};
+
+struct ann_ens_impl {
+    int kind = 0;  // 0 exact, 1 Monte Carlo
+    unsigned N = 0;
+    // Monte Carlo
+    unsigned num_samples = 0, num_sweeps = 0, num_therm = 0, n_chains = 0;
+    int move = 0, n_up = -1, persistent = 0;
+    uint64_t seed = 0;
+    std::vector<uint32_t> bonds;
+    DevBuf bonds_d, chain_conf, chain_counter, acc_rej;
+    bool chains_valid = false;  // chain state holds equilibrated chains
+    unsigned long long last_acc = 0, last_rej = 0;
+    // tape replay
+    DevBuf tape_site, tape_u, tape_init;
+    unsigned tape_len = 0;
+    Rows rows;
+    unsigned num_steps() const {
+        return kind == 0 ? (unsigned)(1ull << N) : (num_samples / n_chains) * n_chains;
+    }
+    double uniform_weight() const { return 1.0 / (double)num_samples; }
+};
+
+struct ann_tdvp_impl {
+    unsigned Np = 0;
+    int s_mode = 0;
+    size_t n_rows = 0, ldO = 0;
+    int O_precision = 0;
+    DevBuf O;                   // n_rows x ldO, kernel precision complex
+    DevBuf stats;               // Stats
+    DevBuf Obar, F, Osum;       // Np complex128
+    DevBuf partial;             // reduction scratch
+    DevBuf S;                   // Np x Np complex128
+    DevBuf L;                   // Cholesky factor (lower), Np x Np complex128
+    DevBuf rhs, delta, resid;   // Np complex128
+    DevBuf herk_in;             // BF16 operand for the tensor-core HERK
+    DevBuf vec_in, vec_tmp;
+    DevBuf wts;                 // per-row weights of the last eval (exact summation)
+    bool wts_exact = false;
+    double w0 = 0.0;            // uniform row weight (Monte Carlo)
+    bool have_S = false;
+    unsigned graph_kernels = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+};
+
+struct Stats {
+    double W;       // total weight
+    double E[2];    // sum w E_loc
+    double E2;      // sum w |E_loc|^2
+    double L[2];    // sum w log psi
+};
+
+// ---- launchers ------------------------------------------------------------------
+struct SampleTargets {
+    Rows* rows;
+    void* O = nullptr;     // rows x ldO (kernel precision) or null
+    size_t ldO = 0;
+    bool want_eloc = true;
+};
+
+void psi_prepare(ann_psi_impl& psi, cudaStream_t st);
+// runs the ensemble (MC sampling or exact enumeration) over psi
+void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t,
+                  cudaStream_t st);
+void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs_dev, size_t n, Rows& rows,
+               void* O, size_t ldO, cudaStream_t st);
+
+// per-precision RBM launchers (rbm_f32.cu / rbm_f64.cu)
+template<typename T> void rbm_prepare_T(ann_psi_impl& psi, cudaStream_t st);
+template<typename T> void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens,
+                                   const SampleTargets& t, cudaStream_t st);
+template<typename T> void rbm_exact_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens,
+                                      const SampleTargets& t, cudaStream_t st);
+template<typename T> void rbm_confs_T(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n,
+                                      Rows& rows, void* O, size_t ldO, cudaStream_t st);
+
+// statistics (stats.cu)
+void row_stats(const Rows& rows, const double* weight_or_null, double w0, Stats* out_dev, DevBuf& scratch,
+               cudaStream_t st);
+// acc_O[k] = sum_s w_s O_sk ; acc_F[k] = sum_s w_s e_s conj(O_sk); then
+// F[k] = acc_F[k] - E conj(acc_O[k]) when `center_with` != null
+void col_stats(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, const double* weight_or_null,
+               double w0, const cplx<double>* e, cplx<double>* Obar, cplx<double>* F, const Stats* center_with,
+               cplx<double>* Osum, DevBuf& scratch, cudaStream_t st);
+void row_dot(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, const cplx<double>* v,
+             cplx<double>* y, cudaStream_t st);
+void finalize_sdotv(cplx<double>* out, const cplx<double>* Obar, const cplx<double>* v, unsigned Np,
+                    cudaStream_t st);
+
+// S = sum_s w_s conj(O_s - Obar) (O_s - Obar) + (1 - W) conj(Obar) Obar^T (herk_simt.cu / herk_tc.cu)
+void herk_simt(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, const double* weight_or_null,
+               double w0, const cplx<double>* Obar, const Stats* stats, cplx<double>* S, cudaStream_t st);
+void herk_tc(ann_tdvp_impl& td, const double* weight_or_null, double w0, bool split, cudaStream_t st);
+
+// FP64 Cholesky SR solve (cholesky.cu)
+void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
+void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
+
+unsigned* status_word();
+
+// PsiCNN (cnn.cu)
+void cnn_prepare(ann_psi_impl& psi, cudaStream_t st);
+void cnn_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st);
+void cnn_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
+               size_t ldO, cudaStream_t st);
+
+// sum_s w_s exp(sum_n c_n <s|P_n|s'>) over the rows (ExpectationValue.cu.template:52-81)
+void exp_sigma_z_sum(const ann_op_impl& op, const Rows& rows, const double* wts, double w0, double* out2,
+                     cudaStream_t st);
+// activation_function(z, layer) evaluated by the device code path
+void activation_host(double re, double im, unsigned layer, int activation, double* out2);
+
+}  // namespace ann

@@ -1,0 +1,298 @@
+// FP64 SR solve on the GPU: (S + shift I) delta = F by a blocked right-looking
+// complex Cholesky factorisation, two blocked triangular solves and one step of
+// iterative refinement against the unfactored matrix.
+//
+// The reference has no solver: TDVP only builds S and F and the caller solves
+// on the host (source/network_functions/TDVP.cu.template:181-302,
+// pyANNonGPU/main.cpp.template:465-489). This file is the project's own.
+//
+// Matrices are row-major complex128, N x N; only the lower triangle of the
+// factor is referenced. Failures never trap: a non-positive or non-finite pivot
+// sets kStatusNotPosDef in the device status word, is replaced by 1 so the
+// remaining kernels stay finite, and the host reports ANN_ERR_NUMERIC.
+#include "ann_internal.hpp"
+
+namespace ann {
+
+namespace {
+
+constexpr int NB = 32;   // panel width
+constexpr int UT = 64;   // trailing-update tile
+
+using zc = cplx<double>;
+
+__global__ void copy_shift_kernel(const zc* __restrict__ S, zc* __restrict__ A, unsigned n, double shift) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)n * n;
+    if(idx >= total) return;
+    zc v = S[idx];
+    const size_t i = idx / n, j = idx % n;
+    if(i == j) v.re += shift;
+    A[idx] = v;
+}
+
+// unblocked Cholesky of the nb x nb diagonal block at (kb, kb)
+__global__ void __launch_bounds__(NB * NB) potrf_diag_kernel(zc* __restrict__ A, unsigned n, unsigned kb,
+                                                             unsigned* status) {
+    __shared__ zc a[NB][NB + 1];
+    const unsigned nb = min((unsigned)NB, n - kb);
+    const unsigned r = threadIdx.x / NB, c = threadIdx.x % NB;
+    if(r < nb && c < nb) a[r][c] = A[(size_t)(kb + r) * n + kb + c];
+    __syncthreads();
+    for(unsigned j = 0; j < nb; j++) {
+        if(threadIdx.x == 0) {
+            double d = a[j][j].re;
+            if(!(d > 0.0) || !isfinite(d)) {
+                atomicOr(status, kStatusNotPosDef);
+                d = 1.0;
+            }
+            a[j][j] = mk(sqrt(d), 0.0);
+        }
+        __syncthreads();
+        if(c == j && r > j && r < nb) {
+            const double inv = 1.0 / a[j][j].re;
+            a[r][j] = inv * a[r][j];
+        }
+        __syncthreads();
+        if(r > j && c > j && c <= r && r < nb) a[r][c] = a[r][c] - a[r][j] * conj(a[c][j]);
+        __syncthreads();
+    }
+    if(r < nb && c <= r) A[(size_t)(kb + r) * n + kb + c] = a[r][c];
+}
+
+// rows below the diagonal block: X <- X L_kk^{-H}, one thread per row
+__global__ void __launch_bounds__(32) trsm_panel_kernel(zc* __restrict__ A, unsigned n, unsigned kb) {
+    __shared__ zc L[NB][NB + 1];
+    __shared__ zc X[32][NB + 1];
+    const unsigned nb = min((unsigned)NB, n - kb);
+    for(unsigned t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+        const unsigned r = t / nb, c = t % nb;
+        L[r][c] = A[(size_t)(kb + r) * n + kb + c];
+    }
+    const unsigned row = kb + nb + blockIdx.x * 32 + threadIdx.x;
+    const bool live = row < n;
+    if(live)
+        for(unsigned p = 0; p < nb; p++) X[threadIdx.x][p] = A[(size_t)row * n + kb + p];
+    __syncthreads();
+    if(!live) return;
+    for(unsigned j = 0; j < nb; j++) {
+        zc x = X[threadIdx.x][j];
+        for(unsigned p = 0; p < j; p++) x = x - X[threadIdx.x][p] * conj(L[j][p]);
+        X[threadIdx.x][j] = (1.0 / L[j][j].re) * x;
+    }
+    for(unsigned p = 0; p < nb; p++) A[(size_t)row * n + kb + p] = X[threadIdx.x][p];
+}
+
+// trailing lower triangle: A[i][j] -= sum_p X[i][p] conj(X[j][p]), i >= j >= t0
+__global__ void __launch_bounds__(256) herk_update_kernel(zc* __restrict__ A, unsigned n, unsigned kb, unsigned nb,
+                                                          unsigned tiles) {
+    __shared__ zc Xi[16][UT];
+    __shared__ zc Xj[16][UT];
+    const unsigned t0 = kb + nb;
+    // lower-triangular tile (ti >= tj)
+    unsigned b = blockIdx.x, ti = 0;
+    while(b > ti) { b -= ti + 1; ti++; }
+    const unsigned tj = b;
+    const unsigned i0 = t0 + ti * UT, j0 = t0 + tj * UT;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    zc acc[4][4];
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+#pragma unroll
+        for(int j = 0; j < 4; j++) acc[i][j] = mk(0.0, 0.0);
+    for(unsigned p0 = 0; p0 < nb; p0 += 16) {
+        __syncthreads();
+        for(int q = threadIdx.x; q < 16 * UT; q += 256) {
+            const int rr = q / 16, pp = q % 16;
+            const unsigned p = p0 + pp;
+            const unsigned gi = i0 + rr, gj = j0 + rr;
+            Xi[pp][rr] = (gi < n && p < nb) ? A[(size_t)gi * n + kb + p] : mk(0.0, 0.0);
+            Xj[pp][rr] = (gj < n && p < nb) ? A[(size_t)gj * n + kb + p] : mk(0.0, 0.0);
+        }
+        __syncthreads();
+#pragma unroll
+        for(int p = 0; p < 16; p++) {
+            zc xa[4], xb[4];
+#pragma unroll
+            for(int i = 0; i < 4; i++) xa[i] = Xi[p][ty + 16 * i];
+#pragma unroll
+            for(int j = 0; j < 4; j++) xb[j] = Xj[p][tx + 16 * j];
+#pragma unroll
+            for(int i = 0; i < 4; i++)
+#pragma unroll
+                for(int j = 0; j < 4; j++) {
+                    acc[i][j].re += xa[i].re * xb[j].re + xa[i].im * xb[j].im;
+                    acc[i][j].im += xa[i].im * xb[j].re - xa[i].re * xb[j].im;
+                }
+        }
+    }
+#pragma unroll
+    for(int i = 0; i < 4; i++) {
+        const unsigned gi = i0 + ty + 16 * i;
+        if(gi >= n) continue;
+#pragma unroll
+        for(int j = 0; j < 4; j++) {
+            const unsigned gj = j0 + tx + 16 * j;
+            if(gj >= n || gj > gi) continue;
+            zc& dst = A[(size_t)gi * n + gj];
+            dst = dst - acc[i][j];
+        }
+    }
+}
+
+// forward substitution step for block kb: every CTA solves L_kk y_k = b_k
+// (identically), CTA 0 stores y_k, and all CTAs update the rows below.
+__global__ void __launch_bounds__(256) fwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
+                                                        zc* __restrict__ b) {
+    __shared__ zc y[NB];
+    const unsigned nb = min((unsigned)NB, n - kb);
+    if(threadIdx.x == 0) {
+        for(unsigned j = 0; j < nb; j++) {
+            zc x = b[kb + j];
+            for(unsigned p = 0; p < j; p++) x = x - L[(size_t)(kb + j) * n + kb + p] * y[p];
+            y[j] = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * x;
+        }
+    }
+    __syncthreads();
+    if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = y[threadIdx.x];
+    for(size_t i = kb + nb + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        zc acc = mk(0.0, 0.0);
+        for(unsigned p = 0; p < nb; p++) acc += L[i * n + kb + p] * y[p];
+        b[i] = b[i] - acc;
+    }
+}
+
+// backward substitution step for block kb with L^H
+__global__ void __launch_bounds__(256) bwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
+                                                        zc* __restrict__ b) {
+    __shared__ zc x[NB];
+    const unsigned nb = min((unsigned)NB, n - kb);
+    if(threadIdx.x == 0) {
+        for(int j = (int)nb - 1; j >= 0; j--) {
+            zc v = b[kb + j];
+            for(unsigned p = j + 1; p < nb; p++) v = v - conj(L[(size_t)(kb + p) * n + kb + j]) * x[p];
+            x[j] = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * v;
+        }
+    }
+    __syncthreads();
+    if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = x[threadIdx.x];
+    for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < kb; i += (size_t)gridDim.x * blockDim.x) {
+        zc acc = mk(0.0, 0.0);
+        for(unsigned q = 0; q < nb; q++) acc += conj(L[(size_t)(kb + q) * n + i]) * x[q];
+        b[i] = b[i] - acc;
+    }
+}
+
+// r = F - (S + shift I) x, one warp per row
+__global__ void residual_kernel(const zc* __restrict__ S, unsigned n, double shift, const zc* __restrict__ x,
+                                const zc* __restrict__ F, zc* __restrict__ r) {
+    const size_t i = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if(i >= n) return;
+    zc acc = mk(0.0, 0.0);
+    for(unsigned j = lane; j < n; j += 32) acc += S[i * n + j] * x[j];
+    acc = warp_sum(acc);
+    if(lane == 0) r[i] = F[i] - acc - shift * x[i];
+}
+
+__global__ void axpy_kernel(zc* __restrict__ x, const zc* __restrict__ c, unsigned n) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n) x[i] += c[i];
+}
+
+// info[0] = ||r|| / ||F|| before refinement, info[1] after
+__global__ void norm_ratio_kernel(const zc* __restrict__ r, const zc* __restrict__ F, unsigned n, double* out) {
+    __shared__ double sh[2][32];
+    double a = 0.0, b = 0.0;
+    for(unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+        a += norm2(r[i]);
+        b += norm2(F[i]);
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if((threadIdx.x & 31) == 0) { sh[0][threadIdx.x >> 5] = a; sh[1][threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for(unsigned w = 0; w < (blockDim.x >> 5); w++) { ta += sh[0][w]; tb += sh[1][w]; }
+        *out = tb > 0.0 ? sqrt(ta / tb) : sqrt(ta);
+    }
+}
+
+void cholesky(zc* A, unsigned n, unsigned* status, cudaStream_t st) {
+    for(unsigned kb = 0; kb < n; kb += NB) {
+        const unsigned nb = min((unsigned)NB, n - kb);
+        potrf_diag_kernel<<<1, NB * NB, 0, st>>>(A, n, kb, status);
+        check_launch("potrf_diag_kernel");
+        const unsigned below = n - kb - nb;
+        if(below == 0) break;
+        trsm_panel_kernel<<<(below + 31) / 32, 32, 0, st>>>(A, n, kb);
+        check_launch("trsm_panel_kernel");
+        const unsigned tiles = (below + UT - 1) / UT;
+        herk_update_kernel<<<tiles * (tiles + 1) / 2, 256, 0, st>>>(A, n, kb, nb, tiles);
+        check_launch("herk_update_kernel");
+    }
+}
+
+void solve_in_place(const zc* L, unsigned n, zc* b, cudaStream_t st) {
+    for(unsigned kb = 0; kb < n; kb += NB) {
+        const unsigned below = n - kb - min((unsigned)NB, n - kb);
+        const unsigned grid = below ? min(132u, (below + 255) / 256) : 1u;
+        fwd_block_kernel<<<grid, 256, 0, st>>>(L, n, kb, b);
+        check_launch("fwd_block_kernel");
+    }
+    const unsigned last = ((n - 1) / NB) * NB;
+    for(int kb = (int)last; kb >= 0; kb -= NB) {
+        const unsigned grid = kb ? min(132u, ((unsigned)kb + 255) / 256) : 1u;
+        bwd_block_kernel<<<grid, 256, 0, st>>>(L, n, (unsigned)kb, b);
+        check_launch("bwd_block_kernel");
+    }
+}
+
+}  // namespace
+
+void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st) {
+    const unsigned n = td.Np;
+    const size_t nn = (size_t)n * n;
+    td.L.ensure(nn * sizeof(zc));
+    td.delta.ensure(n * sizeof(zc));
+    td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
+    zc* A = td.L.as<zc>();
+    zc* x = td.delta.as<zc>();
+    zc* r = td.resid.as<zc>();
+    double* info = reinterpret_cast<double*>(r + 2 * n);
+    const zc* S = td.S.as<zc>();
+    const zc* F = td.F.as<zc>();
+    copy_shift_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(S, A, n, shift);
+    check_launch("copy_shift_kernel");
+    cholesky(A, n, status, st);
+    ANN_CUDA(cudaMemcpyAsync(x, F, n * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+    solve_in_place(A, n, x, st);
+    // one step of iterative refinement against S + shift I
+    residual_kernel<<<(n + 7) / 8, 256, 0, st>>>(S, n, shift, x, F, r);
+    check_launch("residual_kernel");
+    norm_ratio_kernel<<<1, 1024, 0, st>>>(r, F, n, info);
+    check_launch("norm_ratio_kernel");
+    solve_in_place(A, n, r, st);
+    axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, r, n);
+    check_launch("axpy_kernel");
+    residual_kernel<<<(n + 7) / 8, 256, 0, st>>>(S, n, shift, x, F, r + n);
+    check_launch("residual_kernel");
+    norm_ratio_kernel<<<1, 1024, 0, st>>>(r + n, F, n, info + 1);
+    check_launch("norm_ratio_kernel");
+}
+
+namespace {
+__global__ void sr_update_kernel(zc* __restrict__ p, const zc* __restrict__ d, double lr, unsigned n) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n) p[i] = p[i] - lr * d[i];
+}
+}  // namespace
+
+void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st) {
+    sr_update_kernel<<<(psi.Np + 255) / 256, 256, 0, st>>>(psi.params.as<zc>(), delta, lr, psi.Np);
+    check_launch("sr_update_kernel");
+    psi_prepare(psi, st);
+}
+
+}  // namespace ann

@@ -1,0 +1,360 @@
+// Precision-form S matrix on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// The complex HERK S = X^H X over centred, weight-scaled rows
+// X_sk = sqrt(w_s) (O_sk - mu_k), mu = Obar / W (see herk_simt.cu for the
+// identity with the reference's S, source/network_functions/TDVP.cu.template:216-301)
+// is embedded in one real product. With A = Re X, B = Im X:
+//   Re S = A^T A + B^T B,   Im S = A^T B - B^T A.
+// herk_prep_kernel writes the operand XT in BF16, K-major (samples innermost),
+// with the rows of parameter block I (128 parameters) stored as
+// [Re of the block (128 rows) ; Im of the block (128 rows)]. One CTA computes the
+// 128 x 128 complex tile (I, J <= I is mirrored): per K step of 64 samples TMA
+// brings the 256 x 64 blocks of I and J into shared memory (128-byte swizzle) and
+// one elected thread issues, per 16-sample slice,
+//   D1 (TMEM cols   0..255) += Re_I  . [Re_J ; Im_J]^T   (M=128, N=256)
+//   D2 (TMEM cols 256..511) += Im_I  . [Re_J ; Im_J]^T
+// so Re S = D1[:, :128] + D2[:, 128:], Im S = D1[:, 128:] - D2[:, :128], read back
+// by four warps with tcgen05.ld. FP32 accumulation; hi+lo splitting adds the
+// products hi.lo and lo.hi as two more K segments.
+//
+// Every wait on an mbarrier is bounded (globaltimer deadline); a timeout sets
+// kStatusTimeout, makes all roles leave their loops, waits (bounded) for the
+// copies in flight and frees the tensor memory before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "ann_internal.hpp"
+
+namespace ann {
+
+namespace {
+
+constexpr int kBM = 128;                    // parameters per tile side
+constexpr int kRowsPerBlock = 2 * kBM;      // Re + Im rows of one parameter block
+constexpr int kBK = 64;                     // samples per K step (128 bytes of BF16)
+constexpr int kStages = 3;
+constexpr int kStageBytes = 2 * kRowsPerBlock * kBK * 2;  // A block + B block
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr unsigned long long kWaitNs = 2000000000ull;     // 2 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: returns false (and raises the abort flag) on timeout or abort
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity, volatile int* abort_flag,
+                                          unsigned* status) {
+    const unsigned long long t0 = gtime();
+    while(!mbar_try(bar, parity)) {
+        if(*abort_flag) return false;
+        if(gtime() - t0 > kWaitNs) {
+            *abort_flag = 1;
+            atomicOr(status, kStatusTimeout);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// instruction descriptor: kind::f16, A/B BF16, D FP32, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for(int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+struct HerkArgs {
+    unsigned Np;            // parameters
+    unsigned nblk;          // parameter blocks of 128
+    unsigned k_steps;       // K steps of 64 samples per segment
+    unsigned segments;      // 1 (plain BF16) or 3 (hi.hi + hi.lo + lo.hi)
+    unsigned lo_offset;     // column of the lo copy in XT
+    const cplx<double>* Obar;
+    const Stats* stats;
+    cplx<double>* S;
+    unsigned* status;
+};
+
+// lower block triangle (I >= J) from the linear CTA index
+__device__ __forceinline__ void tile_of(unsigned b, unsigned& I, unsigned& J) {
+    I = 0;
+    while(b > I) { b -= I + 1; I++; }
+    J = b;
+}
+
+__global__ void __launch_bounds__(128, 1)
+herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned stage buffers (128-byte swizzle atoms)
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* tail = base + kStages * kStageBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(tail);
+    uint64_t* empty = full + kStages;
+    uint64_t* done = empty + kStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned I, J;
+    tile_of(blockIdx.x, I, J);
+
+    if(threadIdx.x == 0) {
+        for(int s = 0; s < kStages; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncwarp();
+    if(warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const unsigned total = a.segments * a.k_steps;
+    int issued = 0;  // TMA stages issued by the producer (for the drain on abort)
+    if(warp == 0 && lane == 0) {
+        // ---- TMA producer ----
+        for(unsigned kt = 0; kt < total; kt++) {
+            const int s = kt % kStages;
+            const unsigned ph = (kt / kStages) & 1u;
+            if(!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag, a.status)) break;
+            const unsigned seg = kt / a.k_steps, k = kt % a.k_steps;
+            const int xa = (int)(k * kBK + (seg == 2 ? a.lo_offset : 0u));
+            const int xb = (int)(k * kBK + (seg == 1 ? a.lo_offset : 0u));
+            unsigned char* sa = base + s * kStageBytes;
+            unsigned char* sb = sa + kRowsPerBlock * kBK * 2;
+            mbar_expect_tx(smem_u32(&full[s]), kStageBytes);
+            tma_load_2d(smem_u32(sa), &tmap, xa, (int)(I * kRowsPerBlock), smem_u32(&full[s]));
+            tma_load_2d(smem_u32(sb), &tmap, xb, (int)(J * kRowsPerBlock), smem_u32(&full[s]));
+            issued++;
+        }
+    } else if(warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        constexpr uint32_t idesc = idesc_bf16(128, 256);
+        bool ok = true;
+        for(unsigned kt = 0; kt < total && ok; kt++) {
+            const int s = kt % kStages;
+            const unsigned ph = (kt / kStages) & 1u;
+            if(!mbar_wait(smem_u32(&full[s]), ph, abort_flag, a.status)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(base + s * kStageBytes);
+            const uint32_t sb = sa + kRowsPerBlock * kBK * 2;
+#pragma unroll
+            for(int kk = 0; kk < kBK / 16; kk++) {
+                const int acc = (kt > 0 || kk > 0) ? 1 : 0;
+                const uint64_t db = sw128_desc(sb + kk * 32);
+                mma_bf16(tmem, sw128_desc(sa + kk * 32), db, idesc, acc);                        // Re_I rows
+                mma_bf16(tmem + 256, sw128_desc(sa + kBM * 128 + kk * 32), db, idesc, acc);      // Im_I rows
+            }
+            mma_commit(smem_u32(&empty[s]));
+        }
+        mma_commit(smem_u32(done));
+    }
+    __syncwarp();
+
+    // ---- epilogue: all four warps ----
+    bool ok = mbar_wait(smem_u32(done), 0, abort_flag, a.status) && !*abort_flag;
+    ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if(ok) {
+        const double W = a.stats->W;
+        const double corr = 1.0 / W - 1.0;
+        const unsigned i = warp * 32 + lane;  // TMEM lane = row of the tile
+        const unsigned k = I * kBM + i;       // parameter of the row
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        const bool row_ok = k < a.Np;
+        const cplx<double> ok_conj = row_ok ? conj(a.Obar[k]) : mk(0.0, 0.0);
+        for(int c0 = 0; c0 < kBM; c0 += 16) {
+            float rr[16], ri[16], ir[16], ii[16];
+            tmem_ld16(lane_addr + c0, rr);
+            tmem_ld16(lane_addr + kBM + c0, ri);
+            tmem_ld16(lane_addr + 256 + c0, ir);
+            tmem_ld16(lane_addr + 256 + kBM + c0, ii);
+            if(!row_ok) continue;
+#pragma unroll
+            for(int q = 0; q < 16; q++) {
+                const unsigned l = J * kBM + c0 + q;
+                if(l >= a.Np) continue;
+                cplx<double> v = mk((double)rr[q] + (double)ii[q], (double)ri[q] - (double)ir[q]);
+                v = v + corr * (ok_conj * a.Obar[l]);
+                a.S[(size_t)k * a.Np + l] = v;
+                if(I != J) a.S[(size_t)l * a.Np + k] = conj(v);
+            }
+        }
+    } else if(warp == 0 && lane == 0) {
+        // drain: wait (bounded) for every issued copy before the buffers go away
+        for(int q = issued > kStages ? issued - kStages : 0; q < issued; q++) {
+            const int s = q % kStages;
+            const unsigned long long t0 = gtime();
+            while(!mbar_try(smem_u32(&full[s]), (q / kStages) & 1u) && gtime() - t0 < kWaitNs) {}
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+// XT[row][col] (BF16): row = 256 * (k / 128) + (k % 128) for Re, + 128 for Im;
+// col = sample (hi copy) and lo_offset + sample (lo copy, split mode).
+template<typename T>
+__global__ void __launch_bounds__(256)
+herk_prep_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned Np, const double* __restrict__ wts,
+                 double w0, const cplx<double>* __restrict__ Obar, const Stats* __restrict__ stats,
+                 __nv_bfloat16* __restrict__ XT, size_t ldx, unsigned lo_offset, int split) {
+    __shared__ cplx<float> tile[64][65];
+    const size_t s0 = (size_t)blockIdx.y * 64;
+    const unsigned k0 = blockIdx.x * 64;
+    const double invW = 1.0 / stats->W;
+    for(int q = threadIdx.x; q < 64 * 64; q += 256) {
+        const int r = q / 64, c = q % 64;
+        const size_t s = s0 + r;
+        const unsigned k = k0 + c;
+        cplx<float> v = mk(0.f, 0.f);
+        if(s < rows && k < Np) {
+            const double sw = sqrt(wts ? wts[s] : w0);
+            const cplx<double> o = cvt<double>(O[s * ld + k]);
+            const cplx<double> m = invW * Obar[k];
+            v = mk((float)(sw * (o.re - m.re)), (float)(sw * (o.im - m.im)));
+        }
+        tile[r][c] = v;
+    }
+    __syncthreads();
+    // 128 output rows (64 params x Re/Im) of 64 samples = 32 bf16 pairs each
+    for(int q = threadIdx.x; q < 128 * 32; q += 256) {
+        const int orow = q / 32, pair = q % 32;
+        const int c = orow >> 1, part = orow & 1;
+        const unsigned k = k0 + c;
+        const size_t row = (size_t)(k / kBM) * kRowsPerBlock + (k % kBM) + (part ? kBM : 0);
+        const float x0 = part ? tile[2 * pair][c].im : tile[2 * pair][c].re;
+        const float x1 = part ? tile[2 * pair + 1][c].im : tile[2 * pair + 1][c].re;
+        const __nv_bfloat162 hi = __floats2bfloat162_rn(x0, x1);
+        __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(XT + row * ldx + s0) + pair;
+        *dst = hi;
+        if(split) {
+            const float2 h = __bfloat1622float2(hi);
+            *(reinterpret_cast<__nv_bfloat162*>(XT + row * ldx + lo_offset + s0) + pair) =
+                __floats2bfloat162_rn(x0 - h.x, x1 - h.y);
+        }
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if(!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        ANN_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if(q != cudaDriverEntryPointSuccess || !p) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+}  // namespace
+
+void herk_tc(ann_tdvp_impl& td, const double* wts, double w0, bool split, cudaStream_t st) {
+    const unsigned Np = td.Np;
+    const unsigned nblk = (Np + kBM - 1) / kBM;
+    const size_t rows_x = (size_t)nblk * kRowsPerBlock;
+    const size_t ns_pad = (td.n_rows + kBK - 1) / kBK * kBK;
+    const size_t ldx = split ? 2 * ns_pad : ns_pad;
+    td.herk_in.ensure(rows_x * ldx * sizeof(__nv_bfloat16));
+    // padding rows / samples must read as zero
+    ANN_CUDA(cudaMemsetAsync(td.herk_in.p, 0, rows_x * ldx * sizeof(__nv_bfloat16), st));
+    dim3 pg((Np + 63) / 64, (unsigned)(ns_pad / 64));
+    auto* XT = td.herk_in.as<__nv_bfloat16>();
+    if(td.O_precision == 0)
+        herk_prep_kernel<float><<<pg, 256, 0, st>>>(td.O.as<cplx<float>>(), td.n_rows, td.ldO, Np, wts, w0,
+                                                     td.Obar.as<cplx<double>>(), td.stats.as<Stats>(), XT, ldx,
+                                                     (unsigned)ns_pad, split ? 1 : 0);
+    else
+        throw Error(ANN_ERR_UNSUPPORTED, "tensor-core S takes complex64 rows");
+    check_launch("herk_prep_kernel");
+
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)ldx, (cuuint64_t)rows_x};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ldx * sizeof(__nv_bfloat16))};
+    const cuuint32_t box[2] = {kBK, kRowsPerBlock};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, td.herk_in.p, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+
+    HerkArgs a;
+    a.Np = Np;
+    a.nblk = nblk;
+    a.k_steps = (unsigned)(ns_pad / kBK);
+    a.segments = split ? 3 : 1;
+    a.lo_offset = (unsigned)ns_pad;
+    a.Obar = td.Obar.as<cplx<double>>();
+    a.stats = td.stats.as<Stats>();
+    a.S = td.S.as<cplx<double>>();
+    a.status = status_word();
+    static bool attr = false;
+    if(!attr) {
+        ANN_CUDA(cudaFuncSetAttribute(herk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+        attr = true;
+    }
+    const unsigned tiles = nblk * (nblk + 1) / 2;
+    herk_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(map, a);
+    check_launch("herk_tc_kernel");
+}
+
+}  // namespace ann

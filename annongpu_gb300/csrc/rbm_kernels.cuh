@@ -1,0 +1,400 @@
+// RBM-family wavefunctions on the GPU: one warp per Markov chain (or per enumerated
+// configuration), hidden-unit angles held in registers and updated incrementally.
+//
+// Covers the reference's PsiRBM (include/quantum_state/PsiRBM.hpp:69-176) and
+// PsiDeep with one hidden layer (include/quantum_state/PsiDeep.hpp:138-445): both
+// are theta_j = b_j + sum_c W[c,j] s[conn(c,j)], log psi = log_pref + (a.s) +
+// sum_j fw_j f(theta_j). The sampler follows MonteCarlo_t::kernel_foreach /
+// mc_update (include/ensembles/MonteCarlo.hpp:55-177) and the local energy follows
+// StandartOperator::local_energy (include/operator/Operator.hpp:36-121), restated
+// with angle deltas instead of update / full recompute / revert.
+#pragma once
+
+#include "ann_common.cuh"
+
+namespace ann {
+
+constexpr int kWarpsPerBlock = 8;
+
+// Wavefunction as the kernels see it. Unit j of the padded width Mpad = 32 * U
+// lives in lane j % 32, register slot j / 32.
+template<typename T>
+struct RbmDev {
+    unsigned N, M, Mpad, C, Np;
+    int layout;          // 0: params = W (PsiRBM), 1: params = [a | b | W] (PsiDeep)
+    int a_in_log_psi;    // 1: log psi includes a.s
+    int act;             // Activation
+    const cplx<T>* Wd;   // N x Mpad, dense site -> unit weights (sum over connections)
+    const cplx<T>* a;    // N
+    const cplx<T>* b;    // Mpad (zero padded)
+    const cplx<T>* fw;   // Mpad (zero padded)
+    const uint16_t* conn;// C x M: input site of connection (c, j)
+    cplx<T> lp;          // log prefactor
+};
+
+struct McArgs {
+    unsigned n_chains;
+    unsigned samples_per_chain;
+    unsigned num_sweeps;
+    unsigned num_therm;
+    int do_init;              // draw fresh configurations (and thermalise) first
+    int n_up;                 // < 0: unconstrained initial configurations
+    int move_kind;            // 0 single flip, 1 exchange over bonds, 2 exchange over random pairs
+    const uint32_t* bonds;    // [n_bonds][2]
+    unsigned n_bonds;
+    uint32_t k0, k1;          // Philox key
+    uint64_t* chain_conf;     // [n_chains][kMaxWords], in/out
+    uint64_t* chain_counter;  // [n_chains], in/out
+    // proposal tape (parity replay): per chain, num_props sites and uniforms
+    const uint32_t* tape_site;
+    const double* tape_u;
+    unsigned tape_len;
+    unsigned long long* acc_rej;  // [2]
+};
+
+struct SampleOut {
+    uint64_t* conf;           // [rows][kMaxWords]
+    cplx<double>* log_psi;    // [rows]
+    cplx<double>* eloc;       // [rows] (may be null)
+    double* weight;           // [rows] (exact summation only)
+    void* O;                  // [rows][ldO] cplx<T> (may be null)
+    size_t ldO;
+    unsigned* status;
+};
+
+template<typename T, int U>
+struct Lane {
+    cplx<T> th[U];   // angles
+    cplx<T> ft[U];   // fw_j * f(theta_j)
+};
+
+// theta_j = b_j + sum_i s_i Wd[i][j] from scratch
+template<typename T, int NW, int U>
+__device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
+                                          const Conf<NW>& s, Lane<T, U>& L, int lane) {
+#pragma unroll
+    for(int u = 0; u < U; u++) L.th[u] = p.b[u * 32 + lane];
+    for(unsigned i = 0; i < p.N; i++) {
+        const T si = spin_bit(s, i) ? T(1) : T(-1);
+        const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            const cplx<T> w = row[u * 32];
+            L.th[u].re += si * w.re;
+            L.th[u].im += si * w.im;
+        }
+    }
+#pragma unroll
+    for(int u = 0; u < U; u++) L.ft[u] = p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0);
+}
+
+// sum over the warp of fw_j (f(theta_j + dtheta_j) - f(theta_j)) for the sites in `sites`
+template<typename T, int NW, int U>
+__device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
+                                                 const Conf<NW>& s, const Lane<T, U>& L, int lane,
+                                                 const uint16_t* sites, unsigned nsites,
+                                                 cplx<T>* dth, cplx<T>* fnew) {
+#pragma unroll
+    for(int u = 0; u < U; u++) dth[u] = mk<T>(T(0), T(0));
+    cplx<T> dvis = mk<T>(T(0), T(0));
+    for(unsigned q = 0; q < nsites; q++) {
+        const unsigned i = sites[q];
+        const T m2s = spin_bit(s, i) ? T(-2) : T(2);  // s'_i - s_i
+        const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            const cplx<T> w = row[u * 32];
+            dth[u].re += m2s * w.re;
+            dth[u].im += m2s * w.im;
+        }
+        if(p.a_in_log_psi) dvis += m2s * p.a[i];
+    }
+    cplx<T> d = mk<T>(T(0), T(0));
+#pragma unroll
+    for(int u = 0; u < U; u++) {
+        fnew[u] = p.fw[u * 32 + lane] * act_f(L.th[u] + dth[u], p.act, 0);
+        d += fnew[u] - L.ft[u];
+    }
+    d = warp_sum(d);
+    return d + dvis;
+}
+
+// local energy of configuration s (Operator.hpp:86-121 semantics)
+template<typename T, int NW, int U>
+__device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op,
+                                     const Conf<NW>& s, const Lane<T, U>& L, int lane) {
+    // diagonal strings, split over lanes
+    double dre = 0.0, dim = 0.0;
+    for(unsigned n = lane; n < op.n_diag; n += 32) {
+        int neg = 0;
+#pragma unroll
+        for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.diag_mask[n * op.nw + w]);
+        const double sg = (neg & 1) ? -1.0 : 1.0;
+        dre += sg * op.diag_coeff[2 * n];
+        dim += sg * op.diag_coeff[2 * n + 1];
+    }
+    cplx<double> e = mk<double>(warp_sum(dre), warp_sum(dim));
+    cplx<T> dth[U], fnew[U];
+    for(unsigned g = 0; g < op.n_groups; g++) {
+        const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
+        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, op.grp_sites + sb, se - sb, dth, fnew);
+        cplx<double> cg = mk<double>(0.0, 0.0);
+        for(unsigned k = op.grp_str_begin[g]; k < op.grp_str_begin[g + 1]; k++) {
+            int neg = 0;
+#pragma unroll
+            for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.str_mask[k * op.nw + w]);
+            const double sg = (neg & 1) ? -1.0 : 1.0;
+            cg.re += sg * op.str_coeff[2 * k];
+            cg.im += sg * op.str_coeff[2 * k + 1];
+        }
+        const cplx<double> r = cvt<double>(cexp(d));
+        e += cg * r;
+    }
+    return e;
+}
+
+// log psi, local energy, O_k row and sample bookkeeping for one configuration
+template<typename T, int NW, int U>
+__device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev* op,
+                               const Conf<NW>& s, const Lane<T, U>& L, int lane, size_t row,
+                               const SampleOut& out, bool exact_weight) {
+    cplx<T> lsum = mk<T>(T(0), T(0));
+#pragma unroll
+    for(int u = 0; u < U; u++) lsum += L.ft[u];
+    if(p.a_in_log_psi)
+        for(unsigned i = lane; i < p.N; i += 32) lsum += (spin_bit(s, i) ? T(1) : T(-1)) * p.a[i];
+    lsum = warp_sum(lsum);
+    const cplx<double> lpsi = cvt<double>(lsum) + cvt<double>(p.lp);
+    cplx<double> e = mk<double>(0.0, 0.0);
+    if(op) e = local_energy<T, NW, U>(p, Wd, *op, s, L, lane);
+    if(lane == 0) {
+        for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = w < NW ? s.w[w] : 0;
+        out.log_psi[row] = lpsi;
+        if(out.eloc) out.eloc[row] = e;
+        if(exact_weight && out.weight) out.weight[row] = exp(2.0 * lpsi.re);
+        if(!(isfinite(lpsi.re) && isfinite(lpsi.im) && isfinite(e.re) && isfinite(e.im)))
+            atomicOr(out.status, kStatusNonFinite);
+    }
+    if(out.O) {
+        cplx<T>* O = reinterpret_cast<cplx<T>*>(out.O) + row * out.ldO;
+        cplx<T> g[U];
+#pragma unroll
+        for(int u = 0; u < U; u++) g[u] = p.fw[u * 32 + lane] * act_df(L.th[u], p.act, 0);
+        unsigned off = 0;
+        if(p.layout == 1) {
+            for(unsigned i = lane; i < p.N; i += 32) O[i] = mk<T>(spin_bit(s, i) ? T(1) : T(-1), T(0));
+#pragma unroll
+            for(int u = 0; u < U; u++) {
+                const unsigned j = u * 32 + lane;
+                if(j < p.M) O[p.N + j] = g[u];
+            }
+            off = p.N + p.M;
+        }
+        for(unsigned c = 0; c < p.C; c++) {
+            const uint16_t* cr = p.conn + (size_t)c * p.M;
+            cplx<T>* orow = O + off + (size_t)c * p.M;
+#pragma unroll
+            for(int u = 0; u < U; u++) {
+                const unsigned j = u * 32 + lane;
+                if(j < p.M) orow[j] = spin_bit(s, cr[j]) ? g[u] : -g[u];
+            }
+        }
+    }
+}
+
+// Copies Wd to shared memory when it fits (w_smem != 0); returns the pointer to use.
+template<typename T>
+__device__ __forceinline__ const cplx<T>* stage_Wd(const RbmDev<T>& p, int w_smem, cplx<T>* smem) {
+    if(!w_smem) return p.Wd;
+    const size_t n = (size_t)p.N * p.Mpad;
+    const float4* src = reinterpret_cast<const float4*>(p.Wd);
+    float4* dst = reinterpret_cast<float4*>(smem);
+    const size_t n4 = n * sizeof(cplx<T>) / sizeof(float4);
+    for(size_t k = threadIdx.x; k < n4; k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+    return smem;
+}
+
+// ---------------------------------------------------------------------------------
+// Metropolis sampler: one warp per chain.
+template<typename T, int NW, int U>
+__global__ void __launch_bounds__(512)
+rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
+    const int lane = threadIdx.x & 31;
+    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(chain >= a.n_chains) return;
+    const unsigned N = p.N;
+
+    Conf<NW> s;
+    uint64_t t;
+    unsigned tape_pos = 0;
+    const bool tape = a.tape_site != nullptr;
+    if(tape) {
+        for(int w = 0; w < NW; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
+        t = 0;
+    } else if(a.do_init) {
+        t = a.chain_counter[chain];
+        if(a.n_up < 0) {
+            const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)t, (uint32_t)(t >> 32), chain, 1u});
+            s.w[0] = (uint64_t)r.x | ((uint64_t)r.y << 32);
+            if(NW > 1) s.w[NW - 1] = (uint64_t)r.z | ((uint64_t)r.w << 32);
+            for(int w = 0; w < NW; w++) {
+                const unsigned lo = 64u * w;
+                if(N <= lo) s.w[w] = 0;
+                else if(N - lo < 64u) s.w[w] &= ((uint64_t)1 << (N - lo)) - 1u;
+            }
+        } else {
+            for(int w = 0; w < NW; w++) s.w[w] = 0;
+            for(int k = 0; k < a.n_up; k++) {
+                const uint64_t tk = t + (uint64_t)k;
+                const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tk, (uint32_t)(tk >> 32), chain, 2u});
+                unsigned target = mulhi32(r.x, N - (unsigned)k);
+                for(unsigned i = 0; i < N; i++) {
+                    if(!spin_bit(s, i)) {
+                        if(target == 0) { s.w[i >> 6] |= (uint64_t)1 << (i & 63u); break; }
+                        target--;
+                    }
+                }
+            }
+        }
+    } else {
+        for(int w = 0; w < NW; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
+        t = a.chain_counter[chain];
+    }
+
+    Lane<T, U> L;
+    recompute<T, NW, U>(p, Wd, s, L, lane);
+    unsigned long long n_acc = 0, n_rej = 0;
+    const uint64_t t0 = t;
+    u32x4 rr = {0, 0, 0, 0};
+    cplx<T> dth[U], fnew[U];
+
+    auto propose = [&]() {
+        unsigned i, j = 0xFFFFFFFFu;
+        double u;
+        if(tape) {
+            i = a.tape_site[(size_t)chain * a.tape_len + tape_pos];
+            u = a.tape_u[(size_t)chain * a.tape_len + tape_pos];
+            tape_pos++;
+        } else {
+            const unsigned k = (unsigned)(t - t0) & 31u;
+            if(k == 0) {
+                const uint64_t tl = t + lane;
+                rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
+            }
+            const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
+            const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
+            const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
+            const uint32_t r3 = __shfl_sync(0xffffffffu, rr.w, k);
+            t++;
+            i = mulhi32(r0, N);
+            if(a.move_kind == 1) {
+                const unsigned bnd = mulhi32(r0, a.n_bonds);
+                i = a.bonds[2 * bnd];
+                j = a.bonds[2 * bnd + 1];
+            } else if(a.move_kind == 2) {
+                j = mulhi32(r1, N - 1u);
+                j += (j >= i);
+            }
+            u = u53(r2, r3);
+        }
+        uint16_t sites[2];
+        unsigned ns = 1;
+        sites[0] = (uint16_t)i;
+        if(a.move_kind != 0 && !tape) {
+            if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
+            sites[1] = (uint16_t)j;
+            ns = 2;
+        }
+        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, sites, ns, dth, fnew);
+        const T ratio = fexp(T(2) * d.re);
+        // MonteCarlo.hpp:158-160: accept if ratio > 1 or u <= ratio; u < 1 makes
+        // the first clause redundant.
+        if(u <= (double)ratio) {
+#pragma unroll
+            for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.ft[q] = fnew[q]; }
+            for(unsigned q = 0; q < ns; q++) flip(s, sites[q]);
+            n_acc++;
+        } else {
+            n_rej++;
+        }
+    };
+
+    if(a.do_init || tape)
+        for(unsigned k = 0; k < a.num_therm * N; k++) propose();
+    for(unsigned st = 0; st < a.samples_per_chain; st++) {
+        for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
+        recompute<T, NW, U>(p, Wd, s, L, lane);  // removes accumulated rounding of the increments
+        process_sample<T, NW, U>(p, Wd, with_op ? &op : nullptr, s, L, lane,
+                                 (size_t)st * a.n_chains + chain, out, false);
+    }
+    if(lane == 0) {
+        if(!tape) {
+            for(int w = 0; w < kMaxWords; w++) a.chain_conf[(size_t)chain * kMaxWords + w] = w < NW ? s.w[w] : 0;
+            a.chain_counter[chain] = t;
+        }
+        atomicAdd(&a.acc_rej[0], n_acc);
+        atomicAdd(&a.acc_rej[1], n_rej);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Exact summation: one warp per enumerated configuration (ExactSummation.hpp:33-72).
+template<typename T, int NW, int U>
+__global__ void __launch_bounds__(512)
+rbm_exact_kernel(RbmDev<T> p, OpDev op, int with_op, uint64_t n_conf, SampleOut out, int w_smem) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for(uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n_conf; idx += warps) {
+        Conf<NW> s;
+        s.w[0] = idx;
+        for(int w = 1; w < NW; w++) s.w[w] = 0;
+        Lane<T, U> L;
+        recompute<T, NW, U>(p, Wd, s, L, lane);
+        process_sample<T, NW, U>(p, Wd, with_op ? &op : nullptr, s, L, lane, idx, out, true);
+    }
+}
+
+// Explicit configurations (log_psi_s / psi_O_k of single configurations, batches).
+template<typename T, int NW, int U>
+__global__ void __launch_bounds__(512)
+rbm_confs_kernel(RbmDev<T> p, OpDev op, int with_op, const uint64_t* confs, uint64_t n_conf, SampleOut out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(idx >= n_conf) return;
+    Conf<NW> s;
+    for(int w = 0; w < NW; w++) s.w[w] = confs[idx * kMaxWords + w];
+    Lane<T, U> L;
+    recompute<T, NW, U>(p, p.Wd, s, L, lane);
+    process_sample<T, NW, U>(p, p.Wd, with_op ? &op : nullptr, s, L, lane, idx, out, true);
+}
+
+// params (FP64 master copy, layout 0 or 1) -> kernel-precision dense weights.
+// One thread per hidden unit column; no two threads touch the same column.
+template<typename T>
+__global__ void rbm_prepare_kernel(RbmDev<T> p, const cplx<double>* __restrict__ params,
+                                   cplx<T>* Wd, cplx<T>* a, cplx<T>* b) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned off = p.layout == 1 ? p.N + p.M : 0u;
+    if(j < p.Mpad) {
+        for(unsigned i = 0; i < p.N; i++) Wd[(size_t)i * p.Mpad + j] = mk<T>(T(0), T(0));
+        if(j < p.M) {
+            for(unsigned c = 0; c < p.C; c++) {
+                const cplx<double> w = params[off + (size_t)c * p.M + j];
+                cplx<T>& dst = Wd[(size_t)p.conn[(size_t)c * p.M + j] * p.Mpad + j];
+                dst.re += (T)w.re;
+                dst.im += (T)w.im;
+            }
+            b[j] = p.layout == 1 ? cvt<T>(params[p.N + j]) : mk<T>(T(0), T(0));
+        } else {
+            b[j] = mk<T>(T(0), T(0));
+        }
+    }
+    if(j < p.N) a[j] = p.layout == 1 ? cvt<T>(params[j]) : mk<T>(T(0), T(0));
+}
+
+}  // namespace ann

@@ -1,0 +1,367 @@
+"""Benchmark of one SR step of the VMC inner loop on the 2-D TFIM 8x8 workload.
+
+Workload (square lattice 8 x 8, periodic, J = 1, h = 3.04): complex RBM with
+visible bias a(64), hidden bias b(128) and W(64 x 128), Np = 8384, entries
+iid N(0, 0.01^2) in real and imaginary parts (seeded). 16384 Markov chains,
+64 single-flip sweeps between samples, one sample per chain per SR step
+(N_s = 16384). One step = sampling + local energies + O rows + <O>, F +
+S (centred, BF16 tcgen05, FP32 accumulation) + FP64 Cholesky SR solve with one
+refinement step (diagonal shift 1e-3) + parameter update (lr 0.01).
+
+metric: effective samples/s with E_loc = N_s / tau_int / (seconds per SR step),
+tau_int from the Sokal automatic-window estimator (c = 5) on per-chain local
+energy series of a separate sampling run with the same parameters.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form precision|plain]
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+# the CPU legs are single-threaded unless stated otherwise
+for _v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, "1")
+
+import numpy as np  # noqa: E402
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "effective samples/s (with E_loc) and SR steps/s vs plain form at matched energy"
+UNIT = "samples/s"
+L, H_FIELD, ALPHA = 8, 3.04, 2
+N_SITES = L * L
+M_HIDDEN = ALPHA * N_SITES
+N_CHAINS = 16384
+SWEEPS = 64
+THERM = 64
+SHIFT = 1e-3
+LR = 0.01
+SEED = 1234
+
+
+def init_params(rng):
+    s = 0.01
+    a = s * (rng.standard_normal(N_SITES) + 1j * rng.standard_normal(N_SITES))
+    b = s * (rng.standard_normal(M_HIDDEN) + 1j * rng.standard_normal(M_HIDDEN))
+    W = s * (rng.standard_normal((N_SITES, M_HIDDEN)) + 1j * rng.standard_normal((N_SITES, M_HIDDEN)))
+    return a, b, W
+
+
+def config_dict(form, extra=None):
+    d = {"workload": f"2D TFIM {L}x{L} PBC h={H_FIELD}, complex RBM alpha={ALPHA} (Np=8384), "
+                     f"{N_CHAINS} chains, {SWEEPS} sweeps between samples, 1 sample/chain/SR step",
+         "form": form, "N": N_SITES, "M": M_HIDDEN, "num_params": N_SITES + M_HIDDEN + N_SITES * M_HIDDEN,
+         "chains": N_CHAINS, "sweeps_between_samples": SWEEPS, "samples_per_step": N_CHAINS,
+         "diag_shift": SHIFT, "lr": LR,
+         "l2": "inputs larger than L2 (O rows 1.1 GB, S 1.1 GB per step)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ----------------------------------------------------------------------------------
+def tau_int_sokal(series, c=5.0):
+    """Integrated autocorrelation time tau = 1 + 2 sum_t rho(t) with the automatic
+    window W = min{W : W >= c tau(W)}; rho averaged over chains. series: (T, chains)."""
+    x = np.asarray(series, float)
+    x = x - x.mean(axis=0, keepdims=True)
+    T = x.shape[0]
+    var = (x * x).mean()
+    if var <= 0:
+        return 1.0
+    tau = 1.0
+    for t in range(1, T):
+        rho = (x[:-t] * x[t:]).mean() / var
+        tau += 2.0 * rho
+        if t >= c * tau:
+            break
+    return max(tau, 1.0)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ----------------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import annongpu_gb300 as ann
+
+    dist = int(os.environ.get("WORLD_SIZE", "1")) > 1
+    rank = int(os.environ.get("RANK", "0"))
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        ann.setDevice(torch.cuda.current_device())
+    rng = np.random.default_rng(SEED)
+    a, b, W = init_params(rng)
+    H = ann.transverse_field_ising_2d(L, L, h=H_FIELD)
+    op = ann.Operator(H)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    s_mode = "bf16" if args.form == "precision" else "fp32"
+    mc = ann.MonteCarloLoop(N_CHAINS, SWEEPS, THERM, N_CHAINS, True, seed=SEED + 17 * rank, persistent=True)
+    tdvp = ann.TDVP(psi.num_params, s_mode=s_mode)
+    st = torch.cuda.Stream()
+    tdvp.stream = st
+    Np = psi.num_params
+    Ns = N_CHAINS
+
+    # warm-up (the first step thermalises the chains)
+    for _ in range(args.warmup):
+        tdvp.sr_step(op, psi, mc, SHIFT, LR)
+    st.synchronize()
+
+    # timed region: eager steps, phase events on the launching stream
+    lc0 = ann.launch_count()
+    ann._lib.call("ann_set_phase_timing", 1)
+    phase = np.zeros(5)
+    clocks = ClockSampler()
+    clocks.start()
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(st)
+    for _ in range(args.steps):
+        tdvp.sr_step(op, psi, mc, SHIFT, LR)
+        ph = (np.zeros(5, np.float32))
+        ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
+        phase += ph
+    ev1.record(st)
+    torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ann._lib.call("ann_set_phase_timing", 0)
+    launches_per_step = (ann.launch_count() - lc0) / args.steps
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    phase /= args.steps
+    E, _ = tdvp._energy()
+
+    # graph replay of the same step (captured once, replayed)
+    tdvp.capture_sr_step(op, psi, mc, SHIFT, LR, st)
+    st.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(st)
+    for _ in range(args.steps):
+        tdvp.launch_sr_step(st)
+    g1.record(st)
+    st.synchronize()
+    ms_graph = g0.elapsed_time(g1) / args.steps
+
+    # end to end through the public API: parameters from pinned host memory in,
+    # the step's energy out
+    host_params = torch.from_numpy(psi.params.view(np.float64).copy()).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        psi.set_params_async(host_params, st)
+        tdvp.launch_sr_step(st)
+        E_now = tdvp.E_local  # device -> host read of the step's energy (synchronising)
+    st.synchronize()
+    ms_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    # tau_int of the local energy, per-chain series 64 sweeps apart, same parameters
+    T = 24
+    mc_tau = ann.MonteCarloLoop(N_CHAINS * T, SWEEPS, THERM, N_CHAINS, True, seed=SEED + 99, persistent=True)
+    ann.ExpectationValue()(op, psi, mc_tau)
+    _, _, el = mc_tau.samples()
+    tau = tau_int_sokal(el.real.reshape(T, N_CHAINS))
+    acc = mc_tau.acceptance_rate
+
+    pk, pk_kind = peaks()
+    flops_S = 4.0 * Np * (Np + 1) * Ns  # algorithmic HERK count per step
+    achieved = flops_S / (phase[2] * 1e-3) / 1e12
+    peak = pk.get("bf16_tflops", 1900.0) if s_mode == "bf16" else None
+    value = Ns / tau / (ms * 1e-3)
+    e2e_value = Ns / tau / (ms_e2e * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 sampling / bf16 S (fp32 acc) / f64 solve" if s_mode == "bf16" else
+        "c64 sampling / fp32 S / f64 solve", "data": "synthetic (seeded random-init RBM, 2D TFIM)",
+        "config": config_dict(args.form),
+        "sr_steps_per_s": 1e3 / ms, "ms_per_step_graph": ms_graph, "tau_int": tau, "acceptance": acc,
+        "energy_per_site": E.real / N_SITES,
+        "phase_ms": {"sample_eloc_O": phase[0], "reductions": phase[1], "S": phase[2], "solve": phase[3],
+                     "update": phase[4]},
+        "roofline": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c)", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
+                     "peak_kind": pk_kind + " bf16 burst", "traffic": None,
+                     "work": "4*Np*(Np+1)*Ns real flops per step"},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": Np * 16, "d2h_bytes_per_step": 16,
+                "ms_per_step": ms_e2e},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(a, b, W, H, tau, cores=1)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        torch.distributed.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------------
+def cpu_step_seconds(a, b, W, H, n_samples=4, chains=None):
+    """Time the FP64 oracle (a restatement of the reference's host path) on a
+    bounded sample of one SR step and scale to the full step: per-sample work
+    (64 sweeps of single-flip Metropolis, local energy, O_k, S accumulation)
+    times N_s, plus a Cholesky solve timed at n = 2048 and scaled by (Np/2048)^3."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle, RbmDesc
+    o = Oracle()
+    psi = RbmDesc(N_SITES, M_HIDDEN, W, a=a, b=b, layout=1)
+    t0 = time.perf_counter()
+    r = o.mc_philox(psi, H, n_samples, SEED, 1, SWEEPS, 0, init=True)
+    t_mc = (time.perf_counter() - t0) / n_samples
+    t0 = time.perf_counter()
+    o.tdvp_samples(psi, H, r["sconf"], 1.0 / n_samples, want_S=True)
+    t_tdvp = (time.perf_counter() - t0) / n_samples
+    n = 2048
+    A = np.random.default_rng(0).standard_normal((n, n)) + 1j * np.random.default_rng(1).standard_normal((n, n))
+    A = A @ A.conj().T + n * np.eye(n)
+    t0 = time.perf_counter()
+    np.linalg.cholesky(A)
+    t_chol = (time.perf_counter() - t0) * ((N_SITES + M_HIDDEN + N_SITES * M_HIDDEN) / n) ** 3
+    return N_CHAINS * (t_mc + t_tdvp) + t_chol, t_mc, t_tdvp, t_chol
+
+
+def cpu_baseline(a, b, W, H, tau, cores=1):
+    step_s, t_mc, t_tdvp, t_chol = cpu_step_seconds(a, b, W, H)
+    return {"value": N_CHAINS / tau / step_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"4 chains x 1 sample (64 sweeps, E_loc, O_k, S rows) timed and scaled to {N_CHAINS} "
+                      f"samples; Cholesky timed at n=2048 and scaled by n^3 to Np=8384; tau_int from the GPU run",
+            "seconds_per_step": step_s, "s_per_sample_mc": t_mc, "s_per_sample_tdvp": t_tdvp,
+            "s_cholesky": t_chol}
+
+
+def _expression_module():
+    # the Hamiltonian builder alone (pure Python); the CPU legs never load the CUDA library
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_ann_expression",
+                                                  os.path.join(ROOT, "annongpu_gb300", "expression.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _cpu_worker(q):
+    rng = np.random.default_rng(SEED)
+    a, b, W = init_params(rng)
+    H = _expression_module().transverse_field_ising_2d(L, L, h=H_FIELD)
+    q.put(cpu_step_seconds(a, b, W, H, n_samples=2)[0])
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    P = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        q = ctx.Queue()
+        procs = [ctx.Process(target=_cpu_worker, args=(q,)) for _ in range(P)]
+        for p in procs:
+            p.start()
+        vals = [q.get() for _ in procs]
+        for p in procs:
+            p.join()
+        # P independent processes split the samples of one step
+        times.append(float(np.median(vals)) / P)
+    step_s = float(np.median(times))
+    tau = 1.0  # not measured on the CPU: taking 1 makes this an upper bound of the CPU effective rate
+    value = N_CHAINS / tau / step_s
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded random-init RBM, 2D TFIM)",
+           "config": config_dict(args.form), "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": P, "kind": "port",
+                            "sample": f"{P} processes x 2 chains x 1 sample timed per step and scaled to "
+                                      f"{N_CHAINS} samples; Cholesky scaled from n=2048; tau_int = 1 assumed"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "wall_s": time.perf_counter() - t_start}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="precision", choices=["precision", "plain"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

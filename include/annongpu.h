@@ -1,0 +1,258 @@
+/*
+ * annongpu.h -- C ABI of the GB300-native VMC inner loop (libannongpu.so).
+ *
+ * Drop-in boundary for the reference's pybind11 module _pyANNonGPU
+ * (pyANNonGPU/main.cpp.template:65-541): every entry point below replaces one
+ * binding of that module, cited beside it. Plain pointers and sizes only; complex
+ * numbers are interleaved (re, im) doubles; spin configurations are arrays of
+ * 64-bit words (bit i = 1 <-> sigma^z_i = +1, include/basis/Spins.h:104-118).
+ *
+ * Conventions
+ *   - Every function returns ANN_OK (0) or an error code; ann_last_error() gives
+ *     the message of the last failure on the calling thread. The reference turns
+ *     CUDA errors into std::runtime_error (include/types.h:139-147); the Python
+ *     layer turns these codes into RuntimeError.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default
+ *     stream). Functions that return host data synchronise that stream.
+ *   - Handles are not thread-safe; use one handle per thread.
+ *   - There is no CPU fallback: a call without a usable CUDA device fails.
+ */
+#ifndef ANNONGPU_H
+#define ANNONGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ANN_OK 0
+#define ANN_ERR_INVALID 1      /* bad argument or size beyond a documented limit */
+#define ANN_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define ANN_ERR_NUMERIC 3      /* non-finite value or non-positive-definite matrix */
+#define ANN_ERR_UNSUPPORTED 4  /* combination not implemented */
+
+typedef struct ann_psi ann_psi;
+typedef struct ann_op ann_op;
+typedef struct ann_ens ann_ens;
+typedef struct ann_tdvp ann_tdvp;
+
+const char* ann_last_error(void);
+int ann_version(void);
+
+/* setDevice (pyANNonGPU/main.cpp.template:538, source/ANNonGPU.cu:7-9) */
+int ann_set_device(int device);
+/* start_profiling / stop_profiling (main.cpp.template:539-540, source/ANNonGPU.cu:11-17) */
+int ann_profiler_start(void);
+int ann_profiler_stop(void);
+
+/* ---------------------------------------------------------------------------------
+ * Wavefunctions
+ * ------------------------------------------------------------------------------ */
+#define ANN_LAYOUT_RBM 0    /* params = W (N x M)          -- PsiRBM (include/quantum_state/PsiRBM.hpp:251-257) */
+#define ANN_LAYOUT_DEEP 1   /* params = [a | b | W (C x M)] -- PsiDeep (source/quantum_state/PsiDeep.cu:245-270) */
+#define ANN_ACT_POLY 0      /* reference polynomial log cosh (include/quantum_state/psi_functions.hpp:40-48) */
+#define ANN_ACT_LOGCOSH 1   /* exact log cosh / tanh */
+#define ANN_PREC_FP32 0     /* complex64 arithmetic in the kernels */
+#define ANN_PREC_FP64 1     /* complex128 arithmetic in the kernels */
+
+typedef struct {
+    unsigned N;                   /* input sites (<= 128) */
+    unsigned M;                   /* hidden units (<= 256) */
+    unsigned C;                   /* connections per hidden unit (<= N) */
+    const unsigned* connections;  /* C x M, entry (c, j) = input site; NULL = identity (C == N) */
+    const double* params;         /* interleaved complex, laid out as `layout` says */
+    const double* final_weights;  /* M complex */
+    double log_prefactor[2];
+    int layout;                   /* ANN_LAYOUT_* */
+    int a_in_log_psi;             /* 1: log psi includes a.s (standard RBM); 0: reference PsiDeep */
+    int activation;               /* ANN_ACT_* */
+    int precision;                /* ANN_PREC_* */
+} ann_rbm_desc;
+
+/* PsiDeep(...) ctor (main.cpp.template:71-81) and PsiRBM(...) ctor (:120-126) */
+int ann_psi_create_rbm(const ann_rbm_desc* desc, ann_psi** out);
+
+typedef struct {
+    unsigned extent[3];               /* lattice extent (N = product <= 128) */
+    unsigned num_layers;              /* <= 4 */
+    const unsigned* num_channels;     /* num_layers */
+    const unsigned* connectivity;     /* num_layers x 3 (forward-anchored periodic windows) */
+    const unsigned* symmetry_classes; /* N */
+    const double* params;             /* interleaved complex */
+    unsigned num_params;
+    double final_factor;
+    double log_prefactor[2];
+    int activation;                   /* ANN_ACT_POLY: reference layer semantics; ANN_ACT_LOGCOSH: log cosh on every layer */
+    int precision;
+} ann_cnn_desc;
+
+/* PsiCNN(...) ctor (main.cpp.template:160-170) */
+int ann_psi_create_cnn(const ann_cnn_desc* desc, ann_psi** out);
+/* copy() (main.cpp.template:82, 127, 171) */
+int ann_psi_copy(const ann_psi* psi, ann_psi** out);
+int ann_psi_destroy(ann_psi* psi);
+/* num_params (main.cpp.template:93, 138, 191) */
+int ann_psi_num_params(const ann_psi* psi, unsigned* out);
+/* params getter / setter (main.cpp.template:94-101, 139-145, 192-198); 2*num_params doubles */
+int ann_psi_get_params(const ann_psi* psi, double* out);
+int ann_psi_set_params(ann_psi* psi, const double* params);
+/* asynchronous variant: copies from (pinned) host memory on `stream` and re-derives
+   the kernel-precision weights there */
+int ann_psi_set_params_async(ann_psi* psi, const double* params, void* stream);
+/* log_prefactor getter / setter (main.cpp.template:85-89) */
+int ann_psi_get_log_prefactor(const ann_psi* psi, double* out2);
+int ann_psi_set_log_prefactor(ann_psi* psi, double re, double im);
+/* device pointer of the FP64 master parameters (num_params complex128) */
+int ann_psi_params_device(ann_psi* psi, void** out);
+/* re-derive the kernel-precision weights from the device master parameters */
+int ann_psi_sync_device_params(ann_psi* psi, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Operators: Operator(PauliExpression, gpu) (main.cpp.template:321-333,
+ * source/operator/Operator.cpp:18-39). String n uses words [n*num_words,
+ * (n+1)*num_words) of a and b; per site (a,b) = (0,0) I, (1,0) X, (0,1) Y, (1,1) Z.
+ * ------------------------------------------------------------------------------ */
+int ann_op_create_pauli(unsigned n_strings, unsigned num_words, const uint64_t* a, const uint64_t* b,
+                        const double* coeff, ann_op** out);
+int ann_op_destroy(ann_op* op);
+/* num_strings (main.cpp.template:332) */
+int ann_op_num_strings(const ann_op* op, unsigned* out);
+
+/* ---------------------------------------------------------------------------------
+ * Ensembles
+ * ------------------------------------------------------------------------------ */
+/* ExactSummationSpins(num_sites, gpu) (main.cpp.template:395-399, include/ensembles/ExactSummation.hpp:33-72) */
+int ann_ens_create_exact(unsigned num_sites, ann_ens** out);
+
+#define ANN_MOVE_FLIP 0            /* single spin flip (include/ensembles/policies/Update_Policy.hpp:20-33) */
+#define ANN_MOVE_EXCHANGE_BONDS 1  /* swap the spins of a random bond (Sz conserving) */
+#define ANN_MOVE_EXCHANGE_PAIRS 2  /* swap the spins of a random site pair (Sz conserving) */
+
+typedef struct {
+    unsigned num_samples;               /* total samples; per chain num_samples / num_markov_chains */
+    unsigned num_sweeps;                /* sweeps (N proposals each) between samples */
+    unsigned num_thermalization_sweeps;
+    unsigned num_markov_chains;
+    int move;                           /* ANN_MOVE_* */
+    const uint32_t* bonds;              /* n_bonds x 2 site pairs for ANN_MOVE_EXCHANGE_BONDS */
+    unsigned n_bonds;
+    int n_up;                           /* < 0: free; >= 0: initial configurations with exactly n_up up spins */
+    uint64_t seed;                      /* Philox key */
+    int persistent;                     /* 0: every call re-draws and re-thermalises the chains
+                                           (MonteCarlo.hpp:79, 89-93); 1: chains continue across calls */
+} ann_mc_desc;
+
+/* MonteCarloSpins(num_samples, num_sweeps, num_thermalization_sweeps, num_markov_chains, gpu)
+   (main.cpp.template:358-366, include/ensembles/MonteCarlo.hpp:249-259); also MonteCarloLoop */
+int ann_ens_create_mc(const ann_mc_desc* desc, ann_ens** out);
+/* copy constructor MonteCarloSpins(MonteCarloSpins&) (main.cpp.template:360) */
+int ann_ens_copy(const ann_ens* ens, ann_ens** out);
+int ann_ens_destroy(ann_ens* ens);
+/* num_steps (main.cpp.template:363, 398) */
+int ann_ens_num_steps(const ann_ens* ens, unsigned* out);
+/* acceptance_rate of the last sampling call (main.cpp.template:364-366) */
+int ann_ens_acceptance_rate(const ann_ens* ens, double* out);
+/* chain state (configurations num_markov_chains x num_words, Philox counters) */
+int ann_ens_get_chains(const ann_ens* ens, uint64_t* conf, uint64_t* counter);
+int ann_ens_set_chains(ann_ens* ens, const uint64_t* conf, const uint64_t* counter);
+/* Proposal replay (parity checking): per chain, the initial configuration and
+   `len` (site, uniform) pairs consumed in order instead of Philox draws; u = 0
+   marks a proposal the reference accepted without drawing. NULL sites disables. */
+int ann_ens_set_tape(ann_ens* ens, const uint64_t* init_conf, const uint32_t* sites, const double* u,
+                     unsigned len);
+/* configurations of the last sampling call, num_steps x num_words */
+int ann_ens_get_samples(const ann_ens* ens, uint64_t* conf, double* log_psi, double* local_energy);
+
+/* ---------------------------------------------------------------------------------
+ * Network functions (source/network_functions/*.cu.template)
+ * ------------------------------------------------------------------------------ */
+/* ExpectationValue.__call__(op, psi, ens) (ExpectationValue.cu.template:19-50) */
+int ann_expectation(ann_op* op, ann_psi* psi, ann_ens* ens, void* stream, double* out2);
+/* ExpectationValue.__call__(list[op], psi, ens) (ExpectationValue.cu.template:83-128) */
+int ann_expectation_list(ann_op** ops, unsigned n_ops, ann_psi* psi, ann_ens* ens, void* stream, double* out);
+/* ExpectationValue.fluctuation -> (sigma, <A>) (ExpectationValue.cu.template:175-216); out3 = sigma, re, im */
+int ann_fluctuation(ann_op* op, ann_psi* psi, ann_ens* ens, void* stream, double* out3);
+/* ExpectationValue.gradient -> (G, <A>) (ExpectationValue.cu.template:219-275) */
+int ann_gradient(ann_op* op, ann_psi* psi, ann_ens* ens, void* stream, double* grad, double* value2);
+/* ExpectationValue.exp_sigma_z (ExpectationValue.cu.template:52-81) */
+int ann_exp_sigma_z(ann_op* op, ann_psi* psi, ann_ens* ens, void* stream, double* out2);
+/* log_psi_s(psi, Spins) (PsiVector.cu.template:101-133) */
+int ann_log_psi_s(ann_psi* psi, const uint64_t* conf, double* out2);
+/* batched log psi of explicit configurations (n x num_words) */
+int ann_log_psi_batch(ann_psi* psi, const uint64_t* confs, unsigned n, void* stream, double* out);
+/* psi_O_k(psi, Spins) (PsiOkVector.cu.template:40-74) */
+int ann_psi_O_k(ann_psi* psi, const uint64_t* conf, double* out);
+/* psi_O_k_vector(psi, esum): sum_s O_k(s), unweighted (PsiOkVector.cu.template:8-38) */
+int ann_psi_O_k_vector(ann_psi* psi, ann_ens* ens, void* stream, double* out);
+/* log_psi(psi, ens): sum_s w(s) log psi(s) (PsiVector.cu.template:73-99) */
+int ann_log_psi(ann_psi* psi, ann_ens* ens, void* stream, double* out2);
+/* psi_vector / log_psi_vector (PsiVector.cu.template:14-71); 2 * num_steps doubles */
+int ann_psi_vector(ann_psi* psi, ann_ens* ens, void* stream, double* out);
+int ann_log_psi_vector(ann_psi* psi, ann_ens* ens, void* stream, double* out);
+/* norm(esum) = sqrt(sum_s |psi(s)|^2) (PsiNorm.cu.template:13-42) */
+int ann_psi_norm(ann_psi* psi, ann_ens* ens, void* stream, double* out);
+/* apply_operator(psi, op, ens): psi(s) E_loc(s) (ApplyOperator.cu.template:9-44) */
+int ann_apply_operator(ann_psi* psi, ann_op* op, ann_ens* ens, void* stream, double* out);
+/* activation_function(z, layer) (main.cpp.template:534-536) */
+int ann_activation_function(double re, double im, unsigned layer, int activation, double* out2);
+
+/* ---------------------------------------------------------------------------------
+ * TDVP / SR (include/network_functions/TDVP.hpp, source/network_functions/TDVP.cu.template)
+ * ------------------------------------------------------------------------------ */
+#define ANN_S_FP32 0         /* centred O, FP32 SIMT complex HERK (the plain form) */
+#define ANN_S_BF16 1         /* centred O, BF16 tcgen05 real-embedded HERK, FP32 accumulation */
+#define ANN_S_BF16_SPLIT 2   /* as ANN_S_BF16 with hi+lo split products (three BF16 products) */
+
+/* TDVP(num_params, gpu) (main.cpp.template:465-466) */
+int ann_tdvp_create(unsigned num_params, ann_tdvp** out);
+int ann_tdvp_destroy(ann_tdvp* tdvp);
+int ann_tdvp_set_s_mode(ann_tdvp* tdvp, int mode);
+/* eval(op, psi, ens): E, E2, <O>, F and S on the device (TDVP.cu.template:181-302) */
+int ann_tdvp_eval(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, void* stream);
+/* eval_F: E, E2, <O>, F only (TDVP.cu.template:305-334) */
+int ann_tdvp_eval_F(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, void* stream);
+/* results (S_matrix, F_vector, O_k_vector, var_H, total_weight: main.cpp.template:467-472) */
+int ann_tdvp_get_S(ann_tdvp* tdvp, double* out);       /* num_params^2 complex, row-major */
+int ann_tdvp_get_F(ann_tdvp* tdvp, double* out);
+int ann_tdvp_get_O(ann_tdvp* tdvp, double* out);
+int ann_tdvp_get_energy(ann_tdvp* tdvp, double* E2re_im, double* E2);
+int ann_tdvp_get_total_weight(ann_tdvp* tdvp, double* out);
+/* O_k_samples (main.cpp.template:472): num_steps x num_params complex */
+int ann_tdvp_get_O_samples(ann_tdvp* tdvp, double* out);
+/* S_dot_vector(vec, ens) (TDVP.cu.template:336-443), from the stored O samples */
+int ann_tdvp_S_dot_vector(ann_tdvp* tdvp, const double* vec, void* stream, double* out);
+/* SR solve: (S + shift I) delta = F by FP64 Cholesky on the GPU with one step of
+   iterative refinement; writes delta (num_params complex) if out != NULL and the
+   relative residuals before/after refinement to info2 if info2 != NULL. */
+int ann_tdvp_solve(ann_tdvp* tdvp, double diag_shift, void* stream, double* delta_out, double* info2);
+/* SR update: params <- params - lr * delta (device resident; re-derives kernel weights) */
+int ann_sr_update(ann_tdvp* tdvp, ann_psi* psi, double lr, void* stream);
+/* one full SR step = eval + solve + update, on the device */
+int ann_sr_step(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, double diag_shift, double lr,
+                void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * CUDA graph of a whole SR step (capture once, replay many)
+ * ------------------------------------------------------------------------------ */
+int ann_sr_graph_capture(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, double diag_shift, double lr,
+                         void* stream);
+int ann_sr_graph_launch(ann_tdvp* tdvp, void* stream);
+
+/* CUDA-event timing of the SR-step phases on the calling stream (not inside graph
+   capture): ms[0] sampling + local energy + O rows, ms[1] reductions (E, <O>, F),
+   ms[2] S matrix, ms[3] SR solve, ms[4] update; -1 where a phase did not run */
+int ann_set_phase_timing(int enable);
+int ann_get_phase_times(float* ms5);
+
+/* kernels this library launched so far (monotonic counter of its own launches) */
+unsigned long long ann_kernel_launch_count(void);
+/* device status word of the last computation (ANN bit flags; 0 = clean) */
+int ann_status(unsigned* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ANNONGPU_H */

@@ -231,21 +231,23 @@ inline Conf mask_conf(Conf s, unsigned N) {
 
 // Sampler random-number contract (shared with the CUDA sampler):
 //   key = (seed & 0xffffffff, seed >> 32)
-//   initial configuration: counter (0, 0, chain, 1) -> words (r0 | r1 << 32, r2 | r3 << 32)
-//   fixed-magnetisation init: draw k uses counter (k, 0, chain, 2): set the
+//   initial configuration at chain counter t: counter (t_lo, t_hi, chain, 1) ->
+//       words (r0 | r1 << 32, r2 | r3 << 32), masked to N sites
+//   fixed-magnetisation init: draw k uses counter (t + k, chain, 2): set the
 //       mulhi(r0, N - k)-th down spin up
 //   proposal t: counter (t_lo, t_hi, chain, 0): r0 -> first site, r1 -> partner,
-//       (r2, r3) -> uniform u in [0, 1) with 53 bits; accept iff u < exp(2 Re dlogpsi)
-Conf draw_initial(uint32_t k0, uint32_t k1, unsigned chain, unsigned N, int n_up) {
+//       (r2, r3) -> uniform u in [0, 1) with 53 bits; accept iff u <= exp(2 Re dlogpsi)
+Conf draw_initial(uint32_t k0, uint32_t k1, unsigned chain, unsigned N, int n_up, uint64_t t) {
     if(n_up < 0) {
-        uint32_t ctr[4] = {0u, 0u, chain, 1u}, r[4];
+        uint32_t ctr[4] = {(uint32_t)t, (uint32_t)(t >> 32), chain, 1u}, r[4];
         philox(k0, k1, ctr, r);
         Conf s{(uint64_t)r[0] | ((uint64_t)r[1] << 32), (uint64_t)r[2] | ((uint64_t)r[3] << 32)};
         return mask_conf(s, N);
     }
     Conf s{0, 0};
     for(int k = 0; k < n_up; k++) {
-        uint32_t ctr[4] = {(uint32_t)k, 0u, chain, 2u}, r[4];
+        const uint64_t tk = t + (uint64_t)k;
+        uint32_t ctr[4] = {(uint32_t)tk, (uint32_t)(tk >> 32), chain, 2u}, r[4];
         philox(k0, k1, ctr, r);
         unsigned target = mulhi(r[0], N - (unsigned)k);
         for(unsigned i = 0; i < N; i++) {
@@ -510,8 +512,8 @@ void or_rbm_mc_philox(const or_rbm* p, const or_op* op, unsigned n_chains, uint6
     uint64_t acc_total = 0, rej_total = 0;
     double tie = 1e300;
     for(unsigned c = 0; c < n_chains; c++) {
-        Conf s = init ? draw_initial(k0, k1, c, N, n_up) : load_conf(conf + (size_t)c * nw, nw);
-        uint64_t t = init ? 0u : counter[c];
+        uint64_t t = counter[c];
+        Conf s = init ? draw_initial(k0, k1, c, N, n_up, t) : load_conf(conf + (size_t)c * nw, nw);
         std::vector<cd> th;
         psi.angles(s, th);
         auto propose = [&]() {
@@ -553,7 +555,7 @@ void or_rbm_mc_philox(const or_rbm* p, const or_op* op, unsigned n_chains, uint6
             const double ratio = std::exp(2.0 * d.real());
             const double u = u53(r[2], r[3]);
             tie = std::min(tie, std::fabs(ratio - u));
-            if(u < ratio) { s = nx; th = th2; acc_total++; }
+            if(u <= ratio) { s = nx; th = th2; acc_total++; }
             else rej_total++;
         };
         if(init)
@@ -617,6 +619,23 @@ void or_cnn_exact(const or_cnn* p, const or_op* op, double* E, double* norm,
     if(E) put(E, acc.E);
     if(norm) norm[0] = std::sqrt(nrm);
     acc.finish(nullptr, nullptr, tE, tE2, tO, tF, tS);
+}
+
+void or_rbm_tdvp_samples(const or_rbm* p, const or_op* op, const uint64_t* confs, unsigned n, double weight,
+                         double* E, double* tE2, double* tO, double* tF, double* tS) {
+    Rbm psi(p);
+    const unsigned np = psi.num_params(), nw = nwords(p->N);
+    Accum acc(np);
+    std::vector<cd> th, Ok;
+    for(unsigned r = 0; r < n; r++) {
+        const Conf s = load_conf(confs + (size_t)r * nw, nw);
+        psi.angles(s, th);
+        const cd lp = psi.log_psi(s, th);
+        const cd eloc = local_energy_incremental(psi, op, s, lp, th);
+        psi.O_k(s, Ok);
+        acc.add(weight, eloc, Ok, tS != nullptr);
+    }
+    acc.finish(nullptr, nullptr, E, tE2, tO, tF, tS);
 }
 
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

@@ -63,7 +63,7 @@ struct or_cnn {
     unsigned num_params;
     double final_factor;
     double lp_re, lp_im;
-    int activation;                // 0: reference polynomial ; 1: exact (log cosh, then tanh-free identity? see oracle.cpp)
+    int activation;                // 0: reference layer polynomials ; 1: log cosh on every layer
 };
 
 unsigned or_rbm_num_params(const or_rbm* p);
@@ -100,6 +100,11 @@ void or_rbm_mc_philox(const or_rbm* p, const or_op* op, unsigned n_chains, uint6
                       uint64_t* conf, uint64_t* counter,
                       uint64_t* sconf, double* slp, double* seloc,
                       uint64_t* n_accept, uint64_t* n_reject, double* min_tie);
+
+// The reference's TDVP accumulation (TDVP.cu.template:77-126, 216-301) over given
+// configurations with a uniform weight: E, E2, <O>, F and (if tS != NULL) S.
+void or_rbm_tdvp_samples(const or_rbm* p, const or_op* op, const uint64_t* confs, unsigned n, double weight,
+                         double* E, double* tE2, double* tO, double* tF, double* tS);
 
 // PsiCNN (reference activation semantics: layer 0 poly log cosh, deeper layers odd poly)
 void or_cnn_log_psi(const or_cnn* p, const uint64_t* conf, double* out);

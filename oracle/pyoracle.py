@@ -192,6 +192,18 @@ class Oracle:
         r["num_props"] = n
         return r
 
+    def tdvp_samples(self, psi: RbmDesc, expr, confs, weight, want_S=True):
+        """The reference's TDVP accumulation over explicit configurations (uniform weight)."""
+        np_ = psi.num_params
+        op = OpArrays(expr, psi.N)
+        c = np.ascontiguousarray(np.asarray(confs, np.uint64).reshape(-1))
+        n = c.size // max(1, nwords(psi.N))
+        r = dict(E=np.zeros(1, np.complex128), E2=np.zeros(1), O=np.zeros(np_, np.complex128),
+                 F=np.zeros(np_, np.complex128), S=np.zeros((np_, np_), np.complex128) if want_S else None)
+        self.lib.or_rbm_tdvp_samples(ct.byref(psi.struct), ct.byref(op.struct), _ptr(c), ct.c_uint(n),
+                                     ct.c_double(weight), *[_ptr(r[k]) for k in ("E", "E2", "O", "F", "S")])
+        return r
+
     def philox(self, key, ctr):
         out = np.zeros(4, np.uint32)
         c = np.asarray(ctr, np.uint32)
