@@ -332,6 +332,79 @@ class PsiDeep(_Psi):
                        obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu)
 
 
+def _pad3(v):
+    v = [int(x) for x in np.asarray(v).reshape(-1)]
+    return [1] * (3 - len(v)) + v
+
+
+class PsiCNN(_Psi):
+    """Periodic convolutional network (include/quantum_state/PsiCNN.hpp:34-383), one or two layers.
+
+    ``PsiCNN(extent, num_channels_list, connectivity_list, symmetry_classes, params,
+    final_factor, log_prefactor, gpu)`` as the reference (main.cpp.template:161-170):
+    extent and each connectivity are 3-vectors (shorter ones are padded with leading 1s),
+    params are ordered per layer, per channel link (c_in * C_out + c_out), per symmetry
+    class, per window offset (source/quantum_state/PsiCNN.cpp:38-45).
+    ``activation="logcosh"`` uses log cosh on every layer instead of the reference's
+    layer polynomials.
+    """
+
+    dim = 3
+
+    def __init__(self, extent, num_channels_list, connectivity_list, symmetry_classes, params, final_factor=1.0,
+                 log_prefactor=0.0, gpu=True, *, activation="poly", precision="fp32"):
+        self.extent = _pad3(extent)
+        self.num_channels_list = np.asarray(num_channels_list, np.uint32).reshape(-1)
+        L_ = len(self.num_channels_list)
+        conn = np.asarray(connectivity_list).reshape(L_, -1)
+        self.connectivity_list = np.array([_pad3(c) for c in conn], np.uint32)
+        self.N = int(np.prod(self.extent))
+        self.num_sites = self.N
+        sym = np.asarray(symmetry_classes).reshape(-1).astype(np.uint32)
+        self.symmetry_classes = sym
+        self.num_symmetry_classes = len(set(sym.tolist()))
+        self.final_factor = float(final_factor)
+        self.activation = activation
+        self.precision = precision
+        p = c128(params).reshape(-1)
+        lp = complex(log_prefactor)
+        self._keep = (np.ascontiguousarray(self.num_channels_list), np.ascontiguousarray(self.connectivity_list),
+                      np.ascontiguousarray(sym), p)
+        d = L.CnnDesc((ct.c_uint * 3)(*self.extent), L_, ptr(self._keep[0]), ptr(self._keep[1]), ptr(self._keep[2]),
+                      ptr(p), p.size, self.final_factor, (ct.c_double * 2)(lp.real, lp.imag), _ACT[activation],
+                      _PREC[precision])
+        _Handle.__init__(self)
+        call("ann_psi_create_cnn", ct.byref(d), ct.byref(self._h))
+        self._init_common(gpu)
+
+    def init_gradient(self, num_steps):
+        """No-op: O_k rows are written directly (the reference records angles per sample, PsiCNN.cpp:74-78)."""
+
+    # PsiCNN.py:60-83
+    def channel_link(self, layer, i, j):
+        offset = 0
+        vol = [int(np.prod(c)) for c in self.connectivity_list]
+        for l in range(layer):
+            prev = self.num_channels_list[l - 1] if l > 0 else 1
+            offset += int(self.num_channels_list[l] * prev) * self.num_symmetry_classes * vol[l]
+        offset += (i * int(self.num_channels_list[layer]) + j) * self.num_symmetry_classes * vol[layer]
+        return self.params[offset:offset + self.num_symmetry_classes * vol[layer]]
+
+    # PsiCNN.py:7-44
+    def to_json(self):
+        obj = dict(type="PsiCNN", extent=np.array(self.extent), num_channels_list=self.num_channels_list,
+                   connectivity_list=self.connectivity_list, symmetry_classes=self.symmetry_classes,
+                   params=self.params, final_factor=self.final_factor, log_prefactor_re=self.log_prefactor.real,
+                   log_prefactor_im=self.log_prefactor.imag)
+        return json.loads(json.dumps(obj, cls=NumpyEncoder))
+
+    @staticmethod
+    def from_json(json_obj, gpu=True):
+        obj = json.loads(json.dumps(json_obj, cls=NumpyEncoder), cls=NumpyDecoder)
+        return PsiCNN(obj["extent"], obj["num_channels_list"], obj["connectivity_list"], obj["symmetry_classes"],
+                      obj["params"], obj["final_factor"], obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu)
+
+
 # ----------------------------------------------------------------------------------
 class Operator(_Handle):
     """Sum of Pauli strings (include/operator/Operator.hpp:26-214)."""

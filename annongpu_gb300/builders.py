@@ -10,7 +10,7 @@ import math
 
 import numpy as np
 
-from .api import PsiDeep, PsiRBM
+from .api import PsiCNN, PsiDeep, PsiRBM
 
 
 def _noise(rng, shape, scale, complex_=True):
@@ -62,3 +62,30 @@ def new_deep_neural_network(num_sites, N, M, C, initial_value=(0.01 + 1j * math.
     conn = np.array([[(j * delta + i) % N for j in range(m)] for i in range(c)], np.uint32)
     fw = final_weights * np.ones(m) if np.isscalar(final_weights) else np.asarray(final_weights)
     return PsiDeep(num_sites, a, [b], [conn], [w], fw, 0.0, gpu, **kwargs)
+
+
+def new_convolutional_network(L, layers, initial_value=(0.01 + 1j * math.pi / 4), noise=1e-4, final_factor=10,
+                              symmetry_classes=None, real=False, gpu=True, rng=None, **kwargs):
+    """``layers`` = [(channels, connectivity), ...]; kernels start as noise, the first
+    layer with ``initial_value`` at the window centre, deeper layers with a Glorot-scaled
+    real uniform part (pyANNonGPU/new_convolutional_network.py:30-82)."""
+    rng = np.random.default_rng() if rng is None else rng
+    L = list(L) if isinstance(L, (list, tuple)) else [L]
+    channels = [c for c, _ in layers]
+    conns = [list(k) if isinstance(k, (list, tuple)) else [k] for _, k in layers]
+    n_sites = int(np.prod(L))
+    symmetry_classes = np.zeros(n_sites, np.uint32) if symmetry_classes is None else np.asarray(symmetry_classes)
+    ncls = len(set(np.asarray(symmetry_classes).tolist()))
+    params = []
+    for layer, (ch, conn) in enumerate(zip(channels, conns)):
+        vol = int(np.prod(conn))
+        prev = channels[layer - 1] if layer else 1
+        for _ in range(ch * prev):
+            for _ in range(ncls):
+                w = _noise(rng, vol, noise, not real)
+                if layer == 0:
+                    w[vol // 2] = initial_value.real if real else initial_value
+                else:
+                    w = w + math.sqrt(6 / (vol * prev + vol * ch)) * (2 * rng.random(vol) - 1)
+                params.extend(w)
+    return PsiCNN(L, channels, conns, symmetry_classes, np.array(params), final_factor, 0.0, gpu, **kwargs)

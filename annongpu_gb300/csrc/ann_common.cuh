@@ -173,6 +173,45 @@ struct OpDev {
     const unsigned* grp_str_begin;   // [n_groups + 1] into str_*
     const uint64_t* str_mask;        // [n_str][nw]: sites with Z or Y
     const double* str_coeff;         // [n_str][2]: coeff * (-i)^{n_y}
+    const float* diag_coeff_f;       // FP32 copies for complex64 kernels
+    const float* str_coeff_f;
+};
+
+template<typename T> __device__ __forceinline__ const T* diag_coeff(const OpDev& op);
+template<> __device__ __forceinline__ const float* diag_coeff<float>(const OpDev& op) { return op.diag_coeff_f; }
+template<> __device__ __forceinline__ const double* diag_coeff<double>(const OpDev& op) { return op.diag_coeff; }
+template<typename T> __device__ __forceinline__ const T* str_coeff(const OpDev& op);
+template<> __device__ __forceinline__ const float* str_coeff<float>(const OpDev& op) { return op.str_coeff_f; }
+template<> __device__ __forceinline__ const double* str_coeff<double>(const OpDev& op) { return op.str_coeff; }
+
+struct McArgs {
+    unsigned n_chains;
+    unsigned samples_per_chain;
+    unsigned num_sweeps;
+    unsigned num_therm;
+    int do_init;              // draw fresh configurations (and thermalise) first
+    int n_up;                 // < 0: unconstrained initial configurations
+    int move_kind;            // 0 single flip, 1 exchange over bonds, 2 exchange over random pairs
+    const uint32_t* bonds;    // [n_bonds][2]
+    unsigned n_bonds;
+    uint32_t k0, k1;          // Philox key
+    uint64_t* chain_conf;     // [n_chains][kMaxWords], in/out
+    uint64_t* chain_counter;  // [n_chains], in/out
+    // proposal tape (parity replay): per chain, num_props sites and uniforms
+    const uint32_t* tape_site;
+    const double* tape_u;
+    unsigned tape_len;
+    unsigned long long* acc_rej;  // [2]
+};
+
+struct SampleOut {
+    uint64_t* conf;           // [rows][kMaxWords]
+    cplx<double>* log_psi;    // [rows]
+    cplx<double>* eloc;       // [rows] (may be null)
+    double* weight;           // [rows] (exact summation only)
+    void* O;                  // [rows][ldO] cplx<T> (may be null)
+    size_t ldO;
+    unsigned* status;
 };
 
 // device status word bits (returned to the host as C-ABI status)

@@ -23,6 +23,7 @@ struct Error : std::runtime_error {
 };
 
 void cuda_check(cudaError_t e, const char* what);
+void set_last_error(const char* msg);
 #define ANN_CUDA(x) ::ann::cuda_check((x), #x)
 void count_launch(unsigned n = 1);
 void check_launch(const char* what);
@@ -76,7 +77,8 @@ struct ann_op_impl {
     std::vector<zd> coeff;
     // grouped device form
     unsigned n_diag = 0, n_groups = 0;
-    DevBuf diag_mask, diag_coeff, grp_site_begin, grp_sites, grp_str_begin, str_mask, str_coeff;
+    DevBuf diag_mask, diag_coeff, grp_site_begin, grp_sites, grp_str_begin, str_mask, str_coeff, diag_coeff_f,
+        str_coeff_f;
     OpDev view() const;
 };
 
@@ -198,3 +200,9 @@ void exp_sigma_z_sum(const ann_op_impl& op, const Rows& rows, const double* wts,
 void activation_host(double re, double im, unsigned layer, int activation, double* out2);
 
 }  // namespace ann
+
+// the opaque handle types of include/annongpu.h
+struct ann_psi : ann::ann_psi_impl {};
+struct ann_op : ann::ann_op_impl {};
+struct ann_ens : ann::ann_ens_impl {};
+struct ann_tdvp : ann::ann_tdvp_impl {};

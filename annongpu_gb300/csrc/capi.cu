@@ -10,10 +10,6 @@
 
 #include "ann_internal.hpp"
 
-struct ann_psi : ann::ann_psi_impl {};
-struct ann_op : ann::ann_op_impl {};
-struct ann_ens : ann::ann_ens_impl {};
-struct ann_tdvp : ann::ann_tdvp_impl {};
 
 namespace ann {
 
@@ -33,6 +29,7 @@ void cuda_check(cudaError_t e, const char* what) {
     if(e != cudaSuccess) throw Error(ANN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 void count_launch(unsigned n) { g_launches += n; }
+void set_last_error(const char* msg) { g_last_error = msg; }
 void check_launch(const char* what) {
     count_launch();
     cudaError_t e = cudaGetLastError();
@@ -82,6 +79,8 @@ OpDev ann_op_impl::view() const {
     v.grp_str_begin = grp_str_begin.as<unsigned>();
     v.str_mask = str_mask.as<uint64_t>();
     v.str_coeff = str_coeff.as<double>();
+    v.diag_coeff_f = diag_coeff_f.as<float>();
+    v.str_coeff_f = str_coeff_f.as<float>();
     return v;
 }
 
@@ -487,6 +486,9 @@ int ann_op_create_pauli(unsigned n, unsigned nw_in, const uint64_t* a, const uin
             upload(op->grp_str_begin, str_begin.data(), str_begin.size() * 4);
             upload(op->str_mask, smask.data(), smask.size() * 8);
             upload(op->str_coeff, scoef.data(), scoef.size() * 8);
+            std::vector<float> df(dcoef.begin(), dcoef.end()), sf(scoef.begin(), scoef.end());
+            upload(op->diag_coeff_f, df.data(), df.size() * 4);
+            upload(op->str_coeff_f, sf.data(), sf.size() * 4);
         } catch(...) {
             delete op;
             throw;

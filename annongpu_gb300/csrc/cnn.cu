@@ -1,16 +1,668 @@
-// PsiCNN on the GPU (include/quantum_state/PsiCNN.hpp:97-266).
+// PsiCNN on the GPU (include/quantum_state/PsiCNN.hpp:97-266,
+// include/quantum_state/detail/Convolve.hpp:110-173, source/quantum_state/PsiCNN.cpp:9-55).
+//
+// Periodic convolutions with forward-anchored windows on an e0 x e1 x e2 lattice,
+// per-site symmetry classes selecting the kernel, one or two layers, sum pooling:
+//   z^0_c(x) = sum_k w^0[0,c][cls(x), k] s(x + k)
+//   a^0_c(x) = f_0(z^0_c(x))
+//   z^1_d(x) = sum_c sum_k w^1[c,d][cls(x), k] a^0_c(x + k)
+//   log psi  = log_prefactor + final_factor * sum_{d,x} f_1(z^1_d(x))
+// (with one layer the sum runs over f_0(z^0)). Activations follow the reference
+// layer semantics (layer 0: polynomial log cosh, deeper: odd polynomial) or
+// log cosh on every layer.
+//
+// One warp per chain (or enumerated / explicit configuration). Layer-0 activations
+// and back-propagated deltas live in per-warp shared memory; the weights and the
+// neighbour tables (site x, window offset k) -> x + k and its inverse are shared by
+// the CTA. Proposals are evaluated by a full forward pass of the proposed
+// configuration (the reference also recomputes fully, PsiCNN.hpp:177-181).
+#include <algorithm>
+
 #include "ann_internal.hpp"
 
 namespace ann {
 
-void cnn_prepare(ann_psi_impl&, cudaStream_t) { throw Error(ANN_ERR_UNSUPPORTED, "PsiCNN kernels not built yet"); }
-void cnn_run(ann_psi_impl&, const ann_op_impl*, ann_ens_impl&, const SampleTargets&, cudaStream_t) {
-    throw Error(ANN_ERR_UNSUPPORTED, "PsiCNN kernels not built yet");
+namespace {
+
+constexpr int kCnnMaxLayers = 2;
+
+template<typename T>
+struct CnnDev {
+    unsigned N, L, ncls, Np;
+    unsigned ch[kCnnMaxLayers], prev[kCnnMaxLayers], vol[kCnnMaxLayers], woff[kCnnMaxLayers];
+    int act;
+    double ff;
+    cplx<T> lp;
+    const cplx<T>* w;        // Np (global; staged in shared memory)
+    const uint8_t* cls;      // N
+    const uint16_t* nbr;     // [L][N][vol_l] input site of window offset k at site x (layer offsets nbr_off)
+    const uint16_t* inv;     // [L][N][vol_l] site x whose window offset k lands on y
+    unsigned nbr_off[kCnnMaxLayers];
+    unsigned tab_len;        // entries of nbr (= inv)
+};
+
+struct CnnSmem {
+    unsigned w_bytes, tab_bytes, per_warp_bytes;
+};
+
+template<typename T>
+struct CnnCtx {
+    const CnnDev<T>* p;
+    const cplx<T>* w;
+    const uint8_t* cls;
+    const uint16_t* nbr;
+    const uint16_t* inv;
+    cplx<T>* bufA;   // ch[0] x N
+    cplx<T>* bufB;   // ch[1] x N (two layers)
+};
+
+template<typename T>
+__device__ __forceinline__ cplx<T> wgt(const CnnCtx<T>& c, unsigned l, unsigned ci, unsigned cj, unsigned cl, unsigned k) {
+    const CnnDev<T>& p = *c.p;
+    return c.w[p.woff[l] + ((ci * p.ch[l] + cj) * p.ncls + cl) * p.vol[l] + k];
 }
-void cnn_confs(ann_psi_impl&, const ann_op_impl*, const uint64_t*, size_t, Rows&, void*, size_t, cudaStream_t) {
-    throw Error(ANN_ERR_UNSUPPORTED, "PsiCNN kernels not built yet");
+
+template<typename T>
+__device__ __forceinline__ T spin_v(const Conf<2>& s, unsigned i) {
+    return spin_bit(s, i) ? T(1) : T(-1);
+}
+
+// layer-0 pre-activation z^0_c(x)
+template<typename T>
+__device__ __forceinline__ cplx<T> z0(const CnnCtx<T>& c, const Conf<2>& s, unsigned ch, unsigned x) {
+    const CnnDev<T>& p = *c.p;
+    const uint16_t* nb = c.nbr + p.nbr_off[0] + x * p.vol[0];
+    const cplx<T>* wr = c.w + p.woff[0] + (ch * p.ncls + c.cls[x]) * p.vol[0];
+    cplx<T> z = mk<T>(T(0), T(0));
+    for(unsigned k = 0; k < p.vol[0]; k++) {
+        const T sv = spin_v<T>(s, nb[k]);
+        z.re += sv * wr[k].re;
+        z.im += sv * wr[k].im;
+    }
+    return z;
+}
+
+// layer-1 pre-activation z^1_d(x) from layer-0 activations in bufA
+template<typename T>
+__device__ __forceinline__ cplx<T> z1(const CnnCtx<T>& c, unsigned d, unsigned x) {
+    const CnnDev<T>& p = *c.p;
+    const uint16_t* nb = c.nbr + p.nbr_off[1] + x * p.vol[1];
+    cplx<T> z = mk<T>(T(0), T(0));
+    for(unsigned ci = 0; ci < p.ch[0]; ci++) {
+        const cplx<T>* wr = c.w + p.woff[1] + ((ci * p.ch[1] + d) * p.ncls + c.cls[x]) * p.vol[1];
+        const cplx<T>* a = c.bufA + ci * p.N;
+        for(unsigned k = 0; k < p.vol[1]; k++) z += wr[k] * a[nb[k]];
+    }
+    return z;
+}
+
+// full forward pass, warp-cooperative; returns log psi in every lane
+template<typename T>
+__device__ cplx<T> cnn_log_psi(const CnnCtx<T>& c, const Conf<2>& s, int lane) {
+    const CnnDev<T>& p = *c.p;
+    cplx<T> acc = mk<T>(T(0), T(0));
+    if(p.L == 1) {
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+            const unsigned ch = e / p.N, x = e % p.N;
+            acc += act_f(z0(c, s, ch, x), p.act, 0);
+        }
+    } else {
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+            const unsigned ch = e / p.N, x = e % p.N;
+            c.bufA[e] = act_f(z0(c, s, ch, x), p.act, 0);
+        }
+        __syncwarp();
+        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
+            const unsigned d = e / p.N, x = e % p.N;
+            acc += act_f(z1(c, d, x), p.act, 1);
+        }
+        __syncwarp();
+    }
+    acc = warp_sum(acc);
+    return mk<T>((T)(p.ff * (double)acc.re) + p.lp.re, (T)(p.ff * (double)acc.im) + p.lp.im);
+}
+
+// O_k row (back-propagation, PsiCNN.hpp:183-266); forward state is recomputed
+template<typename T>
+__device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T>* O) {
+    const CnnDev<T>& p = *c.p;
+    const T ff = (T)p.ff;
+    if(p.L == 1) {
+        // dlogpsi/dz0 = ff f0'(z0); O[w0[0,c][cls,k]] = sum_{x in cls} ff f0'(z0_c(x)) s(x+k)
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+            const unsigned ch = e / p.N, x = e % p.N;
+            c.bufA[e] = ff * act_df(z0(c, s, ch, x), p.act, 0);
+        }
+        __syncwarp();
+    } else {
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+            const unsigned ch = e / p.N, x = e % p.N;
+            c.bufA[e] = act_f(z0(c, s, ch, x), p.act, 0);
+        }
+        __syncwarp();
+        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
+            const unsigned d = e / p.N, x = e % p.N;
+            c.bufB[e] = ff * act_df(z1(c, d, x), p.act, 1);
+        }
+        __syncwarp();
+        // layer-1 parameters: O[(ci, d), cls, k] = sum_{x: cls(x)=cls} delta1_d(x) a0_ci(x + k)
+        const unsigned n1 = p.ch[0] * p.ch[1] * p.ncls * p.vol[1];
+        for(unsigned q = lane; q < n1; q += 32) {
+            const unsigned k = q % p.vol[1];
+            const unsigned cl = (q / p.vol[1]) % p.ncls;
+            const unsigned link = q / (p.vol[1] * p.ncls);
+            const unsigned ci = link / p.ch[1], d = link % p.ch[1];
+            cplx<T> o = mk<T>(T(0), T(0));
+            const uint16_t* nb = c.nbr + p.nbr_off[1];
+            for(unsigned x = 0; x < p.N; x++) {
+                if(c.cls[x] != cl) continue;
+                o += c.bufB[d * p.N + x] * c.bufA[ci * p.N + nb[x * p.vol[1] + k]];
+            }
+            O[p.woff[1] + q] = o;
+        }
+        __syncwarp();
+        // delta0_ci(y) = f0'(z0_ci(y)) sum_d sum_k w1[ci,d][cls(x), k] delta1_d(x), x = inv(y, k)
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+            const unsigned ci = e / p.N, y = e % p.N;
+            cplx<T> g = mk<T>(T(0), T(0));
+            const uint16_t* iv = c.inv + p.nbr_off[1] + y * p.vol[1];
+            for(unsigned d = 0; d < p.ch[1]; d++)
+                for(unsigned k = 0; k < p.vol[1]; k++) {
+                    const unsigned x = iv[k];
+                    g += wgt(c, 1, ci, d, c.cls[x], k) * c.bufB[d * p.N + x];
+                }
+            // bufA[e] (the activation a0) is read by no other lane from here on
+            c.bufA[e] = g * act_df(z0(c, s, ci, y), p.act, 0);
+        }
+        __syncwarp();
+    }
+    // layer-0 parameters: O[(0, c), cls, k] = sum_{x: cls(x)=cls} delta0_c(x) s(x + k)
+    const unsigned n0 = p.ch[0] * p.ncls * p.vol[0];
+    for(unsigned q = lane; q < n0; q += 32) {
+        const unsigned k = q % p.vol[0];
+        const unsigned cl = (q / p.vol[0]) % p.ncls;
+        const unsigned ch = q / (p.vol[0] * p.ncls);
+        cplx<T> o = mk<T>(T(0), T(0));
+        const uint16_t* nb = c.nbr + p.nbr_off[0];
+        for(unsigned x = 0; x < p.N; x++) {
+            if(c.cls[x] != cl) continue;
+            o += spin_v<T>(s, nb[x * p.vol[0] + k]) * c.bufA[ch * p.N + x];
+        }
+        O[p.woff[0] + q] = o;
+    }
+    __syncwarp();
+}
+
+// local energy with one full forward pass per off-diagonal group (Operator.hpp:36-121)
+template<typename T>
+__device__ cplx<double> cnn_local_energy(const CnnCtx<T>& c, const OpDev& op, const Conf<2>& s, cplx<T> lpsi,
+                                         int lane) {
+    T dre = T(0), dim = T(0);
+    for(unsigned n = lane; n < op.n_diag; n += 32) {
+        int neg = 0;
+        for(int w = 0; w < 2; w++) neg += __popcll((~s.w[w]) & op.diag_mask[n * op.nw + w]);
+        const T c_re = diag_coeff<T>(op)[2 * n], c_im = diag_coeff<T>(op)[2 * n + 1];
+        dre += (neg & 1) ? -c_re : c_re;
+        dim += (neg & 1) ? -c_im : c_im;
+    }
+    cplx<T> e = mk<T>(warp_sum(dre), warp_sum(dim));
+    for(unsigned g = 0; g < op.n_groups; g++) {
+        cplx<T> cg = mk<T>(T(0), T(0));
+        for(unsigned k = op.grp_str_begin[g]; k < op.grp_str_begin[g + 1]; k++) {
+            int neg = 0;
+            for(int w = 0; w < 2; w++) neg += __popcll((~s.w[w]) & op.str_mask[k * op.nw + w]);
+            const T c_re = str_coeff<T>(op)[2 * k], c_im = str_coeff<T>(op)[2 * k + 1];
+            cg.re += (neg & 1) ? -c_re : c_re;
+            cg.im += (neg & 1) ? -c_im : c_im;
+        }
+        if(cg.re == T(0) && cg.im == T(0)) continue;
+        Conf<2> s2 = s;
+        for(unsigned q = op.grp_site_begin[g]; q < op.grp_site_begin[g + 1]; q++) flip(s2, op.grp_sites[q]);
+        const cplx<T> l2 = cnn_log_psi(c, s2, lane);
+        e += cg * cexp(l2 - lpsi);
+    }
+    return cvt<double>(e);
+}
+
+template<typename T>
+__device__ void cnn_process_sample(const CnnCtx<T>& c, const OpDev* op, const Conf<2>& s, int lane, size_t row,
+                                   const SampleOut& out, bool exact_weight) {
+    const cplx<T> lpsi = cnn_log_psi(c, s, lane);
+    cplx<double> e = mk(0.0, 0.0);
+    if(op) e = cnn_local_energy(c, *op, s, lpsi, lane);
+    if(lane == 0) {
+        for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = s.w[w];
+        const cplx<double> l = cvt<double>(lpsi);
+        out.log_psi[row] = l;
+        if(out.eloc) out.eloc[row] = e;
+        if(exact_weight && out.weight) out.weight[row] = exp(2.0 * l.re);
+        if(!(isfinite(l.re) && isfinite(l.im) && isfinite(e.re) && isfinite(e.im))) atomicOr(out.status, kStatusNonFinite);
+    }
+    if(out.O) cnn_O_row(c, s, lane, reinterpret_cast<cplx<T>*>(out.O) + row * out.ldO);
+}
+
+// stages weights and tables in shared memory, carves the per-warp buffers
+template<typename T>
+__device__ CnnCtx<T> cnn_stage(const CnnDev<T>& p, unsigned char* smem) {
+    CnnCtx<T> c;
+    c.p = &p;
+    cplx<T>* w = reinterpret_cast<cplx<T>*>(smem);
+    for(unsigned k = threadIdx.x; k < p.Np; k += blockDim.x) w[k] = p.w[k];
+    unsigned char* q = smem + ((p.Np * sizeof(cplx<T>) + 15) & ~15u);
+    uint16_t* nb = reinterpret_cast<uint16_t*>(q);
+    uint16_t* iv = nb + p.tab_len;
+    for(unsigned k = threadIdx.x; k < p.tab_len; k += blockDim.x) {
+        nb[k] = p.nbr[k];
+        iv[k] = p.inv[k];
+    }
+    q += ((2 * p.tab_len * sizeof(uint16_t) + 15) & ~15u);
+    uint8_t* cl = q;
+    for(unsigned k = threadIdx.x; k < p.N; k += blockDim.x) cl[k] = p.cls[k];
+    q += (p.N + 15) & ~15u;
+    const unsigned per_warp = (p.ch[0] + (p.L > 1 ? p.ch[1] : 0)) * p.N;
+    cplx<T>* buf = reinterpret_cast<cplx<T>*>(q) + (size_t)(threadIdx.x >> 5) * per_warp;
+    c.w = w;
+    c.nbr = nb;
+    c.inv = iv;
+    c.cls = cl;
+    c.bufA = buf;
+    c.bufB = buf + p.ch[0] * p.N;
+    __syncthreads();
+    return c;
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256) cnn_mc_kernel(CnnDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    const int lane = threadIdx.x & 31;
+    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(chain >= a.n_chains) return;
+    const unsigned N = p.N;
+    Conf<2> s;
+    uint64_t t;
+    unsigned tape_pos = 0;
+    const bool tape = a.tape_site != nullptr;
+    if(tape) {
+        for(int w = 0; w < 2; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
+        t = 0;
+    } else if(a.do_init) {
+        t = a.chain_counter[chain];
+        if(a.n_up < 0) {
+            const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)t, (uint32_t)(t >> 32), chain, 1u});
+            s.w[0] = (uint64_t)r.x | ((uint64_t)r.y << 32);
+            s.w[1] = (uint64_t)r.z | ((uint64_t)r.w << 32);
+            for(int w = 0; w < 2; w++) {
+                const unsigned lo = 64u * w;
+                if(N <= lo) s.w[w] = 0;
+                else if(N - lo < 64u) s.w[w] &= ((uint64_t)1 << (N - lo)) - 1u;
+            }
+        } else {
+            s.w[0] = s.w[1] = 0;
+            for(int k = 0; k < a.n_up; k++) {
+                const uint64_t tk = t + (uint64_t)k;
+                const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tk, (uint32_t)(tk >> 32), chain, 2u});
+                unsigned target = mulhi32(r.x, N - (unsigned)k);
+                for(unsigned i = 0; i < N; i++) {
+                    if(!spin_bit(s, i)) {
+                        if(target == 0) { s.w[i >> 6] |= (uint64_t)1 << (i & 63u); break; }
+                        target--;
+                    }
+                }
+            }
+        }
+    } else {
+        for(int w = 0; w < 2; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
+        t = a.chain_counter[chain];
+    }
+    cplx<T> lpsi = cnn_log_psi(c, s, lane);
+    unsigned long long n_acc = 0, n_rej = 0;
+    const uint64_t t0 = t;
+    u32x4 rr = {0, 0, 0, 0};
+    auto propose = [&]() {
+        unsigned i, j = 0xFFFFFFFFu;
+        double u = 0.0;
+        float uf = 0.f;
+        if(tape) {
+            i = a.tape_site[(size_t)chain * a.tape_len + tape_pos];
+            u = a.tape_u[(size_t)chain * a.tape_len + tape_pos];
+            if(sizeof(T) == 4) uf = (float)u;
+            tape_pos++;
+        } else {
+            const unsigned k = (unsigned)(t - t0) & 31u;
+            if(k == 0) {
+                const uint64_t tl = t + lane;
+                rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
+            }
+            const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
+            const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
+            const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
+            const uint32_t r3 = __shfl_sync(0xffffffffu, rr.w, k);
+            t++;
+            i = mulhi32(r0, N);
+            if(a.move_kind == 1) {
+                const unsigned bnd = mulhi32(r0, a.n_bonds);
+                i = a.bonds[2 * bnd];
+                j = a.bonds[2 * bnd + 1];
+            } else if(a.move_kind == 2) {
+                j = mulhi32(r1, N - 1u);
+                j += (j >= i);
+            }
+            u = u53(r2, r3);
+            if(sizeof(T) == 4) uf = __uint2float_rz(r3 >> 8) * 0x1.0p-24f;
+        }
+        Conf<2> s2 = s;
+        flip(s2, i);
+        if(a.move_kind != 0 && !tape) {
+            if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
+            flip(s2, j);
+        }
+        const cplx<T> l2 = cnn_log_psi(c, s2, lane);
+        const T ratio = fexp(T(2) * (l2.re - lpsi.re));
+        const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
+        if(accept) {
+            s = s2;
+            lpsi = l2;
+            n_acc++;
+        } else {
+            n_rej++;
+        }
+    };
+    if(a.do_init || tape)
+        for(unsigned k = 0; k < a.num_therm * N; k++) propose();
+    for(unsigned st = 0; st < a.samples_per_chain; st++) {
+        for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
+        cnn_process_sample(c, with_op ? &op : nullptr, s, lane, (size_t)st * a.n_chains + chain, out, false);
+    }
+    if(lane == 0) {
+        if(!tape) {
+            for(int w = 0; w < kMaxWords; w++) a.chain_conf[(size_t)chain * kMaxWords + w] = s.w[w];
+            a.chain_counter[chain] = t;
+        }
+        atomicAdd(&a.acc_rej[0], n_acc);
+        atomicAdd(&a.acc_rej[1], n_rej);
+    }
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256) cnn_exact_kernel(CnnDev<T> p, OpDev op, int with_op, uint64_t n_conf,
+                                                         SampleOut out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for(uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n_conf; idx += warps) {
+        Conf<2> s;
+        s.w[0] = idx;
+        s.w[1] = 0;
+        cnn_process_sample(c, with_op ? &op : nullptr, s, lane, idx, out, true);
+    }
+}
+
+template<typename T>
+__global__ void __launch_bounds__(256) cnn_confs_kernel(CnnDev<T> p, OpDev op, int with_op, const uint64_t* confs,
+                                                         uint64_t n, SampleOut out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    const int lane = threadIdx.x & 31;
+    const uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(idx >= n) return;
+    Conf<2> s;
+    s.w[0] = confs[idx * kMaxWords];
+    s.w[1] = confs[idx * kMaxWords + 1];
+    cnn_process_sample(c, with_op ? &op : nullptr, s, lane, idx, out, true);
+}
+
+template<typename T>
+__global__ void cnn_prepare_kernel(const cplx<double>* __restrict__ params, cplx<T>* __restrict__ w, unsigned n) {
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k < n) w[k] = cvt<T>(params[k]);
+}
+
+// ----------------------------------------------------------------------------------
+template<typename T>
+CnnDev<T> cnn_view(const ann_psi_impl& psi) {
+    CnnDev<T> p{};
+    p.N = psi.N;
+    p.L = (unsigned)psi.layers.size();
+    p.ncls = psi.ncls;
+    p.Np = psi.Np;
+    unsigned tab = 0;
+    for(unsigned l = 0; l < p.L; l++) {
+        p.ch[l] = psi.layers[l].channels;
+        p.prev[l] = psi.layers[l].prev_channels;
+        p.vol[l] = psi.layers[l].vol;
+        p.woff[l] = psi.layers[l].param_offset;
+        p.nbr_off[l] = tab;
+        tab += psi.N * p.vol[l];
+    }
+    p.tab_len = tab;
+    p.act = psi.act;
+    p.ff = psi.final_factor;
+    p.lp = mk<T>((T)psi.lp.real(), (T)psi.lp.imag());
+    p.w = psi.cnn_w.as<cplx<T>>();
+    const unsigned char* meta = psi.cnn_meta.as<unsigned char>();
+    p.nbr = reinterpret_cast<const uint16_t*>(meta);
+    p.inv = p.nbr + tab;
+    p.cls = meta + 4 * tab;
+    return p;
+}
+
+template<typename T>
+size_t cnn_smem(const CnnDev<T>& p, int warps) {
+    const size_t per_warp = (size_t)(p.ch[0] + (p.L > 1 ? p.ch[1] : 0)) * p.N * sizeof(cplx<T>);
+    return ((p.Np * sizeof(cplx<T>) + 15) & ~(size_t)15) + ((2 * p.tab_len * 2 + 15) & ~(size_t)15) +
+           ((p.N + 15) & ~(size_t)15) + warps * per_warp;
+}
+
+template<typename T>
+int cnn_warps(const CnnDev<T>& p) {
+    int w = 8;
+    while(w > 1 && cnn_smem(p, w) > 200 * 1024) w >>= 1;
+    if(cnn_smem(p, w) > 220 * 1024) throw Error(ANN_ERR_INVALID, "PsiCNN too large for shared memory");
+    return w;
+}
+
+template<typename K>
+void cnn_set_smem(K k, size_t bytes) {
+    if(bytes > 48 * 1024) ANN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+SampleOut cnn_out(Rows& rows, void* O, size_t ldO, bool want_eloc) {
+    SampleOut o;
+    o.conf = rows.conf.as<uint64_t>();
+    o.log_psi = rows.log_psi.as<cplx<double>>();
+    o.eloc = want_eloc ? rows.eloc.as<cplx<double>>() : nullptr;
+    o.weight = rows.weight.as<double>();
+    o.O = O;
+    o.ldO = ldO;
+    o.status = status_word();
+    return o;
+}
+
+void cnn_rows(Rows& rows, size_t n) {
+    rows.n = n;
+    rows.conf.ensure(n * kMaxWords * sizeof(uint64_t));
+    rows.log_psi.ensure(n * sizeof(cplx<double>));
+    rows.eloc.ensure(n * sizeof(cplx<double>));
+    rows.weight.ensure(n * sizeof(double));
+}
+
+template<typename T>
+void cnn_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st) {
+    const CnnDev<T> p = cnn_view<T>(psi);
+    const int wpb = cnn_warps(p);
+    const size_t smem = cnn_smem(p, wpb);
+    OpDev ov{};
+    if(op) ov = op->view();
+    if(ens.kind == 0) {
+        const uint64_t n_conf = 1ull << ens.N;
+        cnn_rows(*t.rows, n_conf);
+        SampleOut out = cnn_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
+        uint64_t blocks = (n_conf + wpb - 1) / wpb;
+        if(blocks > 152ull * 16) blocks = 152ull * 16;
+        cnn_set_smem(cnn_exact_kernel<T>, smem);
+        cnn_exact_kernel<T><<<(unsigned)blocks, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, n_conf, out);
+        check_launch("cnn_exact_kernel");
+        return;
+    }
+    const unsigned spc = ens.num_samples / ens.n_chains;
+    cnn_rows(*t.rows, (size_t)spc * ens.n_chains);
+    McArgs a;
+    a.n_chains = ens.n_chains;
+    a.samples_per_chain = spc;
+    a.num_sweeps = ens.num_sweeps;
+    a.num_therm = ens.num_therm;
+    a.do_init = (!ens.persistent || !ens.chains_valid) ? 1 : 0;
+    a.n_up = ens.n_up;
+    a.move_kind = ens.move;
+    a.bonds = ens.bonds_d.as<uint32_t>();
+    a.n_bonds = (unsigned)(ens.bonds.size() / 2);
+    a.k0 = (uint32_t)ens.seed;
+    a.k1 = (uint32_t)(ens.seed >> 32);
+    a.chain_conf = ens.chain_conf.as<uint64_t>();
+    a.chain_counter = ens.chain_counter.as<uint64_t>();
+    a.tape_site = ens.tape_len ? ens.tape_site.as<uint32_t>() : nullptr;
+    a.tape_u = ens.tape_len ? ens.tape_u.as<double>() : nullptr;
+    a.tape_len = ens.tape_len;
+    a.acc_rej = ens.acc_rej.as<unsigned long long>();
+    if(a.tape_site)
+        ANN_CUDA(cudaMemcpyAsync(ens.chain_conf.p, ens.tape_init.p, (size_t)ens.n_chains * kMaxWords * 8,
+                                 cudaMemcpyDeviceToDevice, st));
+    ANN_CUDA(cudaMemsetAsync(ens.acc_rej.p, 0, 2 * sizeof(unsigned long long), st));
+    SampleOut out = cnn_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
+    cnn_set_smem(cnn_mc_kernel<T>, smem);
+    cnn_mc_kernel<T><<<(ens.n_chains + wpb - 1) / wpb, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out);
+    check_launch("cnn_mc_kernel");
+    ens.chains_valid = true;
+}
+
+template<typename T>
+void cnn_confs_T(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
+                 size_t ldO, cudaStream_t st) {
+    const CnnDev<T> p = cnn_view<T>(psi);
+    const int wpb = cnn_warps(p);
+    const size_t smem = cnn_smem(p, wpb);
+    OpDev ov{};
+    if(op) ov = op->view();
+    cnn_rows(rows, n);
+    SampleOut out = cnn_out(rows, O, ldO, op != nullptr);
+    cnn_set_smem(cnn_confs_kernel<T>, smem);
+    cnn_confs_kernel<T><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, confs, n, out);
+    check_launch("cnn_confs_kernel");
+}
+
+}  // namespace
+
+void cnn_prepare(ann_psi_impl& psi, cudaStream_t st) {
+    const unsigned n = psi.Np;
+    if(psi.precision == 0)
+        cnn_prepare_kernel<float><<<(n + 255) / 256, 256, 0, st>>>(psi.params.as<cplx<double>>(),
+                                                                   psi.cnn_w.as<cplx<float>>(), n);
+    else
+        cnn_prepare_kernel<double><<<(n + 255) / 256, 256, 0, st>>>(psi.params.as<cplx<double>>(),
+                                                                    psi.cnn_w.as<cplx<double>>(), n);
+    check_launch("cnn_prepare_kernel");
+}
+
+void cnn_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st) {
+    if(psi.precision == 0) cnn_run_T<float>(psi, op, ens, t, st);
+    else cnn_run_T<double>(psi, op, ens, t, st);
+}
+
+void cnn_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
+               size_t ldO, cudaStream_t st) {
+    if(psi.precision == 0) cnn_confs_T<float>(psi, op, confs, n, rows, O, ldO, st);
+    else cnn_confs_T<double>(psi, op, confs, n, rows, O, ldO, st);
 }
 
 }  // namespace ann
 
-extern "C" int ann_psi_create_cnn(const ann_cnn_desc*, ann_psi**) { return ANN_ERR_UNSUPPORTED; }
+using namespace ann;
+
+extern "C" int ann_psi_create_cnn(const ann_cnn_desc* d, ann_psi** out) {
+    try {
+        if(!d || !out) throw Error(ANN_ERR_INVALID, "null argument");
+        if(d->num_layers < 1 || d->num_layers > (unsigned)kCnnMaxLayers)
+            throw Error(ANN_ERR_UNSUPPORTED, "PsiCNN supports one or two layers");
+        const unsigned N = d->extent[0] * d->extent[1] * d->extent[2];
+        if(N < 1 || N > 128) throw Error(ANN_ERR_INVALID, "PsiCNN needs 1 <= N <= 128 sites");
+        if(d->precision != ANN_PREC_FP32 && d->precision != ANN_PREC_FP64) throw Error(ANN_ERR_INVALID, "precision");
+        auto* p = new ann_psi();
+        try {
+            p->kind = 1;
+            p->precision = d->precision;
+            p->act = d->activation;
+            p->N = N;
+            p->NW = 2;
+            for(int k = 0; k < 3; k++) p->extent[k] = d->extent[k];
+            p->final_factor = d->final_factor;
+            p->lp = zd(d->log_prefactor[0], d->log_prefactor[1]);
+            p->sym.assign(d->symmetry_classes, d->symmetry_classes + N);
+            std::vector<unsigned> cls_sorted = p->sym;
+            std::sort(cls_sorted.begin(), cls_sorted.end());
+            p->ncls = (unsigned)(std::unique(cls_sorted.begin(), cls_sorted.end()) - cls_sorted.begin());
+            for(unsigned x = 0; x < N; x++)
+                if(p->sym[x] >= p->ncls) throw Error(ANN_ERR_INVALID, "symmetry classes must be 0..n-1");
+            if(p->ncls > 255) throw Error(ANN_ERR_INVALID, "at most 255 symmetry classes");
+            unsigned off = 0;
+            for(unsigned l = 0; l < d->num_layers; l++) {
+                CnnLayerHost L{};
+                L.channels = d->num_channels[l];
+                L.prev_channels = l ? d->num_channels[l - 1] : 1u;
+                L.vol = 1;
+                for(int k = 0; k < 3; k++) {
+                    L.conn[k] = d->connectivity[3 * l + k];
+                    if(L.conn[k] < 1 || L.conn[k] > d->extent[k]) throw Error(ANN_ERR_INVALID, "connectivity > extent");
+                    L.vol *= L.conn[k];
+                }
+                if(L.channels < 1 || L.channels > 64) throw Error(ANN_ERR_INVALID, "1..64 channels per layer");
+                L.param_offset = off;
+                off += L.channels * L.prev_channels * p->ncls * L.vol;
+                p->layers.push_back(L);
+            }
+            if(off != d->num_params) throw Error(ANN_ERR_INVALID, "num_params does not match the layer structure");
+            p->Np = off;
+            // neighbour tables: forward-anchored periodic windows (Convolve<3>::foreach_connection)
+            const unsigned e0 = d->extent[0], e1 = d->extent[1], e2 = d->extent[2];
+            std::vector<uint16_t> nbr, inv;
+            for(auto& L : p->layers) {
+                std::vector<uint16_t> nb(N * L.vol), iv(N * L.vol);
+                for(unsigned x = 0; x < N; x++) {
+                    const unsigned pg = x / (e1 * e2), row = (x % (e1 * e2)) / e2, col = x % e2;
+                    unsigned k = 0;
+                    for(unsigned a = 0; a < L.conn[0]; a++)
+                        for(unsigned b = 0; b < L.conn[1]; b++)
+                            for(unsigned cc = 0; cc < L.conn[2]; cc++) {
+                                const unsigned y = ((pg + a) % e0) * e1 * e2 + ((row + b) % e1) * e2 + (col + cc) % e2;
+                                nb[x * L.vol + k] = (uint16_t)y;
+                                iv[y * L.vol + k] = (uint16_t)x;
+                                k++;
+                            }
+                }
+                nbr.insert(nbr.end(), nb.begin(), nb.end());
+                inv.insert(inv.end(), iv.begin(), iv.end());
+            }
+            std::vector<unsigned char> meta(4 * nbr.size() + N);
+            std::memcpy(meta.data(), nbr.data(), 2 * nbr.size());
+            std::memcpy(meta.data() + 2 * nbr.size(), inv.data(), 2 * inv.size());
+            for(unsigned x = 0; x < N; x++) meta[4 * nbr.size() + x] = (unsigned char)p->sym[x];
+            upload(p->cnn_meta, meta.data(), meta.size());
+            upload(p->params, d->params, (size_t)p->Np * 16);
+            p->cnn_w.ensure((size_t)p->Np * p->elem_bytes());
+            psi_prepare(*p, nullptr);
+            ANN_CUDA(cudaDeviceSynchronize());
+        } catch(...) {
+            delete p;
+            throw;
+        }
+        *out = p;
+        return ANN_OK;
+    } catch(const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch(const std::exception& e) {
+        set_last_error(e.what());
+        return ANN_ERR_INVALID;
+    }
+}

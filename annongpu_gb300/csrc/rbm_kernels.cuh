@@ -32,36 +32,6 @@ struct RbmDev {
     cplx<T> lp;          // log prefactor
 };
 
-struct McArgs {
-    unsigned n_chains;
-    unsigned samples_per_chain;
-    unsigned num_sweeps;
-    unsigned num_therm;
-    int do_init;              // draw fresh configurations (and thermalise) first
-    int n_up;                 // < 0: unconstrained initial configurations
-    int move_kind;            // 0 single flip, 1 exchange over bonds, 2 exchange over random pairs
-    const uint32_t* bonds;    // [n_bonds][2]
-    unsigned n_bonds;
-    uint32_t k0, k1;          // Philox key
-    uint64_t* chain_conf;     // [n_chains][kMaxWords], in/out
-    uint64_t* chain_counter;  // [n_chains], in/out
-    // proposal tape (parity replay): per chain, num_props sites and uniforms
-    const uint32_t* tape_site;
-    const double* tape_u;
-    unsigned tape_len;
-    unsigned long long* acc_rej;  // [2]
-};
-
-struct SampleOut {
-    uint64_t* conf;           // [rows][kMaxWords]
-    cplx<double>* log_psi;    // [rows]
-    cplx<double>* eloc;       // [rows] (may be null)
-    double* weight;           // [rows] (exact summation only)
-    void* O;                  // [rows][ldO] cplx<T> (may be null)
-    size_t ldO;
-    unsigned* status;
-};
-
 template<typename T, int U>
 struct Lane {
     cplx<T> th[U];   // angles
@@ -123,34 +93,38 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
 template<typename T, int NW, int U>
 __device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op,
                                      const Conf<NW>& s, const Lane<T, U>& L, int lane) {
+    // arithmetic in the kernel precision T (coefficients are stored in FP64 and
+    // rounded once); the FP64 pipe is reserved for the final conversion
     // diagonal strings, split over lanes
-    double dre = 0.0, dim = 0.0;
+    T dre = T(0), dim = T(0);
     for(unsigned n = lane; n < op.n_diag; n += 32) {
         int neg = 0;
 #pragma unroll
         for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.diag_mask[n * op.nw + w]);
-        const double sg = (neg & 1) ? -1.0 : 1.0;
-        dre += sg * op.diag_coeff[2 * n];
-        dim += sg * op.diag_coeff[2 * n + 1];
+        const T c_re = diag_coeff<T>(op)[2 * n], c_im = diag_coeff<T>(op)[2 * n + 1];
+        dre += (neg & 1) ? -c_re : c_re;
+        dim += (neg & 1) ? -c_im : c_im;
     }
-    cplx<double> e = mk<double>(warp_sum(dre), warp_sum(dim));
+    cplx<T> e = mk<T>(warp_sum(dre), warp_sum(dim));
     cplx<T> dth[U], fnew[U];
     for(unsigned g = 0; g < op.n_groups; g++) {
-        const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
-        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, op.grp_sites + sb, se - sb, dth, fnew);
-        cplx<double> cg = mk<double>(0.0, 0.0);
+        // summed matrix element of the group first: when it vanishes (e.g. XX + YY on
+        // aligned spins) the psi ratio is not needed
+        cplx<T> cg = mk<T>(T(0), T(0));
         for(unsigned k = op.grp_str_begin[g]; k < op.grp_str_begin[g + 1]; k++) {
             int neg = 0;
 #pragma unroll
             for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.str_mask[k * op.nw + w]);
-            const double sg = (neg & 1) ? -1.0 : 1.0;
-            cg.re += sg * op.str_coeff[2 * k];
-            cg.im += sg * op.str_coeff[2 * k + 1];
+            const T c_re = str_coeff<T>(op)[2 * k], c_im = str_coeff<T>(op)[2 * k + 1];
+            cg.re += (neg & 1) ? -c_re : c_re;
+            cg.im += (neg & 1) ? -c_im : c_im;
         }
-        const cplx<double> r = cvt<double>(cexp(d));
-        e += cg * r;
+        if(cg.re == T(0) && cg.im == T(0)) continue;
+        const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
+        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, op.grp_sites + sb, se - sb, dth, fnew);
+        e += cg * cexp(d);
     }
-    return e;
+    return cvt<double>(e);
 }
 
 // log psi, local energy, O_k row and sample bookkeeping for one configuration
@@ -273,10 +247,12 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
 
     auto propose = [&]() {
         unsigned i, j = 0xFFFFFFFFu;
-        double u;
+        double u = 0.0;
+        float uf = 0.f;
         if(tape) {
             i = a.tape_site[(size_t)chain * a.tape_len + tape_pos];
             u = a.tape_u[(size_t)chain * a.tape_len + tape_pos];
+            if(sizeof(T) == 4) uf = (float)u;
             tape_pos++;
         } else {
             const unsigned k = (unsigned)(t - t0) & 31u;
@@ -299,6 +275,7 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
                 j += (j >= i);
             }
             u = u53(r2, r3);
+            if(sizeof(T) == 4) uf = __uint2float_rz(r3 >> 8) * 0x1.0p-24f;  // top 24 bits of u
         }
         uint16_t sites[2];
         unsigned ns = 1;
@@ -312,7 +289,10 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
         const T ratio = fexp(T(2) * d.re);
         // MonteCarlo.hpp:158-160: accept if ratio > 1 or u <= ratio; u < 1 makes
         // the first clause redundant.
-        if(u <= (double)ratio) {
+        // complex64 chains compare in FP32 (GB300's FP64 rate is 1/64 of FP32):
+        // decisions differ from the FP64 comparison only within 2^-24 of a tie
+        const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
+        if(accept) {
 #pragma unroll
             for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.ft[q] = fnew[q]; }
             for(unsigned q = 0; q < ns; q++) flip(s, sites[q]);

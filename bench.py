@@ -348,6 +348,25 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_profile_case():
+    """Small case for ncu captures (a few GB at most, one SR step after one warm-up):
+    N=32, M=64 complex RBM (Np = 2144), 1-D TFIM, 16384 chains, 4 sweeps between
+    samples, BF16 tensor-core S, FP64 Cholesky solve."""
+    import annongpu_gb300 as ann
+    rng = np.random.default_rng(0)
+    N, M = 32, 64
+    a = 0.01 * (rng.standard_normal(N) + 1j * rng.standard_normal(N))
+    b = 0.01 * (rng.standard_normal(M) + 1j * rng.standard_normal(M))
+    W = 0.01 * (rng.standard_normal((N, M)) + 1j * rng.standard_normal((N, M)))
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(16384, 4, 8, 16384, True, seed=1, persistent=True)
+    td = ann.TDVP(psi.num_params, s_mode="bf16")
+    for _ in range(2):
+        td.sr_step(op, psi, mc, 1e-3, 0.01)
+    print("profile case: E/N =", td.E_local / N)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,7 +375,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="precision", choices=["precision", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
