@@ -30,6 +30,23 @@ template<typename T> __host__ __device__ __forceinline__ cplx<T> conj(cplx<T> a)
 template<typename T> __host__ __device__ __forceinline__ T norm2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
 template<typename D, typename S> __host__ __device__ __forceinline__ cplx<D> cvt(cplx<S> a) { return {(D)a.re, (D)a.im}; }
 
+// acc += a * b and acc += conj(a) * b as four fused multiply-adds (an expression such
+// as acc.re += a.re*b.re - a.im*b.im compiles to a multiply, an FMA and an add)
+template<typename T>
+__host__ __device__ __forceinline__ void cmac(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re);
+    acc.re = fma(-a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im);
+    acc.im = fma(a.im, b.re, acc.im);
+}
+template<typename T>
+__host__ __device__ __forceinline__ void cmac_conj(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re);
+    acc.re = fma(a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im);
+    acc.im = fma(-a.im, b.re, acc.im);
+}
+
 __device__ __forceinline__ float fexp(float x) { return expf(x); }
 __device__ __forceinline__ double fexp(double x) { return exp(x); }
 __device__ __forceinline__ void fsincos(float x, float* s, float* c) { sincosf(x, s, c); }

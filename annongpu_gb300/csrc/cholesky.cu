@@ -60,39 +60,53 @@ __global__ void __launch_bounds__(NB * NB) potrf_diag_kernel(zc* __restrict__ A,
     if(r < nb && c <= r) A[(size_t)(kb + r) * n + kb + c] = a[r][c];
 }
 
-// rows below the diagonal block: X <- X L_kk^{-H}, one thread per row
-__global__ void __launch_bounds__(32) trsm_panel_kernel(zc* __restrict__ A, unsigned n, unsigned kb) {
+// rows below the diagonal block: X <- X L_kk^{-H}, one warp per row, lane j owns
+// column j: x_j = b_j / L_jj, then every later column p subtracts x_j conj(L_pj)
+__global__ void __launch_bounds__(256) trsm_panel_kernel(zc* __restrict__ A, unsigned n, unsigned kb) {
     __shared__ zc L[NB][NB + 1];
-    __shared__ zc X[32][NB + 1];
+    __shared__ double inv_d[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
     for(unsigned t = threadIdx.x; t < nb * nb; t += blockDim.x) {
         const unsigned r = t / nb, c = t % nb;
-        L[r][c] = A[(size_t)(kb + r) * n + kb + c];
+        L[r][c] = r >= c ? A[(size_t)(kb + r) * n + kb + c] : mk(0.0, 0.0);
     }
-    const unsigned row = kb + nb + blockIdx.x * 32 + threadIdx.x;
-    const bool live = row < n;
-    if(live)
-        for(unsigned p = 0; p < nb; p++) X[threadIdx.x][p] = A[(size_t)row * n + kb + p];
     __syncthreads();
-    if(!live) return;
+    if(threadIdx.x < nb) inv_d[threadIdx.x] = 1.0 / L[threadIdx.x][threadIdx.x].re;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
+    const size_t row = kb + nb + (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(row >= n) return;
+    zc b = lane < nb ? A[row * n + kb + lane] : mk(0.0, 0.0);
     for(unsigned j = 0; j < nb; j++) {
-        zc x = X[threadIdx.x][j];
-        for(unsigned p = 0; p < j; p++) x = x - X[threadIdx.x][p] * conj(L[j][p]);
-        X[threadIdx.x][j] = (1.0 / L[j][j].re) * x;
+        zc xj = inv_d[j] * b;
+        xj.re = __shfl_sync(0xffffffffu, xj.re, j);
+        xj.im = __shfl_sync(0xffffffffu, xj.im, j);
+        if(lane == j) b = xj;
+        else if(lane > j && lane < nb) b = b - xj * conj(L[lane][j]);
     }
-    for(unsigned p = 0; p < nb; p++) A[(size_t)row * n + kb + p] = X[threadIdx.x][p];
+    if(lane < nb) A[row * n + kb + lane] = b;
 }
 
-// trailing lower triangle: A[i][j] -= sum_p X[i][p] conj(X[j][p]), i >= j >= t0
+// trailing lower triangle: A[i][j] -= sum_p X[i][p] conj(X[j][p]), i >= j >= t0.
+// col_only: the first tile column (the next panels, updated first for the
+// look-ahead); otherwise the lower-triangular tiles with tile column >= 1.
 __global__ void __launch_bounds__(256) herk_update_kernel(zc* __restrict__ A, unsigned n, unsigned kb, unsigned nb,
-                                                          unsigned tiles) {
+                                                          int col_only) {
     __shared__ zc Xi[16][UT];
     __shared__ zc Xj[16][UT];
     const unsigned t0 = kb + nb;
-    // lower-triangular tile (ti >= tj)
-    unsigned b = blockIdx.x, ti = 0;
-    while(b > ti) { b -= ti + 1; ti++; }
-    const unsigned tj = b;
+    unsigned ti, tj;
+    if(col_only) {
+        ti = blockIdx.x;
+        tj = 0;
+    } else {
+        // lower-triangular tile (ti >= tj) of the sub-grid starting at tile (1, 1)
+        unsigned b = blockIdx.x;
+        ti = 0;
+        while(b > ti) { b -= ti + 1; ti++; }
+        tj = b + 1;
+        ti += 1;
+    }
     const unsigned i0 = t0 + ti * UT, j0 = t0 + tj * UT;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     zc acc[4][4];
@@ -120,10 +134,7 @@ __global__ void __launch_bounds__(256) herk_update_kernel(zc* __restrict__ A, un
 #pragma unroll
             for(int i = 0; i < 4; i++)
 #pragma unroll
-                for(int j = 0; j < 4; j++) {
-                    acc[i][j].re += xa[i].re * xb[j].re + xa[i].im * xb[j].im;
-                    acc[i][j].im += xa[i].im * xb[j].re - xa[i].re * xb[j].im;
-                }
+                for(int j = 0; j < 4; j++) cmac_conj(acc[i][j], xb[j], xa[i]);  // += xa conj(xb)
         }
     }
 #pragma unroll
@@ -140,45 +151,55 @@ __global__ void __launch_bounds__(256) herk_update_kernel(zc* __restrict__ A, un
     }
 }
 
-// forward substitution step for block kb: every CTA solves L_kk y_k = b_k
-// (identically), CTA 0 stores y_k, and all CTAs update the rows below.
+// forward substitution step for block kb: warp 0 of every CTA solves L_kk y_k = b_k
+// (identically; lane j owns y_j), CTA 0 stores y_k, and all CTAs update the rows below.
 __global__ void __launch_bounds__(256) fwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
                                                         zc* __restrict__ b) {
     __shared__ zc y[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
-    if(threadIdx.x == 0) {
+    if(threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        zc v = lane < nb ? b[kb + lane] : mk(0.0, 0.0);
         for(unsigned j = 0; j < nb; j++) {
-            zc x = b[kb + j];
-            for(unsigned p = 0; p < j; p++) x = x - L[(size_t)(kb + j) * n + kb + p] * y[p];
-            y[j] = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * x;
+            zc yj = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * v;
+            yj.re = __shfl_sync(0xffffffffu, yj.re, j);
+            yj.im = __shfl_sync(0xffffffffu, yj.im, j);
+            if(lane == j) v = yj;
+            else if(lane > j && lane < nb) v = v - L[(size_t)(kb + lane) * n + kb + j] * yj;
         }
+        if(lane < nb) y[lane] = v;
     }
     __syncthreads();
     if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = y[threadIdx.x];
     for(size_t i = kb + nb + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         zc acc = mk(0.0, 0.0);
-        for(unsigned p = 0; p < nb; p++) acc += L[i * n + kb + p] * y[p];
+        for(unsigned p = 0; p < nb; p++) cmac(acc, L[i * n + kb + p], y[p]);
         b[i] = b[i] - acc;
     }
 }
 
-// backward substitution step for block kb with L^H
+// backward substitution step for block kb with L^H (lane j owns x_j, last first)
 __global__ void __launch_bounds__(256) bwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
                                                         zc* __restrict__ b) {
     __shared__ zc x[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
-    if(threadIdx.x == 0) {
+    if(threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        zc v = lane < nb ? b[kb + lane] : mk(0.0, 0.0);
         for(int j = (int)nb - 1; j >= 0; j--) {
-            zc v = b[kb + j];
-            for(unsigned p = j + 1; p < nb; p++) v = v - conj(L[(size_t)(kb + p) * n + kb + j]) * x[p];
-            x[j] = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * v;
+            zc xj = (1.0 / L[(size_t)(kb + j) * n + kb + j].re) * v;
+            xj.re = __shfl_sync(0xffffffffu, xj.re, j);
+            xj.im = __shfl_sync(0xffffffffu, xj.im, j);
+            if((int)lane == j) v = xj;
+            else if((int)lane < j) v = v - conj(L[(size_t)(kb + j) * n + kb + lane]) * xj;
         }
+        if(lane < nb) x[lane] = v;
     }
     __syncthreads();
     if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = x[threadIdx.x];
     for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < kb; i += (size_t)gridDim.x * blockDim.x) {
         zc acc = mk(0.0, 0.0);
-        for(unsigned q = 0; q < nb; q++) acc += conj(L[(size_t)(kb + q) * n + i]) * x[q];
+        for(unsigned q = 0; q < nb; q++) cmac_conj(acc, L[(size_t)(kb + q) * n + i], x[q]);
         b[i] = b[i] - acc;
     }
 }
@@ -190,7 +211,7 @@ __global__ void residual_kernel(const zc* __restrict__ S, unsigned n, double shi
     const int lane = threadIdx.x & 31;
     if(i >= n) return;
     zc acc = mk(0.0, 0.0);
-    for(unsigned j = lane; j < n; j += 32) acc += S[i * n + j] * x[j];
+    for(unsigned j = lane; j < n; j += 32) cmac(acc, S[i * n + j], x[j]);
     acc = warp_sum(acc);
     if(lane == 0) r[i] = F[i] - acc - shift * x[i];
 }
@@ -219,18 +240,55 @@ __global__ void norm_ratio_kernel(const zc* __restrict__ r, const zc* __restrict
     }
 }
 
+struct Side {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+Side& side_stream() {
+    static thread_local Side s;
+    if(!s.stream) {
+        ANN_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+        for(auto& e : s.ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    return s;
+}
+
+void panel(zc* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
+    potrf_diag_kernel<<<1, NB * NB, 0, st>>>(A, n, kb, status);
+    check_launch("potrf_diag_kernel");
+    const unsigned nb = min((unsigned)NB, n - kb);
+    const unsigned below = n - kb - nb;
+    if(below) {
+        trsm_panel_kernel<<<(below + 7) / 8, 256, 0, st>>>(A, n, kb);
+        check_launch("trsm_panel_kernel");
+    }
+}
+
+// Right-looking blocked Cholesky with look-ahead: after panel k, the first tile
+// column of the trailing matrix (it holds panels k+1, k+2) is updated first; panel
+// k+1 is then factorised on a side stream while the rest of the trailing update of
+// step k runs, hiding the serial diagonal factorisation and panel solve.
 void cholesky(zc* A, unsigned n, unsigned* status, cudaStream_t st) {
+    Side& sd = side_stream();
+    panel(A, n, 0, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);
-        potrf_diag_kernel<<<1, NB * NB, 0, st>>>(A, n, kb, status);
-        check_launch("potrf_diag_kernel");
         const unsigned below = n - kb - nb;
         if(below == 0) break;
-        trsm_panel_kernel<<<(below + 31) / 32, 32, 0, st>>>(A, n, kb);
-        check_launch("trsm_panel_kernel");
         const unsigned tiles = (below + UT - 1) / UT;
-        herk_update_kernel<<<tiles * (tiles + 1) / 2, 256, 0, st>>>(A, n, kb, nb, tiles);
+        herk_update_kernel<<<tiles, 256, 0, st>>>(A, n, kb, nb, 1);
         check_launch("herk_update_kernel");
+        // panel k+1 on the side stream, after the first-column update
+        ANN_CUDA(cudaEventRecord(sd.ev[0], st));
+        ANN_CUDA(cudaStreamWaitEvent(sd.stream, sd.ev[0], 0));
+        panel(A, n, kb + nb, status, sd.stream);
+        ANN_CUDA(cudaEventRecord(sd.ev[1], sd.stream));
+        if(tiles > 1) {
+            herk_update_kernel<<<(tiles - 1) * tiles / 2, 256, 0, st>>>(A, n, kb, nb, 0);
+            check_launch("herk_update_kernel");
+        }
+        ANN_CUDA(cudaStreamWaitEvent(st, sd.ev[1], 0));
     }
 }
 

@@ -79,11 +79,7 @@ herk_simt_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned
 #pragma unroll
             for(int i = 0; i < 4; i++)
 #pragma unroll
-                for(int j = 0; j < 4; j++) {
-                    // conj(a) * b
-                    acc[i][j].re += a[i].re * bb[j].re + a[i].im * bb[j].im;
-                    acc[i][j].im += a[i].re * bb[j].im - a[i].im * bb[j].re;
-                }
+                for(int j = 0; j < 4; j++) cmac_conj(acc[i][j], a[i], bb[j]);  // += conj(a) b
         }
     }
     const double corr = invW - 1.0;
