@@ -124,6 +124,18 @@ _SIGS = {
     "ann_sr_graph_capture": ([P, P, P, P, D, D, P], I),
     "ann_sr_graph_launch": ([P, P], I),
     "ann_set_phase_timing": ([I], I),
+    "ann_ens_set_proposal": ([P, P, U, D], I),
+    "ann_ens_proposal_stats": ([P, P, P], I),
+    "ann_ens_set_history": ([P, U], I),
+    "ann_made_create": ([U, U, U64, P], I),
+    "ann_made_destroy": ([P], I),
+    "ann_made_get_params": ([P, P, P, P, P], I),
+    "ann_made_set_params": ([P, P, P, P, P], I),
+    "ann_made_log_prob": ([P, P, U, P], I),
+    "ann_made_sample": ([P, U, U64, U64, P, P], I),
+    "ann_made_gradient": ([P, P, U, P, P, P, P, P], I),
+    "ann_made_train": ([P, P, U, U, U, D, P, P], I),
+    "ann_made_train_on_samples": ([P, P, U, U, D, P, P], I),
     "ann_get_phase_times": ([P], I),
 }
 

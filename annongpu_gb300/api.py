@@ -524,7 +524,104 @@ class MonteCarloSpins(_Handle):
         return conf, lp, el
 
 
+    # learned proposal (made.cu)
+    def set_proposal(self, made, indep_per_sample=1, min_acceptance=0.0):
+        """Adds `indep_per_sample` Metropolis-Hastings independence moves drawn from the
+        MADE `made` after the local sweeps of every sample; the proposal is dropped once
+        its acceptance in a call falls below `min_acceptance`."""
+        self._made = made
+        call("ann_ens_set_proposal", self._h, None if made is None else made.handle, int(indep_per_sample),
+             float(min_acceptance))
+
+    @property
+    def proposal_acceptance(self) -> float:
+        out = np.zeros(1)
+        call("ann_ens_proposal_stats", self._h, ptr(out), None)
+        return float(out[0])
+
+    @property
+    def proposal_dropped(self) -> bool:
+        out = ct.c_int()
+        call("ann_ens_proposal_stats", self._h, None, ct.byref(out))
+        return bool(out.value)
+
+    def set_history(self, capacity):
+        """Keeps the configurations of the last `capacity` samples as proposal training data."""
+        call("ann_ens_set_history", self._h, int(capacity))
+
+
 MonteCarloLoop = MonteCarloSpins
+
+
+# ----------------------------------------------------------------------------------
+def _conf_rows(confs) -> np.ndarray:
+    """Configurations (ints or Spins, or a (n,) / (n, 2) uint64 array) -> (n, 2) uint64 rows."""
+    if isinstance(confs, np.ndarray) and confs.dtype == np.uint64:
+        c = confs.reshape(len(confs), -1)
+        if c.shape[1] == 2:
+            return np.ascontiguousarray(c)
+        return np.ascontiguousarray(np.concatenate([c[:, :1], np.zeros((len(c), 1), np.uint64)], axis=1))
+    return np.ascontiguousarray(np.stack([_conf_words(c, 2) for c in confs]) if len(confs) else
+                                np.zeros((0, 2), np.uint64))
+
+
+class MADE(_Handle):
+    """Masked autoregressive MLP q(s) over N spins with one hidden layer of width H
+    (the learned Metropolis-Hastings proposal; this project's own component)."""
+
+    _destroy = "ann_made_destroy"
+
+    def __init__(self, N, H=256, seed=0):
+        _Handle.__init__(self)
+        self.N, self.H = int(N), int(H)
+        call("ann_made_create", self.N, self.H, int(seed) & 0xFFFFFFFFFFFFFFFF, ct.byref(self._h))
+
+    @property
+    def params(self):
+        W1 = np.zeros((self.H, self.N), np.float32)
+        b1 = np.zeros(self.H, np.float32)
+        W2 = np.zeros((self.N, self.H), np.float32)
+        b2 = np.zeros(self.N, np.float32)
+        call("ann_made_get_params", self._h, ptr(W1), ptr(b1), ptr(W2), ptr(b2))
+        return W1, b1, W2, b2
+
+    @params.setter
+    def params(self, value):
+        W1, b1, W2, b2 = (np.ascontiguousarray(np.asarray(v, np.float32)) for v in value)
+        call("ann_made_set_params", self._h, ptr(W1), ptr(b1), ptr(W2), ptr(b2))
+
+    def log_prob(self, confs):
+        rows = _conf_rows(confs)
+        out = np.zeros(len(rows))
+        call("ann_made_log_prob", self._h, ptr(rows), len(rows), ptr(out))
+        return out
+
+    def sample(self, n, seed=0, first=0):
+        confs = np.zeros((n, 2), np.uint64)
+        logq = np.zeros(n)
+        call("ann_made_sample", self._h, int(n), int(seed), int(first), ptr(confs), ptr(logq))
+        return confs, logq
+
+    def gradient(self, confs):
+        rows = _conf_rows(confs)
+        g = [np.zeros((self.H, self.N), np.float32), np.zeros(self.H, np.float32),
+             np.zeros((self.N, self.H), np.float32), np.zeros(self.N, np.float32)]
+        loss = np.zeros(1)
+        call("ann_made_gradient", self._h, ptr(rows), len(rows), *[ptr(x) for x in g], ptr(loss))
+        return (*g, float(loss[0]))
+
+    def train(self, confs, steps, batch=4096, lr=1e-3, stream=None):
+        rows = _conf_rows(confs)
+        loss = np.zeros(1)
+        call("ann_made_train", self._h, ptr(rows), len(rows), int(steps), int(batch), float(lr), stream_ptr(stream),
+             ptr(loss))
+        return float(loss[0])
+
+    def train_on_samples(self, ensemble, steps, batch=4096, lr=1e-3, stream=None):
+        loss = np.zeros(1)
+        call("ann_made_train_on_samples", self._h, ensemble.handle, int(steps), int(batch), float(lr),
+             stream_ptr(stream), ptr(loss))
+        return float(loss[0])
 
 
 # ----------------------------------------------------------------------------------

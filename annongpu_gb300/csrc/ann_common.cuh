@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace ann {
@@ -201,6 +202,15 @@ template<typename T> __device__ __forceinline__ const T* str_coeff(const OpDev& 
 template<> __device__ __forceinline__ const float* str_coeff<float>(const OpDev& op) { return op.str_coeff_f; }
 template<> __device__ __forceinline__ const double* str_coeff<double>(const OpDev& op) { return op.str_coeff; }
 
+// learned proposal weights as the kernels read them (see made.cuh)
+struct MadeDev {
+    unsigned N, H;             // N == 0: no learned proposal
+    const __nv_bfloat16* W1t;  // N x H
+    const float* b1;           // H
+    const __nv_bfloat16* W2t;  // H x N
+    const float* b2;           // N
+};
+
 struct McArgs {
     unsigned n_chains;
     unsigned samples_per_chain;
@@ -218,7 +228,9 @@ struct McArgs {
     const uint32_t* tape_site;
     const double* tape_u;
     unsigned tape_len;
-    unsigned long long* acc_rej;  // [2]
+    unsigned long long* acc_rej;  // [4]: local accepted, rejected; learned accepted, rejected
+    MadeDev made;                 // learned independence proposal (made.N == 0: none)
+    unsigned indep_per_sample;    // independence proposals after the local sweeps of each sample
 };
 
 struct SampleOut {

@@ -43,6 +43,8 @@ struct DevBuf {
 
 void upload(DevBuf& b, const void* src, size_t bytes);
 
+struct ann_made_impl;
+
 // ---------------------------------------------------------------------------------
 struct CnnLayerHost {
     unsigned channels, prev_channels, vol, conn[3], param_offset;
@@ -99,6 +101,15 @@ struct ann_ens_impl {
     DevBuf bonds_d, chain_conf, chain_counter, acc_rej;
     bool chains_valid = false;  // chain state holds equilibrated chains
     unsigned long long last_acc = 0, last_rej = 0;
+    // learned proposal (Metropolis-Hastings independence moves)
+    const ann_made_impl* made = nullptr;
+    unsigned indep_per_sample = 0;
+    double made_min_acceptance = 0.0;
+    bool made_dropped = false;
+    unsigned long long last_made_acc = 0, last_made_rej = 0;
+    // ring buffer of recent sample configurations (training data for the proposal)
+    DevBuf hist;
+    size_t hist_cap = 0, hist_len = 0, hist_pos = 0;
     // tape replay
     DevBuf tape_site, tape_u, tape_init;
     unsigned tape_len = 0;
@@ -107,6 +118,17 @@ struct ann_ens_impl {
         return kind == 0 ? (unsigned)(1ull << N) : (num_samples / n_chains) * n_chains;
     }
     double uniform_weight() const { return 1.0 / (double)num_samples; }
+};
+
+struct ann_made_impl {
+    unsigned N = 0, H = 0, adam_t = 0;
+    uint64_t seed = 0;
+    DevBuf W1, b1, W2, b2;            // FP32 master weights (W1: H x N, W2: N x H)
+    DevBuf W1t, W2t;                  // BF16 transposed copies read by the kernels
+    DevBuf deg;                       // hidden-unit degrees (u16)
+    DevBuf mW1, vW1, mb1, vb1, mW2, vW2, mb2, vb2;  // Adam moments
+    DevBuf gW1, gb1, gW2, gb2;        // gradients
+    DevBuf X, pre, hbuf, l, dl, dh, row_loss;       // training scratch
 };
 
 struct ann_tdvp_impl {
@@ -196,6 +218,11 @@ void cnn_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, 
 // sum_s w_s exp(sum_n c_n <s|P_n|s'>) over the rows (ExpectationValue.cu.template:52-81)
 void exp_sigma_z_sum(const ann_op_impl& op, const Rows& rows, const double* wts, double w0, double* out2,
                      cudaStream_t st);
+// MADE (made.cu)
+struct MadeDev;
+MadeDev made_view(const ann_made_impl& m);
+void made_logq_batch(const ann_made_impl& m, const uint64_t* confs, size_t n, double* out, cudaStream_t st);
+
 // activation_function(z, layer) evaluated by the device code path
 void activation_host(double re, double im, unsigned layer, int activation, double* out2);
 
@@ -206,3 +233,4 @@ struct ann_psi : ann::ann_psi_impl {};
 struct ann_op : ann::ann_op_impl {};
 struct ann_ens : ann::ann_ens_impl {};
 struct ann_tdvp : ann::ann_tdvp_impl {};
+struct ann_made : ann::ann_made_impl {};

@@ -1,5 +1,6 @@
 // C ABI (include/annongpu.h): handle management, argument checking, and the host
 // logic of the reference's network functions on top of the device kernels.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <map>
@@ -108,6 +109,20 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
     } else {
         cnn_run(psi, op, ens, t, st);
     }
+    if(ens.hist_cap) {
+        // append the configurations of this pass to the ring buffer
+        const size_t n = t.rows->n, row = kMaxWords * sizeof(uint64_t);
+        size_t done = 0;
+        while(done < n) {
+            const size_t chunk = std::min(n - done, ens.hist_cap - ens.hist_pos);
+            ANN_CUDA(cudaMemcpyAsync(ens.hist.as<unsigned char>() + ens.hist_pos * row,
+                                     t.rows->conf.as<unsigned char>() + done * row, chunk * row,
+                                     cudaMemcpyDeviceToDevice, st));
+            done += chunk;
+            ens.hist_pos = (ens.hist_pos + chunk) % ens.hist_cap;
+            ens.hist_len = std::min(ens.hist_cap, ens.hist_len + chunk);
+        }
+    }
 }
 
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
@@ -196,11 +211,17 @@ Scratch& scratch() {
 
 void mc_bookkeeping(ann_ens_impl& ens, cudaStream_t st) {
     if(ens.kind != 1) return;
-    unsigned long long ar[2];
+    unsigned long long ar[4];
     ANN_CUDA(cudaMemcpyAsync(ar, ens.acc_rej.p, sizeof(ar), cudaMemcpyDeviceToHost, st));
     sync(st);
     ens.last_acc = ar[0];
     ens.last_rej = ar[1];
+    ens.last_made_acc = ar[2];
+    ens.last_made_rej = ar[3];
+    // the learned proposal is dropped (local Metropolis continues alone) when its
+    // acceptance falls below the set rate
+    const unsigned long long tot = ar[2] + ar[3];
+    if(ens.made && tot > 0 && (double)ar[2] / (double)tot < ens.made_min_acceptance) ens.made_dropped = true;
 }
 
 Stats fetch_stats(const DevBuf& b, cudaStream_t st) {
@@ -544,7 +565,8 @@ int ann_ens_create_mc(const ann_mc_desc* d, ann_ens** out) {
             e->chain_counter.ensure((size_t)e->n_chains * 8);
             ANN_CUDA(cudaMemset(e->chain_conf.p, 0, e->chain_conf.bytes));
             ANN_CUDA(cudaMemset(e->chain_counter.p, 0, e->chain_counter.bytes));
-            e->acc_rej.ensure(2 * sizeof(unsigned long long));
+            e->acc_rej.ensure(4 * sizeof(unsigned long long));
+            ANN_CUDA(cudaMemset(e->acc_rej.p, 0, 4 * sizeof(unsigned long long)));
         } catch(...) {
             delete e;
             throw;
@@ -619,6 +641,32 @@ int ann_ens_set_chains(ann_ens* e, const uint64_t* conf, const uint64_t* counter
         e->chains_valid = true;
     });
 }
+int ann_ens_set_proposal(ann_ens* e, const ann_made* m, unsigned indep_per_sample, double min_acceptance) {
+    return guard([&] {
+        need(e && e->kind == 1, "not a Monte Carlo ensemble");
+        e->made = m;
+        e->indep_per_sample = m ? indep_per_sample : 0;
+        e->made_min_acceptance = min_acceptance;
+        e->made_dropped = false;
+    });
+}
+int ann_ens_proposal_stats(const ann_ens* e, double* acceptance, int* dropped) {
+    return guard([&] {
+        need(e && e->kind == 1, "not a Monte Carlo ensemble");
+        const double tot = (double)(e->last_made_acc + e->last_made_rej);
+        if(acceptance) *acceptance = tot > 0 ? (double)e->last_made_acc / tot : 0.0;
+        if(dropped) *dropped = e->made_dropped ? 1 : 0;
+    });
+}
+int ann_ens_set_history(ann_ens* e, unsigned capacity) {
+    return guard([&] {
+        need(e != nullptr, "null argument");
+        e->hist_cap = capacity;
+        e->hist_len = e->hist_pos = 0;
+        if(capacity) e->hist.ensure((size_t)capacity * kMaxWords * sizeof(uint64_t));
+    });
+}
+
 int ann_ens_set_tape(ann_ens* e, const uint64_t* init, const uint32_t* sites, const double* u, unsigned len) {
     return guard([&] {
         need(e && e->kind == 1, "not a Monte Carlo ensemble");

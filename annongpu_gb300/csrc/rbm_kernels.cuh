@@ -11,6 +11,7 @@
 #pragma once
 
 #include "ann_common.cuh"
+#include "made.cuh"
 
 namespace ann {
 
@@ -192,10 +193,20 @@ __device__ __forceinline__ const cplx<T>* stage_Wd(const RbmDev<T>& p, int w_sme
 // ---------------------------------------------------------------------------------
 // Metropolis sampler: one warp per chain.
 template<typename T, int NW, int U>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(256)
 rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
+    // learned-proposal weights after Wd, then one H-float scratch per warp
+    const bool use_made = a.made.N != 0;
+    MadeSm ms{};
+    float* mh = nullptr;
+    if(use_made) {
+        unsigned char* mbase = smem_raw + (w_smem ? (((size_t)p.N * p.Mpad * sizeof(cplx<T>) + 15) & ~(size_t)15) : 0);
+        ms = made_stage(a.made, mbase);
+        mh = reinterpret_cast<float*>(mbase + made_smem_bytes(a.made.N, a.made.H)) + (threadIdx.x >> 5) * a.made.H;
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if(chain >= a.n_chains) return;
@@ -240,10 +251,14 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
 
     Lane<T, U> L;
     recompute<T, NW, U>(p, Wd, s, L, lane);
-    unsigned long long n_acc = 0, n_rej = 0;
-    const uint64_t t0 = t;
+    unsigned long long n_acc = 0, n_rej = 0, m_acc = 0, m_rej = 0;
+    // Philox words for the 32 counters [rr_base, rr_base + 32), one per lane
+    uint64_t rr_base = 0;
+    bool rr_valid = false;
     u32x4 rr = {0, 0, 0, 0};
     cplx<T> dth[U], fnew[U];
+    float lq_cur = 0.f;
+    bool lq_stale = true;
 
     auto propose = [&]() {
         unsigned i, j = 0xFFFFFFFFu;
@@ -255,11 +270,13 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
             if(sizeof(T) == 4) uf = (float)u;
             tape_pos++;
         } else {
-            const unsigned k = (unsigned)(t - t0) & 31u;
-            if(k == 0) {
+            if(!rr_valid || t - rr_base >= 32u) {
+                rr_valid = true;
+                rr_base = t;
                 const uint64_t tl = t + lane;
                 rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
             }
+            const unsigned k = (unsigned)(t - rr_base);
             const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
             const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
             const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
@@ -297,8 +314,43 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
             for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.ft[q] = fnew[q]; }
             for(unsigned q = 0; q < ns; q++) flip(s, sites[q]);
             n_acc++;
+            lq_stale = true;
         } else {
             n_rej++;
+        }
+    };
+
+    // Metropolis-Hastings independence move with the learned proposal q:
+    // accept s' ~ q with probability min(1, |psi(s')|^2 q(s) / (|psi(s)|^2 q(s')))
+    auto propose_learned = [&]() {
+        const uint64_t tq = t++;
+        Conf<NW> s2;
+        const float lq2 = made_sample<NW, 8>(ms, a.k0, a.k1, (uint32_t)tq, (uint32_t)(tq >> 32), chain, s2, lane);
+        if(lq_stale) {
+            lq_cur = made_logq(ms, s, mh, lane);
+            lq_stale = false;
+        }
+        Lane<T, U> L2;
+        recompute<T, NW, U>(p, Wd, s2, L2, lane);
+        cplx<T> d = mk<T>(T(0), T(0));
+#pragma unroll
+        for(int q = 0; q < U; q++) d += L2.ft[q] - L.ft[q];
+        if(p.a_in_log_psi)
+            for(unsigned i = lane; i < p.N; i += 32) {
+                const int b1 = spin_bit(s2, i), b0 = spin_bit(s, i);
+                if(b1 != b0) d += (b1 ? T(2) : T(-2)) * p.a[i];
+            }
+        d = warp_sum(d);
+        const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tq, (uint32_t)(tq >> 32), chain, 0u});
+        const float lr = 2.f * (float)d.re + lq_cur - lq2;
+        const float uf = __uint2float_rz(r.w >> 8) * 0x1.0p-24f;
+        if(uf <= expf(lr)) {
+            s = s2;
+            L = L2;
+            lq_cur = lq2;
+            m_acc++;
+        } else {
+            m_rej++;
         }
     };
 
@@ -306,6 +358,8 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
         for(unsigned k = 0; k < a.num_therm * N; k++) propose();
     for(unsigned st = 0; st < a.samples_per_chain; st++) {
         for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
+        if(use_made)
+            for(unsigned k = 0; k < a.indep_per_sample; k++) propose_learned();
         recompute<T, NW, U>(p, Wd, s, L, lane);  // removes accumulated rounding of the increments
         process_sample<T, NW, U>(p, Wd, with_op ? &op : nullptr, s, L, lane,
                                  (size_t)st * a.n_chains + chain, out, false);
@@ -317,6 +371,10 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
         }
         atomicAdd(&a.acc_rej[0], n_acc);
         atomicAdd(&a.acc_rej[1], n_rej);
+        if(use_made) {
+            atomicAdd(&a.acc_rej[2], m_acc);
+            atomicAdd(&a.acc_rej[3], m_rej);
+        }
     }
 }
 

@@ -40,8 +40,8 @@ size_t wd_bytes(const ann_psi_impl& psi) {
 }
 
 template<typename T>
-int warps_per_block(size_t smem) {
-    return smem > 100 * 1024 ? 16 : 8;
+int warps_per_block(size_t) {
+    return 8;
 }
 
 SampleOut sample_out(Rows& rows, void* O, size_t ldO, bool want_eloc) {
@@ -128,19 +128,31 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     a.tape_u = ens.tape_len ? ens.tape_u.as<double>() : nullptr;
     a.tape_len = ens.tape_len;
     a.acc_rej = ens.acc_rej.as<unsigned long long>();
+    a.made = MadeDev{};
+    a.indep_per_sample = 0;
+    const bool learned = ens.made && !ens.made_dropped && ens.indep_per_sample > 0 && !a.tape_site;
+    if(learned) {
+        if(ens.made->N != psi.N) throw Error(ANN_ERR_INVALID, "learned proposal size differs from psi.N");
+        if(ens.made->H > 256) throw Error(ANN_ERR_INVALID, "learned proposals in the sampler need H <= 256");
+        if(ens.move != 0) throw Error(ANN_ERR_UNSUPPORTED, "learned proposals combine with single-flip moves");
+        a.made = made_view(*ens.made);
+        a.indep_per_sample = ens.indep_per_sample;
+    }
     if(a.tape_site) {
         // replay starts from the recorded initial configurations every call
         ANN_CUDA(cudaMemcpyAsync(ens.chain_conf.p, ens.tape_init.p, (size_t)ens.n_chains * kMaxWords * 8,
                                  cudaMemcpyDeviceToDevice, st));
     }
-    ANN_CUDA(cudaMemsetAsync(ens.acc_rej.p, 0, 2 * sizeof(unsigned long long), st));
+    ANN_CUDA(cudaMemsetAsync(ens.acc_rej.p, 0, 4 * sizeof(unsigned long long), st));
     SampleOut out = sample_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
     OpDev ov{};
     if(op) ov = op->view();
     const size_t wb = wd_bytes<T>(psi);
-    const int w_smem = wb <= kMaxSmemWd ? 1 : 0;
-    const size_t smem = w_smem ? wb : 0;
-    const int wpb = warps_per_block<T>(smem);
+    const int wpb = warps_per_block<T>(0);
+    const size_t made_bytes = learned ? made_smem_bytes(ens.made->N, ens.made->H) + (size_t)wpb * ens.made->H * 4 : 0;
+    const int w_smem = wb + made_bytes <= kMaxSmemWd ? 1 : 0;
+    const size_t smem = (w_smem ? ((wb + 15) & ~(size_t)15) : 0) + made_bytes;
+    if(smem > 220 * 1024) throw Error(ANN_ERR_INVALID, "learned proposal too large for shared memory");
     const unsigned grid = (ens.n_chains + wpb - 1) / wpb;
     ANN_DISPATCH_NW_U(psi.NW, psi.U, {
         auto k = rbm_mc_kernel<T, NWc, Uc>;

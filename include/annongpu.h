@@ -37,6 +37,7 @@ typedef struct ann_psi ann_psi;
 typedef struct ann_op ann_op;
 typedef struct ann_ens ann_ens;
 typedef struct ann_tdvp ann_tdvp;
+typedef struct ann_made ann_made;
 
 const char* ann_last_error(void);
 int ann_version(void);
@@ -157,6 +158,15 @@ int ann_ens_acceptance_rate(const ann_ens* ens, double* out);
 /* chain state (configurations num_markov_chains x num_words, Philox counters) */
 int ann_ens_get_chains(const ann_ens* ens, uint64_t* conf, uint64_t* counter);
 int ann_ens_set_chains(ann_ens* ens, const uint64_t* conf, const uint64_t* counter);
+/* Learned proposal: after the local sweeps of each sample, `indep_per_sample`
+   Metropolis-Hastings independence moves draw s' from the MADE `m` (NULL disables).
+   When the acceptance of these moves in a call falls below `min_acceptance`, the
+   proposal is dropped and local Metropolis continues alone. */
+int ann_ens_set_proposal(ann_ens* ens, const ann_made* m, unsigned indep_per_sample, double min_acceptance);
+/* acceptance of the learned moves in the last call, and whether the proposal was dropped */
+int ann_ens_proposal_stats(const ann_ens* ens, double* acceptance, int* dropped);
+/* keep the configurations of the last `capacity` samples (ring buffer) as training data */
+int ann_ens_set_history(ann_ens* ens, unsigned capacity);
 /* Proposal replay (parity checking): per chain, the initial configuration and
    `len` (site, uniform) pairs consumed in order instead of Philox draws; u = 0
    marks a proposal the reference accepted without drawing. NULL sites disables. */
@@ -232,6 +242,31 @@ int ann_sr_update(ann_tdvp* tdvp, ann_psi* psi, double lr, void* stream);
 /* one full SR step = eval + solve + update, on the device */
 int ann_sr_step(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, double diag_shift, double lr,
                 void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Learned proposal: masked autoregressive MLP (MADE, one hidden layer of width H,
+ * BF16 weights in the kernels, FP32 master weights, accumulation and Adam moments).
+ * Not in the reference; this project's own component.
+ * Weight layouts: W1 H x N, b1 H, W2 N x H, b2 N (float). Configurations as
+ * 2-word rows (uint64 x 2, bit i = spin up at site i).
+ * ------------------------------------------------------------------------------ */
+int ann_made_create(unsigned N, unsigned H, uint64_t seed, ann_made** out);
+int ann_made_destroy(ann_made* m);
+int ann_made_get_params(const ann_made* m, float* W1, float* b1, float* W2, float* b2);
+int ann_made_set_params(ann_made* m, const float* W1, const float* b1, const float* W2, const float* b2);
+/* log q(s) of n configurations */
+int ann_made_log_prob(ann_made* m, const uint64_t* confs, unsigned n, double* out);
+/* n samples s ~ q with Philox key `seed`, sample indices first .. first + n - 1 */
+int ann_made_sample(ann_made* m, unsigned n, uint64_t seed, uint64_t first, uint64_t* confs, double* logq);
+/* gradient of the mean -log q over n configurations (unmasked entries), and the loss */
+int ann_made_gradient(ann_made* m, const uint64_t* confs, unsigned n, float* gW1, float* gb1, float* gW2,
+                      float* gb2, double* loss);
+/* `steps` Adam steps (learning rate lr) over batches of `batch` configurations */
+int ann_made_train(ann_made* m, const uint64_t* confs, unsigned n, unsigned steps, unsigned batch, double lr,
+                   void* stream, double* loss);
+/* same, on the configurations the ensemble's chains produced (its history buffer if set) */
+int ann_made_train_on_samples(ann_made* m, const ann_ens* ens, unsigned steps, unsigned batch, double lr,
+                              void* stream, double* loss);
 
 /* ---------------------------------------------------------------------------------
  * CUDA graph of a whole SR step (capture once, replay many)
