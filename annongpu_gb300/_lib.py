@@ -124,6 +124,13 @@ _SIGS = {
     "ann_sr_graph_capture": ([P, P, P, P, D, D, P], I),
     "ann_sr_graph_launch": ([P, P], I),
     "ann_set_phase_timing": ([I], I),
+    "ann_batch_create": ([U, P, P, P, P, P], I),
+    "ann_batch_destroy": ([P], I),
+    "ann_batch_sample": ([P, P], I),
+    "ann_batch_energies": ([P, P], I),
+    "ann_batch_sr_step": ([P, D, D, P], I),
+    "ann_batch_graph_capture": ([P, D, D, P], I),
+    "ann_batch_graph_launch": ([P, P], I),
     "ann_ens_set_proposal": ([P, P, U, D], I),
     "ann_ens_proposal_stats": ([P, P, P], I),
     "ann_ens_set_history": ([P, U], I),

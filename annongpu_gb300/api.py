@@ -788,6 +788,41 @@ TDVP.eval_F = _track_rows(TDVP.eval_F)
 
 
 # ----------------------------------------------------------------------------------
+class Batch(_Handle):
+    """Many (psi, operator, Monte Carlo ensemble[, TDVP]) instances of uneven size in one
+    persistent sampling launch, with per-instance SR solves (this project's addition)."""
+
+    _destroy = "ann_batch_destroy"
+
+    def __init__(self, psis, operators, ensembles, tdvps=None, stream=None):
+        _Handle.__init__(self)
+        n = len(psis)
+        self._members = (list(psis), list(operators), list(ensembles), None if tdvps is None else list(tdvps))
+        arr = lambda objs: (ct.c_void_p * n)(*[o.handle.value for o in objs])
+        self.stream = stream
+        call("ann_batch_create", n, arr(psis), arr(operators), arr(ensembles),
+             None if tdvps is None else arr(tdvps), ct.byref(self._h))
+        self.n = n
+
+    def sample(self):
+        call("ann_batch_sample", self._h, stream_ptr(self.stream))
+
+    def energies(self):
+        out = cbuf(self.n)
+        call("ann_batch_energies", self._h, ptr(out))
+        return out
+
+    def sr_step(self, diag_shift, lr):
+        call("ann_batch_sr_step", self._h, float(diag_shift), float(lr), stream_ptr(self.stream))
+
+    def capture_sr_step(self, diag_shift, lr, stream):
+        call("ann_batch_graph_capture", self._h, float(diag_shift), float(lr), stream_ptr(stream))
+
+    def launch_sr_step(self, stream):
+        call("ann_batch_graph_launch", self._h, stream_ptr(stream))
+
+
+# ----------------------------------------------------------------------------------
 # free functions (main.cpp.template:495-540)
 def _nwords(psi):
     return 2 if psi.N > 64 else 1

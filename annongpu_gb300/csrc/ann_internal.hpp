@@ -150,6 +150,8 @@ struct ann_tdvp_impl {
     double w0 = 0.0;            // uniform row weight (Monte Carlo)
     bool have_S = false;
     unsigned graph_kernels = 0;
+    cudaStream_t side = nullptr;          // look-ahead panel stream of the Cholesky
+    cudaEvent_t side_ev[2] = {nullptr, nullptr};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
 };
@@ -202,6 +204,11 @@ void finalize_sdotv(cplx<double>* out, const cplx<double>* Obar, const cplx<doub
 void herk_simt(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, const double* weight_or_null,
                double w0, const cplx<double>* Obar, const Stats* stats, cplx<double>* S, cudaStream_t st);
 void herk_tc(ann_tdvp_impl& td, const double* weight_or_null, double w0, bool split, cudaStream_t st);
+
+// TDVP evaluation split for the batched path (capi.cu): buffers and sample targets,
+// then reductions and S from the sampled rows
+SampleTargets tdvp_prepare(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens);
+void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want_S, cudaStream_t st);
 
 // FP64 Cholesky SR solve (cholesky.cu)
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);

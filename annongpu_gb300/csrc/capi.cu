@@ -947,6 +947,9 @@ int ann_tdvp_destroy(ann_tdvp* t) {
         if(t) {
             if(t->graph_exec) cudaGraphExecDestroy(t->graph_exec);
             if(t->graph) cudaGraphDestroy(t->graph);
+            for(auto e : t->side_ev)
+                if(e) cudaEventDestroy(e);
+            if(t->side) cudaStreamDestroy(t->side);
         }
         delete t;
     });
@@ -958,47 +961,65 @@ int ann_tdvp_set_s_mode(ann_tdvp* t, int mode) {
     });
 }
 
-namespace {
-void tdvp_eval_impl(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, bool want_S, cudaStream_t st) {
-    need(t && op && psi && ens, "null argument");
-    need(t->Np == psi->Np, "TDVP num_params differs from psi.num_params");
-    const size_t rows = ens->num_steps();
-    const size_t ld = ld_for(psi->Np);
-    t->n_rows = rows;
-    t->ldO = ld;
-    t->O_precision = psi->precision;
-    t->O.ensure(rows * ld * psi->elem_bytes());
-    t->stats.ensure(sizeof(Stats));
-    t->Obar.ensure((size_t)psi->Np * 16);
-    t->F.ensure((size_t)psi->Np * 16);
-    mark(0, st);
-    run_ensemble(*psi, op, *ens, SampleTargets{&ens->rows, t->O.p, ld, true}, st);
-    mark(1, st);
-    const double* w = row_weights(*ens);
-    const double w0 = row_w0(*ens);
-    t->wts_exact = ens->kind == 0;
-    t->w0 = w0;
+}  // extern "C"
+
+namespace ann {
+
+SampleTargets tdvp_prepare(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens) {
+    if(t.Np != psi.Np) throw Error(ANN_ERR_INVALID, "TDVP num_params differs from psi.num_params");
+    const size_t rows = ens.num_steps();
+    const size_t ld = ld_for(psi.Np);
+    t.n_rows = rows;
+    t.ldO = ld;
+    t.O_precision = psi.precision;
+    t.O.ensure(rows * ld * psi.elem_bytes());
+    t.stats.ensure(sizeof(Stats));
+    t.Obar.ensure((size_t)psi.Np * 16);
+    t.F.ensure((size_t)psi.Np * 16);
+    return SampleTargets{&ens.rows, t.O.p, ld, true};
+}
+
+void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want_S, cudaStream_t st) {
+    const size_t rows = t.n_rows, ld = t.ldO;
+    const double* w = row_weights(ens);
+    const double w0 = row_w0(ens);
+    t.wts_exact = ens.kind == 0;
+    t.w0 = w0;
     if(w) {
-        t->wts.ensure(rows * sizeof(double));
-        ANN_CUDA(cudaMemcpyAsync(t->wts.p, w, rows * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        t.wts.ensure(rows * sizeof(double));
+        ANN_CUDA(cudaMemcpyAsync(t.wts.p, w, rows * sizeof(double), cudaMemcpyDeviceToDevice, st));
     }
-    const double* tw = w ? t->wts.as<double>() : nullptr;
-    row_stats(ens->rows, tw, w0, t->stats.as<Stats>(), t->partial, st);
-    col_stats(t->O.p, psi->precision, rows, ld, psi->Np, tw, w0, ens->rows.eloc.as<cplx<double>>(),
-              t->Obar.as<cplx<double>>(), t->F.as<cplx<double>>(), t->stats.as<Stats>(), nullptr, t->partial, st);
+    const double* tw = w ? t.wts.as<double>() : nullptr;
+    row_stats(ens.rows, tw, w0, t.stats.as<Stats>(), t.partial, st);
+    col_stats(t.O.p, psi.precision, rows, ld, psi.Np, tw, w0, ens.rows.eloc.as<cplx<double>>(),
+              t.Obar.as<cplx<double>>(), t.F.as<cplx<double>>(), t.stats.as<Stats>(), nullptr, t.partial, st);
     mark(2, st);
     if(want_S) {
-        t->S.ensure((size_t)psi->Np * psi->Np * 16);
-        if(t->s_mode == ANN_S_FP32 || psi->precision == 1)
-            herk_simt(t->O.p, psi->precision, rows, ld, psi->Np, tw, w0, t->Obar.as<cplx<double>>(),
-                      t->stats.as<Stats>(), t->S.as<cplx<double>>(), st);
+        t.S.ensure((size_t)psi.Np * psi.Np * 16);
+        if(t.s_mode == ANN_S_FP32 || psi.precision == 1)
+            herk_simt(t.O.p, psi.precision, rows, ld, psi.Np, tw, w0, t.Obar.as<cplx<double>>(),
+                      t.stats.as<Stats>(), t.S.as<cplx<double>>(), st);
         else
-            herk_tc(*t, tw, w0, t->s_mode == ANN_S_BF16_SPLIT, st);
-        t->have_S = true;
+            herk_tc(t, tw, w0, t.s_mode == ANN_S_BF16_SPLIT, st);
+        t.have_S = true;
     }
     mark(3, st);
 }
+
+}  // namespace ann
+
+namespace {
+void tdvp_eval_impl(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, bool want_S, cudaStream_t st) {
+    need(t && op && psi && ens, "null argument");
+    const SampleTargets tg = tdvp_prepare(*t, *psi, *ens);
+    mark(0, st);
+    run_ensemble(*psi, op, *ens, tg, st);
+    mark(1, st);
+    tdvp_post(*t, *psi, *ens, want_S, st);
+}
 }  // namespace
+
+extern "C" {
 
 int ann_tdvp_eval(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, void* stream) {
     return guard([&] { tdvp_eval_impl(t, op, psi, ens, true, S(stream)); });

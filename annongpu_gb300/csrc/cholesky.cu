@@ -240,20 +240,6 @@ __global__ void norm_ratio_kernel(const zc* __restrict__ r, const zc* __restrict
     }
 }
 
-struct Side {
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-};
-
-Side& side_stream() {
-    static thread_local Side s;
-    if(!s.stream) {
-        ANN_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
-        for(auto& e : s.ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
-    return s;
-}
-
 void panel(zc* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
     potrf_diag_kernel<<<1, NB * NB, 0, st>>>(A, n, kb, status);
     check_launch("potrf_diag_kernel");
@@ -269,8 +255,11 @@ void panel(zc* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
 // column of the trailing matrix (it holds panels k+1, k+2) is updated first; panel
 // k+1 is then factorised on a side stream while the rest of the trailing update of
 // step k runs, hiding the serial diagonal factorisation and panel solve.
-void cholesky(zc* A, unsigned n, unsigned* status, cudaStream_t st) {
-    Side& sd = side_stream();
+void cholesky(ann_tdvp_impl& td, zc* A, unsigned n, unsigned* status, cudaStream_t st) {
+    if(!td.side) {
+        ANN_CUDA(cudaStreamCreateWithFlags(&td.side, cudaStreamNonBlocking));
+        for(auto& e : td.side_ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
     panel(A, n, 0, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);
@@ -280,15 +269,15 @@ void cholesky(zc* A, unsigned n, unsigned* status, cudaStream_t st) {
         herk_update_kernel<<<tiles, 256, 0, st>>>(A, n, kb, nb, 1);
         check_launch("herk_update_kernel");
         // panel k+1 on the side stream, after the first-column update
-        ANN_CUDA(cudaEventRecord(sd.ev[0], st));
-        ANN_CUDA(cudaStreamWaitEvent(sd.stream, sd.ev[0], 0));
-        panel(A, n, kb + nb, status, sd.stream);
-        ANN_CUDA(cudaEventRecord(sd.ev[1], sd.stream));
+        ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
+        ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
+        panel(A, n, kb + nb, status, td.side);
+        ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
         if(tiles > 1) {
             herk_update_kernel<<<(tiles - 1) * tiles / 2, 256, 0, st>>>(A, n, kb, nb, 0);
             check_launch("herk_update_kernel");
         }
-        ANN_CUDA(cudaStreamWaitEvent(st, sd.ev[1], 0));
+        ANN_CUDA(cudaStreamWaitEvent(st, td.side_ev[1], 0));
     }
 }
 
@@ -323,7 +312,7 @@ void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st
     const zc* F = td.F.as<zc>();
     copy_shift_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(S, A, n, shift);
     check_launch("copy_shift_kernel");
-    cholesky(A, n, status, st);
+    cholesky(td, A, n, status, st);
     ANN_CUDA(cudaMemcpyAsync(x, F, n * sizeof(zc), cudaMemcpyDeviceToDevice, st));
     solve_in_place(A, n, x, st);
     // one step of iterative refinement against S + shift I

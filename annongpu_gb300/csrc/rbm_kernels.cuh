@@ -22,6 +22,7 @@ constexpr int kWarpsPerBlock = 8;
 template<typename T>
 struct RbmDev {
     unsigned N, M, Mpad, C, Np;
+    unsigned Uact;       // register slots in use (Mpad / 32 <= U)
     int layout;          // 0: params = W (PsiRBM), 1: params = [a | b | W] (PsiDeep)
     int a_in_log_psi;    // 1: log psi includes a.s
     int act;             // Activation
@@ -44,19 +45,21 @@ template<typename T, int NW, int U>
 __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
                                           const Conf<NW>& s, Lane<T, U>& L, int lane) {
 #pragma unroll
-    for(int u = 0; u < U; u++) L.th[u] = p.b[u * 32 + lane];
+    for(int u = 0; u < U; u++) L.th[u] = (unsigned)u < p.Uact ? p.b[u * 32 + lane] : mk<T>(T(0), T(0));
     for(unsigned i = 0; i < p.N; i++) {
         const T si = spin_bit(s, i) ? T(1) : T(-1);
         const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
 #pragma unroll
         for(int u = 0; u < U; u++) {
+            if((unsigned)u >= p.Uact) break;
             const cplx<T> w = row[u * 32];
             L.th[u].re += si * w.re;
             L.th[u].im += si * w.im;
         }
     }
 #pragma unroll
-    for(int u = 0; u < U; u++) L.ft[u] = p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0);
+    for(int u = 0; u < U; u++)
+        L.ft[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
 }
 
 // sum over the warp of fw_j (f(theta_j + dtheta_j) - f(theta_j)) for the sites in `sites`
@@ -74,6 +77,7 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
         const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
 #pragma unroll
         for(int u = 0; u < U; u++) {
+            if((unsigned)u >= p.Uact) break;
             const cplx<T> w = row[u * 32];
             dth[u].re += m2s * w.re;
             dth[u].im += m2s * w.im;
@@ -83,6 +87,10 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
     cplx<T> d = mk<T>(T(0), T(0));
 #pragma unroll
     for(int u = 0; u < U; u++) {
+        if((unsigned)u >= p.Uact) {
+            fnew[u] = mk<T>(T(0), T(0));
+            continue;
+        }
         fnew[u] = p.fw[u * 32 + lane] * act_f(L.th[u] + dth[u], p.act, 0);
         d += fnew[u] - L.ft[u];
     }
@@ -154,7 +162,8 @@ __device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ W
         cplx<T>* O = reinterpret_cast<cplx<T>*>(out.O) + row * out.ldO;
         cplx<T> g[U];
 #pragma unroll
-        for(int u = 0; u < U; u++) g[u] = p.fw[u * 32 + lane] * act_df(L.th[u], p.act, 0);
+        for(int u = 0; u < U; u++)
+            g[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_df(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
         unsigned off = 0;
         if(p.layout == 1) {
             for(unsigned i = lane; i < p.N; i += 32) O[i] = mk<T>(spin_bit(s, i) ? T(1) : T(-1), T(0));
@@ -190,26 +199,12 @@ __device__ __forceinline__ const cplx<T>* stage_Wd(const RbmDev<T>& p, int w_sme
     return smem;
 }
 
-// ---------------------------------------------------------------------------------
-// Metropolis sampler: one warp per chain.
+// One chain: thermalisation (when drawing fresh configurations), then per sample
+// the local sweeps, the learned independence moves, and the sample bookkeeping.
 template<typename T, int NW, int U>
-__global__ void __launch_bounds__(256)
-rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
-    // learned-proposal weights after Wd, then one H-float scratch per warp
-    const bool use_made = a.made.N != 0;
-    MadeSm ms{};
-    float* mh = nullptr;
-    if(use_made) {
-        unsigned char* mbase = smem_raw + (w_smem ? (((size_t)p.N * p.Mpad * sizeof(cplx<T>) + 15) & ~(size_t)15) : 0);
-        ms = made_stage(a.made, mbase);
-        mh = reinterpret_cast<float*>(mbase + made_smem_bytes(a.made.N, a.made.H)) + (threadIdx.x >> 5) * a.made.H;
-        __syncthreads();
-    }
-    const int lane = threadIdx.x & 31;
-    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if(chain >= a.n_chains) return;
+__device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op, int with_op,
+                         const McArgs& a, const SampleOut& out, unsigned chain, int lane, bool use_made,
+                         const MadeSm& ms, float* mh) {
     const unsigned N = p.N;
 
     Conf<NW> s;
@@ -376,6 +371,30 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
             atomicAdd(&a.acc_rej[3], m_rej);
         }
     }
+}
+
+
+// ---------------------------------------------------------------------------------
+// Metropolis sampler: one warp per chain.
+template<typename T, int NW, int U>
+__global__ void __launch_bounds__(256)
+rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
+    // learned-proposal weights after Wd, then one H-float scratch per warp
+    const bool use_made = a.made.N != 0;
+    MadeSm ms{};
+    float* mh = nullptr;
+    if(use_made) {
+        unsigned char* mbase = smem_raw + (w_smem ? (((size_t)p.N * p.Mpad * sizeof(cplx<T>) + 15) & ~(size_t)15) : 0);
+        ms = made_stage(a.made, mbase);
+        mh = reinterpret_cast<float*>(mbase + made_smem_bytes(a.made.N, a.made.H)) + (threadIdx.x >> 5) * a.made.H;
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if(chain >= a.n_chains) return;
+    mc_chain<T, NW, U>(p, Wd, op, with_op, a, out, chain, lane, use_made, ms, mh);
 }
 
 // ---------------------------------------------------------------------------------

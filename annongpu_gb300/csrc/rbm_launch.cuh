@@ -16,6 +16,7 @@ RbmDev<T> rbm_view(const ann_psi_impl& psi) {
     p.N = psi.N;
     p.M = psi.M;
     p.Mpad = psi.Mpad;
+    p.Uact = psi.Mpad / 32;
     p.C = psi.C;
     p.Np = psi.Np;
     p.layout = psi.layout;

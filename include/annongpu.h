@@ -38,6 +38,7 @@ typedef struct ann_op ann_op;
 typedef struct ann_ens ann_ens;
 typedef struct ann_tdvp ann_tdvp;
 typedef struct ann_made ann_made;
+typedef struct ann_batch ann_batch;
 
 const char* ann_last_error(void);
 int ann_version(void);
@@ -267,6 +268,25 @@ int ann_made_train(ann_made* m, const uint64_t* confs, unsigned n, unsigned step
 /* same, on the configurations the ensemble's chains produced (its history buffer if set) */
 int ann_made_train_on_samples(ann_made* m, const ann_ens* ens, unsigned steps, unsigned batch, double lr,
                               void* stream, double* loss);
+
+/* ---------------------------------------------------------------------------------
+ * Batched uneven instances (no counterpart in the reference, which runs one
+ * Hamiltonian per call): n (psi, op, Monte Carlo ensemble, TDVP) tuples; complex64
+ * RBM-family wavefunctions with N <= 64 and M <= 256, single-flip ensembles. One
+ * persistent launch samples every instance (device work queue, largest first);
+ * the per-instance S, FP64 Cholesky solves and updates run on a stream pool.
+ * ------------------------------------------------------------------------------ */
+int ann_batch_create(unsigned n, ann_psi** psis, ann_op** ops, ann_ens** enss, ann_tdvp** tdvps, ann_batch** out);
+int ann_batch_destroy(ann_batch* b);
+/* sampling + local energies (+ O rows for instances with a TDVP) of every instance */
+int ann_batch_sample(ann_batch* b, void* stream);
+/* <H> of every instance from its last samples (2 n doubles) */
+int ann_batch_energies(ann_batch* b, double* out);
+/* one SR step of every instance (sample, S, F, FP64 Cholesky solve, update) */
+int ann_batch_sr_step(ann_batch* b, double diag_shift, double lr, void* stream);
+/* capture the batched SR step as one CUDA graph (runs one eager step first); replay */
+int ann_batch_graph_capture(ann_batch* b, double diag_shift, double lr, void* stream);
+int ann_batch_graph_launch(ann_batch* b, void* stream);
 
 /* ---------------------------------------------------------------------------------
  * CUDA graph of a whole SR step (capture once, replay many)
