@@ -117,6 +117,7 @@ _SIGS = {
     "ann_tdvp_get_energy": ([P, P, P], I),
     "ann_tdvp_get_total_weight": ([P, P], I),
     "ann_tdvp_get_O_samples": ([P, P], I),
+    "ann_force_vector_noalloc": ([P, ct.c_size_t, ct.c_size_t, U, P, D, P, P, P, P, P], I),
     "ann_tdvp_S_dot_vector": ([P, P, P, P], I),
     "ann_tdvp_solve": ([P, D, P, P, P], I),
     "ann_sr_update": ([P, P, D, P], I),

@@ -234,6 +234,25 @@ int ann_tdvp_get_total_weight(ann_tdvp* tdvp, double* out);
 int ann_tdvp_get_O_samples(ann_tdvp* tdvp, double* out);
 /* S_dot_vector(vec, ens) (TDVP.cu.template:336-443), from the stored O samples */
 int ann_tdvp_S_dot_vector(ann_tdvp* tdvp, const double* vec, void* stream, double* out);
+/* E, <O> and F from caller-owned device arrays, allocating nothing. No counterpart in
+   the reference. It exists for callers that cannot call cudaMalloc at this point:
+   hosts whose allocator already owns the device memory (a raw cudaMalloc would fail or
+   fragment their pool), and latency-critical loops where an allocation could
+   synchronise the device. It computes what ann_tdvp_eval_F stores, with the same
+   definitions: E = sum_s w_s E_s, <O>_k = sum_s w_s O_sk,
+   F_k = sum_s w_s E_s conj(O_sk) - E conj(<O>_k).
+   Inputs (device pointers): O_rows n_rows x ld complex64 (row-major, ld >= num_params),
+   local_energies n_rows complex128, weights n_rows doubles or NULL for uniform_weight.
+   Outputs (device pointers): O_mean and F num_params complex128, energy 1 complex128
+   (may be NULL). Work is queued on `stream` (NULL = legacy default stream).
+   Scratch is a fixed 4 MiB device array inside the library, held on every GPU that
+   loads it until exit; num_params above 130,816 is rejected with ANN_ERR_INVALID.
+   The first call on a device looks up that array's address with the device current,
+   so make it before any stream capture. Every call shares the scratch: calls that
+   overlap on the GPU (other streams or host threads) race. */
+int ann_force_vector_noalloc(const void* O_rows, size_t n_rows, size_t ld, unsigned num_params,
+                             const double* weights, double uniform_weight, const double* local_energies,
+                             double* O_mean, double* F, double* energy, void* stream);
 /* SR solve: (S + shift I) delta = F by FP64 Cholesky on the GPU with one step of
    iterative refinement; writes delta (num_params complex) if out != NULL and the
    relative residuals before/after refinement to info2 if info2 != NULL. */
