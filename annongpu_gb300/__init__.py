@@ -12,7 +12,7 @@ from .expression import (PauliExpression, heisenberg_j1j2_2d, identity, sigma_x,
 from .json_numpy import NumpyDecoder, NumpyEncoder  # noqa: F401
 from .api import (MADE, Batch, ExactSummationSpins, ExpectationValue, MonteCarloLoop, MonteCarloSpins, Operator,  # noqa: F401
                   PsiCNN, PsiDeep, PsiRBM, Spins, TDVP, activation_function, apply_operator, log_psi, log_psi_batch,
-                  log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
+                  local_energies, log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
                   stop_profiling)
 from .builders import new_RBM, new_convolutional_network, new_deep_neural_network  # noqa: F401
 from ._lib import AnnError, launch_count  # noqa: F401

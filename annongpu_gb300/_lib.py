@@ -38,6 +38,7 @@ ACT_POLY, ACT_LOGCOSH = 0, 1
 PREC_FP32, PREC_FP64 = 0, 1
 MOVE_FLIP, MOVE_EXCHANGE_BONDS, MOVE_EXCHANGE_PAIRS = 0, 1, 2
 S_FP32, S_BF16, S_BF16_SPLIT = 0, 1, 2
+SOLVER_FP64, SOLVER_MIXED, SOLVER_FP32 = 0, 1, 2
 
 
 class RbmDesc(ct.Structure):
@@ -86,6 +87,7 @@ _SIGS = {
     "ann_ens_copy": ([P, P], I),
     "ann_ens_destroy": ([P], I),
     "ann_ens_num_steps": ([P, P], I),
+    "ann_ens_refresh_stats": ([P, P], I),
     "ann_ens_acceptance_rate": ([P, P], I),
     "ann_ens_get_chains": ([P, P, P], I),
     "ann_ens_set_chains": ([P, P, P], I),
@@ -98,6 +100,7 @@ _SIGS = {
     "ann_exp_sigma_z": ([P, P, P, P, P], I),
     "ann_log_psi_s": ([P, P, P], I),
     "ann_log_psi_batch": ([P, P, U, P, P], I),
+    "ann_local_energies": ([P, P, P, U, P, P], I),
     "ann_psi_O_k": ([P, P, P], I),
     "ann_psi_O_k_vector": ([P, P, P, P], I),
     "ann_log_psi": ([P, P, P, P], I),
@@ -119,6 +122,8 @@ _SIGS = {
     "ann_tdvp_get_O_samples": ([P, P], I),
     "ann_force_vector_noalloc": ([P, ct.c_size_t, ct.c_size_t, U, P, D, P, P, P, P, P], I),
     "ann_tdvp_S_dot_vector": ([P, P, P, P], I),
+    "ann_tdvp_set_solver": ([P, I, U, D], I),
+    "ann_tdvp_solver_info": ([P, P], I),
     "ann_tdvp_solve": ([P, D, P, P, P], I),
     "ann_sr_update": ([P, P, D, P], I),
     "ann_sr_step": ([P, P, P, P, D, D, P], I),

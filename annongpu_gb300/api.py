@@ -489,6 +489,11 @@ class MonteCarloSpins(_Handle):
         call("ann_ens_acceptance_rate", self._h, ptr(out))
         return float(out[0])
 
+    def refresh_stats(self, stream=None):
+        """Reads the acceptance counters of the last sampling pass and applies the learned
+        proposal's drop rule (TDVP evaluations and SR steps leave this to the caller)."""
+        call("ann_ens_refresh_stats", self._h, stream_ptr(stream))
+
     def get_chains(self):
         conf = np.zeros((self.num_markov_chains, 2), np.uint64)
         ctr = np.zeros(self.num_markov_chains, np.uint64)
@@ -663,6 +668,7 @@ class ExpectationValue:
 
 
 _S_MODES = {"fp32": L.S_FP32, "plain": L.S_FP32, "bf16": L.S_BF16, "bf16_split": L.S_BF16_SPLIT}
+_SOLVERS = {"fp64": L.SOLVER_FP64, "mixed": L.SOLVER_MIXED, "fp32": L.SOLVER_FP32}
 
 
 class TDVP(_Handle):
@@ -671,7 +677,8 @@ class TDVP(_Handle):
 
     _destroy = "ann_tdvp_destroy"
 
-    def __init__(self, num_params, gpu=True, *, s_mode="fp32", stream=None):
+    def __init__(self, num_params, gpu=True, *, s_mode="fp32", solver="fp64", max_iter=6, tol=1e-12,
+                 stream=None):
         _Handle.__init__(self)
         self.num_params = int(num_params)
         self.gpu = bool(gpu)
@@ -679,6 +686,23 @@ class TDVP(_Handle):
         self.stream = stream
         call("ann_tdvp_create", self.num_params, ct.byref(self._h))
         self.s_mode = s_mode
+        self.set_solver(solver, max_iter, tol)
+
+    def set_solver(self, solver="fp64", max_iter=6, tol=1e-12):
+        """SR solver: "fp64" (FP64 Cholesky + one refinement step), "mixed" (FP32
+        Cholesky + refinement with FP64 residuals until ||r||/||F|| <= tol, at most
+        max_iter FP32 solves; a stalled eager solve is redone in FP64) or "fp32" (one
+        FP32 Cholesky solve without refinement, the plain FP32 form)."""
+        call("ann_tdvp_set_solver", self._h, _SOLVERS[solver], int(max_iter), float(tol))
+        self.solver = solver
+
+    @property
+    def solver_info(self):
+        """{'solves', 'residual_first', 'residual_last', 'fell_back'} of the last SR solve."""
+        out = np.zeros(4)
+        call("ann_tdvp_solver_info", self._h, ptr(out))
+        return {"solves": int(out[0]), "residual_first": float(out[1]), "residual_last": float(out[2]),
+                "fell_back": bool(out[3])}
 
     @property
     def s_mode(self):
@@ -753,7 +777,8 @@ class TDVP(_Handle):
         return out
 
     def solve(self, diag_shift, return_info=False):
-        """delta = (S + diag_shift I)^{-1} F by FP64 Cholesky on the GPU (+1 refinement step)."""
+        """delta = (S + diag_shift I)^{-1} F on the GPU with the configured solver; info =
+        relative residuals ||F - (S + shift) delta|| / ||F|| of the first and final solution."""
         delta = cbuf(self.num_params)
         info = np.zeros(2)
         call("ann_tdvp_solve", self._h, float(diag_shift), stream_ptr(self.stream), ptr(delta), ptr(info))
@@ -842,6 +867,16 @@ def log_psi_batch(psi, confs) -> np.ndarray:
                                np.zeros(0, np.uint64))
     out = cbuf(len(confs))
     call("ann_log_psi_batch", psi.handle, ptr(arr), len(confs), None, ptr(out))
+    return out
+
+
+def local_energies(psi, operator, confs) -> np.ndarray:
+    """E_loc(s) of explicit configurations (ints, Spins or (n, 2) uint64 rows) on the device."""
+    rows = _conf_rows(confs)
+    nw = _nwords(psi)
+    arr = np.ascontiguousarray(rows[:, :nw])
+    out = cbuf(len(rows))
+    call("ann_local_energies", psi.handle, operator.handle, ptr(arr), len(rows), None, ptr(out))
     return out
 
 

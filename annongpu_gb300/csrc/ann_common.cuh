@@ -249,6 +249,7 @@ enum StatusBits : unsigned {
     kStatusNotPosDef = 2u,    // Cholesky pivot <= 0
     kStatusTimeout = 4u,      // a bounded device-side wait gave up
     kStatusBadInput = 8u,     // an index or size outside the checked bounds
+    kStatusSolveStalled = 16u,  // mixed-precision SR solve did not reach its tolerance
 };
 
 }  // namespace ann

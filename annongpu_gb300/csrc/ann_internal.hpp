@@ -143,6 +143,15 @@ struct ann_tdvp_impl {
     DevBuf S;                   // Np x Np complex128
     DevBuf L;                   // Cholesky factor (lower), Np x Np complex128
     DevBuf rhs, delta, resid;   // Np complex128
+    DevBuf tmp64;               // Np complex128: intermediate of the FP64 triangular solves
+    // SR solver: ANN_SOLVER_FP64 (FP64 Cholesky + one refinement step), ANN_SOLVER_MIXED
+    // (FP32 Cholesky + FP64 refinement to ir_tol, at most ir_max solves) or
+    // ANN_SOLVER_FP32 (one FP32 Cholesky solve, no refinement)
+    int solver = ANN_SOLVER_FP64;
+    unsigned ir_max = 6;
+    double ir_tol = 1e-12;
+    bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
+    DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
     DevBuf herk_in;             // BF16 operand for the tensor-core HERK
     DevBuf vec_in, vec_tmp;
     DevBuf wts;                 // per-row weights of the last eval (exact summation)
@@ -212,6 +221,13 @@ void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want
 
 // FP64 Cholesky SR solve (cholesky.cu)
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
+// mixed-precision SR solve (cholesky_mixed.cu); out4 = {solves, first and last
+// relative FP64 residual, stalled}
+void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double tol, bool pivots_to_status,
+                    unsigned* status_dev, cudaStream_t st);
+void mixed_solve_info(const ann_tdvp_impl& td, double* out4, cudaStream_t st);
+// the configured solver; an eager mixed solve that stalls is redone in FP64
+void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
 
 unsigned* status_word();

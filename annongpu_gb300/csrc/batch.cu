@@ -227,7 +227,7 @@ void batch_sr(ann_batch_impl& b, double shift, double lr, cudaStream_t st) {
         cudaStream_t s = b.streams[i % b.streams.size()];
         ann_tdvp_impl& t = *b.tdvps[i];
         tdvp_post(t, *b.psis[i], *b.enss[i], true, s);
-        sr_solve(t, shift, status_word(), s);
+        sr_solve_any(t, shift, status_word(), s);
         sr_update(*b.psis[i], t.delta.as<cplx<double>>(), lr, s);
     }
     for(size_t k = 0; k < b.streams.size(); k++) {

@@ -171,6 +171,21 @@ void need(bool ok, const char* msg) {
 
 cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// solves and residuals of the last SR solve (see ann_tdvp_solver_info)
+void solver_info(const ann_tdvp_impl& t, double* out4, cudaStream_t st) {
+    if(t.solver != ANN_SOLVER_FP64 && !t.fell_back && t.ir.p) {
+        mixed_solve_info(t, out4, st);
+        return;
+    }
+    double r[2] = {0.0, 0.0};
+    ANN_CUDA(cudaMemcpyAsync(r, t.resid.as<cplx<double>>() + 2 * t.Np, sizeof(r), cudaMemcpyDeviceToHost, st));
+    ANN_CUDA(cudaStreamSynchronize(st));
+    out4[0] = 1.0;
+    out4[1] = r[0];
+    out4[2] = r[1];
+    out4[3] = t.fell_back ? 1.0 : 0.0;
+}
+
 void sync(cudaStream_t st) { ANN_CUDA(cudaStreamSynchronize(st)); }
 
 void check_status() {
@@ -184,6 +199,7 @@ void check_status() {
         if(v & kStatusNotPosDef) m += " S + shift is not positive definite;";
         if(v & kStatusTimeout) m += " a bounded device wait timed out;";
         if(v & kStatusBadInput) m += " out-of-range index;";
+        if(v & kStatusSolveStalled) m += " mixed-precision SR solve did not converge;";
         throw Error(ANN_ERR_NUMERIC, m);
     }
 }
@@ -618,6 +634,13 @@ int ann_ens_num_steps(const ann_ens* e, unsigned* out) {
         *out = e->kind == 0 ? (unsigned)(1u << e->N) : e->num_samples;
     });
 }
+int ann_ens_refresh_stats(ann_ens* e, void* stream) {
+    return guard([&] {
+        need(e, "null argument");
+        mc_bookkeeping(*e, S(stream));
+    });
+}
+
 int ann_ens_acceptance_rate(const ann_ens* e, double* out) {
     return guard([&] {
         need(e && out, "null argument");
@@ -805,6 +828,23 @@ int ann_log_psi_batch(ann_psi* psi, const uint64_t* confs, unsigned n, void* str
         ANN_CUDA(cudaMemcpyAsync(sc.confs.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice, st));
         run_confs(*psi, nullptr, sc.confs.as<uint64_t>(), n, sc.rows2, nullptr, 0, st);
         ANN_CUDA(cudaMemcpyAsync(out, sc.rows2.log_psi.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        sync(st);
+        check_status();
+    });
+}
+
+int ann_local_energies(ann_psi* psi, ann_op* op, const uint64_t* confs, unsigned n, void* stream, double* out) {
+    return guard([&] {
+        need(psi && op && confs && out, "null argument");
+        auto& sc = scratch();
+        cudaStream_t st = S(stream);
+        std::vector<uint64_t> c((size_t)n * kMaxWords, 0);
+        for(unsigned k = 0; k < n; k++)
+            for(unsigned w = 0; w < psi->NW; w++) c[(size_t)k * kMaxWords + w] = confs[(size_t)k * psi->NW + w];
+        sc.confs.ensure(c.size() * 8);
+        ANN_CUDA(cudaMemcpyAsync(sc.confs.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice, st));
+        run_confs(*psi, op, sc.confs.as<uint64_t>(), n, sc.rows2, nullptr, 0, st);
+        ANN_CUDA(cudaMemcpyAsync(out, sc.rows2.eloc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
         sync(st);
         check_status();
     });
@@ -1111,13 +1151,38 @@ int ann_tdvp_solve(ann_tdvp* t, double shift, void* stream, double* delta_out, d
     return guard([&] {
         need(t && t->have_S, "S not evaluated");
         cudaStream_t st = S(stream);
-        sr_solve(*t, shift, status_word(), st);
+        sr_solve_any(*t, shift, status_word(), st);
         if(delta_out) ANN_CUDA(cudaMemcpyAsync(delta_out, t->delta.p, (size_t)t->Np * 16, cudaMemcpyDeviceToHost, st));
-        if(info2)
-            ANN_CUDA(cudaMemcpyAsync(info2, t->resid.as<cplx<double>>() + 2 * t->Np, 2 * sizeof(double),
-                                     cudaMemcpyDeviceToHost, st));
         sync(st);
         check_status();
+        if(info2) {
+            double info[4];
+            solver_info(*t, info, st);
+            info2[0] = info[1];
+            info2[1] = info[2];
+        }
+    });
+}
+
+int ann_tdvp_set_solver(ann_tdvp* t, int solver, unsigned max_iter, double tol) {
+    return guard([&] {
+        need(t, "null tdvp");
+        need(solver == ANN_SOLVER_FP64 || solver == ANN_SOLVER_MIXED || solver == ANN_SOLVER_FP32,
+             "unknown solver");
+        need(max_iter >= 1 && max_iter <= 64, "max_iter must be in [1, 64]");
+        need(tol > 0.0 && tol < 1.0, "tol must be in (0, 1)");
+        t->solver = solver;
+        t->ir_max = max_iter;
+        t->ir_tol = tol;
+    });
+}
+
+int ann_tdvp_solver_info(ann_tdvp* t, double* out4) {
+    return guard([&] {
+        need(t && out4, "null argument");
+        need(t->delta.p, "no solve yet");
+        ANN_CUDA(cudaDeviceSynchronize());
+        solver_info(*t, out4, nullptr);
     });
 }
 
@@ -1133,7 +1198,7 @@ int ann_sr_step(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, double shif
     return guard([&] {
         cudaStream_t st = S(stream);
         tdvp_eval_impl(t, op, psi, ens, true, st);
-        sr_solve(*t, shift, status_word(), st);
+        sr_solve_any(*t, shift, status_word(), st);
         mark(4, st);
         sr_update(*psi, t->delta.as<cplx<double>>(), lr, st);
         mark(5, st);
@@ -1169,7 +1234,7 @@ int ann_sr_graph_capture(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, do
         // one eager step sizes every buffer and validates the chains, so the
         // captured launches allocate nothing and bake in the steady-state arguments
         tdvp_eval_impl(t, op, psi, ens, true, st);
-        sr_solve(*t, shift, status_word(), st);
+        sr_solve_any(*t, shift, status_word(), st);
         sr_update(*psi, t->delta.as<cplx<double>>(), lr, st);
         sync(st);
         if(t->graph_exec) { cudaGraphExecDestroy(t->graph_exec); t->graph_exec = nullptr; }
@@ -1177,7 +1242,7 @@ int ann_sr_graph_capture(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, do
         ANN_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         try {
             tdvp_eval_impl(t, op, psi, ens, true, st);
-            sr_solve(*t, shift, status_word(), st);
+            sr_solve_any(*t, shift, status_word(), st);
             sr_update(*psi, t->delta.as<cplx<double>>(), lr, st);
         } catch(...) {
             cudaGraph_t g = nullptr;

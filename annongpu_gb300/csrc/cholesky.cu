@@ -152,9 +152,10 @@ __global__ void __launch_bounds__(256) herk_update_kernel(zc* __restrict__ A, un
 }
 
 // forward substitution step for block kb: warp 0 of every CTA solves L_kk y_k = b_k
-// (identically; lane j owns y_j), CTA 0 stores y_k, and all CTAs update the rows below.
+// (identically; lane j owns y_j), CTA 0 stores y_k into y_out (never into b, which
+// CTAs that start later still read), and all CTAs update the rows of b below.
 __global__ void __launch_bounds__(256) fwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
-                                                        zc* __restrict__ b) {
+                                                        zc* __restrict__ b, zc* __restrict__ y_out) {
     __shared__ zc y[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
     if(threadIdx.x < 32) {
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(256) fwd_block_kernel(const zc* __restrict__ L
         if(lane < nb) y[lane] = v;
     }
     __syncthreads();
-    if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = y[threadIdx.x];
+    if(blockIdx.x == 0 && threadIdx.x < nb) y_out[kb + threadIdx.x] = y[threadIdx.x];
     for(size_t i = kb + nb + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         zc acc = mk(0.0, 0.0);
         for(unsigned p = 0; p < nb; p++) cmac(acc, L[i * n + kb + p], y[p]);
@@ -178,9 +179,10 @@ __global__ void __launch_bounds__(256) fwd_block_kernel(const zc* __restrict__ L
     }
 }
 
-// backward substitution step for block kb with L^H (lane j owns x_j, last first)
+// backward substitution step for block kb with L^H (lane j owns x_j, last first);
+// x_k goes to x_out, the rows of b above the block are updated in place
 __global__ void __launch_bounds__(256) bwd_block_kernel(const zc* __restrict__ L, unsigned n, unsigned kb,
-                                                        zc* __restrict__ b) {
+                                                        zc* __restrict__ b, zc* __restrict__ x_out) {
     __shared__ zc x[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
     if(threadIdx.x < 32) {
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(256) bwd_block_kernel(const zc* __restrict__ L
         if(lane < nb) x[lane] = v;
     }
     __syncthreads();
-    if(blockIdx.x == 0 && threadIdx.x < nb) b[kb + threadIdx.x] = x[threadIdx.x];
+    if(blockIdx.x == 0 && threadIdx.x < nb) x_out[kb + threadIdx.x] = x[threadIdx.x];
     for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < kb; i += (size_t)gridDim.x * blockDim.x) {
         zc acc = mk(0.0, 0.0);
         for(unsigned q = 0; q < nb; q++) cmac_conj(acc, L[(size_t)(kb + q) * n + i], x[q]);
@@ -281,17 +283,18 @@ void cholesky(ann_tdvp_impl& td, zc* A, unsigned n, unsigned* status, cudaStream
     }
 }
 
-void solve_in_place(const zc* L, unsigned n, zc* b, cudaStream_t st) {
+// b <- (L L^H)^{-1} b; tmp (n entries) holds the intermediate y = L^{-1} b
+void solve_in_place(const zc* L, unsigned n, zc* b, zc* tmp, cudaStream_t st) {
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned below = n - kb - min((unsigned)NB, n - kb);
         const unsigned grid = below ? min(132u, (below + 255) / 256) : 1u;
-        fwd_block_kernel<<<grid, 256, 0, st>>>(L, n, kb, b);
+        fwd_block_kernel<<<grid, 256, 0, st>>>(L, n, kb, b, tmp);
         check_launch("fwd_block_kernel");
     }
     const unsigned last = ((n - 1) / NB) * NB;
     for(int kb = (int)last; kb >= 0; kb -= NB) {
         const unsigned grid = kb ? min(132u, ((unsigned)kb + 255) / 256) : 1u;
-        bwd_block_kernel<<<grid, 256, 0, st>>>(L, n, (unsigned)kb, b);
+        bwd_block_kernel<<<grid, 256, 0, st>>>(L, n, (unsigned)kb, tmp, b);
         check_launch("bwd_block_kernel");
     }
 }
@@ -304,7 +307,9 @@ void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st
     td.L.ensure(nn * sizeof(zc));
     td.delta.ensure(n * sizeof(zc));
     td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
+    td.tmp64.ensure(n * sizeof(zc));
     zc* A = td.L.as<zc>();
+    zc* tmp = td.tmp64.as<zc>();
     zc* x = td.delta.as<zc>();
     zc* r = td.resid.as<zc>();
     double* info = reinterpret_cast<double*>(r + 2 * n);
@@ -314,13 +319,13 @@ void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st
     check_launch("copy_shift_kernel");
     cholesky(td, A, n, status, st);
     ANN_CUDA(cudaMemcpyAsync(x, F, n * sizeof(zc), cudaMemcpyDeviceToDevice, st));
-    solve_in_place(A, n, x, st);
+    solve_in_place(A, n, x, tmp, st);
     // one step of iterative refinement against S + shift I
     residual_kernel<<<(n + 7) / 8, 256, 0, st>>>(S, n, shift, x, F, r);
     check_launch("residual_kernel");
     norm_ratio_kernel<<<1, 1024, 0, st>>>(r, F, n, info);
     check_launch("norm_ratio_kernel");
-    solve_in_place(A, n, r, st);
+    solve_in_place(A, n, r, tmp, st);
     axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, r, n);
     check_launch("axpy_kernel");
     residual_kernel<<<(n + 7) / 8, 256, 0, st>>>(S, n, shift, x, F, r + n);

@@ -1,18 +1,27 @@
-"""Benchmark of one SR step of the VMC inner loop on the 2-D TFIM 8x8 workload.
+"""Benchmark of the SR step of the VMC inner loop on the 2-D TFIM 8x8 workload,
+plain FP32 form against the precision form on the same GPU in the same run.
 
 Workload (square lattice 8 x 8, periodic, J = 1, h = 3.04): complex RBM with
 visible bias a(64), hidden bias b(128) and W(64 x 128), Np = 8384, entries
 iid N(0, 0.01^2) in real and imaginary parts (seeded). 16384 Markov chains,
-64 single-flip sweeps between samples, one sample per chain per SR step
-(N_s = 16384). One step = sampling + local energies + O rows + <O>, F +
-S (centred, BF16 tcgen05, FP32 accumulation) + FP64 Cholesky SR solve with one
-refinement step (diagonal shift 1e-3) + parameter update (lr 0.01).
+one sample per chain per SR step (N_s = 16384), diagonal shift 1e-3, lr 0.01.
+One step = sampling + local energies + O rows + <O>, F + S + solve + update.
+
+  plain:     64 single-flip sweeps between samples; S in FP32 (SIMT); one FP32
+             Cholesky solve.
+  precision: learned MADE independence moves between samples (N -> 256 -> N,
+             retrained every 10 SR steps on the last 65536 chain configurations,
+             Adam lr 1e-3, batch 4096; dropped below 10 % acceptance); S from centred
+             O in BF16 on tcgen05 with FP32 accumulation; FP32 Cholesky refined with
+             FP64 residuals against the FP64 S to ||r|| / ||F|| <= 1e-12.
 
 metric: effective samples/s with E_loc = N_s / tau_int / (seconds per SR step),
 tau_int from the Sokal automatic-window estimator (c = 5) on per-chain local
-energy series of a separate sampling run with the same parameters.
+energy series of a separate sampling run with the same moves and parameters.
+`value` is the precision form's; `forms` and `vs_plain` carry both forms.
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form precision|plain]
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--form both|precision|plain]
 """
 
 import argparse
@@ -43,6 +52,17 @@ THERM = 64
 SHIFT = 1e-3
 LR = 0.01
 SEED = 1234
+# learned proposal of the precision form: MADE N -> 256 -> N, Adam lr 1e-3, batch 4096,
+# retrained every 10 SR steps on the last 65536 chain configurations
+MADE_H = 256
+MADE_LR = 1e-3
+MADE_BATCH = 4096
+HISTORY = 65536
+RETRAIN_EVERY = 10
+MADE_FIRST_EPOCHS = 4
+LEARNED_SWEEPS = 0       # local sweeps between samples with the learned proposal on
+LEARNED_INDEP = 2        # learned independence moves per sample
+MIN_ACCEPT = 0.1         # the proposal is dropped below this acceptance
 
 
 def init_params(rng):
@@ -139,6 +159,156 @@ def peaks():
 
 
 # ----------------------------------------------------------------------------------
+class Form:
+    """One form of the SR step on the 8x8 workload.
+
+    plain:     complex64 sampling with single-flip Metropolis (64 sweeps between
+               samples), S in FP32 on SIMT cores, one FP32 Cholesky solve.
+    precision: complex64 sampling with learned MADE independence moves (retrained every
+               10 SR steps on the last 65536 chain configurations), S from centred O in
+               BF16 on tcgen05 (FP32 accumulation), FP32 Cholesky + refinement against
+               the FP64 S to ||r||/||F|| <= 1e-12 (FP64 Cholesky when it stalls)."""
+
+    def __init__(self, ann, name, rank):
+        self.ann, self.name = ann, name
+        rng = np.random.default_rng(SEED)
+        a, b, W = init_params(rng)
+        self.H = ann.transverse_field_ising_2d(L, L, h=H_FIELD)
+        self.op = ann.Operator(self.H)
+        self.psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+        self.Np = self.psi.num_params
+        self.rank = rank
+        self.made = None
+        self.retrain_ms = []
+        self.n_steps = 0
+        if name == "plain":
+            self.sweeps, self.indep = SWEEPS, 0
+            self.tdvp = ann.TDVP(self.Np, s_mode="fp32", solver="fp32")
+        else:
+            self.sweeps, self.indep = LEARNED_SWEEPS, LEARNED_INDEP
+            self.tdvp = ann.TDVP(self.Np, s_mode="bf16", solver="mixed", max_iter=6, tol=1e-12)
+            self.made = ann.MADE(N_SITES, MADE_H, seed=SEED + rank)
+        self.mc = self._ensemble(N_CHAINS, SEED + 17 * rank)
+
+    def _ensemble(self, n_samples, seed):
+        mc = self.ann.MonteCarloLoop(n_samples, self.sweeps, THERM, N_CHAINS, True, seed=seed, persistent=True)
+        if self.made is not None:
+            mc.set_history(HISTORY)
+        return mc
+
+    def prepare(self, stream):
+        """Thermalises the chains; the precision form fills its history with chain
+        configurations (local moves), trains the proposal and switches it on."""
+        self.tdvp.stream = stream
+        if self.made is None:
+            return
+        # first training set: 65536 configurations of thermalised chains, one local sweep apart
+        prep = self.ann.MonteCarloLoop(N_CHAINS, 1, THERM, N_CHAINS, True, seed=SEED + 5 + 17 * self.rank,
+                                       persistent=True)
+        prep.set_history(HISTORY)
+        ev = self.ann.ExpectationValue(stream=stream)
+        for _ in range((HISTORY + N_CHAINS - 1) // N_CHAINS):
+            ev(self.op, self.psi, prep)
+        self.made.train_on_samples(prep, steps=MADE_FIRST_EPOCHS * HISTORY // MADE_BATCH, batch=MADE_BATCH,
+                                   lr=MADE_LR, stream=stream)
+        self.mc.set_chains(*prep.get_chains())
+        self.mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=MIN_ACCEPT)
+
+    def retrain(self, stream):
+        import torch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        self.made.train_on_samples(self.mc, steps=HISTORY // MADE_BATCH, batch=MADE_BATCH, lr=MADE_LR,
+                                   stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        self.retrain_ms.append(e0.elapsed_time(e1))
+        self.mc.refresh_stats(stream)  # the drop rule for the learned proposal
+
+    def step(self, stream):
+        # the proposal is retrained every RETRAIN_EVERY SR steps after its first training
+        if self.made is not None and self.n_steps > 0 and self.n_steps % RETRAIN_EVERY == 0:
+            self.retrain(stream)
+        self.tdvp.sr_step(self.op, self.psi, self.mc, SHIFT, LR)
+        self.n_steps += 1
+
+    def tau(self):
+        """tau_int of the local energy from T samples per chain of a separate run with
+        the same moves (fresh chains, thermalised with local sweeps)."""
+        T = 24
+        mc = self.ann.MonteCarloLoop(N_CHAINS * T, self.sweeps, THERM, N_CHAINS, True, seed=SEED + 99,
+                                     persistent=True)
+        if self.made is not None:
+            mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=0.0)
+        self.ann.ExpectationValue()(self.op, self.psi, mc)
+        _, _, el = mc.samples()
+        acc = {"local": mc.acceptance_rate}
+        if self.made is not None:
+            acc["learned"] = mc.proposal_acceptance
+        return tau_int_sokal(el.real.reshape(T, N_CHAINS)), acc
+
+    def energy_check(self):
+        """Per-site energy of the last step's 16384 sample configurations with the current
+        parameters from the complex64 kernels of the step against the FP64 kernels (which
+        match the FP64 oracle to 1e-10) on the same configurations."""
+        conf, _, _ = self.mc.samples()
+        el32 = self.ann.local_energies(self.psi, self.op, conf)
+        psi64 = self.ann.PsiRBM(self.psi.W, 1.0, 0.0, True, a=self.psi.a, b=self.psi.b, precision="fp64")
+        psi64.params = self.psi.params
+        el64 = self.ann.local_energies(psi64, self.op, conf)
+        return {"energy_per_site": float(el32.real.mean() / N_SITES),
+                "abs_diff_per_site_vs_fp64": float(abs(el32.mean() - el64.mean()) / N_SITES),
+                "max_abs_diff_per_sample_per_site": float(np.abs(el32 - el64).max() / N_SITES)}
+
+
+def timed_steps(form, args, stream, dist):
+    import torch
+    import annongpu_gb300 as ann
+    if args.profile_window:
+        ann.start_profiling()  # ncu --profile-from-start off captures the timed steps only
+    lc0 = ann.launch_count()
+    ann._lib.call("ann_set_phase_timing", 1)
+    phase = np.zeros(5)
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(args.steps):
+        form.step(stream)
+        ph = np.zeros(5, np.float32)
+        ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
+        phase += ph
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
+    ann._lib.call("ann_set_phase_timing", 0)
+    if args.profile_window:
+        ann.stop_profiling()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = ann.launch_count() - lc0
+    return ms, phase / args.steps, launches
+
+
+def form_summary(form, ms, phase, tau, acc):
+    Ns = N_CHAINS
+    d = {"ms_per_step": ms, "sr_steps_per_s": 1e3 / ms,
+         "effective_samples_per_s": Ns / tau / (ms * 1e-3),
+         "sampler_effective_samples_per_s": Ns / tau / (phase[0] * 1e-3),
+         "tau_int": tau, "acceptance": acc,
+         "phase_ms": {"sample_eloc_O": phase[0], "reductions": phase[1], "S": phase[2], "solve": phase[3],
+                      "update": phase[4]},
+         "sweeps_between_samples": form.sweeps, "learned_moves_per_sample": form.indep}
+    if form.retrain_ms:
+        d["proposal_retrain_ms"] = float(np.mean(form.retrain_ms))
+    return d
+
+
 def run_ours(args):
     import torch
     import annongpu_gb300 as ann
@@ -150,113 +320,105 @@ def run_ours(args):
         td.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         ann.setDevice(torch.cuda.current_device())
-    rng = np.random.default_rng(SEED)
-    a, b, W = init_params(rng)
-    H = ann.transverse_field_ising_2d(L, L, h=H_FIELD)
-    op = ann.Operator(H)
-    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
-    s_mode = "bf16" if args.form == "precision" else "fp32"
-    mc = ann.MonteCarloLoop(N_CHAINS, SWEEPS, THERM, N_CHAINS, True, seed=SEED + 17 * rank, persistent=True)
-    tdvp = ann.TDVP(psi.num_params, s_mode=s_mode)
     st = torch.cuda.Stream()
-    tdvp.stream = st
-    Np = psi.num_params
-    Ns = N_CHAINS
-
-    # warm-up (the first step thermalises the chains)
-    for _ in range(args.warmup):
-        tdvp.sr_step(op, psi, mc, SHIFT, LR)
-    st.synchronize()
-
-    # timed region: eager steps, phase events on the launching stream
-    lc0 = ann.launch_count()
-    ann._lib.call("ann_set_phase_timing", 1)
-    phase = np.zeros(5)
+    results = {}
     clocks = ClockSampler()
-    clocks.start()
-    if dist:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(st)
-    for _ in range(args.steps):
-        tdvp.sr_step(op, psi, mc, SHIFT, LR)
-        ph = (np.zeros(5, np.float32))
-        ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
-        phase += ph
-    ev1.record(st)
-    torch.cuda.synchronize()
-    if dist:
-        torch.distributed.barrier()
-    clk = clocks.stop()
-    ann._lib.call("ann_set_phase_timing", 0)
-    launches_per_step = (ann.launch_count() - lc0) / args.steps
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    phase /= args.steps
-    E, _ = tdvp._energy()
+    clk = None
+    forms = ["plain", "precision"] if args.form == "both" else [args.form]
+    for name in forms:
+        f = Form(ann, name, rank)
+        f.prepare(st)
+        for _ in range(args.warmup):
+            f.step(st)
+        st.synchronize()
+        if name == "precision" or len(forms) == 1:
+            clocks.start()
+        ms, phase, launches = timed_steps(f, args, st, dist)
+        if name == "precision" or len(forms) == 1:
+            clk = clocks.stop()
+        f.mc.refresh_stats(st)
+        info = f.tdvp.solver_info
+        tau, acc = f.tau()
+        results[name] = (f, ms, phase, launches, tau, acc, info)
+
+    main = results["precision"] if "precision" in results else results[forms[0]]
+    f, ms, phase, launches, tau, acc, info = main
+    Np, Ns = f.Np, N_CHAINS
+    energy = f.energy_check()
+
+    # the same step with the FP64 Cholesky solver (and the solve error of the mixed solver)
+    fp64 = {}
+    if f.name == "precision":
+        d_mixed = f.tdvp.solve(SHIFT)
+        f.tdvp.set_solver("fp64")
+        d_fp64 = f.tdvp.solve(SHIFT)  # same S and F
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        f.step(st)
+        e1.record(st)
+        e1.synchronize()
+        f.tdvp.set_solver("mixed", 6, 1e-12)
+        fp64 = {"ms_per_step_fp64_cholesky": e0.elapsed_time(e1),
+                "solve_rel_err_vs_fp64_cholesky": float(np.linalg.norm(d_mixed - d_fp64) / np.linalg.norm(d_fp64))}
 
     # graph replay of the same step (captured once, replayed)
-    tdvp.capture_sr_step(op, psi, mc, SHIFT, LR, st)
+    f.tdvp.capture_sr_step(f.op, f.psi, f.mc, SHIFT, LR, st)
     st.synchronize()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record(st)
     for _ in range(args.steps):
-        tdvp.launch_sr_step(st)
+        f.tdvp.launch_sr_step(st)
     g1.record(st)
     st.synchronize()
     ms_graph = g0.elapsed_time(g1) / args.steps
 
-    # end to end through the public API: parameters from pinned host memory in,
-    # the step's energy out
-    host_params = torch.from_numpy(psi.params.view(np.float64).copy()).pin_memory()
+    # end to end through the public API: parameters from pinned host memory in, the
+    # step's energy out, every step
+    host_params = torch.from_numpy(f.psi.params.view(np.float64).copy()).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        psi.set_params_async(host_params, st)
-        tdvp.launch_sr_step(st)
-        E_now = tdvp.E_local  # device -> host read of the step's energy (synchronising)
+    for i in range(args.steps):
+        f.psi.set_params_async(host_params, st)
+        f.step(st)
+        _ = f.tdvp.E_local  # device -> host read of the step's energy (synchronising)
     st.synchronize()
     ms_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
 
-    # tau_int of the local energy, per-chain series 64 sweeps apart, same parameters
-    T = 24
-    mc_tau = ann.MonteCarloLoop(N_CHAINS * T, SWEEPS, THERM, N_CHAINS, True, seed=SEED + 99, persistent=True)
-    ann.ExpectationValue()(op, psi, mc_tau)
-    _, _, el = mc_tau.samples()
-    tau = tau_int_sokal(el.real.reshape(T, N_CHAINS))
-    acc = mc_tau.acceptance_rate
-
     pk, pk_kind = peaks()
     flops_S = 4.0 * Np * (Np + 1) * Ns  # algorithmic HERK count per step
-    achieved = flops_S / (phase[2] * 1e-3) / 1e12
-    peak = pk.get("bf16_tflops", 1900.0) if s_mode == "bf16" else None
-    value = Ns / tau / (ms * 1e-3)
-    e2e_value = Ns / tau / (ms_e2e * 1e-3)
+    s_tflops = flops_S / (phase[2] * 1e-3) / 1e12
+    summary = form_summary(f, ms, phase, tau, acc)
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 sampling / bf16 S (fp32 acc) / f64 solve" if s_mode == "bf16" else
-        "c64 sampling / fp32 S / f64 solve", "data": "synthetic (seeded random-init RBM, 2D TFIM)",
-        "config": config_dict(args.form),
+        "metric": METRIC, "value": summary["effective_samples_per_s"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("c64 sampling + learned proposal / bf16 S (fp32 acc) / fp32 Cholesky + f64 refinement"
+                  if f.name == "precision" else "c64 sampling / fp32 S / fp32 Cholesky"),
+        "data": "synthetic (seeded random-init RBM, 2D TFIM)",
+        "config": config_dict(f.name),
         "sr_steps_per_s": 1e3 / ms, "ms_per_step_graph": ms_graph, "tau_int": tau, "acceptance": acc,
-        "energy_per_site": E.real / N_SITES,
-        "phase_ms": {"sample_eloc_O": phase[0], "reductions": phase[1], "S": phase[2], "solve": phase[3],
-                     "update": phase[4]},
-        "roofline": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c)", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
-                     "peak_kind": pk_kind + " bf16 burst", "traffic": None,
+        "energy_per_site": energy["energy_per_site"], "energy_check": energy,
+        "phase_ms": summary["phase_ms"], "solver": info,
+        "roofline": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
+                     "achieved": s_tflops, "peak": pk.get("bf16_tflops", 1900.0) if f.name == "precision" else None,
+                     "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst", "traffic": None,
                      "work": "4*Np*(Np+1)*Ns real flops per step"},
         "clocks": clk,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": Np * 16, "d2h_bytes_per_step": 16,
-                "ms_per_step": ms_e2e},
-        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "e2e": {"value": Ns / tau / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": Np * 16,
+                "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e},
+        "gpu_launches": int(launches),
     }
+    if out["roofline"]["peak"]:
+        out["roofline"]["frac"] = s_tflops / out["roofline"]["peak"]
+    out.update(fp64)
+    out["forms"] = {name: form_summary(r[0], r[1], r[2], r[4], r[5]) for name, r in results.items()}
+    if "plain" in results and "precision" in results:
+        p, q = out["forms"]["plain"], out["forms"]["precision"]
+        out["vs_plain"] = {k: q[k] / p[k] for k in ("sr_steps_per_s", "effective_samples_per_s",
+                                                    "sampler_effective_samples_per_s")}
+        out["forms"]["plain"]["energy_check"] = results["plain"][0].energy_check()
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(a, b, W, H, tau, cores=1)
+        out["cpu_baseline"] = cpu_baseline(*init_params(np.random.default_rng(SEED)), f.H, tau, cores=1)
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -348,10 +510,10 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def run_profile_case():
+def run_profile_case(solver="fp64"):
     """Small case for ncu captures (a few GB at most, one SR step after one warm-up):
     N=32, M=64 complex RBM (Np = 2144), 1-D TFIM, 16384 chains, 4 sweeps between
-    samples, BF16 tensor-core S, FP64 Cholesky solve."""
+    samples, BF16 tensor-core S, SR solve by `solver` (fp64 / mixed / fp32)."""
     import annongpu_gb300 as ann
     rng = np.random.default_rng(0)
     N, M = 32, 64
@@ -361,7 +523,7 @@ def run_profile_case():
     psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
     op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
     mc = ann.MonteCarloLoop(16384, 4, 8, 16384, True, seed=1, persistent=True)
-    td = ann.TDVP(psi.num_params, s_mode="bf16")
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver=solver)
     for _ in range(2):
         td.sr_step(op, psi, mc, 1e-3, 0.01)
     print("profile case: E/N =", td.E_local / N)
@@ -370,15 +532,18 @@ def run_profile_case():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="precision", choices=["precision", "plain"])
+    ap.add_argument("--form", default="both", choices=["both", "precision", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
+    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32"])
+    ap.add_argument("--profile-window", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case()
+        run_profile_case(args.profile_solver)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -156,6 +156,10 @@ int ann_ens_destroy(ann_ens* ens);
 int ann_ens_num_steps(const ann_ens* ens, unsigned* out);
 /* acceptance_rate of the last sampling call (main.cpp.template:364-366) */
 int ann_ens_acceptance_rate(const ann_ens* ens, double* out);
+/* reads the acceptance counters of the last sampling pass (synchronising `stream`) and
+   applies the learned proposal's drop rule; the ExpectationValue family does this after
+   every call, TDVP eval / SR steps leave it to the caller (no per-step host round trip) */
+int ann_ens_refresh_stats(ann_ens* ens, void* stream);
 /* chain state (configurations num_markov_chains x num_words, Philox counters) */
 int ann_ens_get_chains(const ann_ens* ens, uint64_t* conf, uint64_t* counter);
 int ann_ens_set_chains(ann_ens* ens, const uint64_t* conf, const uint64_t* counter);
@@ -193,6 +197,9 @@ int ann_exp_sigma_z(ann_op* op, ann_psi* psi, ann_ens* ens, void* stream, double
 int ann_log_psi_s(ann_psi* psi, const uint64_t* conf, double* out2);
 /* batched log psi of explicit configurations (n x num_words) */
 int ann_log_psi_batch(ann_psi* psi, const uint64_t* confs, unsigned n, void* stream, double* out);
+/* local energies E_loc(s) = sum_n c_n <s|P_n|s'> psi(s')/psi(s) of explicit configurations
+   (n x num_words), the per-sample quantity of ExpectationValue (Operator.hpp:86-121) */
+int ann_local_energies(ann_psi* psi, ann_op* op, const uint64_t* confs, unsigned n, void* stream, double* out);
 /* psi_O_k(psi, Spins) (PsiOkVector.cu.template:40-74) */
 int ann_psi_O_k(ann_psi* psi, const uint64_t* conf, double* out);
 /* psi_O_k_vector(psi, esum): sum_s O_k(s), unweighted (PsiOkVector.cu.template:8-38) */
@@ -253,9 +260,30 @@ int ann_tdvp_S_dot_vector(ann_tdvp* tdvp, const double* vec, void* stream, doubl
 int ann_force_vector_noalloc(const void* O_rows, size_t n_rows, size_t ld, unsigned num_params,
                              const double* weights, double uniform_weight, const double* local_energies,
                              double* O_mean, double* F, double* energy, void* stream);
-/* SR solve: (S + shift I) delta = F by FP64 Cholesky on the GPU with one step of
-   iterative refinement; writes delta (num_params complex) if out != NULL and the
-   relative residuals before/after refinement to info2 if info2 != NULL. */
+/* SR solver selection (no counterpart in the reference, which has no solver;
+   TDVP.cu.template:181-302 leaves the solve to the caller).
+   ANN_SOLVER_FP64: FP64 Cholesky of S + shift I on the GPU, two triangular solves and
+     one step of iterative refinement (the default).
+   ANN_SOLVER_MIXED: FP32 Cholesky of S + shift I, then iterative refinement with the
+     residual F - (S + shift I) x formed in FP64 against the FP64 S, until
+     ||r|| / ||F|| <= tol or max_iter FP32 solves; converges to the FP64 answer when
+     cond(S + shift I) * 6e-8 < 1. An eager solve that does not converge (or whose FP32
+     factorisation meets a non-positive pivot) is redone with ANN_SOLVER_FP64; inside a
+     captured graph it raises ANN_ERR_NUMERIC at the next status check instead.
+   ANN_SOLVER_FP32: the FP32 factorisation and one FP32 solve, no refinement; its FP64
+     residual is still measured and reported by ann_tdvp_solver_info.
+   max_iter and tol apply to ANN_SOLVER_MIXED. */
+#define ANN_SOLVER_FP64 0
+#define ANN_SOLVER_MIXED 1
+#define ANN_SOLVER_FP32 2  /* one FP32 Cholesky solve, no refinement (the plain FP32 form) */
+int ann_tdvp_set_solver(ann_tdvp* tdvp, int solver, unsigned max_iter, double tol);
+/* after a solve: out4 = {FP32 solves used, relative FP64 residual after the first and
+   after the last solve, 1 if the FP64 solve replaced a stalled mixed solve}
+   (ANN_SOLVER_FP64: {1, residual before refinement, after, 0}) */
+int ann_tdvp_solver_info(ann_tdvp* tdvp, double* out4);
+/* SR solve: (S + shift I) delta = F on the GPU with the configured solver; writes delta
+   (num_params complex) if out != NULL and the relative residuals ||F - (S + shift I) x|| /
+   ||F|| of the first and the final solution to info2 if info2 != NULL. */
 int ann_tdvp_solve(ann_tdvp* tdvp, double diag_shift, void* stream, double* delta_out, double* info2);
 /* SR update: params <- params - lr * delta (device resident; re-derives kernel weights) */
 int ann_sr_update(ann_tdvp* tdvp, ann_psi* psi, double lr, void* stream);

@@ -1,0 +1,110 @@
+"""SR solvers on the GPU: the mixed-precision solve (FP32 Cholesky + refinement with
+FP64 residuals) against the FP64 oracle's S and F, against numpy on the GPU's own S
+at sizes with many 64-wide panels, against the FP64 Cholesky solve, its fallback when
+the refinement stalls, and inside a captured SR-step graph.
+
+Tolerances: the refined solution satisfies ||F - (S + shift) x|| / ||F|| <= 1e-12
+(checked on the device), so it agrees with numpy.linalg.solve to rtol 1e-8 at the
+condition numbers used here (shift 1e-3)."""
+
+import numpy as np
+import pytest
+
+from pyoracle import RbmDesc
+
+pytestmark = pytest.mark.gpu
+
+ann = pytest.importorskip("annongpu_gb300")
+
+
+def cplx(rng, shape, scale):
+    return scale * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+
+def test_mixed_solver_matches_oracle(oracle):
+    """Np = 12 + 24 + 288 = 324: five full 64-wide panels and a ragged one."""
+    N, M = 12, 24
+    rng = np.random.default_rng(3)
+    a, b, W = cplx(rng, N, 0.05), cplx(rng, M, 0.05), cplx(rng, (N, M), 0.12)
+    fw = np.ones(M, complex)
+    conn = np.array([[(j + i) % N for j in range(M)] for i in range(N)], np.uint32)
+    psi = ann.PsiDeep(N, a, [b], [conn], [W], fw, 0.0, True, precision="fp64")
+    es = ann.ExactSummationSpins(N)
+    psi.normalize(es)
+    ref_desc = RbmDesc(N, M, W, a=a, b=b, fw=fw, conn=conn, log_prefactor=psi.log_prefactor, layout=1)
+    H = ann.transverse_field_ising_1d(N, 1.0)
+    ref = oracle.exact(ref_desc, H)
+    td = ann.TDVP(psi.num_params, solver="mixed")
+    td.eval(ann.Operator(H), psi, es)
+    shift = 1e-3
+    want = np.linalg.solve(ref["tS"] + shift * np.eye(psi.num_params), ref["tF"])
+    delta, res = td.solve(shift, return_info=True)
+    info = td.solver_info
+    assert not info["fell_back"] and 1 <= info["solves"] <= 6, info
+    assert res[1] <= 1e-12 and info["residual_last"] <= 1e-12, (res, info)
+    np.testing.assert_allclose(delta, want, rtol=1e-8, atol=1e-9 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("N,M", [(32, 64), (24, 100)])
+def test_mixed_solver_matches_numpy_on_gpu_S(N, M):
+    """Monte Carlo S of a complex RBM with biases, Np = 2144 (34 panels) and
+    Np = 2524 (40 panels, ragged last panel), BF16 tensor-core S; the mixed solve
+    against numpy on the same S and against the FP64 Cholesky solve."""
+    rng = np.random.default_rng(N + M)
+    a, b, W = cplx(rng, N, 0.01), cplx(rng, M, 0.01), cplx(rng, (N, M), 0.01)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(4096, 2, 8, 4096, True, seed=11)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    td.eval(op, psi, mc)
+    S, F = td.S_matrix, td.F_vector
+    shift = 1e-3
+    want = np.linalg.solve(S + shift * np.eye(psi.num_params), F)
+    d_mixed = td.solve(shift)
+    info = td.solver_info
+    assert not info["fell_back"] and info["residual_last"] <= 1e-12, info
+    np.testing.assert_allclose(d_mixed, want, rtol=1e-8, atol=1e-9 * np.abs(want).max())
+    td.set_solver("fp64")
+    d_fp64 = td.solve(shift)
+    np.testing.assert_allclose(d_mixed, d_fp64, rtol=1e-8, atol=1e-9 * np.abs(d_fp64).max())
+
+
+def test_mixed_solver_stall_falls_back_to_fp64():
+    """One FP32 solve cannot reach a residual of 1e-15: the eager solve is redone
+    with the FP64 Cholesky and gives exactly its answer."""
+    N, M = 16, 32
+    rng = np.random.default_rng(1)
+    W = cplx(rng, (N, M), 0.05)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(2048, 2, 8, 1024, True, seed=2)
+    td = ann.TDVP(psi.num_params, solver="mixed", max_iter=1, tol=1e-15)
+    td.eval(op, psi, mc)
+    d1 = td.solve(1e-3)
+    assert td.solver_info["fell_back"]
+    td.set_solver("fp64")
+    d2 = td.solve(1e-3)
+    np.testing.assert_array_equal(d1, d2)
+
+
+def test_mixed_solver_graph_replay_equals_eager():
+    import torch
+    N, M = 16, 48
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    rng = np.random.default_rng(8)
+    W = cplx(rng, (N, M), 0.05)
+    p1 = ann.PsiRBM(W, 1.0, 0.0, True, precision="fp32")
+    p2 = ann.PsiRBM(W, 1.0, 0.0, True, precision="fp32")
+    mc1 = ann.MonteCarloSpins(1024 * 2, 2, 5, 1024, True, seed=5, persistent=True)
+    mc2 = ann.MonteCarloSpins(1024 * 2, 2, 5, 1024, True, seed=5, persistent=True)
+    st = torch.cuda.Stream()
+    t1 = ann.TDVP(p1.num_params, s_mode="bf16", solver="mixed", stream=st)
+    t2 = ann.TDVP(p2.num_params, s_mode="bf16", solver="mixed", stream=st)
+    t2.capture_sr_step(op, p2, mc2, 1e-3, 0.01, st)  # runs one eager step first
+    t1.sr_step(op, p1, mc1, 1e-3, 0.01)
+    for _ in range(3):
+        t1.sr_step(op, p1, mc1, 1e-3, 0.01)
+        t2.launch_sr_step(st)
+    st.synchronize()
+    assert not t1.solver_info["fell_back"] and t2.solver_info["residual_last"] <= 1e-12
+    np.testing.assert_array_equal(p1.params, p2.params)
