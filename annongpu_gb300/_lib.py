@@ -124,6 +124,7 @@ _SIGS = {
     "ann_tdvp_S_dot_vector": ([P, P, P, P], I),
     "ann_tdvp_set_solver": ([P, I, U, D], I),
     "ann_tdvp_solver_info": ([P, P], I),
+    "ann_tdvp_set_chol_update": ([P, I], I),
     "ann_tdvp_solve": ([P, D, P, P, P], I),
     "ann_sr_update": ([P, P, D, P], I),
     "ann_sr_step": ([P, P, P, P, D, D, P], I),

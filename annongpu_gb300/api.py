@@ -697,6 +697,16 @@ class TDVP(_Handle):
         self.solver = solver
 
     @property
+    def chol_update(self):
+        """Trailing update of the FP32 Cholesky: "tc" (tcgen05, split TF32) or "simt"."""
+        return getattr(self, "_chol_update", "tc")
+
+    @chol_update.setter
+    def chol_update(self, mode):
+        call("ann_tdvp_set_chol_update", self._h, {"simt": 0, "tc": 1}[mode])
+        self._chol_update = mode
+
+    @property
     def solver_info(self):
         """{'solves', 'residual_first', 'residual_last', 'fell_back'} of the last SR solve."""
         out = np.zeros(4)

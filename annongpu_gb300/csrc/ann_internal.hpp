@@ -152,6 +152,10 @@ struct ann_tdvp_impl {
     double ir_tol = 1e-12;
     bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
+    int chol_tc = 1;            // FP32 Cholesky trailing update: 1 tcgen05 (split TF32), 0 FP32 SIMT
+    DevBuf chol_pt;             // TF32 hi/lo panel operand of the tensor-core update
+    unsigned chol_pt_n = 0;
+    alignas(64) unsigned char chol_map[128];  // its TMA descriptor (CUtensorMap)
     DevBuf herk_in;             // BF16 operand for the tensor-core HERK
     DevBuf vec_in, vec_tmp;
     DevBuf wts;                 // per-row weights of the last eval (exact summation)
@@ -226,6 +230,13 @@ void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_
 void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double tol, bool pivots_to_status,
                     unsigned* status_dev, cudaStream_t st);
 void mixed_solve_info(const ann_tdvp_impl& td, double* out4, cudaStream_t st);
+// tensor-core trailing update of the FP32 Cholesky (chol_update_tc.cu)
+void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n);
+void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st);
+void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, bool col_only, unsigned* status,
+                    cudaStream_t st);
+// the look-ahead side stream of the Cholesky factorisations (high priority)
+void ensure_side_stream(ann_tdvp_impl& td);
 // the configured solver; an eager mixed solve that stalls is redone in FP64
 void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);

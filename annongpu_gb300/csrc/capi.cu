@@ -1177,6 +1177,14 @@ int ann_tdvp_set_solver(ann_tdvp* t, int solver, unsigned max_iter, double tol) 
     });
 }
 
+int ann_tdvp_set_chol_update(ann_tdvp* t, int mode) {
+    return guard([&] {
+        need(t, "null tdvp");
+        need(mode == ANN_CHOL_UPDATE_SIMT || mode == ANN_CHOL_UPDATE_TC, "unknown Cholesky update mode");
+        t->chol_tc = mode;
+    });
+}
+
 int ann_tdvp_solver_info(ann_tdvp* t, double* out4) {
     return guard([&] {
         need(t && out4, "null argument");

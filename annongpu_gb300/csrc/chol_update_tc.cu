@@ -1,0 +1,297 @@
+// Trailing update of the FP32 Cholesky on the tensor cores (tcgen05, kind::tf32):
+//   A22 -= X X^H,  X = the factorised panel (rows below it, 64 complex columns).
+//
+// X is split into TF32 hi and lo parts (x = hi + lo + O(2^-22 |x|)); three products
+// hi.hi + hi.lo + lo.hi restore FP32-level accuracy (the dropped lo.lo is below it),
+// so the factor keeps the quality that the FP64 refinement of the mixed solver needs.
+// chol_prep_tf32_kernel writes the operand PT, K-major: per 128-row block of the
+// trailing rows, [Re rows (128) ; Im rows (128)], each row [hi (64) | lo (64)] floats.
+// One CTA updates the 128 x 128 complex tile (I, J <= I) of the trailing matrix: per
+// K step of 32 TF32 values TMA brings the 256 x 32 blocks of I and J (128-byte
+// swizzle), one elected thread issues per 8-value slice
+//   D1 (TMEM cols   0..255) += Re_I . [Re_J ; Im_J]^T   (M = 128, N = 256)
+//   D2 (TMEM cols 256..511) += Im_I . [Re_J ; Im_J]^T
+// and since (X X^H)_ij = sum_p x_ip conj(x_jp):
+//   Re = D1[:, :128] + D2[:, 128:],  Im = D2[:, :128] - D1[:, 128:],
+// which four warps read back with tcgen05.ld and subtract from A (FP32, row-major).
+//
+// Every mbarrier wait is bounded (globaltimer deadline): a timeout raises
+// kStatusTimeout, all roles leave their loops, the producer waits (bounded) for its
+// copies in flight and the tensor memory is freed before the CTA returns.
+#include "ann_internal.hpp"
+#include "tcgen05.cuh"
+
+namespace ann {
+
+namespace {
+
+using namespace tc;
+using cf = cplx<float>;
+
+constexpr int kBM = 128;                   // tile side (complex rows / columns)
+constexpr int kRows = 2 * kBM;             // Re + Im rows of one 128-row block
+constexpr int kPanel = 64;                 // panel width (complex columns = K)
+constexpr int kRowFloats = 2 * kPanel;     // [hi | lo]
+constexpr int kBK = 32;                    // TF32 values per K step (128 bytes)
+constexpr int kStages = 3;
+constexpr int kStageBytes = 2 * kRows * kBK * 4;  // A block + B block
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr int kSegments = 3;               // hi.hi, hi.lo, lo.hi
+constexpr int kStepsPerSeg = kPanel / kBK;
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+    return __uint_as_float(u);
+}
+
+// PT rows for the trailing rows t0 .. t0 + 128 T (zero beyond n)
+__global__ void __launch_bounds__(256) chol_prep_tf32_kernel(const cf* __restrict__ A, unsigned n, unsigned kb,
+                                                             unsigned t0, unsigned T, float* __restrict__ PT) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t i = idx / kPanel;
+    const unsigned p = (unsigned)(idx % kPanel);
+    if(i >= (size_t)T * kBM) return;
+    const cf v = (t0 + i < n) ? A[(t0 + i) * n + kb + p] : mk(0.f, 0.f);
+    const size_t blk = i / kBM, r = i % kBM;
+    float* re = PT + (blk * kRows + r) * kRowFloats;
+    float* im = PT + (blk * kRows + kBM + r) * kRowFloats;
+    const float hr = tf32_rna(v.re), hi = tf32_rna(v.im);
+    re[p] = hr;
+    re[kPanel + p] = tf32_rna(v.re - hr);
+    im[p] = hi;
+    im[kPanel + p] = tf32_rna(v.im - hi);
+}
+
+struct UpdArgs {
+    cf* A;
+    unsigned n;
+    unsigned t0;        // first trailing row / column
+    int col_only;       // tiles (I, 0) only; otherwise tiles (I, J) with 1 <= J <= I
+    unsigned* status;
+};
+
+__global__ void __launch_bounds__(128, 1)
+chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, UpdArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* tail = base + kStages * kStageBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(tail);
+    uint64_t* empty = full + kStages;
+    uint64_t* done = empty + kStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned I, J;
+    if(a.col_only) {
+        I = blockIdx.x;
+        J = 0;
+    } else {
+        unsigned b = blockIdx.x;
+        I = 0;
+        while(b > I) { b -= I + 1; I++; }
+        J = b + 1;
+        I += 1;
+    }
+
+    if(threadIdx.x == 0) {
+        for(int s = 0; s < kStages; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncwarp();
+    if(warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    constexpr unsigned total = kSegments * kStepsPerSeg;
+    int issued = 0;
+    if(warp == 0 && lane == 0) {
+        // ---- TMA producer ----
+        for(unsigned kt = 0; kt < total; kt++) {
+            const int s = kt % kStages;
+            const unsigned ph = (kt / kStages) & 1u;
+            if(!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag, a.status)) break;
+            const unsigned seg = kt / kStepsPerSeg, k = kt % kStepsPerSeg;
+            const int xa = (int)(k * kBK + (seg == 2 ? kPanel : 0u));  // lo of I in segment lo.hi
+            const int xb = (int)(k * kBK + (seg == 1 ? kPanel : 0u));  // lo of J in segment hi.lo
+            unsigned char* sa = base + s * kStageBytes;
+            unsigned char* sb = sa + kRows * kBK * 4;
+            mbar_expect_tx(smem_u32(&full[s]), kStageBytes);
+            tma_load_2d(smem_u32(sa), &tmap, xa, (int)(I * kRows), smem_u32(&full[s]));
+            tma_load_2d(smem_u32(sb), &tmap, xb, (int)(J * kRows), smem_u32(&full[s]));
+            issued++;
+        }
+    } else if(warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        constexpr uint32_t idesc = idesc_tf32(128, 256);
+        bool ok = true;
+        for(unsigned kt = 0; kt < total && ok; kt++) {
+            const int s = kt % kStages;
+            const unsigned ph = (kt / kStages) & 1u;
+            if(!mbar_wait(smem_u32(&full[s]), ph, abort_flag, a.status)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(base + s * kStageBytes);
+            const uint32_t sb = sa + kRows * kBK * 4;
+#pragma unroll
+            for(int kk = 0; kk < kBK / 8; kk++) {
+                const int acc = (kt > 0 || kk > 0) ? 1 : 0;
+                const uint64_t db = sw128_desc(sb + kk * 32);
+                mma_tf32(tmem, sw128_desc(sa + kk * 32), db, idesc, acc);                    // Re_I rows
+                mma_tf32(tmem + 256, sw128_desc(sa + kBM * 128 + kk * 32), db, idesc, acc);  // Im_I rows
+            }
+            mma_commit(smem_u32(&empty[s]));
+        }
+        mma_commit(smem_u32(done));
+    }
+    __syncwarp();
+
+    // ---- epilogue: all four warps. TMEM lane = row of the tile: the result goes to
+    // shared memory (the drained stage buffers), then the warps update A row by row,
+    // each lane 4 consecutive complex values (coalesced 1 KB rows, 16 loads in flight)
+    bool ok = mbar_wait(smem_u32(done), 0, abort_flag, a.status) && !*abort_flag;
+    ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    cf (*C)[kBM + 1] = reinterpret_cast<cf (*)[kBM + 1]>(base);  // 128 x 129 complex = 132 KB
+    if(ok) {
+        const unsigned i = warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for(int c0 = 0; c0 < kBM; c0 += 16) {
+            float rr[16], ri[16], ir[16], ii[16];
+            tmem_ld16(lane_addr + c0, rr);
+            tmem_ld16(lane_addr + kBM + c0, ri);
+            tmem_ld16(lane_addr + 256 + c0, ir);
+            tmem_ld16(lane_addr + 256 + kBM + c0, ii);
+#pragma unroll
+            for(int q = 0; q < 16; q++) C[i][c0 + q] = mk(rr[q] + ii[q], ir[q] - ri[q]);
+        }
+    }
+    __syncthreads();
+    if(__syncthreads_and(ok ? 1 : 0)) {
+        const size_t row0 = (size_t)a.t0 + (size_t)I * kBM, col0 = (size_t)a.t0 + (size_t)J * kBM;
+        const unsigned jl0 = 4u * lane;
+        const size_t gj0 = col0 + jl0;
+        const bool diag = I == J;
+        constexpr int kRowsPerPass = 8;
+        for(unsigned r0 = warp * 32; r0 < warp * 32 + 32; r0 += kRowsPerPass) {
+            float4 v[kRowsPerPass][2];
+#pragma unroll
+            for(int rr = 0; rr < kRowsPerPass; rr++) {
+                const size_t gi = row0 + r0 + rr;
+                const float4* src = reinterpret_cast<const float4*>(a.A + gi * a.n + gj0);
+                if(gi < a.n && gj0 + 3 < a.n && (a.n & 1u) == 0) {
+                    v[rr][0] = src[0];
+                    v[rr][1] = src[1];
+                } else {
+                    v[rr][0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    v[rr][1] = v[rr][0];
+                    const cf* s1 = a.A + gi * a.n + gj0;
+                    if(gi < a.n) {
+                        if(gj0 < a.n) { v[rr][0].x = s1[0].re; v[rr][0].y = s1[0].im; }
+                        if(gj0 + 1 < a.n) { v[rr][0].z = s1[1].re; v[rr][0].w = s1[1].im; }
+                        if(gj0 + 2 < a.n) { v[rr][1].x = s1[2].re; v[rr][1].y = s1[2].im; }
+                        if(gj0 + 3 < a.n) { v[rr][1].z = s1[3].re; v[rr][1].w = s1[3].im; }
+                    }
+                }
+            }
+#pragma unroll
+            for(int rr = 0; rr < kRowsPerPass; rr++) {
+                const unsigned il = r0 + rr;
+                const size_t gi = row0 + il;
+                if(gi >= a.n) continue;
+                cf* dst = a.A + gi * a.n + gj0;
+                float out[8] = {v[rr][0].x, v[rr][0].y, v[rr][0].z, v[rr][0].w,
+                                v[rr][1].x, v[rr][1].y, v[rr][1].z, v[rr][1].w};
+#pragma unroll
+                for(int q = 0; q < 4; q++) {
+                    const cf c = C[il][jl0 + q];
+                    out[2 * q] -= c.re;
+                    out[2 * q + 1] -= c.im;
+                }
+                const bool full = gj0 + 3 < a.n && (a.n & 1u) == 0 && !(diag && jl0 + 3 > il);
+                if(full) {
+                    float4* d4 = reinterpret_cast<float4*>(dst);
+                    d4[0] = make_float4(out[0], out[1], out[2], out[3]);
+                    d4[1] = make_float4(out[4], out[5], out[6], out[7]);
+                } else {
+#pragma unroll
+                    for(int q = 0; q < 4; q++)
+                        if(gj0 + q < a.n && !(diag && jl0 + q > il)) dst[q] = mk(out[2 * q], out[2 * q + 1]);
+                }
+            }
+        }
+    }
+    if(!ok && warp == 0 && lane == 0) {
+        for(int q = issued > kStages ? issued - kStages : 0; q < issued; q++) {
+            const int s = q % kStages;
+            const unsigned long long t0 = gtime();
+            while(!mbar_try(smem_u32(&full[s]), (q / kStages) & 1u) && gtime() - t0 < kWaitNs) {}
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+}
+
+}  // namespace
+
+void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
+    const unsigned T = (n + kBM - 1) / kBM;
+    const size_t rows = (size_t)T * kRows;
+    const size_t bytes = rows * kRowFloats * sizeof(float);
+    if(td.chol_pt.bytes >= bytes && td.chol_pt_n == n) return;
+    td.chol_pt.ensure(bytes);
+    td.chol_pt_n = n;
+    const cuuint64_t dims[2] = {(cuuint64_t)kRowFloats, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(kRowFloats * sizeof(float))};
+    const cuuint32_t box[2] = {kBK, kRows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(td.chol_map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                   td.chol_pt.p, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
+    static bool attr = false;
+    if(!attr) {
+        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kSmemBytes));
+        attr = true;
+    }
+}
+
+// panel kb (64 columns, factorised, rows below it final) -> its TF32 hi/lo operand
+void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st) {
+    const unsigned t0 = kb + kPanel;
+    const unsigned m = n - t0;
+    const unsigned T = (m + kBM - 1) / kBM;
+    const size_t threads = (size_t)T * kBM * kPanel;
+    chol_prep_tf32_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A, n, kb, t0, T,
+                                                                             td.chol_pt.as<float>());
+    check_launch("chol_prep_tf32_kernel");
+}
+
+// A22 -= X X^H on tiles (I, 0) (col_only) or (I, J >= 1) of the trailing matrix of panel kb
+void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, bool col_only, unsigned* status,
+                    cudaStream_t st) {
+    const unsigned t0 = kb + kPanel;
+    const unsigned m = n - t0;
+    const unsigned T = (m + kBM - 1) / kBM;
+    const unsigned tiles = col_only ? T : T * (T - 1) / 2;
+    if(tiles == 0) return;
+    UpdArgs a{A, n, t0, col_only ? 1 : 0, status};
+    chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(*reinterpret_cast<const CUtensorMap*>(td.chol_map), a);
+    check_launch("chol_update_tc_kernel");
+}
+
+}  // namespace ann

@@ -258,10 +258,7 @@ void panel(zc* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
 // k+1 is then factorised on a side stream while the rest of the trailing update of
 // step k runs, hiding the serial diagonal factorisation and panel solve.
 void cholesky(ann_tdvp_impl& td, zc* A, unsigned n, unsigned* status, cudaStream_t st) {
-    if(!td.side) {
-        ANN_CUDA(cudaStreamCreateWithFlags(&td.side, cudaStreamNonBlocking));
-        for(auto& e : td.side_ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
+    ensure_side_stream(td);
     panel(A, n, 0, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);
@@ -300,6 +297,17 @@ void solve_in_place(const zc* L, unsigned n, zc* b, zc* tmp, cudaStream_t st) {
 }
 
 }  // namespace
+
+// The panel work of the look-ahead runs at the highest stream priority: the CTA
+// scheduler then starts it as soon as an SM frees up, ahead of the queued CTAs of
+// the trailing update it overlaps with.
+void ensure_side_stream(ann_tdvp_impl& td) {
+    if(td.side) return;
+    int lo = 0, hi = 0;
+    ANN_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    ANN_CUDA(cudaStreamCreateWithPriority(&td.side, cudaStreamNonBlocking, hi));
+    for(auto& e : td.side_ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
 
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st) {
     const unsigned n = td.Np;

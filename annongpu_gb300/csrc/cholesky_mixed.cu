@@ -20,6 +20,7 @@
 //
 // The reference has no solver (source/network_functions/TDVP.cu.template:181-302
 // builds S and F; the caller solves). This file is the project's own.
+#include <algorithm>
 #include <cmath>
 
 #include "ann_internal.hpp"
@@ -44,8 +45,11 @@ __global__ void cvt_shift_kernel(const zc* __restrict__ S, cf* __restrict__ A, u
     }
 }
 
-// Cholesky of the nb x nb diagonal block at (kb, kb) in shared memory, then the
-// inverse of the factor, column c by the 16 lanes of group c:
+// Cholesky of the nb x nb diagonal block at (kb, kb), then the inverse of the factor.
+// Factorisation (right-looking): thread t holds a[r][g + 16 m], m = 0..3, of row
+// r = t / 16 (g = t % 16) in registers; per column j the scaled column goes through
+// shared memory and every thread updates its own entries, two barriers per column.
+// Inverse, column c by the 16 lanes of group c:
 //   X[i][c] = (delta_ic - sum_{c <= p < i} L[i][p] X[p][c]) / L[i][i].
 // Dinv[blk] = L_kk^{-1}, DinvH[blk] = L_kk^{-H} (row-major NB x NB, identity
 // beyond nb).
@@ -55,39 +59,46 @@ __global__ void __launch_bounds__(1024) potrf32_kernel(cf* __restrict__ A, unsig
     extern __shared__ float4 smem_raw[];
     cf (*a)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(smem_raw);
     cf (*x)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(reinterpret_cast<cf*>(smem_raw) + NB * (NB + 1));
+    __shared__ cf col[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned tid = threadIdx.x;
-    for(unsigned t = tid; t < NB * NB; t += blockDim.x) {
-        const unsigned r = t / NB, c = t % NB;
+    const unsigned r = tid >> 4, g = tid & 15u;
+    cf e[4];
+#pragma unroll
+    for(int m = 0; m < 4; m++) {
+        const unsigned c = g + 16u * m;
         cf v = mk(0.f, 0.f);
         if(r < nb && c <= r) v = A[(size_t)(kb + r) * n + kb + c];
         else if(r == c) v = mk(1.f, 0.f);
-        a[r][c] = v;
-        x[r][c] = mk(0.f, 0.f);
+        e[m] = v;
     }
-    __syncthreads();
     for(unsigned j = 0; j < NB; j++) {
-        float d = a[j][j].re;
+        const unsigned gj = j & 15u, mj = j >> 4;
+        // the owners of column j publish it (rows >= j), scaled by 1 / sqrt(a[j][j])
+        if(g == gj && r >= j) col[r] = e[mj];
+        __syncthreads();
+        float d = col[j].re;
         if(!(d > 0.f) || !isfinite(d)) {
             if(tid == 0) atomicOr(status, kStatusNotPosDef);
             d = 1.f;
         }
-        const float sd = sqrtf(d);
-        __syncthreads();  // every thread has read the pivot before it changes
-        if(tid == j) a[j][j] = mk(sd, 0.f);
-        else if(tid > j && tid < NB) a[tid][j] = (1.f / sd) * a[tid][j];
-        __syncthreads();
-        for(unsigned t = tid; t < NB * NB; t += blockDim.x) {
-            const unsigned r = t / NB, c = t % NB;
-            if(c > j && c <= r) {
-                cf v = a[r][c];
-                cmac_conj(v, a[c][j], -a[r][j]);   // v -= a[r][j] conj(a[c][j])
-                a[r][c] = v;
-            }
+        const float inv = rsqrtf(d);
+        if(g == gj && r >= j) e[mj] = r == j ? mk(d * inv, 0.f) : inv * e[mj];
+        const cf lr = inv * col[r];
+#pragma unroll
+        for(int m = 0; m < 4; m++) {
+            const unsigned c = g + 16u * m;
+            if(c > j && c <= r) cmac_conj(e[m], col[c], -(inv * lr));  // -= l_rj conj(l_cj)
         }
         __syncthreads();
     }
-    // inverse: group g = tid / 16 owns column g (NB == 64 columns, 1024 threads)
+#pragma unroll
+    for(int m = 0; m < 4; m++) {
+        a[r][g + 16u * m] = e[m];
+        x[r][g + 16u * m] = mk(0.f, 0.f);
+    }
+    __syncthreads();
+    // inverse: group c = tid / 16 owns column c (NB == 64 columns, 1024 threads)
     {
         const unsigned c = tid >> 4, s = tid & 15u;
         const unsigned i0 = c & ~1u;  // both groups of a warp walk the same rows
@@ -110,10 +121,10 @@ __global__ void __launch_bounds__(1024) potrf32_kernel(cf* __restrict__ A, unsig
     __syncthreads();
     const size_t blk = kb / NB;
     for(unsigned t = tid; t < NB * NB; t += blockDim.x) {
-        const unsigned r = t / NB, c = t % NB;
-        if(r < nb && c <= r) A[(size_t)(kb + r) * n + kb + c] = a[r][c];
-        Dinv[blk * NB * NB + t] = x[r][c];
-        DinvH[blk * NB * NB + t] = conj(x[c][r]);
+        const unsigned rr = t / NB, c = t % NB;
+        if(rr < nb && c <= rr) A[(size_t)(kb + rr) * n + kb + c] = a[rr][c];
+        Dinv[blk * NB * NB + t] = x[rr][c];
+        DinvH[blk * NB * NB + t] = conj(x[c][rr]);
     }
 }
 
@@ -227,12 +238,12 @@ struct IrState {
     double last;     // ... after the last one
 };
 
-// y_k = Dk b_k for the diagonal block (Dk = Dinv or DinvH of block kb), by 8 warps,
-// output c by one warp with the 64-term dot split over lanes
+// y_k = Dk b_k for the diagonal block (Dk = Dinv or DinvH of block kb): output c by one
+// warp with the 64-term dot split over lanes
 __device__ __forceinline__ void block_apply(const cf* __restrict__ Dk, const cf* __restrict__ bk, cf* y,
                                             unsigned nb) {
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for(unsigned c = warp; c < NB; c += 8) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for(unsigned c = warp; c < NB; c += nw) {
         cf acc = mk(0.f, 0.f);
         cmac(acc, Dk[c * NB + lane], bk[lane]);
         cmac(acc, Dk[c * NB + lane + 32], bk[lane + 32]);
@@ -241,51 +252,133 @@ __device__ __forceinline__ void block_apply(const cf* __restrict__ Dk, const cf*
     }
 }
 
-// forward step of L y = b for block kb: y_k = L_kk^{-1} b_k (every CTA, redundantly),
-// CTA 0 stores it into y_out (b[kb:] is still read by CTAs that start later), all
-// CTAs subtract L[i][kb:] y_k from the rows of b below (one warp per row)
-__global__ void __launch_bounds__(256) fwd32_kernel(const cf* __restrict__ A, const cf* __restrict__ Dinv,
-                                                    unsigned n, unsigned kb, cf* __restrict__ b,
-                                                    cf* __restrict__ y_out, const IrState* st) {
-    if(st->done) return;
-    __shared__ cf bk[NB], y[NB];
-    const unsigned nb = min((unsigned)NB, n - kb);
-    if(threadIdx.x < NB) bk[threadIdx.x] = threadIdx.x < nb ? b[kb + threadIdx.x] : mk(0.f, 0.f);
-    __syncthreads();
-    block_apply(Dinv + (size_t)(kb / NB) * NB * NB, bk, y, nb);
-    __syncthreads();
-    if(blockIdx.x == 0 && threadIdx.x < nb) y_out[kb + threadIdx.x] = y[threadIdx.x];
-    const unsigned lane = threadIdx.x & 31;
-    const size_t warps = (size_t)gridDim.x * 8;
-    for(size_t i = kb + nb + (size_t)blockIdx.x * 8 + (threadIdx.x >> 5); i < n; i += warps) {
-        const cf* Li = A + i * n + kb;
-        cf acc = mk(0.f, 0.f);
-        if(lane < nb) cmac(acc, Li[lane], y[lane]);
-        if(lane + 32 < nb) cmac(acc, Li[lane + 32], y[lane + 32]);
-        acc = warp_sum(acc);
-        if(lane == 0) b[i] = b[i] - acc;
-    }
+// vectors that other CTAs of the solve update are read and written through L2
+__device__ __forceinline__ cf ld_l2(const cf* p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ void st_l2(cf* p, cf v) { __stcg(reinterpret_cast<float2*>(p), make_float2(v.re, v.im)); }
+
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
-// backward step of L^H x = y for block kb: x_k = L_kk^{-H} y_k into x_out, then every
-// row i < kb of b subtracts sum_p conj(L[kb + p][i]) x_p (thread per i, coalesced
-// along the block rows)
-__global__ void __launch_bounds__(256) bwd32_kernel(const cf* __restrict__ A, const cf* __restrict__ DinvH,
-                                                    unsigned n, unsigned kb, cf* __restrict__ b,
-                                                    cf* __restrict__ x_out, const IrState* st) {
-    if(st->done) return;
-    __shared__ cf bk[NB], x[NB];
-    const unsigned nb = min((unsigned)NB, n - kb);
-    if(threadIdx.x < NB) bk[threadIdx.x] = threadIdx.x < nb ? b[kb + threadIdx.x] : mk(0.f, 0.f);
+constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait on a ready flag
+constexpr int kSolveThreads = 512;
+
+// Waits (thread 0 of the CTA) until flag != 0. Bounded: after kWaitNs it raises
+// kStatusTimeout and the abort flag; every CTA of the solve then stops waiting.
+// Returns false when the solve is being abandoned.
+__device__ bool wait_flag(const int* flag, int* abort_flag, unsigned* status) {
+    __shared__ int ok;
+    if(threadIdx.x == 0) {
+        ok = 1;
+        const volatile int* vf = flag;
+        const volatile int* va = abort_flag;
+        const unsigned long long t0 = gtime();
+        while(*vf == 0) {
+            if(*va) { ok = 0; break; }
+            if(gtime() - t0 > kWaitNs) {
+                atomicExch(abort_flag, 1);
+                atomicOr(status, kStatusTimeout);
+                ok = 0;
+                break;
+            }
+        }
+        __threadfence();
+    }
     __syncthreads();
-    block_apply(DinvH + (size_t)(kb / NB) * NB * NB, bk, x, nb);
+    return ok != 0;
+}
+
+// publishes a block of the solution: the CTA's stores, then its ready flag
+__device__ __forceinline__ void set_flag(int* flag) {
+    __threadfence();
     __syncthreads();
-    if(blockIdx.x == 0 && threadIdx.x < nb) x_out[kb + threadIdx.x] = x[threadIdx.x];
-    for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < kb; i += (size_t)gridDim.x * blockDim.x) {
+    if(threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+// b <- (L L^H)^{-1} b in one cooperative launch without grid barriers. CTA g owns the
+// block rows j = g, g + G, ... (G CTAs, all resident). Forward: y_j = L_jj^{-1} (b_j -
+// sum_{k<j} L_jk y_k), adding each y_k as soon as its ready flag is set. Backward:
+// x_j = L_jj^{-H} (y_j - sum_{k>j} L_kj^H x_k), blocks taken from the last. Every
+// thread adds its contributions in a fixed order, so the result is bit-reproducible.
+// flags: [nblk] forward ready, [nblk] backward ready, [1] abort; zero on entry.
+__global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __restrict__ A,
+                                                                   const cf* __restrict__ Dinv,
+                                                                   const cf* __restrict__ DinvH, unsigned n, cf* b,
+                                                                   cf* y, const IrState* irs, int* flags,
+                                                                   unsigned* status) {
+    if(irs->done) return;
+    __shared__ cf v[NB], z[NB], red[8][NB];
+    const unsigned nblk = (n + NB - 1) / NB;
+    int* fwd_ready = flags;
+    int* bwd_ready = flags + nblk;
+    int* abort_flag = flags + 2 * nblk;
+    const unsigned t = threadIdx.x;
+    // forward: thread t sums row r = t / 8 of the block, columns 8 (t % 8) .. + 7 of each L_jk
+    for(unsigned j = blockIdx.x; j < nblk; j += gridDim.x) {
+        const unsigned jb = j * NB, nbj = min((unsigned)NB, n - jb);
+        const unsigned r = t >> 3, s8 = (t & 7u) * 8u;
         cf acc = mk(0.f, 0.f);
-#pragma unroll 8
-        for(unsigned q = 0; q < nb; q++) cmac_conj(acc, A[(size_t)(kb + q) * n + i], x[q]);
-        b[i] = b[i] - acc;
+        for(unsigned k = 0; k < j; k++) {
+            if(!wait_flag(fwd_ready + k, abort_flag, status)) return;
+            const unsigned kb = k * NB;
+            if(t < NB) v[t] = ld_l2(y + kb + t);
+            __syncthreads();
+            if(r < nbj) {
+                const cf* Lr = A + (size_t)(jb + r) * n + kb + s8;
+#pragma unroll
+                for(int q = 0; q < 8; q++) cmac(acc, Lr[q], v[s8 + q]);
+            }
+            __syncthreads();
+        }
+        // the 8 partial sums of row r are in lanes 8 (r % 4) .. + 7 of one warp
+#pragma unroll
+        for(int o = 4; o > 0; o >>= 1) {
+            acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+            acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+        }
+        if((t & 7u) == 0 && r < NB) v[r] = r < nbj ? b[jb + r] - acc : mk(0.f, 0.f);
+        __syncthreads();
+        block_apply(Dinv + (size_t)j * NB * NB, v, z, nbj);
+        __syncthreads();
+        if(t < nbj) st_l2(y + jb + t, z[t]);
+        set_flag(fwd_ready + j);
+    }
+    // backward: thread t sums column c = t % 64 of L_kj^H over rows q = 8 (t / 64) .. + 7
+    for(int jj = (int)nblk - 1 - (int)blockIdx.x; jj >= 0; jj -= (int)gridDim.x) {
+        const unsigned j = (unsigned)jj, jb = j * NB, nbj = min((unsigned)NB, n - jb);
+        const unsigned c = t & 63u, q8 = (t >> 6) * 8u;
+        cf acc = mk(0.f, 0.f);
+        for(unsigned k = nblk - 1; k > j; k--) {
+            if(!wait_flag(bwd_ready + k, abort_flag, status)) return;
+            const unsigned kb = k * NB, nbk = min((unsigned)NB, n - kb);
+            if(t < NB) v[t] = t < nbk ? ld_l2(b + kb + t) : mk(0.f, 0.f);
+            __syncthreads();
+            if(c < nbj) {
+#pragma unroll
+                for(int q = 0; q < 8; q++)
+                    if(q8 + q < nbk) cmac_conj(acc, A[(size_t)(kb + q8 + q) * n + jb + c], v[q8 + q]);
+            }
+            __syncthreads();
+        }
+        red[t >> 6][c] = acc;
+        // y_j is final once the forward pass published it
+        if(!wait_flag(fwd_ready + j, abort_flag, status)) return;
+        if(t < NB) {
+            cf sum = mk(0.f, 0.f);
+#pragma unroll
+            for(int g = 0; g < 8; g++) sum += red[g][t];
+            v[t] = t < nbj ? ld_l2(y + jb + t) - sum : mk(0.f, 0.f);
+        }
+        __syncthreads();
+        block_apply(DinvH + (size_t)j * NB * NB, v, z, nbj);
+        __syncthreads();
+        if(t < nbj) st_l2(b + jb + t, z[t]);
+        set_flag(bwd_ready + j);
     }
 }
 
@@ -394,12 +487,15 @@ void set_smem_attrs() {
     done = true;
 }
 
-// right-looking blocked Cholesky with look-ahead (the FP32 twin of cholesky.cu's)
+// Right-looking blocked Cholesky with look-ahead (the FP32 twin of cholesky.cu's):
+// after panel k the trailing update first covers the tile column holding panel k+1,
+// which the high-priority side stream then factorises while the rest of the update
+// runs. The update runs on the tensor cores (split TF32, 128 x 128 tiles) or on the
+// FP32 SIMT cores (64 x 64 tiles), as td.chol_tc selects.
 void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsigned* status, cudaStream_t st) {
-    if(!td.side) {
-        ANN_CUDA(cudaStreamCreateWithFlags(&td.side, cudaStreamNonBlocking));
-        for(auto& e : td.side_ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
+    ensure_side_stream(td);
+    const bool tc = td.chol_tc != 0;
+    if(tc) chol_update_tc_prepare(td, n);
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
     panel32(A, n, 0, Dinv, DinvH, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {
@@ -407,13 +503,20 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         const unsigned below = n - kb - nb;
         if(below == 0) break;
         const unsigned tiles = (below + UT - 1) / UT;
-        herk32_kernel<<<tiles, 256, herk_smem, st>>>(A, n, kb, nb, 1);
-        check_launch("herk32_kernel");
+        if(tc) {
+            chol_update_tc_panel(td, A, n, kb, st);
+            chol_update_tc(td, A, n, kb, true, status, st);
+        } else {
+            herk32_kernel<<<tiles, 256, herk_smem, st>>>(A, n, kb, nb, 1);
+            check_launch("herk32_kernel");
+        }
         ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
         ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
         panel32(A, n, kb + nb, Dinv, DinvH, status, td.side);
         ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
-        if(tiles > 1) {
+        if(tc) {
+            chol_update_tc(td, A, n, kb, false, status, st);
+        } else if(tiles > 1) {
             herk32_kernel<<<(tiles - 1) * tiles / 2, 256, herk_smem, st>>>(A, n, kb, nb, 0);
             check_launch("herk32_kernel");
         }
@@ -421,21 +524,34 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
     }
 }
 
-// b <- (L L^H)^{-1} b; tmp (n entries) holds y = L^{-1} b
+// b <- (L L^H)^{-1} b; tmp (n entries) holds y = L^{-1} b; flags (2 nblk + 1 ints) are
+// cleared before the launch
 void solve32(const cf* A, const cf* Dinv, const cf* DinvH, unsigned n, cf* b, cf* tmp, const IrState* irs,
-             cudaStream_t st) {
-    for(unsigned kb = 0; kb < n; kb += NB) {
-        const unsigned below = n - kb - min((unsigned)NB, n - kb);
-        const unsigned grid = below ? min(304u, (below + 7) / 8) : 1u;
-        fwd32_kernel<<<grid, 256, 0, st>>>(A, Dinv, n, kb, b, tmp, irs);
-        check_launch("fwd32_kernel");
+             int* flags, unsigned* status, cudaStream_t st) {
+    static int resident = 0;  // CTAs of trsv_flags_kernel that fit on the GPU at once
+    if(!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        ANN_CUDA(cudaGetDevice(&dev));
+        ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        ANN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_flags_kernel, kSolveThreads, 0));
+        if(per_sm < 1) throw Error(ANN_ERR_CUDA, "trsv_flags_kernel cannot be resident");
+        resident = sms * per_sm;
     }
-    const unsigned last = ((n - 1) / NB) * NB;
-    for(int kb = (int)last; kb >= 0; kb -= NB) {
-        const unsigned grid = kb ? min(304u, ((unsigned)kb + 255) / 256) : 1u;
-        bwd32_kernel<<<grid, 256, 0, st>>>(A, DinvH, n, (unsigned)kb, tmp, b, irs);
-        check_launch("bwd32_kernel");
-    }
+    const unsigned nblk = (n + NB - 1) / NB;
+    const unsigned grid = std::min<unsigned>(nblk, (unsigned)resident);
+    ANN_CUDA(cudaMemsetAsync(flags, 0, (2 * (size_t)nblk + 1) * sizeof(int), st));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident: the flag waits can be met
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ANN_CUDA(cudaLaunchKernelEx(&cfg, trsv_flags_kernel, A, Dinv, DinvH, n, b, tmp, irs, flags, status));
+    check_launch("trsv_flags_kernel");
 }
 
 }  // namespace
@@ -452,7 +568,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
     td.c32.ensure(2 * (size_t)n * sizeof(cf));
     const unsigned res_blocks = (n + 7) / 8;
-    td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double));
+    td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double) + (2 * (size_t)nblk + 2) * sizeof(int));
     cf* A = td.L32.as<cf>();
     cf* Dinv = td.Dinv32.as<cf>();
     cf* DinvH = Dinv + (size_t)nblk * NB * NB;
@@ -461,6 +577,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     cf* c = td.c32.as<cf>();
     IrState* irs = td.ir.as<IrState>();
     double* part = reinterpret_cast<double*>(irs + 1);
+    int* flags = reinterpret_cast<int*>(part + 2 * (size_t)res_blocks);
     const zc* S = td.S.as<zc>();
     const zc* F = td.F.as<zc>();
 
@@ -475,7 +592,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     // the FP64 fallback), or, with no refinement to fall back from, in the status word
     cholesky32(td, A, n, Dinv, DinvH, pivots_to_status ? status : &irs->notpd, st);
     for(unsigned it = 0; it < max_iter; it++) {
-        solve32(A, Dinv, DinvH, n, c, c + n, irs, st);
+        solve32(A, Dinv, DinvH, n, c, c + n, irs, flags, status, st);
         ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs);
         check_launch("ir_axpy_kernel");
         ir_residual_kernel<<<res_blocks, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs);

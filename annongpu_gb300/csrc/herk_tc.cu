@@ -25,10 +25,13 @@
 #include <cudaTypedefs.h>
 
 #include "ann_internal.hpp"
+#include "tcgen05.cuh"
 
 namespace ann {
 
 namespace {
+
+using namespace tc;
 
 constexpr int kBM = 128;                    // parameters per tile side
 constexpr int kRowsPerBlock = 2 * kBM;      // Re + Im rows of one parameter block
@@ -36,81 +39,6 @@ constexpr int kBK = 64;                     // samples per K step (128 bytes of 
 constexpr int kStages = 3;
 constexpr int kStageBytes = 2 * kRowsPerBlock * kBK * 2;  // A block + B block
 constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
-constexpr unsigned long long kWaitNs = 2000000000ull;     // 2 s per wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ unsigned long long gtime() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: returns false (and raises the abort flag) on timeout or abort
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, unsigned parity, volatile int* abort_flag,
-                                          unsigned* status) {
-    const unsigned long long t0 = gtime();
-    while(!mbar_try(bar, parity)) {
-        if(*abort_flag) return false;
-        if(gtime() - t0 > kWaitNs) {
-            *abort_flag = 1;
-            atomicOr(status, kStatusTimeout);
-            return false;
-        }
-    }
-    return true;
-}
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(dst), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-// instruction descriptor: kind::f16, A/B BF16, D FP32, both K-major, M x N
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for(int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
 struct HerkArgs {
     unsigned Np;            // parameters
     unsigned nblk;          // parameter blocks of 128
@@ -258,19 +186,27 @@ herk_prep_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned
                  double w0, const cplx<double>* __restrict__ Obar, const Stats* __restrict__ stats,
                  __nv_bfloat16* __restrict__ XT, size_t ldx, unsigned lo_offset, int split) {
     __shared__ cplx<float> tile[64][65];
+    __shared__ float sw[64];          // sqrt(w_s) of the tile's rows
+    __shared__ cplx<float> mu[64];    // Obar_k / W of the tile's columns
     const size_t s0 = (size_t)blockIdx.y * 64;
     const unsigned k0 = blockIdx.x * 64;
-    const double invW = 1.0 / stats->W;
+    if(threadIdx.x < 64) {
+        const size_t s = s0 + threadIdx.x;
+        sw[threadIdx.x] = s < rows ? (float)sqrt(wts ? wts[s] : w0) : 0.f;
+    } else if(threadIdx.x < 128) {
+        const unsigned c = threadIdx.x - 64, k = k0 + c;
+        mu[c] = k < Np ? cvt<float>((1.0 / stats->W) * Obar[k]) : mk(0.f, 0.f);
+    }
+    __syncthreads();
+    // per element in FP32: the centring and scaling feed BF16 operands
     for(int q = threadIdx.x; q < 64 * 64; q += 256) {
         const int r = q / 64, c = q % 64;
         const size_t s = s0 + r;
         const unsigned k = k0 + c;
         cplx<float> v = mk(0.f, 0.f);
         if(s < rows && k < Np) {
-            const double sw = sqrt(wts ? wts[s] : w0);
-            const cplx<double> o = cvt<double>(O[s * ld + k]);
-            const cplx<double> m = invW * Obar[k];
-            v = mk((float)(sw * (o.re - m.re)), (float)(sw * (o.im - m.im)));
+            const cplx<float> o = cvt<float>(O[s * ld + k]);
+            v = mk(sw[r] * (o.re - mu[c].re), sw[r] * (o.im - mu[c].im));
         }
         tile[r][c] = v;
     }
@@ -294,17 +230,6 @@ herk_prep_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if(!fn) {
-        cudaDriverEntryPointQueryResult q;
-        void* p = nullptr;
-        ANN_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-        if(q != cudaDriverEntryPointSuccess || !p) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
 
 }  // namespace
 

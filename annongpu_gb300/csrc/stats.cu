@@ -1,5 +1,7 @@
-// FP64 reductions over the sample rows: energy, variance, total weight, <O>, F,
-// S.v. Deterministic: fixed partitions, fixed-order combination, no atomics.
+// Reductions over the sample rows: energy, variance, total weight (FP64), <O>, F,
+// S.v (FP64 for complex128 O rows; FP32 within slabs of at most 512 rows and FP64
+// across slabs for complex64 O rows). Deterministic: fixed partitions, fixed-order
+// combination, no atomics.
 //
 // Reference semantics: TDVP::compute_averages (source/network_functions/
 // TDVP.cu.template:77-126) and its host post-processing (:293-301),
@@ -103,8 +105,64 @@ col_stats_kernel(const void* __restrict__ O, size_t rows, size_t ld, unsigned Np
     p[2] = as;
 }
 
+// complex64 O rows: FP32 accumulation over a slab of at most kSlab rows, FP64 across
+// slabs. The slab's weights are scaled by their maximum (exact-summation weights are
+// unnormalised |psi|^2 and may exceed the FP32 range); with `center` the energies are
+// centred, e - E/W, so the sum that becomes F does not cancel:
+//   F = sum w e conj(O) - E conj(Obar) = sum w (e - E/W) conj(O) + E (1/W - 1) conj(Obar).
+constexpr int kSlab = 512;
+
+__global__ void __launch_bounds__(256)
+col_stats_f32_kernel(const cplx<float>* __restrict__ O, size_t rows, size_t ld, unsigned Np, const double* __restrict__ wts,
+                     double w0, const cplx<double>* __restrict__ e, const Stats* __restrict__ center,
+                     cplx<double>* __restrict__ part, int want_sum, unsigned per) {
+    __shared__ float sw[kSlab];
+    __shared__ cplx<float> swe[kSlab];
+    __shared__ double red[8];
+    const size_t r0 = (size_t)blockIdx.y * per, r1 = min(rows, r0 + per);
+    const unsigned nr = (unsigned)(r1 - r0);
+    // slab scale: the largest weight of the slab
+    double wmax = 0.0;
+    for(unsigned t = threadIdx.x; t < nr; t += blockDim.x) wmax = fmax(wmax, wts ? wts[r0 + t] : w0);
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = wmax;
+    __syncthreads();
+    wmax = 0.0;
+    for(int w = 0; w < (int)(blockDim.x >> 5); w++) wmax = fmax(wmax, red[w]);
+    const double scale = wmax > 0.0 ? wmax : 1.0;
+    cplx<double> shift = mk(0.0, 0.0);
+    if(center && e) shift = (1.0 / center->W) * mk(center->E[0], center->E[1]);
+    for(unsigned t = threadIdx.x; t < nr; t += blockDim.x) {
+        const double wn = (wts ? wts[r0 + t] : w0) / scale;
+        sw[t] = (float)wn;
+        swe[t] = e ? cvt<float>(wn * (e[r0 + t] - shift)) : mk(0.f, 0.f);
+    }
+    __syncthreads();
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    if(k >= Np) return;
+    cplx<float> ao = mk(0.f, 0.f), af = mk(0.f, 0.f), as = mk(0.f, 0.f);
+    const cplx<float>* Ok = O + r0 * ld + k;
+#pragma unroll 8
+    for(unsigned t = 0; t < nr; t++) {
+        const cplx<float> o = Ok[(size_t)t * ld];
+        const float w = sw[t];
+        ao.re = fmaf(w, o.re, ao.re);
+        ao.im = fmaf(w, o.im, ao.im);
+        cmac_conj(af, o, swe[t]);  // += w (e - shift) conj(O)
+        as.re += o.re;
+        as.im += o.im;
+    }
+    cplx<double>* p = part + ((size_t)blockIdx.y * Np + k) * 3;
+    p[0] = scale * cvt<double>(ao);
+    p[1] = scale * cvt<double>(af);
+    p[2] = want_sum ? cvt<double>(as) : mk(0.0, 0.0);
+}
+
+// centred: the slab sums of F used centred energies (col_stats_f32_kernel with `center`)
 __global__ void col_stats_final(const cplx<double>* __restrict__ part, int nslab, unsigned Np,
-                                cplx<double>* Obar, cplx<double>* F, const Stats* center, cplx<double>* Osum) {
+                                cplx<double>* Obar, cplx<double>* F, const Stats* center, cplx<double>* Osum,
+                                int centred) {
     const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
     if(k >= Np) return;
     cplx<double> ao = mk(0.0, 0.0), af = mk(0.0, 0.0), as = mk(0.0, 0.0);
@@ -116,7 +174,11 @@ __global__ void col_stats_final(const cplx<double>* __restrict__ part, int nslab
     }
     if(Obar) Obar[k] = ao;
     if(F) {
-        if(center) af = af - mk(center->E[0], center->E[1]) * conj(ao);
+        if(center) {
+            const cplx<double> E = mk(center->E[0], center->E[1]);
+            if(centred) af = af + ((1.0 / center->W) - 1.0) * (E * conj(ao));
+            else af = af - E * conj(ao);
+        }
         F[k] = af;
     }
     if(Osum) Osum[k] = as;
@@ -169,21 +231,30 @@ void col_stats(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, c
                const cplx<double>* e, cplx<double>* Obar, cplx<double>* F, const Stats* center, cplx<double>* Osum,
                DevBuf& scratch, cudaStream_t st) {
     const unsigned cb = (Np + 255) / 256;
-    // enough slabs to fill the GPU, each at least 64 rows
+    // enough slabs to fill the GPU, each at least 64 rows (complex64: at most kSlab rows)
     unsigned slabs = (unsigned)((152u * 8u + cb - 1) / cb);
     const unsigned max_slabs = (unsigned)((rows + 63) / 64);
     if(slabs > max_slabs) slabs = max_slabs;
     if(slabs < 1) slabs = 1;
-    scratch.ensure((size_t)slabs * Np * 3 * sizeof(cplx<double>));
-    dim3 grid(cb, slabs);
-    if(O_prec == 0)
-        col_stats_kernel<float><<<grid, 256, 0, st>>>(O, rows, ld, Np, wts, w0, e, scratch.as<cplx<double>>(),
-                                                       Osum != nullptr);
-    else
-        col_stats_kernel<double><<<grid, 256, 0, st>>>(O, rows, ld, Np, wts, w0, e, scratch.as<cplx<double>>(),
-                                                        Osum != nullptr);
+    int centred = 0;
+    if(O_prec == 0) {
+        unsigned per = (unsigned)((rows + slabs - 1) / slabs);
+        if(per > (unsigned)kSlab) per = kSlab;
+        if(per < 1) per = 1;
+        slabs = (unsigned)((rows + per - 1) / per);
+        if(slabs < 1) slabs = 1;
+        scratch.ensure((size_t)slabs * Np * 3 * sizeof(cplx<double>));
+        col_stats_f32_kernel<<<dim3(cb, slabs), 256, 0, st>>>(reinterpret_cast<const cplx<float>*>(O), rows, ld, Np,
+                                                              wts, w0, e, center, scratch.as<cplx<double>>(),
+                                                              Osum != nullptr, per);
+        centred = center != nullptr && e != nullptr;
+    } else {
+        scratch.ensure((size_t)slabs * Np * 3 * sizeof(cplx<double>));
+        col_stats_kernel<double><<<dim3(cb, slabs), 256, 0, st>>>(O, rows, ld, Np, wts, w0, e,
+                                                                   scratch.as<cplx<double>>(), Osum != nullptr);
+    }
     check_launch("col_stats_kernel");
-    col_stats_final<<<cb, 256, 0, st>>>(scratch.as<cplx<double>>(), (int)slabs, Np, Obar, F, center, Osum);
+    col_stats_final<<<cb, 256, 0, st>>>(scratch.as<cplx<double>>(), (int)slabs, Np, Obar, F, center, Osum, centred);
     check_launch("col_stats_final");
 }
 

@@ -277,6 +277,12 @@ int ann_force_vector_noalloc(const void* O_rows, size_t n_rows, size_t ld, unsig
 #define ANN_SOLVER_MIXED 1
 #define ANN_SOLVER_FP32 2  /* one FP32 Cholesky solve, no refinement (the plain FP32 form) */
 int ann_tdvp_set_solver(ann_tdvp* tdvp, int solver, unsigned max_iter, double tol);
+/* trailing update of the FP32 Cholesky of ANN_SOLVER_MIXED / ANN_SOLVER_FP32:
+   ANN_CHOL_UPDATE_TC (default) on the tensor cores with split-TF32 products (tcgen05),
+   ANN_CHOL_UPDATE_SIMT on the FP32 SIMT cores */
+#define ANN_CHOL_UPDATE_SIMT 0
+#define ANN_CHOL_UPDATE_TC 1
+int ann_tdvp_set_chol_update(ann_tdvp* tdvp, int mode);
 /* after a solve: out4 = {FP32 solves used, relative FP64 residual after the first and
    after the last solve, 1 if the FP64 solve replaced a stalled mixed solve}
    (ANN_SOLVER_FP64: {1, residual before refinement, after, 0}) */

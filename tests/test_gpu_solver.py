@@ -45,10 +45,12 @@ def test_mixed_solver_matches_oracle(oracle):
     np.testing.assert_allclose(delta, want, rtol=1e-8, atol=1e-9 * np.abs(want).max())
 
 
+@pytest.mark.parametrize("update", ["tc", "simt"])
 @pytest.mark.parametrize("N,M", [(32, 64), (24, 100)])
-def test_mixed_solver_matches_numpy_on_gpu_S(N, M):
-    """Monte Carlo S of a complex RBM with biases, Np = 2144 (34 panels) and
-    Np = 2524 (40 panels, ragged last panel), BF16 tensor-core S; the mixed solve
+def test_mixed_solver_matches_numpy_on_gpu_S(N, M, update):
+    """Monte Carlo S of a complex RBM with biases, Np = 2144 (34 panels, 17 tensor-core
+    tiles per side) and Np = 2524 (40 panels, ragged last panel and tile), BF16
+    tensor-core S; the mixed solve with either trailing update of its FP32 Cholesky
     against numpy on the same S and against the FP64 Cholesky solve."""
     rng = np.random.default_rng(N + M)
     a, b, W = cplx(rng, N, 0.01), cplx(rng, M, 0.01), cplx(rng, (N, M), 0.01)
@@ -56,6 +58,7 @@ def test_mixed_solver_matches_numpy_on_gpu_S(N, M):
     op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
     mc = ann.MonteCarloLoop(4096, 2, 8, 4096, True, seed=11)
     td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    td.chol_update = update
     td.eval(op, psi, mc)
     S, F = td.S_matrix, td.F_vector
     shift = 1e-3

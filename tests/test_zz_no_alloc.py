@@ -3,8 +3,10 @@ static scratch, no allocation) called through the C ABI, against ann_tdvp_eval_F
 the same samples, on two calls in a row: the second call has fewer rows and fewer
 parameters than the first, so stale scratch from the first call would show.
 
-Tolerance: both paths accumulate in FP64 in different orders; rtol 1e-10 of the
-largest entry, as for the other FP64-accumulated quantities.
+Tolerance: the energy is an FP64 sum in both paths (rtol 1e-10). For <O> and F the
+no-allocation path accumulates the complex64 rows in FP64, while ann_tdvp_eval_F
+accumulates them in FP32 within slabs of at most 512 rows (FP64 across slabs), so they
+agree to rtol 2e-5 of the largest entry, the bound used for FP32-accumulated sums.
 """
 
 import ctypes as ct
@@ -58,9 +60,9 @@ def call_noalloc(Np, O, el, ld, weights):
     return d_Om.cpu().numpy(), d_F.cpu().numpy(), complex(d_E.cpu().numpy()[0])
 
 
-def close(got, want):
+def close(got, want, rtol):
     scale = np.abs(want).max()
-    assert np.abs(got - want).max() <= 1e-10 * scale + 1e-300, (np.abs(got - want).max(), scale)
+    assert np.abs(got - want).max() <= rtol * scale + 1e-300, (np.abs(got - want).max(), scale)
 
 
 def test_noalloc_force_vector_matches_eval_F_two_calls():
@@ -72,9 +74,9 @@ def test_noalloc_force_vector_matches_eval_F_two_calls():
     n2 = O2.shape[0]
     Om2, F2, E2 = call_noalloc(Np2, O2, el2, ld=Np2, weights=np.full(n2, 1.0 / n2))
     for Om, F, E, td in ((Om1, F1, E1, td1), (Om2, F2, E2, td2)):
-        close(Om, td.O_k_vector)
-        close(F, td.F_vector)
-        close(np.array([E]), np.array([td.E_local]))
+        close(Om, td.O_k_vector, 2e-5)
+        close(F, td.F_vector, 2e-5)
+        close(np.array([E]), np.array([td.E_local]), 1e-10)
 
 
 def test_noalloc_rejects_num_params_beyond_scratch():
