@@ -14,6 +14,7 @@ from .api import (MADE, Batch, ExactSummationSpins, ExpectationValue, MonteCarlo
                   PsiCNN, PsiDeep, PsiRBM, Spins, TDVP, activation_function, apply_operator, log_psi, log_psi_batch,
                   local_energies, log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
                   stop_profiling)
+from .api import autotune, load_tuning, save_tuning, set_tuning, tuning_table  # noqa: F401
 from .builders import new_RBM, new_convolutional_network, new_deep_neural_network  # noqa: F401
 from ._lib import AnnError, launch_count  # noqa: F401
 

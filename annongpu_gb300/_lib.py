@@ -125,6 +125,11 @@ _SIGS = {
     "ann_tdvp_set_solver": ([P, I, U, D], I),
     "ann_tdvp_solver_info": ([P, P], I),
     "ann_tdvp_set_chol_update": ([P, I], I),
+    "ann_autotune": ([P, P, P, P, D, P, P, U, P], I),
+    "ann_tuning_set": ([ct.c_char_p, I], I),
+    "ann_tuning_get": ([ct.c_char_p, P, P], I),
+    "ann_tuning_dump": ([ct.c_char_p, ct.c_size_t, P], I),
+    "ann_tuning_clear": ([], I),
     "ann_tdvp_solve": ([P, D, P, P, P], I),
     "ann_sr_update": ([P, P, D, P], I),
     "ann_sr_step": ([P, P, P, P, D, D, P], I),

@@ -934,6 +934,65 @@ def activation_function(z, layer=0, activation="poly") -> complex:
     return complex(out[0], out[1])
 
 
+# ----------------------------------------------------------------------------------
+# autotuner (tuning.cu; this project's addition)
+_KNOBS = {0: "rbm_mc.wpb", 1: "stats.slab", 2: "chol.update"}
+
+
+def autotune(operator, psi, ensemble, tdvp, diag_shift=1e-3, stream=None):
+    """Times the candidates of every launch / tile knob on this workload and keeps the
+    fastest in the tuning table (sampler warps per CTA, reduction slab rows, Cholesky
+    trailing update). Returns {knob: {candidate: median ms}}."""
+    rep = np.zeros(3 * 32)
+    n = ct.c_uint()
+    call("ann_autotune", tdvp.handle, operator.handle, psi.handle, ensemble.handle, float(diag_shift),
+         stream_ptr(stream), ptr(rep), 32, ct.byref(n))
+    out = {}
+    for k in range(min(n.value, 32)):
+        knob, cand, ms = rep[3 * k: 3 * k + 3]
+        out.setdefault(_KNOBS[int(knob)], {})[int(cand)] = float(ms)
+    return out
+
+
+def tuning_table() -> dict:
+    """The tuning table: {"dev<ordinal>/<knob>/<shape>": value}."""
+    need = ct.c_size_t()
+    call("ann_tuning_dump", None, 0, ct.byref(need))
+    buf = ct.create_string_buffer(need.value + 1)
+    call("ann_tuning_dump", buf, need.value + 1, ct.byref(need))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        k, v = line.rsplit(" ", 1)
+        out[k] = int(v)
+    return out
+
+
+def set_tuning(table: dict, clear=False):
+    if clear:
+        call("ann_tuning_clear")
+    for k, v in table.items():
+        call("ann_tuning_set", k.encode(), int(v))
+
+
+def save_tuning(path):
+    import json
+    import torch
+    with open(path, "w") as f:
+        json.dump({"device": torch.cuda.get_device_name(), "table": tuning_table()}, f, indent=1)
+
+
+def load_tuning(path):
+    """Loads a table saved by save_tuning; entries tuned on another GPU model are ignored."""
+    import json
+    import torch
+    with open(path) as f:
+        d = json.load(f)
+    if d.get("device") == torch.cuda.get_device_name():
+        set_tuning(d["table"])
+        return True
+    return False
+
+
 def setDevice(device: int):
     call("ann_set_device", int(device))
 

@@ -153,6 +153,7 @@ struct ann_tdvp_impl {
     bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
     int chol_tc = 1;            // FP32 Cholesky trailing update: 1 tcgen05 (split TF32), 0 FP32 SIMT
+    bool chol_tc_set = false;   // chosen explicitly (ann_tdvp_set_chol_update): the tuning table is not read
     DevBuf chol_pt;             // TF32 hi/lo panel operand of the tensor-core update
     unsigned chol_pt_n = 0;
     alignas(64) unsigned char chol_map[128];  // its TMA descriptor (CUtensorMap)
@@ -242,6 +243,15 @@ void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStr
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
 
 unsigned* status_word();
+::ann_ens* ens_clone(const ann_ens_impl& src);  // capi.cu (release with ann_ens_destroy)
+
+// ---- tuning table (tuning.cu): launch and tile choices per device and shape ----
+// key: "<knob>/<shape>"; absent keys fall back to the built-in default
+int tuning_get(const std::string& key, int dflt);
+void tuning_set(const std::string& key, int value);
+std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens);
+std::string key_slab(size_t rows, unsigned Np);
+std::string key_chol_update(unsigned n);
 
 // PsiCNN (cnn.cu)
 void cnn_prepare(ann_psi_impl& psi, cudaStream_t st);

@@ -68,6 +68,43 @@ unsigned* status_word() {
     return p;
 }
 
+// copy of an ensemble: sizes, moves, chain state (configurations and Philox
+// counters) and the learned proposal; not the sample rows, tape or history
+::ann_ens* ens_clone(const ann_ens_impl& src) {
+    auto* e = new ann_ens();
+    try {
+        e->kind = src.kind;
+        e->N = src.N;
+        e->num_samples = src.num_samples;
+        e->num_sweeps = src.num_sweeps;
+        e->num_therm = src.num_therm;
+        e->n_chains = src.n_chains;
+        e->move = src.move;
+        e->n_up = src.n_up;
+        e->persistent = src.persistent;
+        e->seed = src.seed;
+        e->bonds = src.bonds;
+        e->chains_valid = src.chains_valid;
+        e->made = src.made;
+        e->indep_per_sample = src.indep_per_sample;
+        e->made_min_acceptance = src.made_min_acceptance;
+        e->made_dropped = src.made_dropped;
+        auto clone = [](DevBuf& dst, const DevBuf& s) {
+            if(!s.p) return;
+            dst.ensure(s.bytes);
+            ANN_CUDA(cudaMemcpy(dst.p, s.p, s.bytes, cudaMemcpyDeviceToDevice));
+        };
+        clone(e->bonds_d, src.bonds_d);
+        clone(e->chain_conf, src.chain_conf);
+        clone(e->chain_counter, src.chain_counter);
+        clone(e->acc_rej, src.acc_rej);
+    } catch(...) {
+        delete e;
+        throw;
+    }
+    return e;
+}
+
 OpDev ann_op_impl::view() const {
     OpDev v;
     v.nw = nw;
@@ -594,34 +631,7 @@ int ann_ens_create_mc(const ann_mc_desc* d, ann_ens** out) {
 int ann_ens_copy(const ann_ens* src, ann_ens** out) {
     return guard([&] {
         need(src && out, "null argument");
-        auto* e = new ann_ens();
-        try {
-            e->kind = src->kind;
-            e->N = src->N;
-            e->num_samples = src->num_samples;
-            e->num_sweeps = src->num_sweeps;
-            e->num_therm = src->num_therm;
-            e->n_chains = src->n_chains;
-            e->move = src->move;
-            e->n_up = src->n_up;
-            e->persistent = src->persistent;
-            e->seed = src->seed;
-            e->bonds = src->bonds;
-            e->chains_valid = src->chains_valid;
-            auto clone = [](DevBuf& dst, const DevBuf& s) {
-                if(!s.p) return;
-                dst.ensure(s.bytes);
-                ANN_CUDA(cudaMemcpy(dst.p, s.p, s.bytes, cudaMemcpyDeviceToDevice));
-            };
-            clone(e->bonds_d, src->bonds_d);
-            clone(e->chain_conf, src->chain_conf);
-            clone(e->chain_counter, src->chain_counter);
-            clone(e->acc_rej, src->acc_rej);
-        } catch(...) {
-            delete e;
-            throw;
-        }
-        *out = e;
+        *out = ens_clone(*src);
     });
 }
 
@@ -1182,6 +1192,7 @@ int ann_tdvp_set_chol_update(ann_tdvp* t, int mode) {
         need(t, "null tdvp");
         need(mode == ANN_CHOL_UPDATE_SIMT || mode == ANN_CHOL_UPDATE_TC, "unknown Cholesky update mode");
         t->chol_tc = mode;
+        t->chol_tc_set = true;
     });
 }
 

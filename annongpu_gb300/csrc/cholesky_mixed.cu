@@ -494,7 +494,8 @@ void set_smem_attrs() {
 // FP32 SIMT cores (64 x 64 tiles), as td.chol_tc selects.
 void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsigned* status, cudaStream_t st) {
     ensure_side_stream(td);
-    const bool tc = td.chol_tc != 0;
+    // an explicit choice, else the autotuned one for this size, else the default
+    const bool tc = td.chol_tc_set ? td.chol_tc != 0 : tuning_get(key_chol_update(n), td.chol_tc) != 0;
     if(tc) chol_update_tc_prepare(td, n);
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
     panel32(A, n, 0, Dinv, DinvH, status, st);

@@ -149,7 +149,9 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     OpDev ov{};
     if(op) ov = op->view();
     const size_t wb = wd_bytes<T>(psi);
-    const int wpb = warps_per_block<T>(0);
+    // chains (warps) per CTA: the autotuned choice for this shape, else the default
+    int wpb = tuning_get(key_mc_wpb(psi, ens), warps_per_block<T>(0));
+    if(wpb < 1 || wpb > 8) wpb = warps_per_block<T>(0);
     const size_t made_bytes = learned ? made_smem_bytes(ens.made->N, ens.made->H) + (size_t)wpb * ens.made->H * 4 : 0;
     const int w_smem = wb + made_bytes <= kMaxSmemWd ? 1 : 0;
     const size_t smem = (w_smem ? ((wb + 15) & ~(size_t)15) : 0) + made_bytes;

@@ -9,6 +9,8 @@
 // TDVP::S_dot_vector (TDVP.cu.template:336-443). The reference accumulates with
 // global FP64 atomics; here every block reduces a fixed slab and a second pass
 // adds the slabs in order.
+#include <algorithm>
+
 #include "ann_internal.hpp"
 
 namespace ann {
@@ -241,6 +243,9 @@ void col_stats(const void* O, int O_prec, size_t rows, size_t ld, unsigned Np, c
         unsigned per = (unsigned)((rows + slabs - 1) / slabs);
         if(per > (unsigned)kSlab) per = kSlab;
         if(per < 1) per = 1;
+        // the autotuned slab for this shape, when there is one
+        const int tuned = tuning_get(key_slab(rows, Np), 0);
+        if(tuned > 0) per = (unsigned)std::min(std::max(tuned, 32), kSlab);
         slabs = (unsigned)((rows + per - 1) / per);
         if(slabs < 1) slabs = 1;
         scratch.ensure((size_t)slabs * Np * 3 * sizeof(cplx<double>));

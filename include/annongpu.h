@@ -283,6 +283,26 @@ int ann_tdvp_set_solver(ann_tdvp* tdvp, int solver, unsigned max_iter, double to
 #define ANN_CHOL_UPDATE_SIMT 0
 #define ANN_CHOL_UPDATE_TC 1
 int ann_tdvp_set_chol_update(ann_tdvp* tdvp, int mode);
+
+/* ---------------------------------------------------------------------------------
+ * Autotuner (no counterpart in the reference, whose launch shape is fixed: one CTA
+ * per chain with blockDim = hidden width, include/ensembles/MonteCarlo.hpp:223-228).
+ * ann_autotune times every candidate of each knob on the given workload (CUDA events,
+ * median of repeats; the sampler runs on a copy of the ensemble) and stores the
+ * fastest in the per-process tuning table that the launchers read:
+ *   knob 0  sampler warps (chains) per CTA: 2, 4, 8
+ *   knob 1  rows per FP32 slab of the <O> / F reductions: 128, 256, 512
+ *   knob 2  FP32 Cholesky trailing update: 1 = 128 x 128 tcgen05 tiles, 0 = 64 x 64 SIMT
+ *           (mixed / FP32 solvers without an explicit ann_tdvp_set_chol_update)
+ * report (3 doubles per timed candidate: knob, candidate, median ms) may be NULL;
+ * n_report receives the number of rows. Table keys are "dev<ordinal>/<knob>/<shape>". */
+int ann_autotune(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, double diag_shift, void* stream,
+                 double* report, unsigned report_cap, unsigned* n_report);
+int ann_tuning_set(const char* key, int value);
+int ann_tuning_get(const char* key, int* value, int* found);
+/* "key value" lines; len receives the full length (call with buf NULL to size it) */
+int ann_tuning_dump(char* buf, size_t cap, size_t* len);
+int ann_tuning_clear(void);
 /* after a solve: out4 = {FP32 solves used, relative FP64 residual after the first and
    after the last solve, 1 if the FP64 solve replaced a stalled mixed solve}
    (ANN_SOLVER_FP64: {1, residual before refinement, after, 0}) */

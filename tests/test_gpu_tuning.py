@@ -1,0 +1,68 @@
+"""Autotuner on the GPU: every knob is timed on the workload and the fastest choice
+lands in the tuning table; the choices change speed, not results (sampler launch
+shapes give bit-identical chains, reduction slabs agree to the FP32-sum bound
+rtol 2e-5, the two Cholesky trailing updates give the same refined solve to rtol 1e-8,
+the bound of solves refined to ||r||/||F|| <= 1e-12 at condition numbers near 1e3)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ann = pytest.importorskip("annongpu_gb300")
+
+
+def workload(seed=3, N=16, M=32, chains=2048):
+    rng = np.random.default_rng(seed)
+    c = lambda *s: 0.02 * (rng.standard_normal(s) + 1j * rng.standard_normal(s))  # noqa: E731
+    psi = ann.PsiRBM(c(N, M), 1.0, 0.0, True, a=c(N), b=c(M), precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(chains, 2, 8, chains, True, seed=seed, persistent=True)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    return psi, op, mc, td
+
+
+def test_autotune_fills_table_and_choices_keep_results():
+    ann.set_tuning({}, clear=True)
+    psi, op, mc, td = workload()
+    td.eval(op, psi, mc)  # thermalises the persistent chains
+    conf0, ctr0 = mc.get_chains()
+    rep = ann.autotune(op, psi, mc, td)
+    assert set(rep) == {"rbm_mc.wpb", "stats.slab", "chol.update"}, rep
+    assert set(rep["rbm_mc.wpb"]) == {2, 4, 8} and set(rep["chol.update"]) == {0, 1}
+    assert all(ms > 0 for d in rep.values() for ms in d.values())
+    # the caller's chains did not move (the sampler was timed on a copy)
+    conf1, ctr1 = mc.get_chains()
+    assert np.array_equal(conf0, conf1) and np.array_equal(ctr0, ctr1)
+    table = ann.tuning_table()
+    assert len(table) == 3
+    wkey = next(k for k in table if "/rbm_mc.wpb/" in k)
+    skey = next(k for k in table if "/stats.slab/" in k)
+    ckey = next(k for k in table if "/chol.update/" in k)
+    # every sampler launch shape gives the same chains, samples and O rows
+    results = []
+    for w in (2, 4, 8):
+        ann.set_tuning({wkey: w})
+        mc.set_chains(conf0, ctr0)
+        td.eval(op, psi, mc)
+        results.append((mc.samples(), td.F_vector))
+    for (s, F) in results[1:]:
+        for x, y in zip(s, results[0][0]):
+            assert np.array_equal(x, y)
+        np.testing.assert_array_equal(F, results[0][1])
+    # reduction slabs: same F up to FP32 summation order
+    Fs = []
+    for sl in (128, 512):
+        ann.set_tuning({skey: sl})
+        mc.set_chains(conf0, ctr0)
+        td.eval(op, psi, mc)
+        Fs.append(td.F_vector)
+    assert np.abs(Fs[0] - Fs[1]).max() <= 2e-5 * np.abs(Fs[1]).max()
+    # Cholesky trailing update: the refined solutions agree
+    d = []
+    for m in (0, 1):
+        ann.set_tuning({ckey: m})
+        d.append(td.solve(1e-3))
+        assert not td.solver_info["fell_back"]
+    np.testing.assert_allclose(d[0], d[1], rtol=1e-8, atol=1e-8 * np.abs(d[1]).max())
+    ann.set_tuning({}, clear=True)
