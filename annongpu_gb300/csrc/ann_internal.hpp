@@ -129,6 +129,7 @@ struct ann_made_impl {
     DevBuf mW1, vW1, mb1, vb1, mW2, vW2, mb2, vb2;  // Adam moments
     DevBuf gW1, gb1, gW2, gb2;        // gradients
     DevBuf X, pre, hbuf, l, dl, dh, row_loss;       // training scratch
+    DevBuf kpart;                                   // split-K partial tiles of the weight gradients
 };
 
 struct ann_tdvp_impl {
@@ -157,6 +158,8 @@ struct ann_tdvp_impl {
     DevBuf chol_pt;             // TF32 hi/lo panel operand of the tensor-core update
     unsigned chol_pt_n = 0;
     alignas(64) unsigned char chol_map[128];  // its TMA descriptor (CUtensorMap)
+    alignas(64) unsigned char chol_amap[128]; // TMA descriptor of the FP32 factor (reduce-add epilogue)
+    int chol_reduce = 0;                      // chol_amap is bound (n even)
     DevBuf herk_in;             // BF16 operand for the tensor-core HERK
     DevBuf vec_in, vec_tmp;
     DevBuf wts;                 // per-row weights of the last eval (exact summation)
@@ -233,6 +236,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
 void mixed_solve_info(const ann_tdvp_impl& td, double* out4, cudaStream_t st);
 // tensor-core trailing update of the FP32 Cholesky (chol_update_tc.cu)
 void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n);
+bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n);
 void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st);
 void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, bool col_only, unsigned* status,
                     cudaStream_t st);

@@ -68,11 +68,19 @@ struct UpdArgs {
     unsigned n;
     unsigned t0;        // first trailing row / column
     int col_only;       // tiles (I, 0) only; otherwise tiles (I, J) with 1 <= J <= I
+    int tma_reduce;     // epilogue by TMA reduce-add through amap (n even), else row updates
     unsigned* status;
 };
 
+// bulk tensor reduce-add of a shared-memory box into global memory (L2 performs the adds)
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+    asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"((unsigned long long)map), "r"(x), "r"(y), "r"(src)
+                 : "memory");
+}
+
 __global__ void __launch_bounds__(128, 1)
-chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, UpdArgs a) {
+chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap amap, UpdArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* tail = base + kStages * kStageBytes;
@@ -163,8 +171,46 @@ chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, UpdArgs a) {
     bool ok = mbar_wait(smem_u32(done), 0, abort_flag, a.status) && !*abort_flag;
     ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if(a.tma_reduce) {
+        // -X X^H into shared memory as eight 128-row boxes of 16 complex (128 B rows,
+        // 128-byte swizzle: 16-byte unit u of row r at u ^ (r % 8)), then eight bulk
+        // tensor reduce-adds into A. Upper-triangle entries of a diagonal tile add 0.
+        if(ok) {
+            const unsigned i = warp * 32 + lane;
+            const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+            const bool diag = I == J;
+            for(int c = 0; c < kBM / 16; c++) {
+                float rr[16], ri[16], ir[16], ii[16];
+                tmem_ld16(lane_addr + c * 16, rr);
+                tmem_ld16(lane_addr + kBM + c * 16, ri);
+                tmem_ld16(lane_addr + 256 + c * 16, ir);
+                tmem_ld16(lane_addr + 256 + kBM + c * 16, ii);
+                unsigned char* box = base + (size_t)c * (kBM * 128) + (size_t)i * 128;
+#pragma unroll
+                for(int u = 0; u < 8; u++) {
+                    float4 v;
+                    const int q0 = 2 * u, q1 = 2 * u + 1;
+                    const bool z0 = diag && (unsigned)(c * 16 + q0) > i, z1 = diag && (unsigned)(c * 16 + q1) > i;
+                    v.x = z0 ? 0.f : -(rr[q0] + ii[q0]);
+                    v.y = z0 ? 0.f : -(ir[q0] - ri[q0]);
+                    v.z = z1 ? 0.f : -(rr[q1] + ii[q1]);
+                    v.w = z1 ? 0.f : -(ir[q1] - ri[q1]);
+                    *reinterpret_cast<float4*>(box + ((u ^ (i & 7u)) << 4)) = v;
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        if(__syncthreads_and(ok ? 1 : 0) && threadIdx.x == 0) {
+            const int y = (int)(a.t0 + I * kBM);
+            for(int c = 0; c < kBM / 16; c++)
+                tma_reduce_add_2d(&amap, (int)(2 * (a.t0 + J * kBM) + 32 * c), y,
+                                  smem_u32(base + (size_t)c * (kBM * 128)));
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        }
+    }
     cf (*C)[kBM + 1] = reinterpret_cast<cf (*)[kBM + 1]>(base);  // 128 x 129 complex = 132 KB
-    if(ok) {
+    if(ok && !a.tma_reduce) {
         const unsigned i = warp * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
         for(int c0 = 0; c0 < kBM; c0 += 16) {
@@ -178,7 +224,7 @@ chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, UpdArgs a) {
         }
     }
     __syncthreads();
-    if(__syncthreads_and(ok ? 1 : 0)) {
+    if(__syncthreads_and(ok && !a.tma_reduce ? 1 : 0)) {
         const size_t row0 = (size_t)a.t0 + (size_t)I * kBM, col0 = (size_t)a.t0 + (size_t)J * kBM;
         const unsigned jl0 = 4u * lane;
         const size_t gj0 = col0 + jl0;
@@ -270,6 +316,24 @@ void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
     }
 }
 
+// TMA descriptor of the FP32 factor A (n x n complex64 = n rows of 2n floats) for the
+// reduce-add epilogue; needs 16-byte row pitch, i.e. n even
+bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n) {
+    td.chol_reduce = 0;
+    if(n & 1u) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * n, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)2 * n * sizeof(float)};
+    const cuuint32_t box[2] = {32, kBM};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(td.chol_amap), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                   A, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if(r != CUDA_SUCCESS) return false;
+    td.chol_reduce = 1;
+    return true;
+}
+
 // panel kb (64 columns, factorised, rows below it final) -> its TF32 hi/lo operand
 void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st) {
     const unsigned t0 = kb + kPanel;
@@ -289,8 +353,9 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
     const unsigned T = (m + kBM - 1) / kBM;
     const unsigned tiles = col_only ? T : T * (T - 1) / 2;
     if(tiles == 0) return;
-    UpdArgs a{A, n, t0, col_only ? 1 : 0, status};
-    chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(*reinterpret_cast<const CUtensorMap*>(td.chol_map), a);
+    UpdArgs a{A, n, t0, col_only ? 1 : 0, td.chol_reduce, status};
+    chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(*reinterpret_cast<const CUtensorMap*>(td.chol_map),
+                                                         *reinterpret_cast<const CUtensorMap*>(td.chol_amap), a);
     check_launch("chol_update_tc_kernel");
 }
 

@@ -496,7 +496,10 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
     ensure_side_stream(td);
     // an explicit choice, else the autotuned one for this size, else the default
     const bool tc = td.chol_tc_set ? td.chol_tc != 0 : tuning_get(key_chol_update(n), td.chol_tc) != 0;
-    if(tc) chol_update_tc_prepare(td, n);
+    if(tc) {
+        chol_update_tc_prepare(td, n);
+        chol_update_tc_bind(td, A, n);
+    }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
     panel32(A, n, 0, Dinv, DinvH, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {

@@ -25,10 +25,18 @@ template<typename TB>
 __global__ void __launch_bounds__(256)
 sgemm_kernel(unsigned Mm, unsigned Nn, unsigned K, const float* __restrict__ A, size_t sam, size_t sak,
              const TB* __restrict__ B, size_t sbk, size_t sbn, float* __restrict__ C, size_t ldc, float alpha,
-             const float* __restrict__ bias, const float* __restrict__ aux) {
+             const float* __restrict__ bias, const float* __restrict__ aux, unsigned kchunk = 0) {
     __shared__ float As[16][64];
     __shared__ float Bs[16][64];
     const unsigned m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    if(kchunk) {
+        // split K: this CTA sums k in [z kchunk, (z + 1) kchunk) into partial tile z
+        const unsigned k0 = blockIdx.z * kchunk;
+        K = min(K - k0, kchunk);
+        A += (size_t)k0 * sak;
+        B += (size_t)k0 * sbk;
+        C += (size_t)blockIdx.z * Mm * ldc;
+    }
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float acc[4][4] = {};
     for(unsigned k0 = 0; k0 < K; k0 += 16) {
@@ -82,6 +90,34 @@ void sgemm(unsigned Mm, unsigned Nn, unsigned K, const float* A, size_t sam, siz
     check_launch("sgemm_kernel");
 }
 
+// C = sum over K split into chunks of kSplitK: grid.z chunks write partial tiles to
+// P[z] (Mm x Nn), split_reduce_kernel adds them in chunk order (deterministic). For
+// the weight gradients, whose outputs are small (N x H) and whose K is the batch.
+constexpr unsigned kSplitK = 128;
+
+__global__ void split_reduce_kernel(const float* __restrict__ P, unsigned splits, size_t mn, float* __restrict__ C) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= mn) return;
+    float acc = 0.f;
+    for(unsigned z = 0; z < splits; z++) acc += P[(size_t)z * mn + i];
+    C[i] = acc;
+}
+
+template<typename TB>
+void sgemm_splitk(unsigned Mm, unsigned Nn, unsigned K, const float* A, size_t sam, size_t sak, const TB* B,
+                  size_t sbk, size_t sbn, float* C, DevBuf& scratch, cudaStream_t st) {
+    const unsigned splits = (K + kSplitK - 1) / kSplitK;
+    const size_t mn = (size_t)Mm * Nn;
+    scratch.ensure(splits * mn * sizeof(float));
+    float* P = scratch.as<float>();
+    dim3 grid((Nn + 63) / 64, (Mm + 63) / 64, splits);
+    sgemm_kernel<TB><<<grid, 256, 0, st>>>(Mm, Nn, K, A, sam, sak, B, sbk, sbn, P, Nn, 1.f, nullptr, nullptr,
+                                           kSplitK);
+    check_launch("sgemm_kernel");
+    split_reduce_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(P, splits, mn, C);
+    check_launch("split_reduce_kernel");
+}
+
 __global__ void bits_kernel(const uint64_t* __restrict__ confs, unsigned B, unsigned N, float* __restrict__ X) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if(idx >= (size_t)B * N) return;
@@ -112,12 +148,15 @@ __global__ void dlogits_kernel(const float* __restrict__ l, const float* __restr
 }
 
 // column sums: out[n] = sum_m X[m][n]
-__global__ void colsum_kernel(const float* __restrict__ X, unsigned M, unsigned Nn, float* __restrict__ out) {
+// partial column sums over slabs of kSplitK rows (blockIdx.y); split_reduce_kernel
+// adds the slabs in order
+__global__ void colsum_kernel(const float* __restrict__ X, unsigned M, unsigned Nn, float* __restrict__ part) {
     const unsigned n = blockIdx.x * blockDim.x + threadIdx.x;
     if(n >= Nn) return;
+    const unsigned m0 = blockIdx.y * 128u, m1 = min(M, m0 + 128u);
     float s = 0.f;
-    for(unsigned m = 0; m < M; m++) s += X[(size_t)m * Nn + n];
-    out[n] = s;
+    for(unsigned m = m0; m < m1; m++) s += X[(size_t)m * Nn + n];
+    part[(size_t)blockIdx.y * Nn + n] = s;
 }
 
 struct AdamArgs {
@@ -263,6 +302,15 @@ void made_init(ann_made_impl& m, uint64_t seed) {
 }
 
 // gradient of the mean -log q over confs[0..B) into m.g*; loss to *loss_dev
+void colsum(const float* X, unsigned M, unsigned Nn, float* out, DevBuf& scratch, cudaStream_t st) {
+    const unsigned slabs = (M + kSplitK - 1) / kSplitK;
+    scratch.ensure((size_t)slabs * Nn * sizeof(float));
+    colsum_kernel<<<dim3((Nn + 127) / 128, slabs), 128, 0, st>>>(X, M, Nn, scratch.as<float>());
+    check_launch("colsum_kernel");
+    split_reduce_kernel<<<(Nn + 255) / 256, 256, 0, st>>>(scratch.as<float>(), slabs, Nn, out);
+    check_launch("split_reduce_kernel");
+}
+
 void made_gradient(ann_made_impl& m, const uint64_t* confs, unsigned B, double* loss_dev, cudaStream_t st) {
     const unsigned N = m.N, H = m.H;
     m.X.ensure((size_t)B * N * 4);
@@ -293,15 +341,13 @@ void made_gradient(ann_made_impl& m, const uint64_t* confs, unsigned B, double* 
     loss_sum_kernel<<<1, 256, 0, st>>>(m.row_loss.as<float>(), B, loss_dev);
     check_launch("loss_sum_kernel");
     // dW2[j][k] = sum_b dl[b][j] h[b][k]
-    sgemm<float>(N, H, B, dl, 1, N, h, H, 1, m.gW2.as<float>(), H, 1.f, nullptr, nullptr, st);
-    colsum_kernel<<<(N + 127) / 128, 128, 0, st>>>(dl, B, N, m.gb2.as<float>());
-    check_launch("colsum_kernel");
+    sgemm_splitk<float>(N, H, B, dl, 1, N, h, H, 1, m.gW2.as<float>(), m.kpart, st);
+    colsum(dl, B, N, m.gb2.as<float>(), m.kpart, st);
     // dh[b][k] = sum_j dl[b][j] W2t[k][j] * [pre > 0]   (the weights the forward pass used)
     sgemm<__nv_bfloat16>(B, H, N, dl, N, 1, W2t, 1, N, dh, H, 1.f, nullptr, pre, st);
     // dW1[k][i] = sum_b dh[b][k] X[b][i]
-    sgemm<float>(H, N, B, dh, 1, H, X, N, 1, m.gW1.as<float>(), N, 1.f, nullptr, nullptr, st);
-    colsum_kernel<<<(H + 127) / 128, 128, 0, st>>>(dh, B, H, m.gb1.as<float>());
-    check_launch("colsum_kernel");
+    sgemm_splitk<float>(H, N, B, dh, 1, H, X, N, 1, m.gW1.as<float>(), m.kpart, st);
+    colsum(dh, B, H, m.gb1.as<float>(), m.kpart, st);
 }
 
 void made_adam(ann_made_impl& m, float lr, cudaStream_t st) {

@@ -4,8 +4,9 @@
 // i < d_k and it feeds output j iff d_k <= j, so logit j depends on spins < j only.
 //     pre = W1 x + b1,  h = relu(pre),  l = W2 h + b2,  x_j = 1 for spin up
 //     q(s) = prod_j sigmoid(l_j)^{x_j} sigmoid(-l_j)^{1 - x_j}
-// The kernels read BF16 copies of the weights (stored transposed: W1t[i][k], W2t[k][j])
-// and accumulate in FP32. Masked weights are held at exactly zero, so the forward pass
+// The kernels read BF16 copies of the weights (global: W1t[i][k], W2t[k][j]; staged in
+// shared memory as W1t[i][k] and W2[j][k], so a warp reading one row with lanes over
+// the hidden units k touches consecutive addresses) and accumulate in FP32. Masked weights are held at exactly zero, so the forward pass
 // needs no mask.
 //
 // Used by the sampler as a Metropolis-Hastings independence proposal: s' ~ q,
@@ -24,9 +25,9 @@ constexpr unsigned kMadeMaxN = 128;
 // weights staged in shared memory by the calling CTA
 struct MadeSm {
     unsigned N, H;
-    const __nv_bfloat16* W1t;
+    const __nv_bfloat16* W1t;  // [i][k]
     const float* b1;
-    const __nv_bfloat16* W2t;
+    const __nv_bfloat16* W2;   // [j][k]
     const float* b2;
 };
 
@@ -45,13 +46,14 @@ __device__ inline MadeSm made_stage(const MadeDev& m, unsigned char* smem) {
     const size_t nw = (size_t)m.N * m.H;
     for(size_t k = threadIdx.x; k < nw; k += blockDim.x) {
         w1[k] = m.W1t[k];
-        w2[k] = m.W2t[k];
+        const size_t j = k / m.H, kk = k % m.H;
+        w2[k] = m.W2t[kk * m.N + j];  // W2[j][kk]
     }
     for(unsigned k = threadIdx.x; k < m.H; k += blockDim.x) b1[k] = m.b1[k];
     for(unsigned k = threadIdx.x; k < m.N; k += blockDim.x) b2[k] = m.b2[k];
     s.W1t = w1;
     s.b1 = b1;
-    s.W2t = w2;
+    s.W2 = w2;
     s.b2 = b2;
     return s;
 }
@@ -75,14 +77,16 @@ __device__ float made_logq(const MadeSm& m, const Conf<NW>& s, float* h, int lan
         h[k] = fmaxf(pre, 0.f);
     }
     __syncwarp();
+    // logit j: lanes split the hidden units (consecutive W2[j][k]), butterfly sum
     float acc = 0.f;
-    for(unsigned j = lane; j < m.N; j += 32) {
-        float l = m.b2[j];
-        for(unsigned k = 0; k < m.H; k++) l = fmaf(__bfloat162float(m.W2t[k * m.N + j]), h[k], l);
+    for(unsigned j = 0; j < m.N; j++) {
+        float part = 0.f;
+        for(unsigned k = lane; k < m.H; k += 32) part = fmaf(__bfloat162float(m.W2[j * m.H + k]), h[k], part);
+        const float l = m.b2[j] + warp_sum(part);
         acc -= spin_bit(s, j) ? softplusf(-l) : softplusf(l);
     }
     __syncwarp();
-    return warp_sum(acc);
+    return acc;
 }
 
 // Draws s ~ q autoregressively; uniforms from Philox counters (c0, c1, c2, 3 + 4 b),
@@ -105,7 +109,7 @@ __device__ float made_sample(const MadeSm& m, uint32_t k0, uint32_t k1, uint32_t
 #pragma unroll
         for(int u = 0; u < HU; u++) {
             const unsigned k = u * 32 + lane;
-            if(k < m.H) part = fmaf(__bfloat162float(m.W2t[k * m.N + j]), fmaxf(pre[u], 0.f), part);
+            if(k < m.H) part = fmaf(__bfloat162float(m.W2[j * m.H + k]), fmaxf(pre[u], 0.f), part);
         }
         const float l = m.b2[j] + warp_sum(part);
         const uint32_t word_src = (j & 3u) == 0 ? rr.x : (j & 3u) == 1 ? rr.y : (j & 3u) == 2 ? rr.z : rr.w;

@@ -61,9 +61,10 @@ MADE_BATCH = 4096
 HISTORY = 65536
 RETRAIN_EVERY = 10
 MADE_FIRST_EPOCHS = 4
-LEARNED_SWEEPS = 0       # local sweeps between samples with the learned proposal on
+LEARNED_SWEEPS = 1       # local sweeps between samples with the learned proposal on
 LEARNED_INDEP = 2        # learned independence moves per sample
 MIN_ACCEPT = 0.1         # the proposal is dropped below this acceptance
+TUNING_FILE = None       # --tuning: load the tuning table instead of autotuning
 
 
 def init_params(rng):
@@ -216,8 +217,13 @@ class Form:
                                    lr=MADE_LR, stream=stream)
         self.mc.set_chains(*prep.get_chains())
         self.mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=MIN_ACCEPT)
-        # launch and tile shapes for this workload (outside the timed region)
-        self.tuning = self.ann.autotune(self.op, self.psi, self.mc, self.tdvp, SHIFT, stream)
+        # launch and tile shapes for this workload (outside the timed region), or a table
+        # saved by an earlier run (profiling runs: ncu serialises and slows every launch)
+        if TUNING_FILE:
+            if not self.ann.load_tuning(TUNING_FILE):
+                raise RuntimeError(f"{TUNING_FILE} was tuned on another GPU model")
+        else:
+            self.tuning = self.ann.autotune(self.op, self.psi, self.mc, self.tdvp, SHIFT, stream)
 
     def retrain(self, stream):
         import torch
@@ -237,20 +243,31 @@ class Form:
         self.tdvp.sr_step(self.op, self.psi, self.mc, SHIFT, LR)
         self.n_steps += 1
 
-    def tau(self):
+    def tau(self, sweeps=None, indep=None):
         """tau_int of the local energy from T samples per chain of a separate run with
         the same moves (fresh chains, thermalised with local sweeps)."""
         T = 24
-        mc = self.ann.MonteCarloLoop(N_CHAINS * T, self.sweeps, THERM, N_CHAINS, True, seed=SEED + 99,
+        sweeps = self.sweeps if sweeps is None else sweeps
+        indep = self.indep if indep is None else indep
+        mc = self.ann.MonteCarloLoop(N_CHAINS * T, sweeps, THERM, N_CHAINS, True, seed=SEED + 99,
                                      persistent=True)
-        if self.made is not None:
-            mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=0.0)
+        if self.made is not None and indep:
+            mc.set_proposal(self.made, indep_per_sample=indep, min_acceptance=0.0)
         self.ann.ExpectationValue()(self.op, self.psi, mc)
         _, _, el = mc.samples()
         acc = {"local": mc.acceptance_rate}
-        if self.made is not None:
+        if self.made is not None and indep:
             acc["learned"] = mc.proposal_acceptance
         return tau_int_sokal(el.real.reshape(T, N_CHAINS)), acc
+
+    def tau_ablation(self):
+        """tau_int with the learned moves alone, the local sweeps alone, and both."""
+        out = {}
+        for name, sw, ind in (("learned_only", 0, self.indep), ("local_only", self.sweeps, 0),
+                              ("local_and_learned", self.sweeps, self.indep)):
+            t, a = self.tau(sw, ind)
+            out[name] = {"sweeps": sw, "learned_moves": ind, "tau_int": t, "acceptance": a}
+        return out
 
     def energy_check(self):
         """Per-site energy of the last step's 16384 sample configurations with the current
@@ -352,6 +369,7 @@ def run_ours(args):
     f, ms, phase, launches, tau, acc, info = main
     Np, Ns = f.Np, N_CHAINS
     energy = f.energy_check()
+    ablation = f.tau_ablation() if f.made is not None else None
 
     # the same step with the FP64 Cholesky solver (and the solve error of the mixed solver)
     fp64 = {}
@@ -418,6 +436,8 @@ def run_ours(args):
     if out["roofline"]["peak"]:
         out["roofline"]["frac"] = s_tflops / out["roofline"]["peak"]
     out.update(fp64)
+    if ablation:
+        out["tau_ablation"] = ablation
     out["forms"] = {name: form_summary(r[0], r[1], r[2], r[4], r[5]) for name, r in results.items()}
     if "plain" in results and "precision" in results:
         p, q = out["forms"]["plain"], out["forms"]["precision"]
@@ -546,16 +566,23 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
     ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32"])
+    ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
+    ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_solver)
         return
+    global TUNING_FILE
+    TUNING_FILE = args.tuning
     if args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+        if args.save_tuning:
+            import annongpu_gb300 as ann
+            ann.save_tuning(args.save_tuning)
 
 
 if __name__ == "__main__":
