@@ -45,73 +45,98 @@ __global__ void cvt_shift_kernel(const zc* __restrict__ S, cf* __restrict__ A, u
     }
 }
 
-// Cholesky of the nb x nb diagonal block at (kb, kb), then the inverse of the factor.
-// Factorisation (right-looking): thread t holds a[r][g + 16 m], m = 0..3, of row
-// r = t / 16 (g = t % 16) in registers; per column j the scaled column goes through
-// shared memory and every thread updates its own entries, two barriers per column.
-// Inverse, column c by the 16 lanes of group c:
-//   X[i][c] = (delta_ic - sum_{c <= p < i} L[i][p] X[p][c]) / L[i][i].
-// Dinv[blk] = L_kk^{-1}, DinvH[blk] = L_kk^{-H} (row-major NB x NB, identity
-// beyond nb).
-__global__ void __launch_bounds__(1024) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
-                                                       cf* __restrict__ Dinv, cf* __restrict__ DinvH,
-                                                       unsigned* status) {
-    extern __shared__ float4 smem_raw[];
-    cf (*a)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(smem_raw);
-    cf (*x)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(reinterpret_cast<cf*>(smem_raw) + NB * (NB + 1));
-    __shared__ cf col[NB];
+// Cholesky of the nb x nb diagonal block at (kb, kb), factor only (the critical path of
+// the factorisation; the inverses of the diagonal blocks are formed afterwards by
+// diag_inv_kernel). Right-looking on the block in shared memory with the pivots left
+// unscaled: per column j every lower entry (r, c), j < c <= r, takes
+//   a_rc -= a_rj conj(a_cj) / a_jj,
+// the entries enumerated column-major so that the work of column j is one contiguous
+// suffix split evenly over the threads; one barrier per column. At the end
+// L_rc = a_rc / sqrt(a_cc) (r > c), L_cc = sqrt(a_cc).
+constexpr int kPotrfThreads = 128;
+constexpr int kTri = NB * (NB + 1) / 2;  // lower-triangle entries of a block
+
+__global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
+                                                                unsigned* status) {
+    __shared__ cf a[NB][NB + 1];
+    __shared__ uint16_t pr[kTri];      // (c << 8) | r, column-major
+    __shared__ unsigned short off[NB + 1];
+    __shared__ float piv[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned tid = threadIdx.x;
-    const unsigned r = tid >> 4, g = tid & 15u;
-    cf e[4];
+    {
+        cf v[NB * NB / kPotrfThreads];
 #pragma unroll
-    for(int m = 0; m < 4; m++) {
-        const unsigned c = g + 16u * m;
-        cf v = mk(0.f, 0.f);
-        if(r < nb && c <= r) v = A[(size_t)(kb + r) * n + kb + c];
-        else if(r == c) v = mk(1.f, 0.f);
-        e[m] = v;
+        for(int q = 0; q < NB * NB / kPotrfThreads; q++) {
+            const unsigned t = tid + q * kPotrfThreads, r = t / NB, c = t % NB;
+            v[q] = (r < nb && c <= r) ? A[(size_t)(kb + r) * n + kb + c] : mk(r == c ? 1.f : 0.f, 0.f);
+        }
+#pragma unroll
+        for(int q = 0; q < NB * NB / kPotrfThreads; q++) {
+            const unsigned t = tid + q * kPotrfThreads;
+            a[t / NB][t % NB] = v[q];
+        }
     }
+    if(tid <= NB) off[tid] = (unsigned short)(tid * NB - tid * (tid - 1) / 2);  // first entry of column tid
+    if(tid < NB) {
+        const unsigned c = tid, o = c * NB - c * (c - 1) / 2;
+        for(unsigned r = c; r < NB; r++) pr[o + r - c] = (uint16_t)((c << 8) | r);
+    }
+    __syncthreads();
     for(unsigned j = 0; j < NB; j++) {
-        const unsigned gj = j & 15u, mj = j >> 4;
-        // the owners of column j publish it (rows >= j), scaled by 1 / sqrt(a[j][j])
-        if(g == gj && r >= j) col[r] = e[mj];
-        __syncthreads();
-        float d = col[j].re;
+        float d = a[j][j].re;
         if(!(d > 0.f) || !isfinite(d)) {
             if(tid == 0) atomicOr(status, kStatusNotPosDef);
             d = 1.f;
         }
-        const float inv = rsqrtf(d);
-        if(g == gj && r >= j) e[mj] = r == j ? mk(d * inv, 0.f) : inv * e[mj];
-        const cf lr = inv * col[r];
-#pragma unroll
-        for(int m = 0; m < 4; m++) {
-            const unsigned c = g + 16u * m;
-            if(c > j && c <= r) cmac_conj(e[m], col[c], -(inv * lr));  // -= l_rj conj(l_cj)
+        if(tid == 0) piv[j] = d;
+        const float id = 1.f / d;
+        for(unsigned t = off[j + 1] + tid; t < (unsigned)kTri; t += kPotrfThreads) {
+            const unsigned c = pr[t] >> 8, r = pr[t] & 255u;
+            cf v = a[r][c];
+            cmac_conj(v, a[c][j], -(id * a[r][j]));  // -= a_rj conj(a_cj) / a_jj
+            a[r][c] = v;
         }
         __syncthreads();
     }
-#pragma unroll
-    for(int m = 0; m < 4; m++) {
-        a[r][g + 16u * m] = e[m];
-        x[r][g + 16u * m] = mk(0.f, 0.f);
+    for(unsigned t = tid; t < (unsigned)kTri; t += kPotrfThreads) {
+        const unsigned c = pr[t] >> 8, r = pr[t] & 255u;
+        if(r < nb) {
+            const float sc = sqrtf(piv[c]);
+            A[(size_t)(kb + r) * n + kb + c] = r == c ? mk(sc, 0.f) : (1.f / sc) * a[r][c];
+        }
+    }
+}
+
+// inverse of every diagonal block of the factor (one CTA per block, 16 threads per
+// column c): X[i][c] = (delta_ic - sum_{c <= p < i} L[i][p] X[p][c]) / L[i][i];
+// Dinv[blk] = L_kk^{-1}, DinvH[blk] = L_kk^{-H} (row-major NB x NB, identity beyond nb)
+__global__ void __launch_bounds__(1024) diag_inv_kernel(const cf* __restrict__ A, unsigned n, cf* __restrict__ Dinv,
+                                                        cf* __restrict__ DinvH) {
+    extern __shared__ float4 smem_raw[];
+    cf (*Ls)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(smem_raw);
+    cf (*x)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(reinterpret_cast<cf*>(smem_raw) + NB * (NB + 1));
+    const unsigned kb = blockIdx.x * NB, nb = min((unsigned)NB, n - kb);
+    const unsigned tid = threadIdx.x;
+    for(unsigned t = tid; t < NB * NB; t += blockDim.x) {
+        const unsigned r = t / NB, c = t % NB;
+        Ls[r][c] = (r < nb && c <= r) ? A[(size_t)(kb + r) * n + kb + c] : mk(r == c ? 1.f : 0.f, 0.f);
+        x[r][c] = mk(0.f, 0.f);
     }
     __syncthreads();
-    // inverse: group c = tid / 16 owns column c (NB == 64 columns, 1024 threads)
     {
         const unsigned c = tid >> 4, s = tid & 15u;
         const unsigned i0 = c & ~1u;  // both groups of a warp walk the same rows
         for(unsigned i = i0; i < NB; i++) {
             cf part = mk(0.f, 0.f);
-            for(unsigned p = i0 + s; p < i; p += 16) cmac(part, a[i][p], x[p][c]);
+            for(unsigned p = i0 + s; p < i; p += 16) cmac(part, Ls[i][p], x[p][c]);
 #pragma unroll
             for(int o = 8; o > 0; o >>= 1) {
                 part.re += __shfl_xor_sync(0xffffffffu, part.re, o, 16);
                 part.im += __shfl_xor_sync(0xffffffffu, part.im, o, 16);
             }
             if(s == 0) {
-                const float inv = 1.f / a[i][i].re;
+                const float inv = 1.f / Ls[i][i].re;
                 const float dre = (i == c) ? 1.f : 0.f;
                 x[i][c] = mk(inv * (dre - part.re), -inv * part.im);
             }
@@ -119,50 +144,57 @@ __global__ void __launch_bounds__(1024) potrf32_kernel(cf* __restrict__ A, unsig
         }
     }
     __syncthreads();
-    const size_t blk = kb / NB;
+    const size_t blk = blockIdx.x;
     for(unsigned t = tid; t < NB * NB; t += blockDim.x) {
-        const unsigned rr = t / NB, c = t % NB;
-        if(rr < nb && c <= rr) A[(size_t)(kb + rr) * n + kb + c] = a[rr][c];
-        Dinv[blk * NB * NB + t] = x[rr][c];
-        DinvH[blk * NB * NB + t] = conj(x[c][rr]);
+        const unsigned r = t / NB, c = t % NB;
+        Dinv[blk * NB * NB + t] = x[r][c];
+        DinvH[blk * NB * NB + t] = conj(x[c][r]);
     }
 }
 
-// rows below the diagonal block: X <- X L_kk^{-H}, out[c] = sum_{p <= c} X[p] conj(Dinv[c][p]).
-// One warp per row, lane owns columns lane and lane + 32; DinvH staged in shared memory.
-__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
-                                                     const cf* __restrict__ DinvH) {
-    __shared__ cf D[NB][NB + 1];  // D[p][c] = DinvH[p][c] = conj(Dinv[c][p])
-    const size_t blk = kb / NB;
-    for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) D[t / NB][t % NB] = DinvH[blk * NB * NB + t];
+constexpr unsigned kTrsmRows = 16;  // rows per CTA: many short CTAs, the panel is on the critical path
+
+// rows below the diagonal block: X <- X L_kk^{-H} by substitution, one warp per row,
+// lane owning columns lane and lane + 32: for c = 0..63 the owner finalises
+//   x_c = (x_c - sum_{p<c} x_p conj(L_cp)) / L_cc,
+// broadcasts it, and the lanes subtract x_c conj(L_qc) from their columns q > c.
+// L_kk (just factorised) is staged transposed in shared memory: Lt[c][q] = L_qc.
+__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb) {
+    __shared__ cf Lt[NB][NB + 1];
+    __shared__ float inv_d[NB];
+    for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+        const unsigned q = t / NB, c = t % NB;  // element (q, c) of L_kk
+        Lt[c][q] = c <= q ? A[(size_t)(kb + q) * n + kb + c] : mk(0.f, 0.f);
+    }
+    __syncthreads();
+    if(threadIdx.x < NB) inv_d[threadIdx.x] = 1.f / Lt[threadIdx.x][threadIdx.x].re;
     __syncthreads();
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const unsigned nb = min((unsigned)NB, n - kb);
-    const size_t row0 = (size_t)kb + nb + (size_t)blockIdx.x * 64;
-    for(unsigned rr = warp; rr < 64; rr += 8) {
+    const size_t row0 = (size_t)kb + NB + (size_t)blockIdx.x * kTrsmRows;
+    for(unsigned rr = warp; rr < kTrsmRows; rr += 8) {
         const size_t row = row0 + rr;
         if(row >= n) break;
         cf* X = A + row * n + kb;
-        const cf x0 = lane < nb ? X[lane] : mk(0.f, 0.f);
-        const cf x1 = lane + 32 < nb ? X[lane + 32] : mk(0.f, 0.f);
-        cf o0 = mk(0.f, 0.f), o1 = mk(0.f, 0.f);
-#pragma unroll 8
-        for(unsigned p = 0; p < 32; p++) {
-            cf xp;
-            xp.re = __shfl_sync(0xffffffffu, x0.re, p);
-            xp.im = __shfl_sync(0xffffffffu, x0.im, p);
-            cmac(o0, xp, D[p][lane]);
-            cmac(o1, xp, D[p][lane + 32]);
+        cf x0 = X[lane], x1 = X[lane + 32];
+        for(unsigned c = 0; c < 32; c++) {
+            cf xc;
+            xc.re = __shfl_sync(0xffffffffu, x0.re, c);
+            xc.im = __shfl_sync(0xffffffffu, x0.im, c);
+            xc = inv_d[c] * xc;
+            if(lane == c) x0 = xc;
+            else if(lane > c) cmac_conj(x0, Lt[c][lane], -xc);  // -= x_c conj(L_qc)
+            cmac_conj(x1, Lt[c][lane + 32], -xc);
         }
-#pragma unroll 8
-        for(unsigned p = 0; p < 32; p++) {
-            cf xp;
-            xp.re = __shfl_sync(0xffffffffu, x1.re, p);
-            xp.im = __shfl_sync(0xffffffffu, x1.im, p);
-            cmac(o1, xp, D[p + 32][lane + 32]);
+        for(unsigned c = 32; c < NB; c++) {
+            cf xc;
+            xc.re = __shfl_sync(0xffffffffu, x1.re, c - 32);
+            xc.im = __shfl_sync(0xffffffffu, x1.im, c - 32);
+            xc = inv_d[c] * xc;
+            if(lane + 32 == c) x1 = xc;
+            else if(lane + 32 > c) cmac_conj(x1, Lt[c][lane + 32], -xc);
         }
-        if(lane < nb) X[lane] = o0;
-        if(lane + 32 < nb) X[lane + 32] = o1;
+        X[lane] = x0;
+        X[lane + 32] = x1;
     }
 }
 
@@ -300,11 +332,26 @@ __device__ __forceinline__ void set_flag(int* flag) {
     if(threadIdx.x == 0) atomicExch(flag, 1);
 }
 
+// y = D x for a diagonal block held in shared memory (D[c][p], row-major)
+__device__ __forceinline__ void block_apply_sm(const cf (*D)[NB], const cf* __restrict__ x, cf* y, unsigned nb) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for(unsigned c = warp; c < NB; c += nw) {
+        cf acc = mk(0.f, 0.f);
+        cmac(acc, D[c][lane], x[lane]);
+        cmac(acc, D[c][lane + 32], x[lane + 32]);
+        acc = warp_sum(acc);
+        if(lane == 0) y[c] = c < nb ? acc : mk(0.f, 0.f);
+    }
+}
+
 // b <- (L L^H)^{-1} b in one cooperative launch without grid barriers. CTA g owns the
 // block rows j = g, g + G, ... (G CTAs, all resident). Forward: y_j = L_jj^{-1} (b_j -
 // sum_{k<j} L_jk y_k), adding each y_k as soon as its ready flag is set. Backward:
 // x_j = L_jj^{-H} (y_j - sum_{k>j} L_kj^H x_k), blocks taken from the last. Every
 // thread adds its contributions in a fixed order, so the result is bit-reproducible.
+// The critical path is the chain of ready flags, so everything that does not depend
+// on the awaited block (the next L block, the inverted diagonal block) is loaded
+// before the wait.
 // flags: [nblk] forward ready, [nblk] backward ready, [1] abort; zero on entry.
 __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __restrict__ A,
                                                                    const cf* __restrict__ Dinv,
@@ -313,6 +360,7 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
                                                                    unsigned* status) {
     if(irs->done) return;
     __shared__ cf v[NB], z[NB], red[8][NB];
+    __shared__ cf D[NB][NB];
     const unsigned nblk = (n + NB - 1) / NB;
     int* fwd_ready = flags;
     int* bwd_ready = flags + nblk;
@@ -322,16 +370,28 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
     for(unsigned j = blockIdx.x; j < nblk; j += gridDim.x) {
         const unsigned jb = j * NB, nbj = min((unsigned)NB, n - jb);
         const unsigned r = t >> 3, s8 = (t & 7u) * 8u;
+        for(unsigned q = t; q < NB * NB; q += blockDim.x) D[q / NB][q % NB] = Dinv[(size_t)j * NB * NB + q];
         cf acc = mk(0.f, 0.f);
+        cf Ln[8];
+        const cf* Lrow = A + (size_t)(jb + min(r, nbj - 1)) * n + s8;
+        if(j > 0) {
+#pragma unroll
+            for(int q = 0; q < 8; q++) Ln[q] = Lrow[q];
+        }
         for(unsigned k = 0; k < j; k++) {
+            cf Lc[8];
+#pragma unroll
+            for(int q = 0; q < 8; q++) Lc[q] = Ln[q];
+            if(k + 1 < j) {
+#pragma unroll
+                for(int q = 0; q < 8; q++) Ln[q] = Lrow[(k + 1) * NB + q];
+            }
             if(!wait_flag(fwd_ready + k, abort_flag, status)) return;
-            const unsigned kb = k * NB;
-            if(t < NB) v[t] = ld_l2(y + kb + t);
+            if(t < NB) v[t] = ld_l2(y + k * NB + t);
             __syncthreads();
             if(r < nbj) {
-                const cf* Lr = A + (size_t)(jb + r) * n + kb + s8;
 #pragma unroll
-                for(int q = 0; q < 8; q++) cmac(acc, Lr[q], v[s8 + q]);
+                for(int q = 0; q < 8; q++) cmac(acc, Lc[q], v[s8 + q]);
             }
             __syncthreads();
         }
@@ -343,7 +403,7 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
         }
         if((t & 7u) == 0 && r < NB) v[r] = r < nbj ? b[jb + r] - acc : mk(0.f, 0.f);
         __syncthreads();
-        block_apply(Dinv + (size_t)j * NB * NB, v, z, nbj);
+        block_apply_sm(D, v, z, nbj);
         __syncthreads();
         if(t < nbj) st_l2(y + jb + t, z[t]);
         set_flag(fwd_ready + j);
@@ -352,17 +412,28 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
     for(int jj = (int)nblk - 1 - (int)blockIdx.x; jj >= 0; jj -= (int)gridDim.x) {
         const unsigned j = (unsigned)jj, jb = j * NB, nbj = min((unsigned)NB, n - jb);
         const unsigned c = t & 63u, q8 = (t >> 6) * 8u;
+        for(unsigned q = t; q < NB * NB; q += blockDim.x) D[q / NB][q % NB] = DinvH[(size_t)j * NB * NB + q];
         cf acc = mk(0.f, 0.f);
+        // L[kb + q8 + q][jb + c] of block k, rows past n read as zero
+        auto load_col = [&](unsigned k, cf* out) {
+            const unsigned kb = k * NB, nbk = min((unsigned)NB, n - kb);
+#pragma unroll
+            for(int q = 0; q < 8; q++)
+                out[q] = (c < nbj && q8 + q < nbk) ? A[(size_t)(kb + q8 + q) * n + jb + c] : mk(0.f, 0.f);
+        };
+        cf Ln[8];
+        if(j + 1 < nblk) load_col(nblk - 1, Ln);
         for(unsigned k = nblk - 1; k > j; k--) {
+            cf Lc[8];
+#pragma unroll
+            for(int q = 0; q < 8; q++) Lc[q] = Ln[q];
+            if(k - 1 > j) load_col(k - 1, Ln);
             if(!wait_flag(bwd_ready + k, abort_flag, status)) return;
             const unsigned kb = k * NB, nbk = min((unsigned)NB, n - kb);
             if(t < NB) v[t] = t < nbk ? ld_l2(b + kb + t) : mk(0.f, 0.f);
             __syncthreads();
-            if(c < nbj) {
 #pragma unroll
-                for(int q = 0; q < 8; q++)
-                    if(q8 + q < nbk) cmac_conj(acc, A[(size_t)(kb + q8 + q) * n + jb + c], v[q8 + q]);
-            }
+            for(int q = 0; q < 8; q++) cmac_conj(acc, Lc[q], v[q8 + q]);
             __syncthreads();
         }
         red[t >> 6][c] = acc;
@@ -375,7 +446,7 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
             v[t] = t < nbj ? ld_l2(y + jb + t) - sum : mk(0.f, 0.f);
         }
         __syncthreads();
-        block_apply(DinvH + (size_t)j * NB * NB, v, z, nbj);
+        block_apply_sm(D, v, z, nbj);
         __syncthreads();
         if(t < nbj) st_l2(b + jb + t, z[t]);
         set_flag(bwd_ready + j);
@@ -466,13 +537,13 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
     }
 }
 
-void panel32(cf* A, unsigned n, unsigned kb, cf* Dinv, cf* DinvH, unsigned* status, cudaStream_t st) {
-    potrf32_kernel<<<1, 1024, 2 * NB * (NB + 1) * sizeof(cf), st>>>(A, n, kb, Dinv, DinvH, status);
+void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
+    potrf32_kernel<<<1, kPotrfThreads, 0, st>>>(A, n, kb, status);
     check_launch("potrf32_kernel");
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned below = n - kb - nb;
     if(below) {
-        trsm32_kernel<<<(below + 63) / 64, 256, 0, st>>>(A, n, kb, DinvH);
+        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb);
         check_launch("trsm32_kernel");
     }
 }
@@ -480,7 +551,7 @@ void panel32(cf* A, unsigned n, unsigned kb, cf* Dinv, cf* DinvH, unsigned* stat
 void set_smem_attrs() {
     static bool done = false;  // per process: the attribute is per function and device-independent
     if(done) return;
-    ANN_CUDA(cudaFuncSetAttribute(potrf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ANN_CUDA(cudaFuncSetAttribute(diag_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   2 * NB * (NB + 1) * (int)sizeof(cf)));
     ANN_CUDA(cudaFuncSetAttribute(herk32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   2 * NB * (UT + 1) * (int)sizeof(cf)));
@@ -501,7 +572,7 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         chol_update_tc_bind(td, A, n);
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
-    panel32(A, n, 0, Dinv, DinvH, status, st);
+    panel32(A, n, 0, status, st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);
         const unsigned below = n - kb - nb;
@@ -516,7 +587,7 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         }
         ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
         ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
-        panel32(A, n, kb + nb, Dinv, DinvH, status, td.side);
+        panel32(A, n, kb + nb, status, td.side);
         ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
         if(tc) {
             chol_update_tc(td, A, n, kb, false, status, st);
@@ -526,6 +597,9 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         }
         ANN_CUDA(cudaStreamWaitEvent(st, td.side_ev[1], 0));
     }
+    // inverses of the diagonal blocks for the triangular solves, all blocks at once
+    diag_inv_kernel<<<(n + NB - 1) / NB, 1024, 2 * NB * (NB + 1) * sizeof(cf), st>>>(A, n, Dinv, DinvH);
+    check_launch("diag_inv_kernel");
 }
 
 // b <- (L L^H)^{-1} b; tmp (n entries) holds y = L^{-1} b; flags (2 nblk + 1 ints) are
