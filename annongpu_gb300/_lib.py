@@ -155,6 +155,7 @@ _SIGS = {
     "ann_made_gradient": ([P, P, U, P, P, P, P, P], I),
     "ann_made_train": ([P, P, U, U, U, D, P, P], I),
     "ann_made_train_on_samples": ([P, P, U, U, D, P, P], I),
+    "ann_get_solve_times": ([P], I),
     "ann_get_phase_times": ([P], I),
 }
 

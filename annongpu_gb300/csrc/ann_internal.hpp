@@ -244,6 +244,8 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
 void ensure_side_stream(ann_tdvp_impl& td);
 // the configured solver; an eager mixed solve that stalls is redone in FP64
 void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
+// CUDA-event marks around the FP32 factorisation when phase timing is on (capi.cu)
+void solve_mark(int i, cudaStream_t st);
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
 
 unsigned* status_word();

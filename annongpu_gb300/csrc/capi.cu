@@ -172,6 +172,22 @@ void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, 
     }
 }
 
+// sub-phases of the mixed solve: factorisation start / end (events 0, 1)
+namespace {
+cudaEvent_t g_sev[2] = {};
+bool g_sev_used[2] = {};
+}  // namespace
+
+void solve_mark(int i, cudaStream_t st) {
+    if(!g_timing) return;
+    cudaStreamCaptureStatus cs;
+    ANN_CUDA(cudaStreamIsCapturing(st, &cs));
+    if(cs != cudaStreamCaptureStatusNone) return;
+    if(!g_sev[i]) ANN_CUDA(cudaEventCreate(&g_sev[i]));
+    ANN_CUDA(cudaEventRecord(g_sev[i], st));
+    g_sev_used[i] = true;
+}
+
 }  // namespace ann
 
 using namespace ann;
@@ -1228,6 +1244,18 @@ int ann_set_phase_timing(int enable) {
     return guard([&] {
         g_timing = enable != 0;
         for(auto& u : g_ev_used) u = false;
+        for(auto& u : g_sev_used) u = false;
+    });
+}
+
+int ann_get_solve_times(float* ms1) {
+    return guard([&] {
+        need(ms1, "null argument");
+        ms1[0] = -1.f;
+        if(g_sev_used[0] && g_sev_used[1]) {
+            ANN_CUDA(cudaEventSynchronize(g_sev[1]));
+            ANN_CUDA(cudaEventElapsedTime(&ms1[0], g_sev[0], g_sev[1]));
+        }
     });
 }
 

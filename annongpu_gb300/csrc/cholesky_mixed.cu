@@ -668,7 +668,9 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     check_launch("cvt_shift_kernel");
     // FP32 pivot failures are recorded in the refinement state (they end in a stall and
     // the FP64 fallback), or, with no refinement to fall back from, in the status word
+    solve_mark(0, st);
     cholesky32(td, A, n, Dinv, DinvH, pivots_to_status ? status : &irs->notpd, st);
+    solve_mark(1, st);
     for(unsigned it = 0; it < max_iter; it++) {
         solve32(A, Dinv, DinvH, n, c, c + n, irs, flags, status, st);
         ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs);

@@ -184,6 +184,7 @@ class Form:
         self.retrain_ms = []
         self.n_steps = 0
         self.tuning = None
+        self.t_factor_ms = None
         if name == "plain":
             self.sweeps, self.indep = SWEEPS, 0
             self.tdvp = ann.TDVP(self.Np, s_mode="fp32", solver="fp32")
@@ -291,6 +292,7 @@ def timed_steps(form, args, stream, dist):
     lc0 = ann.launch_count()
     ann._lib.call("ann_set_phase_timing", 1)
     phase = np.zeros(5)
+    t_factor = []
     if dist:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -301,6 +303,10 @@ def timed_steps(form, args, stream, dist):
         ph = np.zeros(5, np.float32)
         ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
         phase += ph
+        sf = np.zeros(1, np.float32)
+        ann._lib.call("ann_get_solve_times", ann._lib.ptr(sf))
+        if sf[0] > 0:
+            t_factor.append(float(sf[0]))
     ev1.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -314,6 +320,7 @@ def timed_steps(form, args, stream, dist):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     launches = ann.launch_count() - lc0
+    form.t_factor_ms = float(np.mean(t_factor)) if t_factor else None
     return ms, phase / args.steps, launches
 
 
@@ -435,6 +442,16 @@ def run_ours(args):
     }
     if out["roofline"]["peak"]:
         out["roofline"]["frac"] = s_tflops / out["roofline"]["peak"]
+    if getattr(f, "t_factor_ms", None):
+        # FP32 Cholesky: (4/3) Np^3 real flops of complex factorisation; its trailing
+        # updates run as three TF32 products on tcgen05 (TF32 rate = half the BF16 rate)
+        chol_tflops = (4.0 / 3.0) * Np ** 3 / (f.t_factor_ms * 1e-3) / 1e12
+        tf32x3_peak = pk.get("bf16_tflops", 1900.0) / 2 / 3
+        out["roofline_cholesky"] = {"bound": "tensor", "kernel": "FP32 Cholesky (chol_update_tc + panel path)",
+                                    "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
+                                    "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
+                                    "peak_kind": pk_kind + " bf16 burst / 2 (TF32) / 3 (split products)",
+                                    "work": "(4/3)*Np^3 real flops per factorisation"}
     out.update(fp64)
     if ablation:
         out["tau_ablation"] = ablation
@@ -528,7 +545,7 @@ def run_reference(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded random-init RBM, 2D TFIM)",
-           "config": config_dict(args.form), "impl": "reference",
+           "config": config_dict("precision" if args.form == "both" else args.form), "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": P, "kind": "port",
                             "sample": f"{P} processes x 2 chains x 1 sample timed per step and scaled to "
                                       f"{N_CHAINS} samples; Cholesky scaled from n=2048; tau_int = 1 assumed"},
@@ -556,6 +573,32 @@ def run_profile_case(solver="fp64"):
     print("profile case: E/N =", td.E_local / N)
 
 
+def run_profile_case_learned():
+    """Small case for ncu captures of the sampler with learned moves: the 8x8 workload's
+    shapes (N = 64, M = 128, h = 3.04) with 4096 chains (O rows 275 MB), one local sweep
+    and two learned independence moves per sample, the proposal trained on 16384
+    configurations first; two SR steps (BF16 tensor-core S, mixed solver)."""
+    import annongpu_gb300 as ann
+    rng = np.random.default_rng(SEED)
+    a, b, W = init_params(rng)
+    op = ann.Operator(ann.transverse_field_ising_2d(L, L, h=H_FIELD))
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    chains = 4096
+    prep = ann.MonteCarloLoop(chains, 1, THERM, chains, True, seed=5, persistent=True)
+    prep.set_history(4 * chains)
+    for _ in range(4):
+        ann.ExpectationValue()(op, psi, prep)
+    made = ann.MADE(N_SITES, MADE_H, seed=1)
+    made.train_on_samples(prep, steps=16, batch=MADE_BATCH, lr=MADE_LR)
+    mc = ann.MonteCarloLoop(chains, LEARNED_SWEEPS, THERM, chains, True, seed=6, persistent=True)
+    mc.set_chains(*prep.get_chains())
+    mc.set_proposal(made, indep_per_sample=LEARNED_INDEP, min_acceptance=0.0)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    for _ in range(2):
+        td.sr_step(op, psi, mc, SHIFT, LR)
+    print("profile case (learned): E/N =", td.E_local / N_SITES)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,14 +608,18 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "precision", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
-    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32"])
+    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "learned"],
+                    help="SR solver of the small profile case; 'learned': the learned-proposal sampler case")
     ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
     ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_solver)
+        if args.profile_solver == "learned":
+            run_profile_case_learned()
+        else:
+            run_profile_case(args.profile_solver)
         return
     global TUNING_FILE
     TUNING_FILE = args.tuning

@@ -373,6 +373,9 @@ int ann_sr_graph_launch(ann_tdvp* tdvp, void* stream);
    ms[2] S matrix, ms[3] SR solve, ms[4] update; -1 where a phase did not run */
 int ann_set_phase_timing(int enable);
 int ann_get_phase_times(float* ms5);
+/* with phase timing on: duration (ms) of the FP32 Cholesky factorisation inside the
+   last mixed / FP32 SR solve (-1 if none was timed) */
+int ann_get_solve_times(float* ms1);
 
 /* kernels this library launched so far (monotonic counter of its own launches) */
 unsigned long long ann_kernel_launch_count(void);
