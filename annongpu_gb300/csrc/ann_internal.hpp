@@ -155,9 +155,9 @@ struct ann_tdvp_impl {
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
     int chol_tc = 1;            // FP32 Cholesky trailing update: 1 tcgen05 (split TF32), 0 FP32 SIMT
     bool chol_tc_set = false;   // chosen explicitly (ann_tdvp_set_chol_update): the tuning table is not read
-    DevBuf chol_pt;             // TF32 hi/lo panel operand of the tensor-core update
+    DevBuf chol_pt;             // TF32 hi/lo panel operands (two buffers) of the tensor-core update
     unsigned chol_pt_n = 0;
-    alignas(64) unsigned char chol_map[128];  // its TMA descriptor (CUtensorMap)
+    alignas(64) unsigned char chol_map[2][128];  // TMA descriptors of its two buffers (CUtensorMap)
     alignas(64) unsigned char chol_amap[128]; // TMA descriptor of the FP32 factor (reduce-add epilogue)
     int chol_reduce = 0;                      // chol_amap is bound (n even)
     DevBuf herk_in;             // BF16 operand for the tensor-core HERK
@@ -237,7 +237,8 @@ void mixed_solve_info(const ann_tdvp_impl& td, double* out4, cudaStream_t st);
 // tensor-core trailing update of the FP32 Cholesky (chol_update_tc.cu)
 void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n);
 bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n);
-void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st);
+// operand buffer 0 / 1 (panel k uses k % 2), written by the panel solve
+float* chol_update_tc_operand(ann_tdvp_impl& td, unsigned buf);
 void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, bool col_only, unsigned* status,
                     cudaStream_t st);
 // the look-ahead side stream of the Cholesky factorisations (high priority)
@@ -256,6 +257,7 @@ unsigned* status_word();
 int tuning_get(const std::string& key, int dflt);
 void tuning_set(const std::string& key, int value);
 std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens);
+std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_slab(size_t rows, unsigned Np);
 std::string key_chol_update(unsigned n);
 

@@ -4,8 +4,8 @@
 // X is split into TF32 hi and lo parts (x = hi + lo + O(2^-22 |x|)); three products
 // hi.hi + hi.lo + lo.hi restore FP32-level accuracy (the dropped lo.lo is below it),
 // so the factor keeps the quality that the FP64 refinement of the mixed solver needs.
-// chol_prep_tf32_kernel writes the operand PT, K-major: per 128-row block of the
-// trailing rows, [Re rows (128) ; Im rows (128)], each row [hi (64) | lo (64)] floats.
+// The panel solve (trsm32_kernel) writes the operand PT, K-major: per 128-row block of
+// the trailing rows, [Re rows (128) ; Im rows (128)], each row [hi (64) | lo (64)] floats.
 // One CTA updates the 128 x 128 complex tile (I, J <= I) of the trailing matrix: per
 // K step of 32 TF32 values TMA brings the 256 x 32 blocks of I and J (128-byte
 // swizzle), one elected thread issues per 8-value slice
@@ -38,30 +38,6 @@ constexpr int kStageBytes = 2 * kRows * kBK * 4;  // A block + B block
 constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
 constexpr int kSegments = 3;               // hi.hi, hi.lo, lo.hi
 constexpr int kStepsPerSeg = kPanel / kBK;
-
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t u;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
-    return __uint_as_float(u);
-}
-
-// PT rows for the trailing rows t0 .. t0 + 128 T (zero beyond n)
-__global__ void __launch_bounds__(256) chol_prep_tf32_kernel(const cf* __restrict__ A, unsigned n, unsigned kb,
-                                                             unsigned t0, unsigned T, float* __restrict__ PT) {
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t i = idx / kPanel;
-    const unsigned p = (unsigned)(idx % kPanel);
-    if(i >= (size_t)T * kBM) return;
-    const cf v = (t0 + i < n) ? A[(t0 + i) * n + kb + p] : mk(0.f, 0.f);
-    const size_t blk = i / kBM, r = i % kBM;
-    float* re = PT + (blk * kRows + r) * kRowFloats;
-    float* im = PT + (blk * kRows + kBM + r) * kRowFloats;
-    const float hr = tf32_rna(v.re), hi = tf32_rna(v.im);
-    re[p] = hr;
-    re[kPanel + p] = tf32_rna(v.re - hr);
-    im[p] = hi;
-    im[kPanel + p] = tf32_rna(v.im - hi);
-}
 
 struct UpdArgs {
     cf* A;
@@ -292,22 +268,28 @@ chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_con
 
 }  // namespace
 
+// two operand buffers (panel k uses buffer k % 2), each with its TMA descriptor; rows
+// past the trailing matrix only reach outputs past n, which are never written
+size_t pt_bytes(unsigned n) { return (size_t)((n + kBM - 1) / kBM) * kRows * kRowFloats * sizeof(float); }
+
 void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
-    const unsigned T = (n + kBM - 1) / kBM;
-    const size_t rows = (size_t)T * kRows;
-    const size_t bytes = rows * kRowFloats * sizeof(float);
-    if(td.chol_pt.bytes >= bytes && td.chol_pt_n == n) return;
-    td.chol_pt.ensure(bytes);
+    const size_t bytes = pt_bytes(n);
+    const size_t rows = bytes / (kRowFloats * sizeof(float));
+    if(td.chol_pt.bytes >= 2 * bytes && td.chol_pt_n == n) return;
+    td.chol_pt.ensure(2 * bytes);
+    ANN_CUDA(cudaMemset(td.chol_pt.p, 0, 2 * bytes));
     td.chol_pt_n = n;
-    const cuuint64_t dims[2] = {(cuuint64_t)kRowFloats, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)(kRowFloats * sizeof(float))};
-    const cuuint32_t box[2] = {kBK, kRows};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(td.chol_map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
-                                   td.chol_pt.p, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
+    for(int b = 0; b < 2; b++) {
+        const cuuint64_t dims[2] = {(cuuint64_t)kRowFloats, (cuuint64_t)rows};
+        const cuuint64_t strides[1] = {(cuuint64_t)(kRowFloats * sizeof(float))};
+        const cuuint32_t box[2] = {kBK, kRows};
+        const cuuint32_t estr[2] = {1, 1};
+        const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(td.chol_map[b]), CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                       2, td.chol_pt.as<unsigned char>() + b * bytes, dims, strides, box, estr,
+                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
+    }
     static bool attr = false;
     if(!attr) {
         ANN_CUDA(cudaFuncSetAttribute(chol_update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -334,15 +316,8 @@ bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n) {
     return true;
 }
 
-// panel kb (64 columns, factorised, rows below it final) -> its TF32 hi/lo operand
-void chol_update_tc_panel(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, cudaStream_t st) {
-    const unsigned t0 = kb + kPanel;
-    const unsigned m = n - t0;
-    const unsigned T = (m + kBM - 1) / kBM;
-    const size_t threads = (size_t)T * kBM * kPanel;
-    chol_prep_tf32_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(A, n, kb, t0, T,
-                                                                             td.chol_pt.as<float>());
-    check_launch("chol_prep_tf32_kernel");
+float* chol_update_tc_operand(ann_tdvp_impl& td, unsigned buf) {
+    return reinterpret_cast<float*>(td.chol_pt.as<unsigned char>() + buf * pt_bytes(td.chol_pt_n));
 }
 
 // A22 -= X X^H on tiles (I, 0) (col_only) or (I, J >= 1) of the trailing matrix of panel kb
@@ -354,7 +329,7 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
     const unsigned tiles = col_only ? T : T * (T - 1) / 2;
     if(tiles == 0) return;
     UpdArgs a{A, n, t0, col_only ? 1 : 0, td.chol_reduce, status};
-    chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(*reinterpret_cast<const CUtensorMap*>(td.chol_map),
+    chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(*reinterpret_cast<const CUtensorMap*>(td.chol_map[(kb / kPanel) & 1u]),
                                                          *reinterpret_cast<const CUtensorMap*>(td.chol_amap), a);
     check_launch("chol_update_tc_kernel");
 }

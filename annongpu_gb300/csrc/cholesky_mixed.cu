@@ -53,7 +53,7 @@ __global__ void cvt_shift_kernel(const zc* __restrict__ S, cf* __restrict__ A, u
 // the entries enumerated column-major so that the work of column j is one contiguous
 // suffix split evenly over the threads; one barrier per column. At the end
 // L_rc = a_rc / sqrt(a_cc) (r > c), L_cc = sqrt(a_cc).
-constexpr int kPotrfThreads = 128;
+constexpr int kPotrfThreads = 512;
 constexpr int kTri = NB * (NB + 1) / 2;  // lower-triangle entries of a block
 
 __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
@@ -159,7 +159,29 @@ constexpr unsigned kTrsmRows = 16;  // rows per CTA: many short CTAs, the panel 
 //   x_c = (x_c - sum_{p<c} x_p conj(L_cp)) / L_cc,
 // broadcasts it, and the lanes subtract x_c conj(L_qc) from their columns q > c.
 // L_kk (just factorised) is staged transposed in shared memory: Lt[c][q] = L_qc.
-__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb) {
+__device__ __forceinline__ float tf32_round(float x) {
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+    return __uint_as_float(u);
+}
+
+// The panel rows are also the operand of the next tensor-core trailing update: with
+// PT != null each row is written there as well, split into TF32 hi and lo (the layout
+// of chol_update_tc.cu: per 128-row block of the rows below the panel,
+// [Re rows ; Im rows], each row [hi (64) | lo (64)] floats).
+__device__ __forceinline__ void put_tf32(float* PT, size_t i, unsigned p, cf v) {
+    const size_t blk = i / 128, r = i % 128;
+    float* re = PT + (blk * 256 + r) * 128;
+    float* im = PT + (blk * 256 + 128 + r) * 128;
+    const float hr = tf32_round(v.re), hi = tf32_round(v.im);
+    re[p] = hr;
+    re[64 + p] = tf32_round(v.re - hr);
+    im[p] = hi;
+    im[64 + p] = tf32_round(v.im - hi);
+}
+
+__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
+                                                     float* __restrict__ PT) {
     __shared__ cf Lt[NB][NB + 1];
     __shared__ float inv_d[NB];
     for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
@@ -195,6 +217,11 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
         }
         X[lane] = x0;
         X[lane + 32] = x1;
+        if(PT) {
+            const size_t i = row - (kb + NB);
+            put_tf32(PT, i, lane, x0);
+            put_tf32(PT, i, lane + 32, x1);
+        }
     }
 }
 
@@ -537,13 +564,14 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
     }
 }
 
-void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, cudaStream_t st) {
+// diagonal block, then the rows below it (and, for the tensor-core update, its operand)
+void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, float* PT, cudaStream_t st) {
     potrf32_kernel<<<1, kPotrfThreads, 0, st>>>(A, n, kb, status);
     check_launch("potrf32_kernel");
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned below = n - kb - nb;
     if(below) {
-        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb);
+        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb, PT);
         check_launch("trsm32_kernel");
     }
 }
@@ -572,14 +600,16 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         chol_update_tc_bind(td, A, n);
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
-    panel32(A, n, 0, status, st);
+    // panel k's rows go to operand buffer k % 2: panel k+1 (side stream) fills the other
+    // buffer while the rest of update k still reads this one
+    auto pt = [&](unsigned kb) { return tc ? chol_update_tc_operand(td, (kb / NB) & 1u) : nullptr; };
+    panel32(A, n, 0, status, pt(0), st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);
         const unsigned below = n - kb - nb;
         if(below == 0) break;
         const unsigned tiles = (below + UT - 1) / UT;
         if(tc) {
-            chol_update_tc_panel(td, A, n, kb, st);
             chol_update_tc(td, A, n, kb, true, status, st);
         } else {
             herk32_kernel<<<tiles, 256, herk_smem, st>>>(A, n, kb, nb, 1);
@@ -587,7 +617,7 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         }
         ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
         ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
-        panel32(A, n, kb + nb, status, td.side);
+        panel32(A, n, kb + nb, status, pt(kb + nb), td.side);
         ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
         if(tc) {
             chol_update_tc(td, A, n, kb, false, status, st);

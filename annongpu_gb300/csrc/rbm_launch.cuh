@@ -153,7 +153,9 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     int wpb = tuning_get(key_mc_wpb(psi, ens), warps_per_block<T>(0));
     if(wpb < 1 || wpb > 8) wpb = warps_per_block<T>(0);
     const size_t made_bytes = learned ? made_smem_bytes(ens.made->N, ens.made->H) + (size_t)wpb * ens.made->H * 4 : 0;
-    const int w_smem = wb + made_bytes <= kMaxSmemWd ? 1 : 0;
+    // W staged in shared memory when it fits, unless the tuning table prefers reading it
+    // through L1 (fewer bytes of shared memory per CTA, more CTAs per SM)
+    const int w_smem = (wb + made_bytes <= kMaxSmemWd && tuning_get(key_mc_wsmem(psi, ens), 1)) ? 1 : 0;
     const size_t smem = (w_smem ? ((wb + 15) & ~(size_t)15) : 0) + made_bytes;
     if(smem > 220 * 1024) throw Error(ANN_ERR_INVALID, "learned proposal too large for shared memory");
     const unsigned grid = (ens.n_chains + wpb - 1) / wpb;

@@ -6,6 +6,7 @@
 // workload by timing every candidate of each knob on it with CUDA events (median of
 // repeats) and keeping the fastest:
 //   rbm_mc.wpb      warps (chains) per CTA of the Metropolis sampler: 2, 4, 8
+//   rbm_mc.wsmem    sampler weights W staged in shared memory (1) or read through L1 (0)
 //   stats.slab      rows per FP32 slab of the <O> / F reductions: 128, 256, 512
 //   chol.update     trailing update of the FP32 Cholesky: 128 x 128 tcgen05 tiles
 //                   (split TF32) or 64 x 64 FP32 SIMT tiles
@@ -81,6 +82,11 @@ std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens) {
     o << "rbm_mc.wpb/N" << psi.N << ".M" << psi.Mpad << ".U" << psi.U << ".P" << psi.precision << ".made"
       << (ens.made && !ens.made_dropped && ens.indep_per_sample ? 1 : 0);
     return o.str();
+}
+
+std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens) {
+    std::string k = key_mc_wpb(psi, ens);
+    return "rbm_mc.wsmem" + k.substr(k.find('/'));
 }
 
 std::string key_slab(size_t rows, unsigned Np) {
@@ -189,6 +195,18 @@ int ann_autotune(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, double dia
                     if(ms < best) { best = ms; best_w = w; }
                 }
                 tuning_set(key, best_w);
+                // W in shared memory or read through L1, at the chosen CTA size
+                const std::string kw = key_mc_wsmem(*psi, *e2);
+                double best_ws = 1e300;
+                int best_s = 1;
+                for(int ws : {1, 0}) {
+                    tuning_set(kw, ws);
+                    const SampleTargets tg = tdvp_prepare(*t, *psi, *e2);
+                    const double ms = time_ms([&] { run_ensemble(*psi, op, *e2, tg, st); }, 3, st);
+                    record(3, ws, ms);
+                    if(ms < best_ws) { best_ws = ms; best_s = ws; }
+                }
+                tuning_set(kw, best_s);
             }
             // one evaluation on the copy: O rows and S for the remaining knobs
             {

@@ -28,21 +28,22 @@ def test_autotune_fills_table_and_choices_keep_results():
     td.eval(op, psi, mc)  # thermalises the persistent chains
     conf0, ctr0 = mc.get_chains()
     rep = ann.autotune(op, psi, mc, td)
-    assert set(rep) == {"rbm_mc.wpb", "stats.slab", "chol.update"}, rep
+    assert set(rep) == {"rbm_mc.wpb", "rbm_mc.wsmem", "stats.slab", "chol.update"}, rep
     assert set(rep["rbm_mc.wpb"]) == {2, 4, 8} and set(rep["chol.update"]) == {0, 1}
     assert all(ms > 0 for d in rep.values() for ms in d.values())
     # the caller's chains did not move (the sampler was timed on a copy)
     conf1, ctr1 = mc.get_chains()
     assert np.array_equal(conf0, conf1) and np.array_equal(ctr0, ctr1)
     table = ann.tuning_table()
-    assert len(table) == 3
+    assert len(table) == 4
     wkey = next(k for k in table if "/rbm_mc.wpb/" in k)
     skey = next(k for k in table if "/stats.slab/" in k)
     ckey = next(k for k in table if "/chol.update/" in k)
     # every sampler launch shape gives the same chains, samples and O rows
+    mkey = next(k for k in table if "/rbm_mc.wsmem/" in k)
     results = []
-    for w in (2, 4, 8):
-        ann.set_tuning({wkey: w})
+    for w, m in ((2, 1), (4, 0), (8, 1), (8, 0)):
+        ann.set_tuning({wkey: w, mkey: m})
         mc.set_chains(conf0, ctr0)
         td.eval(op, psi, mc)
         results.append((mc.samples(), td.F_vector))
