@@ -20,7 +20,7 @@ namespace {
 
 constexpr int kBatchU = 8;       // register slots: hidden width up to 256
 constexpr int kBatchWarps = 8;   // chains per work item
-constexpr int kBatchStreams = 8;
+constexpr int kBatchStreams = 16;
 
 struct BatchInst {
     RbmDev<float> p;
@@ -223,8 +223,22 @@ void batch_sr(ann_batch_impl& b, double shift, double lr, cudaStream_t st) {
     batch_streams(b);
     ANN_CUDA(cudaEventRecord(b.fork, st));
     for(auto s : b.streams) ANN_CUDA(cudaStreamWaitEvent(s, b.fork, 0));
-    for(size_t i = 0; i < b.psis.size(); i++) {
-        cudaStream_t s = b.streams[i % b.streams.size()];
+    // longest first onto the least-loaded stream; the estimated cost (us) of an instance
+    // is its solve: a latency-bound chain of Np / 64 panels plus the (4/3) Np^3 update
+    // work, and the S product over its rows
+    const size_t n = b.psis.size();
+    std::vector<size_t> order(n);
+    std::vector<double> cost(n), load(b.streams.size(), 0.0);
+    for(size_t i = 0; i < n; i++) {
+        const double np = b.psis[i]->Np, ns = (double)b.enss[i]->num_steps();
+        cost[i] = np / 64.0 * 40.0 + (4.0 / 3.0) * np * np * np / 5e7 + 4.0 * np * np * ns / 1e9;
+        order[i] = i;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+    for(size_t i : order) {
+        const size_t k = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += cost[i];
+        cudaStream_t s = b.streams[k];
         ann_tdvp_impl& t = *b.tdvps[i];
         tdvp_post(t, *b.psis[i], *b.enss[i], true, s);
         sr_solve_any(t, shift, status_word(), s);

@@ -340,6 +340,84 @@ def form_summary(form, ms, phase, tau, acc):
     return d
 
 
+# ----------------------------------------------------------------------------------
+# Batched uneven instances (BASELINE config 5): 96 1-D TFIM chains, L uniform on
+# {12, 16, ..., 48}, h uniform on [0.5, 1.5], J = 1, complex RBM with alpha from
+# {1, 2, 4} and a per-instance seed; chains 512 .. 8192 in proportion to Np.
+N_INST = 96
+BATCH_SWEEPS = 4
+
+
+def batched_instances(ann, st, steps):
+    """One persistent sampling + E_loc launch for all instances, per-instance S (BF16
+    tcgen05) and mixed solves on a stream pool, the whole step one CUDA graph; against the
+    same instances stepped one after another (one CUDA graph each). Energies of the
+    instances with L <= 20 against exact summation."""
+    import torch
+    rng = np.random.default_rng(SEED + 5)
+    specs = [(int(rng.choice(np.arange(12, 49, 4))), float(rng.uniform(0.5, 1.5)), int(rng.choice([1, 2, 4])))
+             for _ in range(N_INST)]
+    nps = [L + al * L + al * L * L for L, _, al in specs]
+    lo, hi = min(nps), max(nps)
+    chains = [int(round((512 + (8192 - 512) * (n - lo) / max(hi - lo, 1)) / 64)) * 64 for n in nps]
+
+    def make(k):
+        L, h, al = specs[k]
+        r = np.random.default_rng(SEED + 1000 + k)
+        c = lambda *sh: 0.01 * (r.standard_normal(sh) + 1j * r.standard_normal(sh))  # noqa: E731
+        psi = ann.PsiRBM(c(L, al * L), 1.0, 0.0, True, a=c(L), b=c(al * L), precision="fp32")
+        op = ann.Operator(ann.transverse_field_ising_1d(L, h))
+        mc = ann.MonteCarloLoop(chains[k], BATCH_SWEEPS, 16, chains[k], True, seed=SEED + 2000 + k, persistent=True)
+        td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed", stream=st)
+        return psi, op, mc, td
+
+    def timed(fn, n):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(n):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    # batched: one graph per step
+    inst = [make(k) for k in range(N_INST)]
+    batch = ann.Batch(*[list(x) for x in zip(*inst)], stream=st)
+    batch.capture_sr_step(SHIFT, LR, st)  # runs one eager step (thermalises) first
+    batch.launch_sr_step(st)
+    ms_batched = timed(lambda: batch.launch_sr_step(st), steps)
+    # energies after the timed steps (persistent, equilibrated chains)
+    batch.sample()
+    E = batch.energies()
+    checks = []
+    for k, (L, h, al) in enumerate(specs):
+        if L <= 20:
+            psi, op, mc, td = inst[k]
+            es = ann.ExactSummationSpins(L)
+            psi.normalize(es)
+            e_ex = ann.ExpectationValue()(op, psi, es).real
+            _, _, el = mc.samples()
+            se = el.real.std() / np.sqrt(len(el))
+            checks.append({"L": L, "alpha": al, "h": round(h, 4), "E_mc": float(E[k].real), "E_exact": float(e_ex),
+                           "abs_diff_per_site": float(abs(E[k].real - e_ex) / L),
+                           "diff_in_se": float(abs(E[k].real - e_ex) / se)})
+    del batch, inst
+    torch.cuda.empty_cache()
+    # one instance after another: a captured SR step per instance, launched in turn
+    seq = [make(k) for k in range(N_INST)]
+    for psi, op, mc, td in seq:
+        td.capture_sr_step(op, psi, mc, SHIFT, LR, st)
+    ms_seq = timed(lambda: [td.launch_sr_step(st) for (_, _, _, td) in seq], steps)
+    samples = sum(chains)
+    return {"instances": N_INST, "samples_per_step": samples, "num_params_range": [lo, hi],
+            "chains_range": [min(chains), max(chains)], "sweeps_between_samples": BATCH_SWEEPS,
+            "ms_per_step_batched": ms_batched, "ms_per_step_one_by_one": ms_seq,
+            "speedup": ms_seq / ms_batched, "samples_per_s_batched": samples / (ms_batched * 1e-3),
+            "exact_summation_checks": checks,
+            "max_diff_in_standard_errors": max(c["diff_in_se"] for c in checks) if checks else None}
+
+
 def run_ours(args):
     import torch
     import annongpu_gb300 as ann
@@ -461,6 +539,8 @@ def run_ours(args):
         out["vs_plain"] = {k: q[k] / p[k] for k in ("sr_steps_per_s", "effective_samples_per_s",
                                                     "sampler_effective_samples_per_s")}
         out["forms"]["plain"]["energy_check"] = results["plain"][0].energy_check()
+    if not args.no_batched and f.name == "precision":
+        out["batched_instances"] = batched_instances(ann, st, max(2, args.steps // 5))
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(*init_params(np.random.default_rng(SEED)), f.H, tau, cores=1)
     if rank == 0:
@@ -607,6 +687,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="both", choices=["both", "precision", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances measurement")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
     ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "learned"],
                     help="SR solver of the small profile case; 'learned': the learned-proposal sampler case")
