@@ -126,6 +126,8 @@ _SIGS = {
     "ann_tdvp_solver_info": ([P, P], I),
     "ann_tdvp_set_chol_update": ([P, I], I),
     "ann_autotune": ([P, P, P, P, D, P, P, U, P], I),
+    "ann_hsd_distance": ([P, P, P, I, P, P, P], I),
+    "ann_hsd_gradient": ([P, P, P, I, P, D, P, P, P], I),
     "ann_tuning_set": ([ct.c_char_p, I], I),
     "ann_tuning_get": ([ct.c_char_p, P, P], I),
     "ann_tuning_dump": ([ct.c_char_p, ct.c_size_t, P], I),

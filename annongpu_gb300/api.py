@@ -823,6 +823,32 @@ TDVP.eval_F = _track_rows(TDVP.eval_F)
 
 
 # ----------------------------------------------------------------------------------
+class HilbertSpaceDistance:
+    """Distance between psi_prime and U psi and its gradient in the parameters of psi_prime
+    (source/network_functions/HilbertSpaceDistance.cu.template:16-168; binding
+    pyANNonGPU/main.cpp.template:436-442)."""
+
+    def __init__(self, num_params, gpu=True, stream=None):
+        self.num_params = int(num_params)
+        self.gpu = bool(gpu)
+        self.stream = stream
+
+    def __call__(self, psi, psi_prime, operator_, is_unitary, spin_ensemble) -> float:
+        out = np.zeros(1)
+        call("ann_hsd_distance", psi.handle, psi_prime.handle, operator_.handle, int(bool(is_unitary)),
+             spin_ensemble.handle, stream_ptr(self.stream), ptr(out))
+        return float(out[0])
+
+    def gradient(self, psi, psi_prime, operator_, is_unitary, spin_ensemble, nu=1.0):
+        """(gradient, distance), as gradient_py (HilbertSpaceDistance.hpp:103-112)."""
+        grad = cbuf(psi_prime.num_params)
+        d = np.zeros(1)
+        call("ann_hsd_gradient", psi.handle, psi_prime.handle, operator_.handle, int(bool(is_unitary)),
+             spin_ensemble.handle, float(nu), stream_ptr(self.stream), ptr(grad), ptr(d))
+        return grad, float(d[0])
+
+
+# ----------------------------------------------------------------------------------
 class Batch(_Handle):
     """Many (psi, operator, Monte Carlo ensemble[, TDVP]) instances of uneven size in one
     persistent sampling launch, with per-instance SR solves (this project's addition)."""

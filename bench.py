@@ -418,6 +418,25 @@ def batched_instances(ann, st, steps):
             "max_diff_in_standard_errors": max(c["diff_in_se"] for c in checks) if checks else None}
 
 
+def hsd_timing(ann, f, st):
+    """HilbertSpaceDistance gradient on the 8x8 workload: psi' = the current psi, U = 1 + i H t
+    (t = 0.01), 16384 Monte Carlo samples from psi's persistent chains (one sampling pass with
+    E_loc, log psi' and O' rows, the reductions) per call."""
+    import torch
+    psi_p = +f.psi
+    op = ann.Operator(ann.identity() + 0.01j * f.H)
+    hsd = ann.HilbertSpaceDistance(psi_p.num_params, stream=st)
+    hsd.gradient(f.psi, psi_p, op, True, f.mc, 1.0)
+    reps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        _, d = hsd.gradient(f.psi, psi_p, op, True, f.mc, 1.0)
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    return {"ms_per_gradient_call": ms, "samples": N_CHAINS, "distance": d,
+            "note": "host-synchronous calls (the gradient returns to the host), sampling included"}
+
+
 def run_ours(args):
     import torch
     import annongpu_gb300 as ann
@@ -539,6 +558,8 @@ def run_ours(args):
         out["vs_plain"] = {k: q[k] / p[k] for k in ("sr_steps_per_s", "effective_samples_per_s",
                                                     "sampler_effective_samples_per_s")}
         out["forms"]["plain"]["energy_check"] = results["plain"][0].energy_check()
+    if f.name == "precision":
+        out["hilbert_space_distance"] = hsd_timing(ann, f, st)
     if not args.no_batched and f.name == "precision":
         out["batched_instances"] = batched_instances(ann, st, max(2, args.steps // 5))
     if rank == 0 and not args.no_cpu:

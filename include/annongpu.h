@@ -285,6 +285,18 @@ int ann_tdvp_set_solver(ann_tdvp* tdvp, int solver, unsigned max_iter, double to
 int ann_tdvp_set_chol_update(ann_tdvp* tdvp, int mode);
 
 /* ---------------------------------------------------------------------------------
+ * HilbertSpaceDistance (HilbertSpaceDistance(num_params, gpu), main.cpp.template:436-442;
+ * source/network_functions/HilbertSpaceDistance.cu.template:16-168): distance between
+ * psi_prime and U psi with U = op (is_unitary: U a unitary-like sum; otherwise exp of the
+ * local energy), sampled from psi's ensemble; the gradient is with respect to the
+ * parameters of psi_prime (num_params(psi_prime) complex values), scaled by 1 / distance^nu.
+ * ------------------------------------------------------------------------------ */
+int ann_hsd_distance(ann_psi* psi, ann_psi* psi_prime, ann_op* op, int is_unitary, ann_ens* ens, void* stream,
+                     double* distance);
+int ann_hsd_gradient(ann_psi* psi, ann_psi* psi_prime, ann_op* op, int is_unitary, ann_ens* ens, double nu,
+                     void* stream, double* grad, double* distance);
+
+/* ---------------------------------------------------------------------------------
  * Autotuner (no counterpart in the reference, whose launch shape is fixed: one CTA
  * per chain with blockDim = hidden width, include/ensembles/MonteCarlo.hpp:223-228).
  * ann_autotune times every candidate of each knob on the given workload (CUDA events,

@@ -176,6 +176,33 @@ class Oracle:
                                                      "eloc")])
         return r
 
+    def hsd_exact(self, psi: RbmDesc, psi_p: RbmDesc, expr, unitary, nu=1.0):
+        """HilbertSpaceDistance over all 2^N configurations with the exact-summation weights
+        |psi(s)|^2: the per-sample sums of source/network_functions/
+        HilbertSpaceDistance.cu.template:16-86 and the distance / gradient of :118-168
+        (gradient with respect to the parameters of psi_p). Returns (distance, gradient)."""
+        r = self.exact(psi, expr, want_S=False)
+        rp = self.exact(psi_p, None, want_S=False)
+        lp, lpp, e = r["log_vec"], rp["log_vec"], r["eloc"]
+        w = np.exp(2.0 * lp.real)
+        d = np.conj(lpp - lp)
+        if unitary:
+            omega = np.exp(d) * e
+            nxt = np.abs(e) ** 2
+        else:
+            omega = np.exp(e + d)
+            nxt = np.exp(2.0 * e.real)
+        ratio = np.exp(2.0 * (lpp.real - lp.real))
+        om, pr, nn = np.sum(w * omega), np.sum(w * ratio), np.sum(w * nxt)
+        u = abs(om) ** 2
+        v = nn * pr
+        dist = np.sqrt(max(1.0 - u / v, 1e-8))
+        O = np.array([self.O_k(psi_p, s) for s in range(1 << psi.N)])
+        oO = (w * omega) @ np.conj(O)
+        rO = (w * ratio) @ np.conj(O)
+        grad = -(np.conj(om) * oO * v - u * nn * rO) / v ** 2 / dist ** nu
+        return dist, grad
+
     def mc_reference(self, psi: RbmDesc, expr, num_samples, num_sweeps, num_therm, seed=0, max_props=None):
         N = psi.N
         total = num_therm * N + num_samples * num_sweeps * N

@@ -137,3 +137,40 @@ def test_expression_matrix_matches_exact_energy(oracle):
     r = oracle.exact(psi, H, want_S=False)
     v = r["vec"]
     close(np.vdot(v, H.matrix(N) @ v), r["E"][0], rtol=1e-10)
+
+
+def test_hsd_restatement_distance_and_gradient():
+    """The oracle's HilbertSpaceDistance restatement against the reference's own checks
+    (test/test_HilbertSpaceDistance.py): the distance of psi' = psi to U psi with
+    U = 1 + i H t against dense matrices, and the gradient against central finite
+    differences (d/dRe + i d/dIm, eps 1e-6) of the distance."""
+    import annongpu_gb300.expression as ex
+    from pyoracle import Oracle
+    o = Oracle()
+    N, M = 4, 4
+    rng = np.random.default_rng(5)
+    c = lambda *s: 0.1 * (rng.standard_normal(s) + 1j * rng.standard_normal(s))  # noqa: E731
+    a, b, W = c(N), c(M), c(N, M)
+    make = lambda p: RbmDesc(N, M, p[N + M:].reshape(N, M), a=p[:N], b=p[N:N + M], layout=1)  # noqa: E731
+    p0 = np.concatenate([a, b, W.reshape(-1)])
+    H = ex.transverse_field_ising_1d(N, 0.9)
+    U = ex.identity() + 0.01j * H
+    d, _ = o.hsd_exact(make(p0), make(p0), U, True)
+    v = o.exact(make(p0), None, want_S=False)["vec"]
+    vp = U.matrix(N) @ v
+    d_ref = np.sqrt(1.0 - abs(np.vdot(v / np.linalg.norm(v), vp / np.linalg.norm(vp))) ** 2)
+    assert d == pytest.approx(d_ref, rel=1e-9)
+    # gradient in psi' for psi' != psi (exponential form), against finite differences
+    p1 = p0 + c(p0.size) * 0.3
+    op = 0.2j * H
+    _, g = o.hsd_exact(make(p0), make(p1), op, False)
+    eps = 1e-6
+    g_ref = np.zeros(p1.size, complex)
+    for k in range(p1.size):
+        for unit in (1.0, 1j):
+            dp = np.zeros(p1.size, complex)
+            dp[k] = eps * unit
+            fd = (o.hsd_exact(make(p0), make(p1 + dp), op, False)[0] -
+                  o.hsd_exact(make(p0), make(p1 - dp), op, False)[0]) / (2 * eps)
+            g_ref[k] += unit * fd
+    np.testing.assert_allclose(g, g_ref, rtol=1e-4, atol=1e-7)
