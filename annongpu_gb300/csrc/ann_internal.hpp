@@ -108,8 +108,8 @@ struct ann_ens_impl {
     bool made_dropped = false;
     unsigned long long last_made_acc = 0, last_made_rej = 0;
     // ring buffer of recent sample configurations (training data for the proposal)
-    DevBuf hist;
-    size_t hist_cap = 0, hist_len = 0, hist_pos = 0;
+    DevBuf hist, hist_posd;        // rows; device write position (advanced by every pass)
+    size_t hist_cap = 0, hist_len = 0;
     // tape replay
     DevBuf tape_site, tape_u, tape_init;
     unsigned tape_len = 0;

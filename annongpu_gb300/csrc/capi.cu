@@ -55,6 +55,18 @@ void upload(DevBuf& b, const void* src, size_t bytes) {
     if(bytes) ANN_CUDA(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
 }
 
+namespace {
+// ring buffer of sample configurations: row (pos + i) % cap <- row i of this pass
+__global__ void hist_append_kernel(const uint64_t* __restrict__ conf, size_t n, uint64_t* __restrict__ hist,
+                                   size_t cap, const unsigned long long* __restrict__ pos) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= n) return;
+    const size_t r = (size_t)((*pos + i) % cap);
+    for(int w = 0; w < kMaxWords; w++) hist[r * kMaxWords + w] = conf[i * kMaxWords + w];
+}
+__global__ void hist_advance_kernel(unsigned long long* pos, size_t n) { *pos += n; }
+}  // namespace
+
 unsigned* status_word() {
     int dev = 0;
     ANN_CUDA(cudaGetDevice(&dev));
@@ -147,18 +159,15 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
         cnn_run(psi, op, ens, t, st);
     }
     if(ens.hist_cap) {
-        // append the configurations of this pass to the ring buffer
-        const size_t n = t.rows->n, row = kMaxWords * sizeof(uint64_t);
-        size_t done = 0;
-        while(done < n) {
-            const size_t chunk = std::min(n - done, ens.hist_cap - ens.hist_pos);
-            ANN_CUDA(cudaMemcpyAsync(ens.hist.as<unsigned char>() + ens.hist_pos * row,
-                                     t.rows->conf.as<unsigned char>() + done * row, chunk * row,
-                                     cudaMemcpyDeviceToDevice, st));
-            done += chunk;
-            ens.hist_pos = (ens.hist_pos + chunk) % ens.hist_cap;
-            ens.hist_len = std::min(ens.hist_cap, ens.hist_len + chunk);
-        }
+        // append the configurations of this pass to the ring buffer; the write position is
+        // a device counter, so replays of a captured step keep advancing it
+        const size_t n = t.rows->n;
+        hist_append_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            t.rows->conf.as<uint64_t>(), n, ens.hist.as<uint64_t>(), ens.hist_cap, ens.hist_posd.as<unsigned long long>());
+        check_launch("hist_append_kernel");
+        hist_advance_kernel<<<1, 1, 0, st>>>(ens.hist_posd.as<unsigned long long>(), n);
+        check_launch("hist_advance_kernel");
+        ens.hist_len = std::min(ens.hist_cap, ens.hist_len + n);  // rows valid once written (host bound)
     }
 }
 
@@ -711,8 +720,12 @@ int ann_ens_set_history(ann_ens* e, unsigned capacity) {
     return guard([&] {
         need(e != nullptr, "null argument");
         e->hist_cap = capacity;
-        e->hist_len = e->hist_pos = 0;
-        if(capacity) e->hist.ensure((size_t)capacity * kMaxWords * sizeof(uint64_t));
+        e->hist_len = 0;
+        if(capacity) {
+            e->hist.ensure((size_t)capacity * kMaxWords * sizeof(uint64_t));
+            e->hist_posd.ensure(sizeof(unsigned long long));
+            ANN_CUDA(cudaMemset(e->hist_posd.p, 0, sizeof(unsigned long long)));
+        }
     });
 }
 
