@@ -377,6 +377,223 @@ struct Cnn {
     }
 };
 
+
+// ---- PsiDeep of any depth: PsiDeep.hpp:171-215 (forward_pass), :345-445 (foreach_O_k),
+//      PsiDeep.cu:142-183 (init_kernel: parameter offsets) ----
+struct Deep {
+    const or_deep* p;
+    unsigned N, L, np;
+    std::vector<unsigned> size, C, conn_off, b_off, w_off;
+    std::vector<cd> prm, fw;
+    cd lp;
+    explicit Deep(const or_deep* p_) : p(p_), N(p_->N), L(p_->num_layers) {
+        unsigned off = N, coff = 0;
+        for(unsigned l = 0; l < L; l++) {
+            size.push_back(p->sizes[l]);
+            C.push_back(p->connectivity[l]);
+            conn_off.push_back(coff);
+            coff += C[l] * size[l];
+            b_off.push_back(off);
+            off += size[l];
+            w_off.push_back(off);
+            off += C[l] * size[l];
+        }
+        np = off;
+        prm.resize(np);
+        for(unsigned k = 0; k < np; k++) prm[k] = cx(p->params, k);
+        fw.resize(size[L - 1]);
+        for(unsigned j = 0; j < size[L - 1]; j++) fw[j] = cx(p->fw, j);
+        lp = cd(p->lp_re, p->lp_im);
+    }
+    unsigned conn(unsigned l, unsigned i, unsigned j) const { return p->connections[conn_off[l] + i * size[l] + j]; }
+    cd W(unsigned l, unsigned i, unsigned j) const { return prm[w_off[l] + i * size[l] + j]; }
+    // layer 0 uses my_logcosh(., 0) / my_tanh(., 0); deeper layers index >= 1 (PsiDeep.hpp:182, 207, 369-377)
+    cd f(cd z, unsigned l) const { return act_f(z, l, p->activation); }
+    cd df(cd z, unsigned l) const { return act_df(z, l, p->activation); }
+    // pre-activations z[l][j]; returns log psi
+    cd forward(const Conf& s, std::vector<std::vector<cd>>& z) const {
+        std::vector<cd> in(N);
+        for(unsigned x = 0; x < N; x++) in[x] = spin(s, x);
+        z.assign(L, {});
+        for(unsigned l = 0; l < L; l++) {
+            z[l].assign(size[l], cd(0.0));
+            std::vector<cd> out(size[l]);
+            for(unsigned j = 0; j < size[l]; j++) {
+                cd acc(0.0);
+                for(unsigned i = 0; i < C[l]; i++) acc += W(l, i, j) * in[conn(l, i, j)];
+                acc += prm[b_off[l] + j];
+                z[l][j] = acc;
+                out[j] = f(acc, l);
+            }
+            in = out;
+        }
+        cd r = lp;
+        for(unsigned j = 0; j < size[L - 1]; j++) r += in[j] * fw[j];
+        if(p->a_in_log_psi)
+            for(unsigned x = 0; x < N; x++) r += prm[x] * spin(s, x);
+        return r;
+    }
+    cd log_psi(const Conf& s) const {
+        std::vector<std::vector<cd>> z;
+        return forward(s, z);
+    }
+    void O_k(const Conf& s, std::vector<cd>& O) const {
+        std::vector<std::vector<cd>> z;
+        forward(s, z);
+        O.assign(np, cd(0.0));
+        for(unsigned x = 0; x < N; x++) O[x] = spin(s, x);
+        // dlogpsi / dz for the top layer, then down through the rhs connections
+        std::vector<cd> delta(size[L - 1]);
+        for(unsigned j = 0; j < size[L - 1]; j++) delta[j] = fw[j] * df(z[L - 1][j], L - 1);
+        for(int l = (int)L - 1; l >= 0; l--) {
+            const unsigned in_size = l ? size[l - 1] : N;
+            std::vector<cd> up(in_size, cd(0.0));
+            for(unsigned j = 0; j < size[l]; j++) {
+                O[b_off[l] + j] = delta[j];
+                for(unsigned i = 0; i < C[l]; i++) {
+                    const unsigned u = conn(l, i, j);
+                    const cd inp = l == 0 ? cd(spin(s, u)) : f(z[l - 1][u], l - 1);
+                    O[w_off[l] + i * size[l] + j] = delta[j] * inp;
+                    up[u] += W(l, i, j) * delta[j];
+                }
+            }
+            if(l > 0) {
+                delta.assign(in_size, cd(0.0));
+                for(unsigned u = 0; u < in_size; u++) delta[u] = up[u] * df(z[l - 1][u], l - 1);
+            }
+        }
+    }
+    cd local_energy(const or_op* op, const Conf& s, cd lpsi) const {
+        cd r(0.0);
+        for(unsigned n = 0; n < op->n; n++) {
+            ME me = pauli_apply(op->a + n * op->nw, op->b + n * op->nw, op->nw, s);
+            me.factor *= cx(op->coeff, n);
+            if(me.conf != s) r += me.factor * std::exp(log_psi(me.conf) - lpsi);
+            else r += me.factor;
+        }
+        return r;
+    }
+};
+
+// Counter-based Metropolis chains (the sampler contract above). The model supplies
+//   reset(s)              state for configuration s
+//   dre(s, nx)            Re dlogpsi of the move s -> nx, keeping the proposed state
+//   accept()              the proposed state becomes current
+//   sample(s, op, eloc)   log psi of s from a fresh state; local energy into *eloc
+template<typename Model>
+void philox_chains(Model& m, unsigned N, const or_op* op, unsigned n_chains, uint64_t seed,
+                   unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
+                   int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
+                   uint64_t* conf, uint64_t* counter, uint64_t* sconf, double* slp, double* seloc,
+                   uint64_t* n_accept, uint64_t* n_reject, double* min_tie) {
+    const unsigned nw = nwords(N);
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    uint64_t acc_total = 0, rej_total = 0;
+    double tie = 1e300;
+    for(unsigned c = 0; c < n_chains; c++) {
+        uint64_t t = counter[c];
+        Conf s = init ? draw_initial(k0, k1, c, N, n_up, t) : load_conf(conf + (size_t)c * nw, nw);
+        m.reset(s);
+        auto propose = [&]() {
+            uint32_t ctr[4] = {(uint32_t)t, (uint32_t)(t >> 32), c, 0u}, r[4];
+            philox(k0, k1, ctr, r);
+            t++;
+            unsigned i = mulhi(r[0], N), j = i;
+            if(move_kind == 1) {
+                const unsigned bnd = mulhi(r[0], n_bonds);
+                i = bonds[2 * bnd];
+                j = bonds[2 * bnd + 1];
+            } else if(move_kind == 2) {
+                j = mulhi(r[1], N - 1u);
+                j += (j >= i);
+            }
+            Conf nx = s;
+            if(move_kind == 0) {
+                nx[i >> 6] ^= (uint64_t)1 << (i & 63u);
+            } else {
+                if(spin(s, i) == spin(s, j)) { rej_total++; return; }
+                nx[i >> 6] ^= (uint64_t)1 << (i & 63u);
+                nx[j >> 6] ^= (uint64_t)1 << (j & 63u);
+            }
+            const double ratio = std::exp(2.0 * m.dre(s, nx));
+            const double u = u53(r[2], r[3]);
+            tie = std::min(tie, std::fabs(ratio - u));
+            if(u <= ratio) { s = nx; m.accept(); acc_total++; }
+            else rej_total++;
+        };
+        if(init)
+            for(unsigned k = 0; k < num_therm * N; k++) propose();
+        for(unsigned st = 0; st < samples_per_chain; st++) {
+            for(unsigned k = 0; k < num_sweeps * N; k++) propose();
+            cd el(0.0);
+            const cd lp = m.sample(s, op, seloc ? &el : nullptr);
+            const size_t row = (size_t)st * n_chains + c;
+            if(sconf) for(unsigned w = 0; w < nw; w++) sconf[row * nw + w] = s[w];
+            if(slp) put(slp + 2 * row, lp);
+            if(seloc && op) put(seloc + 2 * row, el);
+        }
+        for(unsigned w = 0; w < nw; w++) conf[(size_t)c * nw + w] = s[w];
+        counter[c] = t;
+    }
+    if(n_accept) *n_accept = acc_total;
+    if(n_reject) *n_reject = rej_total;
+    if(min_tie) *min_tie = tie;
+}
+
+// RBM family: dlogpsi from the angle deltas (the sampler's incremental form);
+// samples recompute the angles
+struct RbmChain {
+    const Rbm& psi;
+    std::vector<cd> th, th2;
+    explicit RbmChain(const Rbm& p) : psi(p) {}
+    void reset(const Conf& s) { psi.angles(s, th); }
+    double dre(const Conf& s, const Conf& nx) {
+        th2 = th;
+        psi.update(th2, s, nx);
+        const int act = psi.p->activation;
+        cd d(0.0);
+        for(unsigned q = 0; q < psi.M; q++) d += (act_f(th2[q], 0, act) - act_f(th[q], 0, act)) * psi.fw[q];
+        if(psi.p->a_in_log_psi)
+            for(unsigned w = 0; w < 2; w++) {
+                uint64_t dm = s[w] ^ nx[w];
+                while(dm) {
+                    const unsigned pos = 64u * w + __builtin_ctzll(dm);
+                    dm &= dm - 1;
+                    d += psi.a[pos] * (spin(nx, pos) - spin(s, pos));
+                }
+            }
+        return d.real();
+    }
+    void accept() { th = th2; }
+    cd sample(const Conf& s, const or_op* op, cd* eloc) {
+        psi.angles(s, th);
+        const cd lp = psi.log_psi(s, th);
+        if(op && eloc) {
+            std::vector<cd> th3 = th;
+            *eloc = local_energy_incremental(psi, op, s, lp, th3);
+        }
+        return lp;
+    }
+};
+
+// PsiDeep: full forward passes
+struct DeepChain {
+    const Deep& psi;
+    cd lp{0.0}, lp2{0.0};
+    explicit DeepChain(const Deep& p) : psi(p) {}
+    void reset(const Conf& s) { lp = psi.log_psi(s); }
+    double dre(const Conf&, const Conf& nx) {
+        lp2 = psi.log_psi(nx);
+        return lp2.real() - lp.real();
+    }
+    void accept() { lp = lp2; }
+    cd sample(const Conf& s, const or_op* op, cd* eloc) {
+        lp = psi.log_psi(s);
+        if(op && eloc) *eloc = psi.local_energy(op, s, lp);
+        return lp;
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -507,78 +724,9 @@ void or_rbm_mc_philox(const or_rbm* p, const or_op* op, unsigned n_chains, uint6
                       uint64_t* sconf, double* slp, double* seloc,
                       uint64_t* n_accept, uint64_t* n_reject, double* min_tie) {
     Rbm psi(p);
-    const unsigned N = p->N, nw = nwords(N);
-    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    uint64_t acc_total = 0, rej_total = 0;
-    double tie = 1e300;
-    for(unsigned c = 0; c < n_chains; c++) {
-        uint64_t t = counter[c];
-        Conf s = init ? draw_initial(k0, k1, c, N, n_up, t) : load_conf(conf + (size_t)c * nw, nw);
-        std::vector<cd> th;
-        psi.angles(s, th);
-        auto propose = [&]() {
-            uint32_t ctr[4] = {(uint32_t)t, (uint32_t)(t >> 32), c, 0u}, r[4];
-            philox(k0, k1, ctr, r);
-            t++;
-            unsigned i = mulhi(r[0], N), j = i;
-            if(move_kind == 1) {
-                const unsigned bnd = mulhi(r[0], n_bonds);
-                i = bonds[2 * bnd];
-                j = bonds[2 * bnd + 1];
-            } else if(move_kind == 2) {
-                j = mulhi(r[1], N - 1u);
-                j += (j >= i);
-            }
-            Conf nx = s;
-            if(move_kind == 0) {
-                nx[i >> 6] ^= (uint64_t)1 << (i & 63u);
-            } else {
-                if(spin(s, i) == spin(s, j)) { rej_total++; return; }
-                nx[i >> 6] ^= (uint64_t)1 << (i & 63u);
-                nx[j >> 6] ^= (uint64_t)1 << (j & 63u);
-            }
-            // dlogpsi from the angle deltas (the sampler's incremental form)
-            std::vector<cd> th2 = th;
-            psi.update(th2, s, nx);
-            cd d(0.0);
-            for(unsigned q = 0; q < psi.M; q++)
-                d += (act_f(th2[q], 0, p->activation) - act_f(th[q], 0, p->activation)) * psi.fw[q];
-            if(p->a_in_log_psi)
-                for(unsigned w = 0; w < 2; w++) {
-                    uint64_t dm = s[w] ^ nx[w];
-                    while(dm) {
-                        const unsigned pos = 64u * w + __builtin_ctzll(dm);
-                        dm &= dm - 1;
-                        d += psi.a[pos] * (spin(nx, pos) - spin(s, pos));
-                    }
-                }
-            const double ratio = std::exp(2.0 * d.real());
-            const double u = u53(r[2], r[3]);
-            tie = std::min(tie, std::fabs(ratio - u));
-            if(u <= ratio) { s = nx; th = th2; acc_total++; }
-            else rej_total++;
-        };
-        if(init)
-            for(unsigned k = 0; k < num_therm * N; k++) propose();
-        for(unsigned st = 0; st < samples_per_chain; st++) {
-            for(unsigned k = 0; k < num_sweeps * N; k++) propose();
-            // samples: recomputed angles, full log psi, local energy
-            psi.angles(s, th);
-            const cd lp = psi.log_psi(s, th);
-            const size_t row = (size_t)st * n_chains + c;
-            if(sconf) for(unsigned w = 0; w < nw; w++) sconf[row * nw + w] = s[w];
-            if(slp) put(slp + 2 * row, lp);
-            if(seloc && op) {
-                std::vector<cd> th3 = th;
-                put(seloc + 2 * row, local_energy_incremental(psi, op, s, lp, th3));
-            }
-        }
-        for(unsigned w = 0; w < nw; w++) conf[(size_t)c * nw + w] = s[w];
-        counter[c] = t;
-    }
-    if(n_accept) *n_accept = acc_total;
-    if(n_reject) *n_reject = rej_total;
-    if(min_tie) *min_tie = tie;
+    RbmChain m(psi);
+    philox_chains(m, p->N, op, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind, bonds, n_bonds,
+                  init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
 }
 
 void or_cnn_log_psi(const or_cnn* p, const uint64_t* conf, double* out) {
@@ -636,6 +784,59 @@ void or_rbm_tdvp_samples(const or_rbm* p, const or_op* op, const uint64_t* confs
         acc.add(weight, eloc, Ok, tS != nullptr);
     }
     acc.finish(nullptr, nullptr, E, tE2, tO, tF, tS);
+}
+
+unsigned or_deep_num_params(const or_deep* p) { return Deep(p).np; }
+
+void or_deep_log_psi(const or_deep* p, const uint64_t* conf, double* out) {
+    Deep psi(p);
+    put(out, psi.log_psi(load_conf(conf, nwords(p->N))));
+}
+
+void or_deep_O_k(const or_deep* p, const uint64_t* conf, double* out) {
+    Deep psi(p);
+    std::vector<cd> O;
+    psi.O_k(load_conf(conf, nwords(p->N)), O);
+    for(size_t k = 0; k < O.size(); k++) put(out + 2 * k, O[k]);
+}
+
+void or_deep_local_energy(const or_deep* p, const or_op* op, const uint64_t* conf, double* out) {
+    Deep psi(p);
+    const Conf s = load_conf(conf, nwords(p->N));
+    put(out, psi.local_energy(op, s, psi.log_psi(s)));
+}
+
+void or_deep_exact(const or_deep* p, const or_op* op, double* E, double* norm,
+                   double* tE, double* tE2, double* tO, double* tF, double* tS) {
+    Deep psi(p);
+    Accum acc(psi.np);
+    double nrm = 0.0;
+    std::vector<cd> Ok;
+    for(uint64_t idx = 0; idx < ((uint64_t)1 << psi.N); idx++) {
+        const Conf s = enumerate(idx);
+        const cd lp = psi.log_psi(s);
+        const double w = std::exp(2.0 * lp.real());
+        const cd eloc = op ? psi.local_energy(op, s, lp) : cd(0.0);
+        if(tO || tF || tS) psi.O_k(s, Ok);
+        else Ok.assign(psi.np, cd(0.0));
+        acc.add(w, eloc, Ok, tS != nullptr);
+        nrm += w;
+    }
+    if(E) put(E, acc.E);
+    if(norm) norm[0] = std::sqrt(nrm);
+    acc.finish(nullptr, nullptr, tE, tE2, tO, tF, tS);
+}
+
+void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uint64_t seed,
+                       unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
+                       int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
+                       uint64_t* conf, uint64_t* counter,
+                       uint64_t* sconf, double* slp, double* seloc,
+                       uint64_t* n_accept, uint64_t* n_reject, double* min_tie) {
+    Deep psi(p);
+    DeepChain m(psi);
+    philox_chains(m, p->N, op, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind, bonds, n_bonds,
+                  init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
 }
 
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

@@ -11,6 +11,9 @@
 //   PsiRBM ........................ include/quantum_state/PsiRBM.hpp:69-176
 //   PsiDeep (1 hidden layer) ...... include/quantum_state/PsiDeep.hpp:138-445,
 //                                   source/quantum_state/PsiDeep.cu:142-305
+//   PsiDeep (any depth) ........... include/quantum_state/PsiDeep.hpp:171-215 (forward),
+//                                   :345-445 (O_k back-propagation),
+//                                   source/quantum_state/PsiDeep.cu:142-183 (parameter layout)
 //   PsiCNN ........................ include/quantum_state/PsiCNN.hpp:97-266,
 //                                   include/quantum_state/detail/Convolve.hpp:15-173
 //   MonteCarlo host path .......... include/ensembles/MonteCarlo.hpp:55-177,
@@ -66,6 +69,25 @@ struct or_cnn {
     int activation;                // 0: reference layer polynomials ; 1: log cosh on every layer
 };
 
+// PsiDeep with any number of hidden layers. Layer l (0-based) has sizes[l] units;
+// unit j of layer l reads connectivity[l] units of the layer below (the spins for
+// l = 0): entry (i, j) of its connection block is the index of the i-th of them.
+// params = [a(N) | b_0 | W_0 | b_1 | W_1 | ...], W_l entry (i, j) at i*sizes[l] + j.
+// log psi = lp (+ a.s) + sum_j fw_j f_L(z_L,j); f on layer 0 is the log-cosh
+// polynomial, on deeper layers the odd (tanh-like) polynomial.
+struct or_deep {
+    unsigned N;
+    unsigned num_layers;
+    const unsigned* sizes;         // num_layers
+    const unsigned* connectivity;  // num_layers
+    const unsigned* connections;   // concatenated blocks, connectivity[l] x sizes[l] each
+    const double* params;          // interleaved complex
+    const double* fw;              // sizes[num_layers - 1] complex final weights
+    double lp_re, lp_im;
+    int a_in_log_psi;              // 0 reproduces the reference (PsiDeep.hpp:260-264)
+    int activation;                // 0: reference layer polynomials ; 1: log cosh on every layer
+};
+
 unsigned or_rbm_num_params(const or_rbm* p);
 void or_rbm_log_psi(const or_rbm* p, const uint64_t* conf, double* out);
 void or_rbm_O_k(const or_rbm* p, const uint64_t* conf, double* out);
@@ -112,6 +134,20 @@ void or_cnn_O_k(const or_cnn* p, const uint64_t* conf, double* out);
 void or_cnn_local_energy(const or_cnn* p, const or_op* op, const uint64_t* conf, double* out);
 void or_cnn_exact(const or_cnn* p, const or_op* op, double* E, double* norm,
                   double* tE, double* tE2, double* tO, double* tF, double* tS);
+
+unsigned or_deep_num_params(const or_deep* p);
+void or_deep_log_psi(const or_deep* p, const uint64_t* conf, double* out);
+void or_deep_O_k(const or_deep* p, const uint64_t* conf, double* out);
+void or_deep_local_energy(const or_deep* p, const or_op* op, const uint64_t* conf, double* out);
+void or_deep_exact(const or_deep* p, const or_op* op, double* E, double* norm,
+                   double* tE, double* tE2, double* tO, double* tF, double* tS);
+// counter-based chains (same contract as or_rbm_mc_philox); dlogpsi from full forward passes
+void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uint64_t seed,
+                       unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
+                       int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
+                       uint64_t* conf, uint64_t* counter,
+                       uint64_t* sconf, double* slp, double* seloc,
+                       uint64_t* n_accept, uint64_t* n_reject, double* min_tie);
 
 // Pauli application, single string (for KATs).
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

@@ -49,6 +49,12 @@ class OrCnn(ct.Structure):
                 ("lp_re", ct.c_double), ("lp_im", ct.c_double), ("activation", ct.c_int)]
 
 
+class OrDeep(ct.Structure):
+    _fields_ = [("N", ct.c_uint), ("num_layers", ct.c_uint), ("sizes", P), ("connectivity", P),
+                ("connections", P), ("params", P), ("fw", P), ("lp_re", ct.c_double), ("lp_im", ct.c_double),
+                ("a_in_log_psi", ct.c_int), ("activation", ct.c_int)]
+
+
 def nwords(N):
     return (N + 63) // 64
 
@@ -126,6 +132,34 @@ class CnnDesc:
         return self.params.size
 
 
+class DeepDesc:
+    """PsiDeep with any number of hidden layers for the oracle.
+
+    ``connections[l]`` is the (C_l x M_l) block of layer l (entry (i, j): the i-th unit
+    of the layer below read by unit j); params = [a | b_0 | W_0 | b_1 | W_1 | ...].
+    """
+
+    def __init__(self, N, connections, params, fw, log_prefactor=0j, a_in_log_psi=True, activation=0):
+        self.N = int(N)
+        blocks = [np.asarray(c, np.uint32) for c in connections]
+        self.sizes = np.ascontiguousarray([b.shape[1] for b in blocks], np.uint32)
+        self.connectivity = np.ascontiguousarray([b.shape[0] for b in blocks], np.uint32)
+        self.connections = np.ascontiguousarray(np.concatenate([b.reshape(-1) for b in blocks]))
+        self.params = np.ascontiguousarray(np.asarray(params, np.complex128))
+        self.fw = np.ascontiguousarray(np.broadcast_to(np.asarray(fw, np.complex128), (int(self.sizes[-1]),)))
+        self.lp = complex(log_prefactor)
+        expect = self.N + int(sum(int(m) * (1 + int(c)) for m, c in zip(self.sizes, self.connectivity)))
+        if self.params.size != expect:
+            raise ValueError(f"params has {self.params.size} entries, the layer structure needs {expect}")
+        self.struct = OrDeep(self.N, len(blocks), _ptr(self.sizes), _ptr(self.connectivity),
+                             _ptr(self.connections), _ptr(self.params), _ptr(self.fw), self.lp.real, self.lp.imag,
+                             int(a_in_log_psi), int(activation))
+
+    @property
+    def num_params(self):
+        return self.params.size
+
+
 class Oracle:
     def __init__(self):
         self.lib = ct.CDLL(build_oracle())
@@ -138,6 +172,8 @@ class Oracle:
         L.or_rbm_mc_reference.argtypes = [P, P, ct.c_uint, ct.c_uint, ct.c_uint, ct.c_uint,
                                           P, P, P, P, P, P, P, ct.c_uint, P]
         L.or_activation.argtypes = [ct.c_double, ct.c_double, ct.c_uint, ct.c_int, P, P]
+        L.or_deep_num_params.restype = ct.c_uint
+        L.or_deep_mc_philox.argtypes = L.or_rbm_mc_philox.argtypes
 
     # ---- RBM family ----
     def log_psi(self, psi: RbmDesc, conf):
@@ -238,7 +274,7 @@ class Oracle:
         return out
 
     def mc_philox(self, psi: RbmDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
-                  move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None):
+                  move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None, _fn=None):
         N = psi.N
         nw = max(1, nwords(N))
         op = OpArrays(expr, N) if expr is not None else None
@@ -250,11 +286,11 @@ class Oracle:
         r = dict(sconf=np.zeros(ns * nw, np.uint64), slp=np.zeros(ns, np.complex128),
                  seloc=np.zeros(ns, np.complex128), acc=np.zeros(1, np.uint64), rej=np.zeros(1, np.uint64),
                  tie=np.zeros(1))
-        self.lib.or_rbm_mc_philox(ct.byref(psi.struct), ct.byref(op.struct) if op else None, n_chains, seed,
-                                  samples_per_chain, num_sweeps, num_therm, move_kind, _ptr(bonds_a),
-                                  0 if bonds_a is None else bonds_a.size // 2, int(init), n_up,
-                                  _ptr(conf), _ptr(counter), _ptr(r["sconf"]), _ptr(r["slp"]),
-                                  _ptr(r["seloc"]), _ptr(r["acc"]), _ptr(r["rej"]), _ptr(r["tie"]))
+        fn = self.lib.or_rbm_mc_philox if _fn is None else _fn
+        fn(ct.byref(psi.struct), ct.byref(op.struct) if op else None, n_chains, seed, samples_per_chain, num_sweeps,
+           num_therm, move_kind, _ptr(bonds_a), 0 if bonds_a is None else bonds_a.size // 2, int(init), n_up,
+           _ptr(conf), _ptr(counter), _ptr(r["sconf"]), _ptr(r["slp"]), _ptr(r["seloc"]), _ptr(r["acc"]),
+           _ptr(r["rej"]), _ptr(r["tie"]))
         r["conf"] = conf
         r["counter"] = counter
         return r
@@ -289,6 +325,41 @@ class Oracle:
                               *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
         return r
 
+    # ---- PsiDeep, any depth ----
+    def deep_log_psi(self, psi: DeepDesc, conf):
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_deep_log_psi(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def deep_O_k(self, psi: DeepDesc, conf):
+        out = np.zeros(psi.num_params, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_deep_O_k(ct.byref(psi.struct), _ptr(w), _ptr(out))
+        return out
+
+    def deep_local_energy(self, psi: DeepDesc, expr, conf):
+        op = OpArrays(expr, psi.N)
+        out = np.zeros(1, np.complex128)
+        w = conf_words(conf, psi.N)
+        self.lib.or_deep_local_energy(ct.byref(psi.struct), ct.byref(op.struct), _ptr(w), _ptr(out))
+        return out[0]
+
+    def deep_exact(self, psi: DeepDesc, expr, want_S=False):
+        np_ = psi.num_params
+        r = dict(E=np.zeros(1, np.complex128), norm=np.zeros(1), tE=np.zeros(1, np.complex128), tE2=np.zeros(1),
+                 tO=np.zeros(np_, np.complex128), tF=np.zeros(np_, np.complex128),
+                 tS=np.zeros((np_, np_), np.complex128) if want_S else None)
+        op = OpArrays(expr, psi.N)
+        self.lib.or_deep_exact(ct.byref(psi.struct), ct.byref(op.struct),
+                               *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
+        return r
+
+    def deep_mc_philox(self, psi: DeepDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
+                       move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None):
+        return self.mc_philox(psi, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind,
+                              bonds, init, n_up, conf, counter, _fn=self.lib.or_deep_mc_philox)
+
     def pauli_apply(self, a, b, conf, N):
         nw = max(1, nwords(N))
         aw, bw, cw = conf_words(a, N), conf_words(b, N), conf_words(conf, N)
@@ -321,4 +392,8 @@ class RefHarness:
         self.lib.ref_cnn_O_k.argtypes = [P, U, P, P, P, P, U, D, P, ct.c_uint64, P]
         self.lib.ref_cnn_exact_energy.argtypes = [P, U, P, P, P, P, U, D, P, P, P, P, U, P, P]
         self.lib.ref_activation.argtypes = [D, D, U, P, P]
+        self.lib.ref_deepml_num_params.restype = U
+        self.lib.ref_deepml_num_params.argtypes = [U, U, P, P, P, P, P, P]
+        self.lib.ref_deepml_log_psi_s.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, P]
+        self.lib.ref_deepml_O_k.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, P]
         self.lib.ref_pauli_apply.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64, U, P, P]

@@ -8,6 +8,8 @@
 // Every computation below runs the reference's templates with gpu=false:
 //   * Operator / PauliString::apply / local_energy  include/operator/Operator.hpp:36-121
 //   * PsiDeep (1 hidden layer, ENABLE_NETWORK_BASES) include/quantum_state/PsiDeep.hpp:138-445
+//   * PsiDeep (several hidden layers)                the same kernel, layers assembled as
+//                                                    the Python constructor does (PsiDeep.hpp:488-560)
 //   * PsiRBM kernel                                 include/quantum_state/PsiRBM.hpp:69-176
 //   * PsiCNN kernel                                 include/quantum_state/PsiCNN.hpp:97-266
 //   * MonteCarlo_t::kernel_foreach / mc_update       include/ensembles/MonteCarlo.hpp:55-177
@@ -229,6 +231,60 @@ PsiDeep make_deep(const DeepDesc& d) {
     return psi;
 }
 
+// Several hidden layers: the reference's multi-layer constructor is __PYTHONCC__-only
+// (PsiDeep.hpp:488-560); this assembles the same layer list (input layer first, each
+// layer's rhs lists compiled from the next layer's connections) and lets the
+// reference's init_kernel / set_params fill offsets and weights.
+struct DeepMLDesc {
+    unsigned N, L;
+    const unsigned* sizes;         // L
+    const unsigned* connectivity;  // L
+    const unsigned* conn;          // concatenated C_l x sizes[l] blocks
+    const double* params;          // [a | b_0 | W_0 | ...] interleaved complex
+    const double* final_w;         // sizes[L-1] complex
+    const double* log_pref;
+};
+
+PsiDeep make_deep_ml(const DeepMLDesc& d) {
+    PsiDeep psi(d.N, d.sizes[0], false);
+    psi.layers.clear();
+    psi.num_layers = d.L + 1u;
+    psi.width = d.N;
+    psi.num_units = 0u;
+    std::vector<unsigned> coff(d.L, 0u);
+    for(auto l = 1u; l < d.L; l++) coff[l] = coff[l - 1] + d.connectivity[l - 1] * d.sizes[l - 1];
+    Array<unsigned int> rhs_c(0, false);
+    Array<complex_t> rhs_w(0, false);
+    for(int l = int(d.L) - 1; l >= 0; l--) {
+        const unsigned size = d.sizes[l], C = d.connectivity[l];
+        Array<unsigned int> lc(C * size, false);
+        Array<complex_t> lw(C * size, false), bs(size, false);
+        for(auto k = 0u; k < C * size; k++) {
+            lc[k] = d.conn[coff[l] + k];
+            lw[k] = complex_t(0.0, 0.0);
+        }
+        for(auto j = 0u; j < size; j++) bs[j] = complex_t(0.0, 0.0);
+        if(size > psi.width) psi.width = size;
+        psi.num_units += size;
+        auto rhs = psi.compile_rhs_connections_and_weights(l > 0 ? d.sizes[l - 1] : d.N, size, C, lc, lw);
+        psi.layers.push_front({size, C, std::move(lc), std::move(rhs_c), std::move(lw), std::move(rhs_w),
+                               std::move(bs)});
+        rhs_c = std::move(rhs.first);
+        rhs_w = std::move(rhs.second);
+    }
+    psi.layers.push_front({d.N, 0u, Array<unsigned int>(1, false), std::move(rhs_c), Array<complex_t>(1, false),
+                           std::move(rhs_w), Array<complex_t>(1, false)});
+    const unsigned last = d.sizes[d.L - 1];
+    psi.final_weights.resize(last);
+    for(auto j = 0u; j < last; j++) psi.final_weights[j] = complex_t(d.final_w[2 * j], d.final_w[2 * j + 1]);
+    psi.log_prefactor = complex_t(d.log_pref[0], d.log_pref[1]);
+    psi.init_kernel();
+    Array<complex_t> p(psi.num_params, false);
+    for(auto k = 0u; k < psi.num_params; k++) p[k] = complex_t(d.params[2 * k], d.params[2 * k + 1]);
+    psi.set_params(p);
+    return psi;
+}
+
 void put(double* out, const complex_t& z) { out[0] = z.real(); out[1] = z.imag(); }
 void put(double* out, const std::complex<double>& z) { out[0] = z.real(); out[1] = z.imag(); }
 
@@ -341,6 +397,32 @@ unsigned ref_deep_mc(unsigned N, unsigned M, unsigned C, const unsigned* conn, c
     auto psi = make_deep({N, M, C, conn, params, fw, lp});
     return mc_trace(psi, {a, b, coeff, n_strings}, num_samples, num_sweeps, num_therm,
                     sconf, slp, seloc, pconf, psite, max_props, mc_energy);
+}
+
+// ---- PsiDeep (several hidden layers) ----
+unsigned ref_deepml_num_params(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                               const unsigned* conn, const double* params, const double* fw, const double* lp) {
+    return make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp}).num_params;
+}
+void ref_deepml_log_psi_s(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                          const unsigned* conn, const double* params, const double* fw, const double* lp,
+                          uint64_t conf, double* out) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp});
+    psi_log_psi_s(psi, conf, out);
+}
+void ref_deepml_O_k(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                    const unsigned* conn, const double* params, const double* fw, const double* lp,
+                    uint64_t conf, double* out) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp});
+    psi_O_k(psi, conf, out);
+}
+void ref_deepml_exact(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                      const unsigned* conn, const double* params, const double* fw, const double* lp,
+                      const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                      double* E, double* fluct, double* grad, double* tE, double* tE2, double* tO,
+                      double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp});
+    exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
 }
 
 // ---- PsiRBM (no biases) ----

@@ -6,7 +6,7 @@ stores inputs and outputs as .npz files. The fixtures pin the FP64 oracle
 (oracle/oracle.cpp) and, through it, the CUDA path. The reference checkout is
 needed only to regenerate them:
 
-    make -C oracle ref && python tests/golden/gen_golden.py
+    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml]
 """
 
 import ctypes as ct
@@ -182,6 +182,47 @@ def gen_cnn(ref, rng):
                         ex_E=E, ex_norm=norm)
 
 
+def builder_connections(N, M, C):
+    """Connection blocks of the reference's deep-network constructor for a 1-d input
+    (pyANNonGPU/new_neural_network.py:88-112): unit j of a layer reads (j * delta + i) % n."""
+    out = []
+    for n, m, c in zip([N] + M[:-1], M, C):
+        delta = 1 if m > n else (n // m if n % m == 0 else c)
+        out.append(np.array([[(j * delta + i) % n for j in range(m)] for i in range(c)], np.uint32))
+    return out
+
+
+def gen_deep_ml(ref, rng, name, N, M, C):
+    """PsiDeep with several hidden layers through the reference's own kernel."""
+    blocks = builder_connections(N, M, C)
+    sizes = np.array(M, np.uint32)
+    conn_c = np.array(C, np.uint32)
+    conn = np.ascontiguousarray(np.concatenate([b.reshape(-1) for b in blocks]))
+    np_ = N + sum(m * (1 + c) for m, c in zip(M, C))
+    params = cplx(rng, np_, 0.15)
+    fw = (1.0 + cplx(rng, M[-1], 0.1)).astype(np.complex128)
+    lp = np.array([0.03 - 0.2j])
+    H = mixed_hamiltonian(N) if N >= 6 else transverse_field_ising_1d(N, h=0.9, J=1.1)
+    a, b, c, n = op_arrays(H)
+    confs = np.arange(1 << N, dtype=np.uint64) if N <= 4 else rng.integers(0, 1 << N, 12).astype(np.uint64)
+    args = (N, len(M), P(sizes), P(conn_c), P(conn), P(params), P(fw), P(lp))
+    assert ref.lib.ref_deepml_num_params(*args) == np_
+    lps, oks = [], []
+    for s in confs:
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_deepml_log_psi_s(*args, int(s), P(r))
+        lps.append(r[0])
+        o = np.zeros(np_, np.complex128)
+        ref.lib.ref_deepml_O_k(*args, int(s), P(o))
+        oks.append(o)
+    ex = exact_outputs(np_, N)
+    ref.lib.ref_deepml_exact(*args, P(a), P(b), P(c), n, *[P(ex[k]) for k in KEYS])
+    out = {"N": N, "sizes": sizes, "connectivity": conn_c, "conn": conn, "params": params, "fw": fw, "lp": lp,
+           "op_a": a, "op_b": b, "op_c": c, "confs": confs, "log_psi": np.array(lps), "O_k": np.array(oks)}
+    out.update({"ex_" + k: v for k, v in ex.items()})
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
 def gen_kats(ref, rng):
     zs = cplx(rng, 24, 0.6)
     f = np.zeros((2, 24), np.complex128)
@@ -208,8 +249,11 @@ def gen_kats(ref, rng):
                         pauli_b=pb, pauli_conf=pc, pauli_factor=fac, pauli_out=oc)
 
 
-def main():
+def main(only=None):
     ref = RefHarness()
+    if only == "deep_ml":
+        gen_deep_ml_all(ref)
+        return
     rng = np.random.default_rng(20261203)
     gen_kats(ref, rng)
     gen_rbm(ref, rng)
@@ -219,8 +263,18 @@ def main():
     gen_deep(ref, rng, "deep_n6_m12_c3", n, m, c, conn)
     gen_deep(ref, rng, "deep_n16_m16", 16, 16, 16, None, with_S=False, mc=False, confs_n=6)
     gen_cnn(ref, rng)
+    gen_deep_ml_all(ref)
     print("fixtures written to", HERE)
 
 
+def gen_deep_ml_all(ref):
+    # own generator, so these fixtures do not depend on the ones above
+    rng = np.random.default_rng(20261204)
+    # the shape of the reference test suite's deep-network fixture (test/conftest.py)
+    gen_deep_ml(ref, rng, "deep3_n3_18_9_3", 3, [18, 9, 3], [3, 2, 3])
+    gen_deep_ml(ref, rng, "deep3_n8_16_8_4", 8, [16, 8, 4], [4, 4, 2])
+    gen_deep_ml(ref, rng, "deep2_n6_12_6", 6, [12, 6], [3, 4])
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

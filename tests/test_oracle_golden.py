@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from pyoracle import CnnDesc, RbmDesc
+from pyoracle import CnnDesc, DeepDesc, RbmDesc
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -35,6 +35,19 @@ def deep_from(g):
     p = g["params"]
     return RbmDesc(N, M, p[N + M:], a=p[:N], b=p[N:N + M], fw=g["fw"], conn=g.get("conn"),
                    log_prefactor=g["lp"][0], layout=1, a_in_log_psi=False)
+
+
+def deep_ml_from(g):
+    """A multi-layer fixture as the oracle's DeepDesc (reference semantics: no a.s in log psi)."""
+    N = int(g["N"])
+    blocks, off = [], 0
+    for m, c in zip(g["sizes"], g["connectivity"]):
+        blocks.append(g["conn"][off:off + int(m) * int(c)].reshape(int(c), int(m)))
+        off += int(m) * int(c)
+    return DeepDesc(N, blocks, g["params"], g["fw"], log_prefactor=g["lp"][0], a_in_log_psi=False)
+
+
+DEEP_ML = ["deep3_n3_18_9_3.npz", "deep3_n8_16_8_4.npz", "deep2_n6_12_6.npz"]
 
 
 def close(x, y, rtol=1e-10, atol=1e-12):
@@ -111,6 +124,39 @@ def test_mc_trace_bit_exact(oracle, name):
     close(r["slp"], g["mc_slp"])
     close(r["seloc"], g["mc_seloc"], rtol=1e-9, atol=1e-11)
     close(r["energy"][0], g["mc_mc_energy"][0], rtol=1e-9)
+
+
+@pytest.mark.parametrize("name", DEEP_ML)
+def test_deep_multilayer(oracle, name):
+    """PsiDeep with two and three hidden layers: log psi, O_k (back-propagation) and the
+    exact-summation TDVP quantities of the reference's own kernel."""
+    g = load(name)
+    psi = deep_ml_from(g)
+    for k, s in enumerate(g["confs"]):
+        close(oracle.deep_log_psi(psi, int(s)), g["log_psi"][k])
+        close(oracle.deep_O_k(psi, int(s)), g["O_k"][k], rtol=1e-10, atol=1e-12)
+    r = oracle.deep_exact(psi, _Expr(g["op_a"], g["op_b"], g["op_c"]), want_S=True)
+    close(r["E"][0], g["ex_E"][0])
+    close(r["norm"][0], g["ex_norm"][0])
+    close(r["tE"][0], g["ex_tE"][0])
+    close(r["tE2"][0], g["ex_tE2"][0])
+    close(r["tO"], g["ex_tO"])
+    close(r["tF"], g["ex_tF"], rtol=1e-9, atol=1e-10)
+    close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-10)
+
+
+def test_deep_one_layer_equals_rbm_family(oracle):
+    """The any-depth restatement with one hidden layer is the RBM-family PsiDeep."""
+    g = load("deep_n6_m12_c3.npz")
+    N, M, C = int(g["N"]), int(g["M"]), int(g["C"])
+    rb = deep_from(g)
+    dp = DeepDesc(N, [g["conn"].reshape(C, M)], g["params"], g["fw"], log_prefactor=g["lp"][0],
+                  a_in_log_psi=False)
+    expr = _Expr(g["op_a"], g["op_b"], g["op_c"])
+    for s in range(0, 1 << N, 7):
+        close(oracle.deep_log_psi(dp, s), oracle.log_psi(rb, s), rtol=1e-13)
+        close(oracle.deep_O_k(dp, s), oracle.O_k(rb, s), rtol=1e-13, atol=1e-14)
+        close(oracle.deep_local_energy(dp, expr, s), oracle.local_energy(rb, expr, s), rtol=1e-11, atol=1e-12)
 
 
 def test_cnn(oracle):
