@@ -53,6 +53,12 @@ class CnnDesc(ct.Structure):
                 ("log_prefactor", D * 2), ("activation", I), ("precision", I)]
 
 
+class DeepDesc(ct.Structure):
+    _fields_ = [("N", U), ("num_layers", U), ("sizes", P), ("connectivity", P), ("connections", P),
+                ("params", P), ("num_params", U), ("final_weights", P), ("log_prefactor", D * 2),
+                ("a_in_log_psi", I), ("activation", I), ("precision", I)]
+
+
 class McDesc(ct.Structure):
     _fields_ = [("num_samples", U), ("num_sweeps", U), ("num_thermalization_sweeps", U),
                 ("num_markov_chains", U), ("move", I), ("bonds", P), ("n_bonds", U), ("n_up", I),
@@ -69,6 +75,7 @@ _SIGS = {
     "ann_status": ([P], I),
     "ann_psi_create_rbm": ([P, P], I),
     "ann_psi_create_cnn": ([P, P], I),
+    "ann_psi_create_deep": ([P, P], I),
     "ann_psi_copy": ([P, P], I),
     "ann_psi_destroy": ([P], I),
     "ann_psi_num_params": ([P, P], I),

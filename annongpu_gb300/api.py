@@ -258,9 +258,18 @@ def _json_default(o):
 
 
 class PsiDeep(_Psi):
-    """Feed-forward network with sparse connectivity (include/quantum_state/PsiDeep.hpp:70-471),
-    one hidden layer: theta_j = b_j + sum_c W[c,j] s[connections[c,j]],
-    log psi = log_prefactor + (a.s) + sum_j final_weights_j f(theta_j), params = [a | b | W].
+    """Feed-forward network with sparse connectivity (include/quantum_state/PsiDeep.hpp:70-471).
+
+    Hidden layer l has M_l units; unit j reads C_l units of the layer below (the spins
+    for l = 0) through ``connections[l]`` (C_l x M_l):
+        z_0,j = b_0,j + sum_i W_0[i,j] s[connections[0][i,j]]
+        z_l,j = b_l,j + sum_i W_l[i,j] f(z_{l-1})[connections[l][i,j]]
+        log psi = log_prefactor + (a.s) + sum_j final_weights_j f(z_L,j)
+    params = [a | b_0 | W_0 | b_1 | W_1 | ...]. f is the reference's log-cosh polynomial
+    on the first layer and its odd polynomial deeper (``activation="logcosh"``: log cosh
+    on every layer). One hidden layer runs on the RBM-family kernels (which also take the
+    learned proposal); more layers (up to 4; the reference allows 3) on kernels that keep
+    the first layer's pre-activations per chain and run the deeper layers in full.
 
     ``a_in_log_psi=False`` reproduces the reference exactly, whose log psi omits a.s
     (PsiDeep.hpp:260-264) while its O_k still reports s for the a entries.
@@ -270,27 +279,63 @@ class PsiDeep(_Psi):
                  a_in_log_psi=True, activation="poly", precision="fp32"):
         if isinstance(b, np.ndarray) and b.ndim == 1:
             b, connections, W = [b], [connections], [W]
-        if len(W) != 1:
-            raise NotImplementedError("this build supports PsiDeep with one hidden layer")
-        a = c128(a)
-        b0 = c128(b[0])
-        W0 = c128(W[0])
-        conn0 = np.asarray(connections[0], np.uint32)
-        C, M = W0.shape
+        if not (len(b) == len(connections) == len(W)) or len(W) < 1:
+            raise ValueError("b, connections and W need one entry per hidden layer")
+        a = c128(a).reshape(-1)
+        bs = [c128(x).reshape(-1) for x in b]
+        Ws = [c128(x) for x in W]
+        conns = [np.asarray(x, np.uint32) for x in connections]
         N = a.size
+        below = N
+        for l, (bl, Wl, cl) in enumerate(zip(bs, Ws, conns)):
+            if Wl.ndim != 2 or cl.shape != Wl.shape or Wl.shape[1] != bl.size:
+                raise ValueError(f"layer {l}: W and connections must be (C, M) with M = len(b)")
+            if cl.size and int(cl.max()) >= below:
+                raise ValueError(f"layer {l}: connection index beyond the {below} units below")
+            below = bl.size
         self.num_sites = int(num_sites)
         self.N = N
         self.N_i = 0
         self.N_j = 0
-        self._M, self._C = M, C
-        self._connections = [conn0.copy()]
+        self._sizes = [bl.size for bl in bs]
+        self._C = [Wl.shape[0] for Wl in Ws]
+        self._M, self._C0 = self._sizes[0], self._C[0]
+        self._connections = [c.copy() for c in conns]
         self._final_weights = c128(final_weights).reshape(-1)
+        if self._final_weights.size == 1 and self._sizes[-1] > 1:
+            self._final_weights = np.full(self._sizes[-1], self._final_weights[0])
+        if self._final_weights.size != self._sizes[-1]:
+            raise ValueError("final_weights needs one entry per unit of the last layer")
         self.activation = activation
         self.precision = precision
         self.a_in_log_psi = a_in_log_psi
-        params = np.concatenate([a, b0, W0.reshape(-1)])
-        _make_rbm(self, N, M, C, conn0, params, self._final_weights, log_prefactor, L.LAYOUT_DEEP, a_in_log_psi,
-                  activation, precision, gpu)
+        params = np.concatenate([a] + [np.concatenate([bl, Wl.reshape(-1)]) for bl, Wl in zip(bs, Ws)])
+        if len(Ws) == 1:
+            _make_rbm(self, N, self._M, self._C0, conns[0], params, self._final_weights, log_prefactor,
+                      L.LAYOUT_DEEP, a_in_log_psi, activation, precision, gpu)
+            return
+        sizes = np.ascontiguousarray(self._sizes, np.uint32)
+        cc = np.ascontiguousarray(self._C, np.uint32)
+        cat = np.ascontiguousarray(np.concatenate([c.reshape(-1) for c in conns]).astype(np.uint32))
+        fw = np.ascontiguousarray(self._final_weights)
+        lp = complex(log_prefactor)
+        d = L.DeepDesc(N, len(Ws), ptr(sizes), ptr(cc), ptr(cat), ptr(params), params.size, ptr(fw),
+                       (ct.c_double * 2)(lp.real, lp.imag), int(bool(a_in_log_psi)), _ACT[activation],
+                       _PREC[precision])
+        _Handle.__init__(self)
+        call("ann_psi_create_deep", ct.byref(d), ct.byref(self._h))
+        self._init_common(gpu)
+
+    @property
+    def num_layers(self):
+        return len(self._sizes)
+
+    def _layer_offsets(self):
+        off, out = self.N, []
+        for m, c in zip(self._sizes, self._C):
+            out.append((off, off + m, off + m + c * m))
+            off += m * (1 + c)
+        return out
 
     @property
     def a(self):
@@ -300,11 +345,13 @@ class PsiDeep(_Psi):
 
     @property
     def b(self):
-        return [self.params[self.N:self.N + self._M]]
+        p = self.params
+        return [p[b0:w0] for b0, w0, _ in self._layer_offsets()]
 
     @property
     def W(self):
-        return [self.params[self.N + self._M:].reshape(self._C, self._M)]
+        p = self.params
+        return [p[w0:e].reshape(c, m) for (_, w0, e), m, c in zip(self._layer_offsets(), self._sizes, self._C)]
 
     @property
     def connections(self):
@@ -316,7 +363,7 @@ class PsiDeep(_Psi):
 
     @property
     def first_layer_params_slice(self):
-        return slice(self.N, self.N + self.W[0].size + self.b[0].size)
+        return slice(self.N, self.N + self._M * (1 + self._C0))
 
     # PsiDeep.py:7-44
     def to_json(self):
@@ -326,10 +373,11 @@ class PsiDeep(_Psi):
         return json.loads(json.dumps(obj, cls=NumpyEncoder))
 
     @staticmethod
-    def from_json(json_obj, gpu=True):
+    def from_json(json_obj, gpu=True, **kwargs):
+        """``kwargs`` (activation, precision, a_in_log_psi) are not part of the reference's format."""
         obj = json.loads(json.dumps(json_obj, cls=NumpyEncoder), cls=NumpyDecoder)
         return PsiDeep(obj["num_sites"], obj["a"], obj["b"], obj["connections"], obj["W"], obj["final_weights"],
-                       obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu)
+                       obj["log_prefactor_re"] + 1j * obj["log_prefactor_im"], gpu, **kwargs)
 
 
 def _pad3(v):

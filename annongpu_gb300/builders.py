@@ -32,7 +32,7 @@ def new_RBM(N, M, initial_value=(0.01 + 1j * math.pi / 4), noise=1e-4, gpu=True,
 
 
 def _block_offset(n, m, c):
-    # stride between the windows of consecutive hidden units
+    # stride between the windows of consecutive units of a layer
     if m > n:
         return 1
     if n % m == 0:
@@ -40,28 +40,66 @@ def _block_offset(n, m, c):
     return c
 
 
+def _layer_connections(n, m, c):
+    """Connection block (C x M) of a layer over a lattice of shape n (1 to 3 dimensions):
+    unit j (multi-index j_ids over m) reads units (j_d * delta_d + i_d) % n_d for every
+    window multi-index i_ids over c, flattened row-major."""
+    n, m, c = [list(x) for x in (n, m, c)]
+    deltas = [_block_offset(n_, m_, c_) for n_, m_, c_ in zip(n, m, c)]
+    strides = [int(np.prod(n[d + 1:])) for d in range(len(n))]
+    rows = []
+    for i_ids in np.ndindex(*c):
+        rows.append([sum(((jd * dd + idd) % nd) * sd for jd, dd, idd, nd, sd in zip(j_ids, deltas, i_ids, n, strides))
+                     for j_ids in np.ndindex(*m)])
+    return np.array(rows, np.uint32)
+
+
 def new_deep_neural_network(num_sites, N, M, C, initial_value=(0.01 + 1j * math.pi / 4), a=0, noise=1e-4,
                             gpu=True, noise_modulation="auto", final_weights=10, rng=None, **kwargs):
-    """One hidden layer: M = [m], C = [c]; hidden unit j connects to sites (j * delta + i) % N, i < c."""
-    if not isinstance(M, (list, tuple)):
-        M, C = [M], [C]
-    if len(M) != 1:
-        raise NotImplementedError("this build supports PsiDeep with one hidden layer")
-    if isinstance(N, (list, tuple)):
-        raise NotImplementedError("multi-dimensional PsiDeep layouts are not built")
-    m, c = M[0], C[0]
-    if (m * c) % N != 0 or c > N:
-        raise ValueError("need (M * C) % N == 0 and C <= N")
+    """PsiDeep with len(M) hidden layers (pyANNonGPU/new_neural_network.py:31-131).
+
+    N, and each entry of M and C, is an int (1-d chain of units) or a 2-/3-tuple
+    (lattice of units, flattened row-major). Layer k has M[k] units; each reads a window
+    of C[k] units of the layer below, windows spaced as the reference spaces them. The
+    first layer's weights are noise plus ``initial_value`` on the window centre row;
+    deeper layers are a real Glorot-uniform term of scale sqrt(6 / (C_k + C_{k+1})) plus
+    noise. Biases are noise; ``final_weights`` a scalar or one value per last-layer unit.
+    As in the reference, an explicit ``noise_modulation`` list only bounds the number of
+    deeper layers built; their scale is the Glorot one.
+    """
     rng = np.random.default_rng() if rng is None else rng
-    a = np.full(N, a, dtype=np.complex128) if np.isscalar(a) else np.asarray(a, np.complex128)
+    dim = len(N) if isinstance(N, (list, tuple)) else 1
+    if not isinstance(M, (list, tuple)) or (dim > 1 and not isinstance(M[0], (list, tuple))):
+        M, C = [M], [C]
+    M, C = list(M), list(C)
+    as_shape = (lambda x: [int(x)]) if dim == 1 else (lambda x: [int(v) for v in x])
+    shapes = [as_shape(N)] + [as_shape(m) for m in M]
+    windows = [as_shape(c) for c in C]
+    for n, m, c in zip(shapes[:-1], shapes[1:], windows):
+        for nd, md, cd in zip(n, m, c):
+            if (md * cd) % nd != 0 or cd > nd:
+                raise ValueError("every layer needs (M * C) % N == 0 and C <= N in each dimension")
+    N_lin = int(np.prod(shapes[0]))
+    M_lin = [int(np.prod(m)) for m in shapes[1:]]
+    C_lin = [int(np.prod(c)) for c in windows]
+    a = np.full(N_lin, a, dtype=np.complex128) if np.isscalar(a) else np.asarray(a, np.complex128)
     is_real = complex(initial_value).imag == 0
-    b = _noise(rng, m, noise, not is_real)
-    w = _noise(rng, (c, m), noise, not is_real)
-    w[c // 2, :] += initial_value
-    delta = _block_offset(N, m, c)
-    conn = np.array([[(j * delta + i) % N for j in range(m)] for i in range(c)], np.uint32)
-    fw = final_weights * np.ones(m) if np.isscalar(final_weights) else np.asarray(final_weights)
-    return PsiDeep(num_sites, a, [b], [conn], [w], fw, 0.0, gpu, **kwargs)
+    b = [_noise(rng, m, noise, not is_real) for m in M_lin]
+    w0 = _noise(rng, (C_lin[0], M_lin[0]), noise, not is_real)
+    w0[C_lin[0] // 2, :] += initial_value
+    W = [w0]
+    nexts = C_lin[2:] + [1]
+    if noise_modulation == "auto":
+        noise_modulation = [math.sqrt(6 / (c + nc)) for c, nc in zip(C_lin[1:], nexts)]
+    for c, m, nc, _ in zip(C_lin[1:], M_lin[1:], nexts, noise_modulation):
+        W.append(math.sqrt(6 / (c + nc)) * (2 * rng.random((c, m)) - 1) + _noise(rng, (c, m), noise, not is_real))
+    if len(W) < len(M_lin):
+        raise ValueError("noise_modulation has fewer entries than deeper layers")
+    conns = [_layer_connections(n, m, c) for n, m, c in zip(shapes[:-1], shapes[1:], windows)]
+    fw = final_weights * np.ones(M_lin[-1]) if np.isscalar(final_weights) else np.asarray(final_weights)
+    if fw.size != M_lin[-1]:
+        raise ValueError("final_weights needs one entry per unit of the last layer")
+    return PsiDeep(num_sites, a, b, conns, W, fw, 0.0, gpu, **kwargs)
 
 
 def new_convolutional_network(L, layers, initial_value=(0.01 + 1j * math.pi / 4), noise=1e-4, final_factor=10,

@@ -50,8 +50,16 @@ struct CnnLayerHost {
     unsigned channels, prev_channels, vol, conn[3], param_offset;
 };
 
+// PsiDeep with several hidden layers: layer structure and the offsets of its tables
+struct DeepHost {
+    std::vector<unsigned> sizes, C, conn;          // units, connections per unit, connection blocks
+    std::vector<unsigned> conn_off, rbeg_off, rq_off;  // offsets into the device table (u16 entries)
+    unsigned tab_len = 0;
+    int dup0 = 0;   // a site appears twice in one first-layer window
+};
+
 struct ann_psi_impl {
-    int kind = 0;       // 0 RBM family, 1 CNN
+    int kind = 0;       // 0 RBM family, 1 CNN, 2 PsiDeep with several hidden layers
     int precision = 0;  // 0 fp32, 1 fp64
     int act = 0;
     unsigned N = 0, NW = 1, Np = 0;
@@ -69,7 +77,10 @@ struct ann_psi_impl {
     std::vector<unsigned> sym;
     unsigned ncls = 1;
     double final_factor = 1.0;
-    DevBuf cnn_w, cnn_meta;  // kernel-precision weights; packed metadata
+    DevBuf cnn_w, cnn_meta;  // kernel-precision weights (CNN, multi-layer PsiDeep); packed CNN metadata
+    // multi-layer PsiDeep (final weights in fw / fwd)
+    DeepHost deep;
+    DevBuf deep_tab;
     size_t elem_bytes() const { return precision ? 16 : 8; }
 };
 
@@ -262,6 +273,10 @@ std::string key_slab(size_t rows, unsigned Np);
 std::string key_chol_update(unsigned n);
 
 // PsiCNN (cnn.cu)
+void deep_prepare(ann_psi_impl& psi, cudaStream_t st);
+void deep_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st);
+void deep_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
+                size_t ldO, cudaStream_t st);
 void cnn_prepare(ann_psi_impl& psi, cudaStream_t st);
 void cnn_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st);
 void cnn_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,

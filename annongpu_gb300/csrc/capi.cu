@@ -138,8 +138,10 @@ void psi_prepare(ann_psi_impl& psi, cudaStream_t st) {
     if(psi.kind == 0) {
         if(psi.precision == 0) rbm_prepare_T<float>(psi, st);
         else rbm_prepare_T<double>(psi, st);
-    } else {
+    } else if(psi.kind == 1) {
         cnn_prepare(psi, st);
+    } else {
+        deep_prepare(psi, st);
     }
 }
 
@@ -147,6 +149,8 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
                   cudaStream_t st) {
     if(op && op->max_site > psi.N) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
     if(ens.kind == 0 && ens.N != psi.N) throw Error(ANN_ERR_INVALID, "exact summation size differs from psi.N");
+    if(psi.kind != 0 && ens.kind == 1 && ens.made && ens.indep_per_sample)
+        throw Error(ANN_ERR_UNSUPPORTED, "the learned proposal is built for the RBM family (PsiRBM, one-layer PsiDeep)");
     if(psi.kind == 0) {
         if(ens.kind == 0) {
             if(psi.precision == 0) rbm_exact_T<float>(psi, op, ens, t, st);
@@ -155,8 +159,10 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
             if(psi.precision == 0) rbm_mc_T<float>(psi, op, ens, t, st);
             else rbm_mc_T<double>(psi, op, ens, t, st);
         }
-    } else {
+    } else if(psi.kind == 1) {
         cnn_run(psi, op, ens, t, st);
+    } else {
+        deep_run(psi, op, ens, t, st);
     }
     if(ens.hist_cap) {
         // append the configurations of this pass to the ring buffer; the write position is
@@ -173,11 +179,14 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
 
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
                size_t ldO, cudaStream_t st) {
+    if(op && op->max_site > psi.N) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
     if(psi.kind == 0) {
         if(psi.precision == 0) rbm_confs_T<float>(psi, op, confs, n, rows, O, ldO, st);
         else rbm_confs_T<double>(psi, op, confs, n, rows, O, ldO, st);
-    } else {
+    } else if(psi.kind == 1) {
         cnn_confs(psi, op, confs, n, rows, O, ldO, st);
+    } else {
+        deep_confs(psi, op, confs, n, rows, O, ldO, st);
     }
 }
 
@@ -422,6 +431,7 @@ int ann_psi_copy(const ann_psi* src, ann_psi** out) {
             p->sym = src->sym;
             p->ncls = src->ncls;
             p->final_factor = src->final_factor;
+            p->deep = src->deep;
             auto clone = [](DevBuf& dst, const DevBuf& s) {
                 if(!s.p) return;
                 dst.ensure(s.bytes);
@@ -435,6 +445,7 @@ int ann_psi_copy(const ann_psi* src, ann_psi** out) {
             clone(p->connd, src->connd);
             clone(p->cnn_w, src->cnn_w);
             clone(p->cnn_meta, src->cnn_meta);
+            clone(p->deep_tab, src->deep_tab);
         } catch(...) {
             delete p;
             throw;

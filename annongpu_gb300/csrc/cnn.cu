@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "ann_internal.hpp"
+#include "chain.cuh"
 
 namespace ann {
 
@@ -280,80 +281,19 @@ __global__ void __launch_bounds__(256) cnn_mc_kernel(CnnDev<T> p, OpDev op, int 
     if(chain >= a.n_chains) return;
     const unsigned N = p.N;
     Conf<2> s;
-    uint64_t t;
-    unsigned tape_pos = 0;
-    const bool tape = a.tape_site != nullptr;
-    if(tape) {
-        for(int w = 0; w < 2; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
-        t = 0;
-    } else if(a.do_init) {
-        t = a.chain_counter[chain];
-        if(a.n_up < 0) {
-            const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)t, (uint32_t)(t >> 32), chain, 1u});
-            s.w[0] = (uint64_t)r.x | ((uint64_t)r.y << 32);
-            s.w[1] = (uint64_t)r.z | ((uint64_t)r.w << 32);
-            for(int w = 0; w < 2; w++) {
-                const unsigned lo = 64u * w;
-                if(N <= lo) s.w[w] = 0;
-                else if(N - lo < 64u) s.w[w] &= ((uint64_t)1 << (N - lo)) - 1u;
-            }
-        } else {
-            s.w[0] = s.w[1] = 0;
-            for(int k = 0; k < a.n_up; k++) {
-                const uint64_t tk = t + (uint64_t)k;
-                const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tk, (uint32_t)(tk >> 32), chain, 2u});
-                unsigned target = mulhi32(r.x, N - (unsigned)k);
-                for(unsigned i = 0; i < N; i++) {
-                    if(!spin_bit(s, i)) {
-                        if(target == 0) { s.w[i >> 6] |= (uint64_t)1 << (i & 63u); break; }
-                        target--;
-                    }
-                }
-            }
-        }
-    } else {
-        for(int w = 0; w < 2; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
-        t = a.chain_counter[chain];
-    }
+    ChainDraw dr;
+    chain_start(a, chain, N, s, dr.t);
+    dr.t0 = dr.t;
     cplx<T> lpsi = cnn_log_psi(c, s, lane);
     unsigned long long n_acc = 0, n_rej = 0;
-    const uint64_t t0 = t;
-    u32x4 rr = {0, 0, 0, 0};
     auto propose = [&]() {
-        unsigned i, j = 0xFFFFFFFFu;
-        double u = 0.0;
-        float uf = 0.f;
-        if(tape) {
-            i = a.tape_site[(size_t)chain * a.tape_len + tape_pos];
-            u = a.tape_u[(size_t)chain * a.tape_len + tape_pos];
-            if(sizeof(T) == 4) uf = (float)u;
-            tape_pos++;
-        } else {
-            const unsigned k = (unsigned)(t - t0) & 31u;
-            if(k == 0) {
-                const uint64_t tl = t + lane;
-                rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
-            }
-            const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
-            const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
-            const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
-            const uint32_t r3 = __shfl_sync(0xffffffffu, rr.w, k);
-            t++;
-            i = mulhi32(r0, N);
-            if(a.move_kind == 1) {
-                const unsigned bnd = mulhi32(r0, a.n_bonds);
-                i = a.bonds[2 * bnd];
-                j = a.bonds[2 * bnd + 1];
-            } else if(a.move_kind == 2) {
-                j = mulhi32(r1, N - 1u);
-                j += (j >= i);
-            }
-            u = u53(r2, r3);
-            if(sizeof(T) == 4) uf = __uint2float_rz(r3 >> 8) * 0x1.0p-24f;
-        }
+        unsigned i, j;
+        double u;
+        float uf;
+        dr.next(a, chain, N, lane, i, j, u, uf);
         Conf<2> s2 = s;
         flip(s2, i);
-        if(a.move_kind != 0 && !tape) {
+        if(j != 0xFFFFFFFFu) {
             if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
             flip(s2, j);
         }
@@ -368,16 +308,16 @@ __global__ void __launch_bounds__(256) cnn_mc_kernel(CnnDev<T> p, OpDev op, int 
             n_rej++;
         }
     };
-    if(a.do_init || tape)
+    if(a.do_init || a.tape_site)
         for(unsigned k = 0; k < a.num_therm * N; k++) propose();
     for(unsigned st = 0; st < a.samples_per_chain; st++) {
         for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
         cnn_process_sample(c, with_op ? &op : nullptr, s, lane, (size_t)st * a.n_chains + chain, out, false);
     }
     if(lane == 0) {
-        if(!tape) {
+        if(!a.tape_site) {
             for(int w = 0; w < kMaxWords; w++) a.chain_conf[(size_t)chain * kMaxWords + w] = s.w[w];
-            a.chain_counter[chain] = t;
+            a.chain_counter[chain] = dr.t;
         }
         atomicAdd(&a.acc_rej[0], n_acc);
         atomicAdd(&a.acc_rej[1], n_rej);

@@ -92,6 +92,27 @@ typedef struct {
 
 /* PsiCNN(...) ctor (main.cpp.template:160-170) */
 int ann_psi_create_cnn(const ann_cnn_desc* desc, ann_psi** out);
+typedef struct {
+    unsigned N;                     /* input units (spins), <= 128 */
+    unsigned num_layers;            /* hidden layers, 1..4 (the reference allows 3, PsiDeep.hpp:88) */
+    const unsigned* sizes;          /* num_layers: units per layer, <= 1024 */
+    const unsigned* connectivity;   /* num_layers: connections per unit C_l (<= units of the layer below) */
+    const unsigned* connections;    /* concatenated C_l x sizes[l] blocks; entry (i, j) at i*sizes[l] + j is the
+                                       unit of the layer below (spin for l = 0) read by unit j */
+    const double* params;           /* [a(N) | b_0 | W_0 | b_1 | W_1 | ...] interleaved complex */
+    unsigned num_params;            /* N + sum_l sizes[l] * (1 + connectivity[l]) */
+    const double* final_weights;    /* sizes[num_layers-1] complex (fixed, not variational) */
+    double log_prefactor[2];
+    int a_in_log_psi;               /* 0 reproduces the reference, whose log psi omits a.s (PsiDeep.hpp:260-264) */
+    int activation;                 /* ANN_ACT_POLY: log-cosh polynomial on layer 0, odd polynomial deeper;
+                                       ANN_ACT_LOGCOSH: log cosh on every layer */
+    int precision;
+} ann_deep_desc;
+
+/* PsiDeep(num_sites, a, b, connections, W, final_weights, log_prefactor, gpu) with several
+   hidden layers (main.cpp.template:71-81, include/quantum_state/PsiDeep.hpp:488-560) */
+int ann_psi_create_deep(const ann_deep_desc* desc, ann_psi** out);
+
 /* copy() (main.cpp.template:82, 127, 171) */
 int ann_psi_copy(const ann_psi* psi, ann_psi** out);
 int ann_psi_destroy(ann_psi* psi);
