@@ -405,6 +405,16 @@ struct Deep {
         for(unsigned j = 0; j < size[L - 1]; j++) fw[j] = cx(p->fw, j);
         lp = cd(p->lp_re, p->lp_im);
     }
+    bool paulis() const { return p->basis == 1; }
+    unsigned sites() const { return paulis() ? N / 3u : N; }
+    // input unit u: a spin, or for Pauli strings +1 iff site u/3 holds X, Y, Z for u%3 = 0, 1, 2
+    // (PauliString.hpp:84-90: type = a_bit | b_bit << 1)
+    double in_val(const Conf& s, unsigned u) const {
+        if(!paulis()) return spin(s, u);
+        const unsigned x = u / 3u;
+        const unsigned t = (unsigned)((s[0] >> x) & 1u) | ((unsigned)((s[1] >> x) & 1u) << 1);
+        return t == u % 3u + 1u ? 1.0 : -1.0;
+    }
     unsigned conn(unsigned l, unsigned i, unsigned j) const { return p->connections[conn_off[l] + i * size[l] + j]; }
     cd W(unsigned l, unsigned i, unsigned j) const { return prm[w_off[l] + i * size[l] + j]; }
     // layer 0 uses my_logcosh(., 0) / my_tanh(., 0); deeper layers index >= 1 (PsiDeep.hpp:182, 207, 369-377)
@@ -413,7 +423,7 @@ struct Deep {
     // pre-activations z[l][j]; returns log psi
     cd forward(const Conf& s, std::vector<std::vector<cd>>& z) const {
         std::vector<cd> in(N);
-        for(unsigned x = 0; x < N; x++) in[x] = spin(s, x);
+        for(unsigned x = 0; x < N; x++) in[x] = in_val(s, x);
         z.assign(L, {});
         for(unsigned l = 0; l < L; l++) {
             z[l].assign(size[l], cd(0.0));
@@ -430,18 +440,30 @@ struct Deep {
         cd r = lp;
         for(unsigned j = 0; j < size[L - 1]; j++) r += in[j] * fw[j];
         if(p->a_in_log_psi)
-            for(unsigned x = 0; x < N; x++) r += prm[x] * spin(s, x);
+            for(unsigned x = 0; x < N; x++) r += prm[x] * in_val(s, x);
         return r;
     }
     cd log_psi(const Conf& s) const {
         std::vector<std::vector<cd>> z;
         return forward(s, z);
     }
+    // configuration index of the exact sum: bits (spins) or base-4 digits per site
+    // (PauliString::enumerate, PauliString.hpp:30-35)
+    Conf enumerate_conf(uint64_t idx) const {
+        if(!paulis()) return enumerate(idx);
+        Conf c{0, 0};
+        for(unsigned x = 0; x < sites(); x++) {
+            c[0] |= ((idx >> (2 * x)) & 1u) << x;
+            c[1] |= ((idx >> (2 * x + 1)) & 1u) << x;
+        }
+        return c;
+    }
+    uint64_t num_confs() const { return (uint64_t)1 << (paulis() ? 2 * sites() : N); }
     void O_k(const Conf& s, std::vector<cd>& O) const {
         std::vector<std::vector<cd>> z;
         forward(s, z);
         O.assign(np, cd(0.0));
-        for(unsigned x = 0; x < N; x++) O[x] = spin(s, x);
+        for(unsigned x = 0; x < N; x++) O[x] = in_val(s, x);
         // dlogpsi / dz for the top layer, then down through the rhs connections
         std::vector<cd> delta(size[L - 1]);
         for(unsigned j = 0; j < size[L - 1]; j++) delta[j] = fw[j] * df(z[L - 1][j], L - 1);
@@ -452,7 +474,7 @@ struct Deep {
                 O[b_off[l] + j] = delta[j];
                 for(unsigned i = 0; i < C[l]; i++) {
                     const unsigned u = conn(l, i, j);
-                    const cd inp = l == 0 ? cd(spin(s, u)) : f(z[l - 1][u], l - 1);
+                    const cd inp = l == 0 ? cd(in_val(s, u)) : f(z[l - 1][u], l - 1);
                     O[w_off[l] + i * size[l] + j] = delta[j] * inp;
                     up[u] += W(l, i, j) * delta[j];
                 }
@@ -466,12 +488,27 @@ struct Deep {
     cd local_energy(const or_op* op, const Conf& s, cd lpsi) const {
         cd r(0.0);
         for(unsigned n = 0; n < op->n; n++) {
-            ME me = pauli_apply(op->a + n * op->nw, op->b + n * op->nw, op->nw, s);
+            ME me = paulis() ? pauli_times_string(op->a[n * op->nw], op->b[n * op->nw], s)
+                             : pauli_apply(op->a + n * op->nw, op->b + n * op->nw, op->nw, s);
             me.factor *= cx(op->coeff, n);
             if(me.conf != s) r += me.factor * std::exp(log_psi(me.conf) - lpsi);
             else r += me.factor;
         }
         return r;
+    }
+    // P x for Pauli strings P = (pa, pb) and x = (s[0], s[1]) (PauliString.hpp:256-276):
+    // the product string P ^ x with phase (-1)^{#(XZ, YX, ZY) pairs} (-i)^{n_eps}, n_eps = sites
+    // where both are non-trivial and differ
+    static ME pauli_times_string(uint64_t pa, uint64_t pb, const Conf& s) {
+        const uint64_t xa = s[0], xb = s[1];
+        const uint64_t pX = pa & ~pb, pY = ~pa & pb, pZ = pa & pb;
+        const uint64_t xX = xa & ~xb, xY = ~xa & xb, xZ = xa & xb;
+        cd f(1.0, 0.0);
+        if(popc((pX & xZ) | (pY & xX) | (pZ & xY)) & 1) f *= -1.0;
+        const int ne = popc((pa | pb) & (xa | xb) & ((pa ^ xa) | (pb ^ xb)));
+        if((ne & 3) > 1) f *= -1.0;
+        if(ne & 1) f *= cd(0.0, -1.0);
+        return {f, Conf{pa ^ xa, pb ^ xb}};
     }
 };
 
@@ -790,19 +827,19 @@ unsigned or_deep_num_params(const or_deep* p) { return Deep(p).np; }
 
 void or_deep_log_psi(const or_deep* p, const uint64_t* conf, double* out) {
     Deep psi(p);
-    put(out, psi.log_psi(load_conf(conf, nwords(p->N))));
+    put(out, psi.log_psi(load_conf(conf, psi.paulis() ? 2u : nwords(p->N))));
 }
 
 void or_deep_O_k(const or_deep* p, const uint64_t* conf, double* out) {
     Deep psi(p);
     std::vector<cd> O;
-    psi.O_k(load_conf(conf, nwords(p->N)), O);
+    psi.O_k(load_conf(conf, psi.paulis() ? 2u : nwords(p->N)), O);
     for(size_t k = 0; k < O.size(); k++) put(out + 2 * k, O[k]);
 }
 
 void or_deep_local_energy(const or_deep* p, const or_op* op, const uint64_t* conf, double* out) {
     Deep psi(p);
-    const Conf s = load_conf(conf, nwords(p->N));
+    const Conf s = load_conf(conf, psi.paulis() ? 2u : nwords(p->N));
     put(out, psi.local_energy(op, s, psi.log_psi(s)));
 }
 
@@ -812,8 +849,8 @@ void or_deep_exact(const or_deep* p, const or_op* op, double* E, double* norm,
     Accum acc(psi.np);
     double nrm = 0.0;
     std::vector<cd> Ok;
-    for(uint64_t idx = 0; idx < ((uint64_t)1 << psi.N); idx++) {
-        const Conf s = enumerate(idx);
+    for(uint64_t idx = 0; idx < psi.num_confs(); idx++) {
+        const Conf s = psi.enumerate_conf(idx);
         const cd lp = psi.log_psi(s);
         const double w = std::exp(2.0 * lp.real());
         const cd eloc = op ? psi.local_energy(op, s, lp) : cd(0.0);
@@ -834,9 +871,61 @@ void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uin
                        uint64_t* sconf, double* slp, double* seloc,
                        uint64_t* n_accept, uint64_t* n_reject, double* min_tie) {
     Deep psi(p);
-    DeepChain m(psi);
-    philox_chains(m, p->N, op, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind, bonds, n_bonds,
-                  init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
+    if(!psi.paulis()) {
+        DeepChain m(psi);
+        philox_chains(m, p->N, op, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind, bonds,
+                      n_bonds, init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
+        return;
+    }
+    // Pauli-string chains: one sweep = N/3 proposals
+    const unsigned S = psi.sites();
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    uint64_t acc_total = 0, rej_total = 0;
+    double tie = 1e300;
+    for(unsigned c = 0; c < n_chains; c++) {
+        uint64_t t = counter[c];
+        Conf s;
+        if(init) {
+            uint32_t ctr[4] = {(uint32_t)t, (uint32_t)(t >> 32), c, 1u}, r[4];
+            philox(k0, k1, ctr, r);
+            const uint64_t mask = S >= 64 ? ~(uint64_t)0 : (((uint64_t)1 << S) - 1u);
+            s = Conf{((uint64_t)r[0] | ((uint64_t)r[1] << 32)) & mask, ((uint64_t)r[2] | ((uint64_t)r[3] << 32)) & mask};
+        } else {
+            s = Conf{conf[(size_t)c * 2], conf[(size_t)c * 2 + 1]};
+        }
+        cd lp = psi.log_psi(s);
+        auto propose = [&]() {
+            uint32_t ctr[4] = {(uint32_t)t, (uint32_t)(t >> 32), c, 0u}, r[4];
+            philox(k0, k1, ctr, r);
+            t++;
+            const unsigned x = mulhi(r[0], S), type = r[1] >> 30;
+            Conf nx = s;
+            nx[0] = (nx[0] & ~((uint64_t)1 << x)) | ((uint64_t)(type & 1u) << x);
+            nx[1] = (nx[1] & ~((uint64_t)1 << x)) | ((uint64_t)(type >> 1) << x);
+            const cd lp2 = psi.log_psi(nx);
+            const double ratio = std::exp(2.0 * (lp2.real() - lp.real()));
+            const double u = u53(r[2], r[3]);
+            tie = std::min(tie, std::fabs(ratio - u));
+            if(u <= ratio) { s = nx; lp = lp2; acc_total++; }
+            else rej_total++;
+        };
+        if(init)
+            for(unsigned k = 0; k < num_therm * S; k++) propose();
+        for(unsigned st = 0; st < samples_per_chain; st++) {
+            for(unsigned k = 0; k < num_sweeps * S; k++) propose();
+            lp = psi.log_psi(s);
+            const size_t row = (size_t)st * n_chains + c;
+            if(sconf) { sconf[row * 2] = s[0]; sconf[row * 2 + 1] = s[1]; }
+            if(slp) put(slp + 2 * row, lp);
+            if(seloc && op) put(seloc + 2 * row, psi.local_energy(op, s, lp));
+        }
+        conf[(size_t)c * 2] = s[0];
+        conf[(size_t)c * 2 + 1] = s[1];
+        counter[c] = t;
+    }
+    if(n_accept) *n_accept = acc_total;
+    if(n_reject) *n_reject = rej_total;
+    if(min_tie) *min_tie = tie;
 }
 
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

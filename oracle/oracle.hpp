@@ -86,6 +86,7 @@ struct or_deep {
     double lp_re, lp_im;
     int a_in_log_psi;              // 0 reproduces the reference (PsiDeep.hpp:260-264)
     int activation;                // 0: reference layer polynomials ; 1: log cosh on every layer
+    int basis;                     // 0 spins (conf = bits); 1 Pauli strings (conf = words a, b; N = 3 x sites)
 };
 
 unsigned or_rbm_num_params(const or_rbm* p);
@@ -141,7 +142,11 @@ void or_deep_O_k(const or_deep* p, const uint64_t* conf, double* out);
 void or_deep_local_energy(const or_deep* p, const or_op* op, const uint64_t* conf, double* out);
 void or_deep_exact(const or_deep* p, const or_op* op, double* E, double* norm,
                    double* tE, double* tE2, double* tO, double* tF, double* tS);
-// counter-based chains (same contract as or_rbm_mc_philox); dlogpsi from full forward passes
+// counter-based chains (same contract as or_rbm_mc_philox); dlogpsi from full forward passes.
+// Pauli-string basis (basis = 1; move_kind, bonds and n_up unused): initial string at counter
+// (t, chain, 1): a = r0 | r1 << 32, b = r2 | r3 << 32 masked to N/3 sites; proposal t at
+// (t, chain, 0): site mulhi(r0, N/3) set to type r1 >> 30 (the reference draws x % sites and
+// x >> 30 from one word, Update_Policy.hpp:41-57), u from (r2, r3).
 void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uint64_t seed,
                        unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
                        int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,

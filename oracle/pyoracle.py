@@ -52,7 +52,7 @@ class OrCnn(ct.Structure):
 class OrDeep(ct.Structure):
     _fields_ = [("N", ct.c_uint), ("num_layers", ct.c_uint), ("sizes", P), ("connectivity", P),
                 ("connections", P), ("params", P), ("fw", P), ("lp_re", ct.c_double), ("lp_im", ct.c_double),
-                ("a_in_log_psi", ct.c_int), ("activation", ct.c_int)]
+                ("a_in_log_psi", ct.c_int), ("activation", ct.c_int), ("basis", ct.c_int)]
 
 
 def nwords(N):
@@ -139,8 +139,11 @@ class DeepDesc:
     of the layer below read by unit j); params = [a | b_0 | W_0 | b_1 | W_1 | ...].
     """
 
-    def __init__(self, N, connections, params, fw, log_prefactor=0j, a_in_log_psi=True, activation=0):
+    def __init__(self, N, connections, params, fw, log_prefactor=0j, a_in_log_psi=True, activation=0, paulis=False):
+        """``paulis``: the Pauli-string basis (N = 3 input units per site; configurations are
+        (a, b) word pairs)."""
         self.N = int(N)
+        self.paulis = bool(paulis)
         blocks = [np.asarray(c, np.uint32) for c in connections]
         self.sizes = np.ascontiguousarray([b.shape[1] for b in blocks], np.uint32)
         self.connectivity = np.ascontiguousarray([b.shape[0] for b in blocks], np.uint32)
@@ -153,11 +156,18 @@ class DeepDesc:
             raise ValueError(f"params has {self.params.size} entries, the layer structure needs {expect}")
         self.struct = OrDeep(self.N, len(blocks), _ptr(self.sizes), _ptr(self.connectivity),
                              _ptr(self.connections), _ptr(self.params), _ptr(self.fw), self.lp.real, self.lp.imag,
-                             int(a_in_log_psi), int(activation))
+                             int(a_in_log_psi), int(activation), int(self.paulis))
 
     @property
     def num_params(self):
         return self.params.size
+
+    def words(self, conf):
+        """A configuration as the oracle's words: spins as bits; Pauli strings as (a, b)."""
+        if self.paulis:
+            a, b = conf
+            return np.array([a, b], np.uint64)
+        return conf_words(conf, self.N)
 
 
 class Oracle:
@@ -276,8 +286,9 @@ class Oracle:
     def mc_philox(self, psi: RbmDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
                   move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None, _fn=None):
         N = psi.N
-        nw = max(1, nwords(N))
-        op = OpArrays(expr, N) if expr is not None else None
+        pauli = getattr(psi, "paulis", False)
+        nw = 2 if pauli else max(1, nwords(N))
+        op = OpArrays(expr, N // 3 if pauli else N) if expr is not None else None
         conf = np.zeros(n_chains * nw, np.uint64) if conf is None else np.ascontiguousarray(conf, np.uint64).copy()
         counter = np.zeros(n_chains, np.uint64) if counter is None else np.ascontiguousarray(counter,
                                                                                             np.uint64).copy()
@@ -328,20 +339,20 @@ class Oracle:
     # ---- PsiDeep, any depth ----
     def deep_log_psi(self, psi: DeepDesc, conf):
         out = np.zeros(1, np.complex128)
-        w = conf_words(conf, psi.N)
+        w = psi.words(conf)
         self.lib.or_deep_log_psi(ct.byref(psi.struct), _ptr(w), _ptr(out))
         return out[0]
 
     def deep_O_k(self, psi: DeepDesc, conf):
         out = np.zeros(psi.num_params, np.complex128)
-        w = conf_words(conf, psi.N)
+        w = psi.words(conf)
         self.lib.or_deep_O_k(ct.byref(psi.struct), _ptr(w), _ptr(out))
         return out
 
     def deep_local_energy(self, psi: DeepDesc, expr, conf):
-        op = OpArrays(expr, psi.N)
+        op = OpArrays(expr, psi.N // 3 if psi.paulis else psi.N)
         out = np.zeros(1, np.complex128)
-        w = conf_words(conf, psi.N)
+        w = psi.words(conf)
         self.lib.or_deep_local_energy(ct.byref(psi.struct), ct.byref(op.struct), _ptr(w), _ptr(out))
         return out[0]
 
@@ -350,7 +361,7 @@ class Oracle:
         r = dict(E=np.zeros(1, np.complex128), norm=np.zeros(1), tE=np.zeros(1, np.complex128), tE2=np.zeros(1),
                  tO=np.zeros(np_, np.complex128), tF=np.zeros(np_, np.complex128),
                  tS=np.zeros((np_, np_), np.complex128) if want_S else None)
-        op = OpArrays(expr, psi.N)
+        op = OpArrays(expr, psi.N // 3 if psi.paulis else psi.N)
         self.lib.or_deep_exact(ct.byref(psi.struct), ct.byref(op.struct),
                                *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
         return r
@@ -396,4 +407,6 @@ class RefHarness:
         self.lib.ref_deepml_num_params.argtypes = [U, U, P, P, P, P, P, P]
         self.lib.ref_deepml_log_psi_s.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, P]
         self.lib.ref_deepml_O_k.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, P]
+        self.lib.ref_deepml_pauli_log_psi_s.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, ct.c_uint64, P]
+        self.lib.ref_deepml_pauli_O_k.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, ct.c_uint64, P]
         self.lib.ref_pauli_apply.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64, U, P, P]

@@ -236,13 +236,14 @@ PsiDeep make_deep(const DeepDesc& d) {
 // layer's rhs lists compiled from the next layer's connections) and lets the
 // reference's init_kernel / set_params fill offsets and weights.
 struct DeepMLDesc {
-    unsigned N, L;
+    unsigned N, L;                 // N input units (3 per site for the Pauli-string basis)
     const unsigned* sizes;         // L
     const unsigned* connectivity;  // L
     const unsigned* conn;          // concatenated C_l x sizes[l] blocks
     const double* params;          // [a | b_0 | W_0 | ...] interleaved complex
     const double* final_w;         // sizes[L-1] complex
     const double* log_pref;
+    unsigned num_sites = 0;        // 0: N
 };
 
 PsiDeep make_deep_ml(const DeepMLDesc& d) {
@@ -279,6 +280,7 @@ PsiDeep make_deep_ml(const DeepMLDesc& d) {
     for(auto j = 0u; j < last; j++) psi.final_weights[j] = complex_t(d.final_w[2 * j], d.final_w[2 * j + 1]);
     psi.log_prefactor = complex_t(d.log_pref[0], d.log_pref[1]);
     psi.init_kernel();
+    if(d.num_sites) psi.num_sites = d.num_sites;
     Array<complex_t> p(psi.num_params, false);
     for(auto k = 0u; k < psi.num_params; k++) p[k] = complex_t(d.params[2 * k], d.params[2 * k + 1]);
     psi.set_params(p);
@@ -301,12 +303,12 @@ void psi_O_k(Psi& psi, uint64_t conf, double* out) {
 
 // Exact-summation quantities: <A> (unnormalised weights), fluctuation, gradient,
 // TDVP E/E2/O/F/S, psi vector, norm, <log psi>.
-template<typename Psi>
+template<typename Psi, typename Exact = ExactSummationSpins>
 void exact_all(Psi& psi, const HarnessExpr& expr, double* E, double* fluct, double* grad,
                double* tdvp_E, double* tdvp_E2, double* tdvp_O, double* tdvp_F, double* tdvp_S,
                double* vec, double* norm, double* mean_log_psi, double* O_sum) {
     Operator op(expr, false);
-    ExactSummationSpins es(psi.num_sites, false);
+    Exact es(psi.num_sites, false);
     ExpectationValue ev(false);
     put(E, ev(op, psi, es));
     auto fl = ev.fluctuation(op, psi, es);
@@ -423,6 +425,30 @@ void ref_deepml_exact(unsigned N, unsigned L, const unsigned* sizes, const unsig
                       double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
     auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp});
     exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
+}
+
+// ---- PsiDeep over the Pauli-string basis: 3 input units per site (PauliString.hpp:84-90) ----
+void ref_deepml_pauli_log_psi_s(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                                const unsigned* conn, const double* params, const double* fw, const double* lp,
+                                uint64_t a, uint64_t b, double* out) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp, N / 3u});
+    put(out, log_psi_s(psi, PauliString(a, b)));
+}
+void ref_deepml_pauli_O_k(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                          const unsigned* conn, const double* params, const double* fw, const double* lp,
+                          uint64_t a, uint64_t b, double* out) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp, N / 3u});
+    auto r = ann_on_gpu::psi_O_k(psi, PauliString(a, b));
+    for(auto k = 0u; k < r.size(); k++) put(out + 2 * k, r[k]);
+}
+void ref_deepml_pauli_exact(unsigned N, unsigned L, const unsigned* sizes, const unsigned* connectivity,
+                            const unsigned* conn, const double* params, const double* fw, const double* lp,
+                            const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                            double* E, double* fluct, double* grad, double* tE, double* tE2, double* tO,
+                            double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
+    auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp, N / 3u});
+    exact_all<PsiDeep, ExactSummationPaulis>(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS,
+                                             vec, norm, mlp, O_sum);
 }
 
 // ---- PsiRBM (no biases) ----

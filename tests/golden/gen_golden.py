@@ -6,7 +6,7 @@ stores inputs and outputs as .npz files. The fixtures pin the FP64 oracle
 (oracle/oracle.cpp) and, through it, the CUDA path. The reference checkout is
 needed only to regenerate them:
 
-    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml]
+    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml | deep_pauli]
 """
 
 import ctypes as ct
@@ -223,6 +223,41 @@ def gen_deep_ml(ref, rng, name, N, M, C):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
+def gen_deep_pauli(ref, rng, name, num_sites, M, C):
+    """PsiDeep over the Pauli-string basis (3 input units per site) through the reference's
+    own kernel, ExactSummationPaulis and Pauli-string operator products."""
+    N = 3 * num_sites
+    blocks = builder_connections(N, M, C)
+    sizes = np.array(M, np.uint32)
+    conn_c = np.array(C, np.uint32)
+    conn = np.ascontiguousarray(np.concatenate([b.reshape(-1) for b in blocks]))
+    np_ = N + sum(m * (1 + c) for m, c in zip(M, C))
+    params = cplx(rng, np_, 0.15)
+    fw = (1.0 + cplx(rng, M[-1], 0.1)).astype(np.complex128)
+    lp = np.array([0.1 - 0.3j])
+    H = transverse_field_ising_1d(num_sites, h=0.7) + 0.3 * sigma_y(0) * sigma_x(1)
+    H = H + 0.2 * sigma_z(num_sites - 1) * sigma_y(1) + 0.15 * sigma_y(2)
+    a, b, c, n = op_arrays(H)
+    pa = rng.integers(0, 1 << num_sites, 12).astype(np.uint64)
+    pb = rng.integers(0, 1 << num_sites, 12).astype(np.uint64)
+    args = (N, len(M), P(sizes), P(conn_c), P(conn), P(params), P(fw), P(lp))
+    lps, oks = [], []
+    for x, y in zip(pa, pb):
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_deepml_pauli_log_psi_s(*args, int(x), int(y), P(r))
+        lps.append(r[0])
+        o = np.zeros(np_, np.complex128)
+        ref.lib.ref_deepml_pauli_O_k(*args, int(x), int(y), P(o))
+        oks.append(o)
+    ex = exact_outputs(np_, 2 * num_sites)
+    ref.lib.ref_deepml_pauli_exact(*args, P(a), P(b), P(c), n, *[P(ex[k]) for k in KEYS])
+    out = {"num_sites": num_sites, "N": N, "sizes": sizes, "connectivity": conn_c, "conn": conn, "params": params,
+           "fw": fw, "lp": lp, "op_a": a, "op_b": b, "op_c": c, "conf_a": pa, "conf_b": pb, "log_psi": np.array(lps),
+           "O_k": np.array(oks)}
+    out.update({"ex_" + k: v for k, v in ex.items()})
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
 def gen_kats(ref, rng):
     zs = cplx(rng, 24, 0.6)
     f = np.zeros((2, 24), np.complex128)
@@ -254,6 +289,9 @@ def main(only=None):
     if only == "deep_ml":
         gen_deep_ml_all(ref)
         return
+    if only == "deep_pauli":
+        gen_deep_pauli_all(ref)
+        return
     rng = np.random.default_rng(20261203)
     gen_kats(ref, rng)
     gen_rbm(ref, rng)
@@ -264,6 +302,7 @@ def main(only=None):
     gen_deep(ref, rng, "deep_n16_m16", 16, 16, 16, None, with_S=False, mc=False, confs_n=6)
     gen_cnn(ref, rng)
     gen_deep_ml_all(ref)
+    gen_deep_pauli_all(ref)
     print("fixtures written to", HERE)
 
 
@@ -274,6 +313,12 @@ def gen_deep_ml_all(ref):
     gen_deep_ml(ref, rng, "deep3_n3_18_9_3", 3, [18, 9, 3], [3, 2, 3])
     gen_deep_ml(ref, rng, "deep3_n8_16_8_4", 8, [16, 8, 4], [4, 4, 2])
     gen_deep_ml(ref, rng, "deep2_n6_12_6", 6, [12, 6], [3, 4])
+
+
+def gen_deep_pauli_all(ref):
+    rng = np.random.default_rng(20261205)
+    gen_deep_pauli(ref, rng, "deep_pauli_s3_9_6", 3, [9, 6], [3, 3])
+    gen_deep_pauli(ref, rng, "deep_pauli_s4_12_6_3", 4, [12, 6, 3], [4, 4, 2])
 
 
 if __name__ == "__main__":

@@ -145,6 +145,29 @@ def test_deep_multilayer(oracle, name):
     close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-10)
 
 
+@pytest.mark.parametrize("name", ["deep_pauli_s3_9_6.npz", "deep_pauli_s4_12_6_3.npz"])
+def test_deep_pauli_string_basis(oracle, name):
+    """PsiDeep over Pauli strings (three input units per site), Pauli-string operator
+    products and ExactSummationPaulis, against the reference's own kernel."""
+    g = load(name)
+    N = int(g["N"])
+    blocks, off = [], 0
+    for m, c in zip(g["sizes"], g["connectivity"]):
+        blocks.append(g["conn"][off:off + int(m) * int(c)].reshape(int(c), int(m)))
+        off += int(m) * int(c)
+    psi = DeepDesc(N, blocks, g["params"], g["fw"], log_prefactor=g["lp"][0], a_in_log_psi=False, paulis=True)
+    for k, (a, b) in enumerate(zip(g["conf_a"], g["conf_b"])):
+        close(oracle.deep_log_psi(psi, (int(a), int(b))), g["log_psi"][k])
+        close(oracle.deep_O_k(psi, (int(a), int(b))), g["O_k"][k])
+    r = oracle.deep_exact(psi, _Expr(g["op_a"], g["op_b"], g["op_c"]), want_S=True)
+    close(r["E"][0], g["ex_E"][0])
+    close(r["norm"][0], g["ex_norm"][0])
+    close(r["tE2"][0], g["ex_tE2"][0])
+    close(r["tO"], g["ex_tO"])
+    close(r["tF"], g["ex_tF"], rtol=1e-9, atol=1e-10)
+    close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-10)
+
+
 def test_deep_one_layer_equals_rbm_family(oracle):
     """The any-depth restatement with one hidden layer is the RBM-family PsiDeep."""
     g = load("deep_n6_m12_c3.npz")
