@@ -2,15 +2,17 @@
 
     import annongpu_gb300 as pyANNonGPU
 
-exposes PsiRBM, PsiDeep, Operator, Spins, MonteCarloSpins / MonteCarloLoop,
-ExactSummationSpins, ExpectationValue, TDVP and the free functions of the
+exposes PsiRBM, PsiDeep, PsiCNN, Operator, Spins, PauliString, MonteCarloSpins /
+MonteCarloLoop, MonteCarloPaulis, ExactSummationSpins, ExactSummationPaulis,
+ExpectationValue, TDVP, HilbertSpaceDistance and the free functions of the
 reference's _pyANNonGPU module, backed by libannongpu.so (CUDA, sm_103a).
 """
 
 from .expression import (PauliExpression, heisenberg_j1j2_2d, identity, sigma_x, sigma_y, sigma_z,  # noqa: F401
                          square_lattice_bonds, transverse_field_ising_1d, transverse_field_ising_2d)
 from .json_numpy import NumpyDecoder, NumpyEncoder  # noqa: F401
-from .api import (MADE, Batch, ExactSummationSpins, ExpectationValue, HilbertSpaceDistance, MonteCarloLoop, MonteCarloSpins, Operator,  # noqa: F401
+from .api import (MADE, Batch, ExactSummationPaulis, ExactSummationSpins, ExpectationValue, HilbertSpaceDistance,  # noqa: F401
+                  MonteCarloLoop, MonteCarloPaulis, MonteCarloSpins, Operator, PauliString,
                   PsiCNN, PsiDeep, PsiRBM, Spins, TDVP, activation_function, apply_operator, log_psi, log_psi_batch,
                   local_energies, log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
                   stop_profiling)

@@ -38,6 +38,7 @@ ACT_POLY, ACT_LOGCOSH = 0, 1
 PREC_FP32, PREC_FP64 = 0, 1
 MOVE_FLIP, MOVE_EXCHANGE_BONDS, MOVE_EXCHANGE_PAIRS = 0, 1, 2
 S_FP32, S_BF16, S_BF16_SPLIT = 0, 1, 2
+BASIS_SPINS, BASIS_PAULIS = 0, 1
 SOLVER_FP64, SOLVER_MIXED, SOLVER_FP32 = 0, 1, 2
 
 
@@ -76,6 +77,10 @@ _SIGS = {
     "ann_psi_create_rbm": ([P, P], I),
     "ann_psi_create_cnn": ([P, P], I),
     "ann_psi_create_deep": ([P, P], I),
+    "ann_ens_set_basis": ([P, I], I),
+    "ann_log_psi_paulis": ([P, P, U, P, P], I),
+    "ann_psi_O_k_paulis": ([P, P, P], I),
+    "ann_local_energies_paulis": ([P, P, P, U, P, P], I),
     "ann_psi_copy": ([P, P], I),
     "ann_psi_destroy": ([P], I),
     "ann_psi_num_params": ([P, P], I),

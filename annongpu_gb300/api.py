@@ -474,6 +474,45 @@ class Operator(_Handle):
 
 
 # ----------------------------------------------------------------------------------
+class PauliString:
+    """A Pauli string over sites as the words (a, b): per site (a, b) = (0, 0) I, (1, 0) X,
+    (0, 1) Y, (1, 1) Z; ``[i]`` is the type 0..3 of site i (include/basis/PauliString.hpp:18-80)."""
+
+    def __init__(self, a: int, b: int):
+        self.a, self.b = int(a), int(b)
+
+    @staticmethod
+    def enumerate(index: int) -> "PauliString":
+        """Base-4 digit i of ``index`` is the type of site i (PauliString.hpp:30-35)."""
+        index = int(index)
+        a = b = 0
+        for i in range(32):
+            a |= ((index >> (2 * i)) & 1) << i
+            b |= ((index >> (2 * i + 1)) & 1) << i
+        return PauliString(a, b)
+
+    def __getitem__(self, i: int) -> int:
+        return ((self.a >> i) & 1) | (((self.b >> i) & 1) << 1)
+
+    def array(self, num_sites: int) -> np.ndarray:
+        return np.array([self[i] for i in range(num_sites)], np.uint32)
+
+    def __eq__(self, other):
+        return isinstance(other, PauliString) and (self.a, self.b) == (other.a, other.b)
+
+    def __hash__(self):
+        return hash((self.a, self.b))
+
+    def __repr__(self):
+        return f"PauliString(a={self.a:#x}, b={self.b:#x})"
+
+
+def _pauli_rows(strings) -> np.ndarray:
+    """PauliStrings or (a, b) pairs -> (n, 2) uint64 rows."""
+    rows = [(p.a, p.b) if isinstance(p, PauliString) else (int(p[0]), int(p[1])) for p in strings]
+    return np.ascontiguousarray(np.array(rows, np.uint64).reshape(-1, 2))
+
+
 class ExactSummationSpins(_Handle):
     """All 2^N configurations, weight |psi(s)|^2 unnormalised (include/ensembles/ExactSummation.hpp:33-72)."""
 
@@ -488,6 +527,20 @@ class ExactSummationSpins(_Handle):
     @property
     def num_steps(self) -> int:
         return 1 << self.num_sites
+
+
+class ExactSummationPaulis(ExactSummationSpins):
+    """All 4^N Pauli strings over N sites, weight |psi(x)|^2 unnormalised
+    (ExactSummation_t<PauliString>, include/ensembles/ExactSummation.hpp:125). The
+    wavefunction sees three input units per site (PsiDeep of any depth, 3 N inputs)."""
+
+    def __init__(self, num_sites, gpu=True):
+        ExactSummationSpins.__init__(self, num_sites, gpu)
+        call("ann_ens_set_basis", self._h, L.BASIS_PAULIS)
+
+    @property
+    def num_steps(self) -> int:
+        return 1 << (2 * self.num_sites)
 
 
 _MOVES = {"single_flip": L.MOVE_FLIP, "flip": L.MOVE_FLIP, "exchange": L.MOVE_EXCHANGE_BONDS,
@@ -604,6 +657,22 @@ class MonteCarloSpins(_Handle):
 
 
 MonteCarloLoop = MonteCarloSpins
+
+
+class MonteCarloPaulis(MonteCarloSpins):
+    """Metropolis chains over Pauli strings (MonteCarlo_tt<PauliString>,
+    include/ensembles/MonteCarlo.hpp:266-280): each move sets a random site to a random
+    type I, X, Y, Z (Update_Policy.hpp:41-57); a sweep is one move per input unit of the
+    wavefunction (3 per site). ``seed`` and ``persistent`` as for MonteCarloSpins."""
+
+    def __init__(self, num_samples, num_sweeps=None, num_thermalization_sweeps=None, num_markov_chains=None,
+                 gpu=True, *, seed=0, persistent=False):
+        if isinstance(num_samples, MonteCarloPaulis):
+            MonteCarloSpins.__init__(self, num_samples)
+            return
+        MonteCarloSpins.__init__(self, num_samples, num_sweeps, num_thermalization_sweeps, num_markov_chains, gpu,
+                                 seed=seed, persistent=persistent)
+        call("ann_ens_set_basis", self._h, L.BASIS_PAULIS)
 
 
 # ----------------------------------------------------------------------------------
@@ -938,6 +1007,9 @@ def _nwords(psi):
 
 
 def log_psi_s(psi, spins) -> complex:
+    """log psi of one configuration: Spins (or an int) or a PauliString."""
+    if isinstance(spins, PauliString):
+        return complex(log_psi_batch(psi, [spins])[0])
     w = _conf_words(spins, _nwords(psi))
     out = np.zeros(2)
     call("ann_log_psi_s", psi.handle, ptr(w), ptr(out))
@@ -946,6 +1018,11 @@ def log_psi_s(psi, spins) -> complex:
 
 def log_psi_batch(psi, confs) -> np.ndarray:
     confs = list(confs)
+    if confs and isinstance(confs[0], PauliString):
+        rows = _pauli_rows(confs)
+        out = cbuf(len(rows))
+        call("ann_log_psi_paulis", psi.handle, ptr(rows), len(rows), None, ptr(out))
+        return out
     nw = _nwords(psi)
     arr = np.ascontiguousarray(np.concatenate([_conf_words(c, nw) for c in confs]) if confs else
                                np.zeros(0, np.uint64))
@@ -955,7 +1032,13 @@ def log_psi_batch(psi, confs) -> np.ndarray:
 
 
 def local_energies(psi, operator, confs) -> np.ndarray:
-    """E_loc(s) of explicit configurations (ints, Spins or (n, 2) uint64 rows) on the device."""
+    """E_loc(s) of explicit configurations (ints, Spins or (n, 2) uint64 rows) on the device;
+    a list of PauliStrings is read in the Pauli-string basis."""
+    if len(confs) and isinstance(confs[0], PauliString):
+        rows = _pauli_rows(confs)
+        out = cbuf(len(rows))
+        call("ann_local_energies_paulis", psi.handle, operator.handle, ptr(rows), len(rows), None, ptr(out))
+        return out
     rows = _conf_rows(confs)
     nw = _nwords(psi)
     arr = np.ascontiguousarray(rows[:, :nw])
@@ -965,8 +1048,11 @@ def local_energies(psi, operator, confs) -> np.ndarray:
 
 
 def psi_O_k(psi, spins) -> np.ndarray:
-    w = _conf_words(spins, _nwords(psi))
     out = cbuf(psi.num_params)
+    if isinstance(spins, PauliString):
+        call("ann_psi_O_k_paulis", psi.handle, ptr(_pauli_rows([spins])), ptr(out))
+        return out
+    w = _conf_words(spins, _nwords(psi))
     call("ann_psi_O_k", psi.handle, ptr(w), ptr(out))
     return out
 

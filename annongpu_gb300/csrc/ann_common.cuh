@@ -193,11 +193,20 @@ struct OpDev {
     const double* str_coeff;         // [n_str][2]: coeff * (-i)^{n_y}
     const float* diag_coeff_f;       // FP32 copies for complex64 kernels
     const float* str_coeff_f;
+    // every string as given (Pauli-string basis, first word; sites < 64)
+    unsigned n_raw;
+    const uint64_t* raw_a;
+    const uint64_t* raw_b;
+    const double* raw_coeff;         // [n_raw][2]
+    const float* raw_coeff_f;
 };
 
 template<typename T> __device__ __forceinline__ const T* diag_coeff(const OpDev& op);
 template<> __device__ __forceinline__ const float* diag_coeff<float>(const OpDev& op) { return op.diag_coeff_f; }
 template<> __device__ __forceinline__ const double* diag_coeff<double>(const OpDev& op) { return op.diag_coeff; }
+template<typename T> __device__ __forceinline__ const T* raw_coeff(const OpDev& op);
+template<> __device__ __forceinline__ const float* raw_coeff<float>(const OpDev& op) { return op.raw_coeff_f; }
+template<> __device__ __forceinline__ const double* raw_coeff<double>(const OpDev& op) { return op.raw_coeff; }
 template<typename T> __device__ __forceinline__ const T* str_coeff(const OpDev& op);
 template<> __device__ __forceinline__ const float* str_coeff<float>(const OpDev& op) { return op.str_coeff_f; }
 template<> __device__ __forceinline__ const double* str_coeff<double>(const OpDev& op) { return op.str_coeff; }

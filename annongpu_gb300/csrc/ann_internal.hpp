@@ -92,6 +92,7 @@ struct ann_op_impl {
     unsigned n_diag = 0, n_groups = 0;
     DevBuf diag_mask, diag_coeff, grp_site_begin, grp_sites, grp_str_begin, str_mask, str_coeff, diag_coeff_f,
         str_coeff_f;
+    DevBuf raw_a, raw_b, raw_c, raw_cf;   // strings as given (Pauli-string basis)
     OpDev view() const;
 };
 
@@ -103,6 +104,7 @@ struct Rows {
 
 struct ann_ens_impl {
     int kind = 0;  // 0 exact, 1 Monte Carlo
+    int basis = 0; // ANN_BASIS_SPINS or ANN_BASIS_PAULIS
     unsigned N = 0;
     // Monte Carlo
     unsigned num_samples = 0, num_sweeps = 0, num_therm = 0, n_chains = 0;
@@ -126,7 +128,7 @@ struct ann_ens_impl {
     unsigned tape_len = 0;
     Rows rows;
     unsigned num_steps() const {
-        return kind == 0 ? (unsigned)(1ull << N) : (num_samples / n_chains) * n_chains;
+        return kind == 0 ? (unsigned)(1ull << (basis ? 2 * N : N)) : (num_samples / n_chains) * n_chains;
     }
     double uniform_weight() const { return 1.0 / (double)num_samples; }
 };
@@ -204,7 +206,7 @@ void psi_prepare(ann_psi_impl& psi, cudaStream_t st);
 void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t,
                   cudaStream_t st);
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs_dev, size_t n, Rows& rows,
-               void* O, size_t ldO, cudaStream_t st);
+               void* O, size_t ldO, cudaStream_t st, int basis = ANN_BASIS_SPINS);
 
 // per-precision RBM launchers (rbm_f32.cu / rbm_f64.cu)
 template<typename T> void rbm_prepare_T(ann_psi_impl& psi, cudaStream_t st);
@@ -274,9 +276,12 @@ std::string key_chol_update(unsigned n);
 
 // PsiCNN (cnn.cu)
 void deep_prepare(ann_psi_impl& psi, cudaStream_t st);
+// builds the layer tables of the multi-layer kernels for a one-layer PsiDeep (RBM family,
+// [a | b | W] parameters) the first time a Pauli-string ensemble or configuration meets it
+void deep_ensure(ann_psi_impl& psi);
 void deep_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st);
 void deep_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
-                size_t ldO, cudaStream_t st);
+                size_t ldO, cudaStream_t st, int basis);
 void cnn_prepare(ann_psi_impl& psi, cudaStream_t st);
 void cnn_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st);
 void cnn_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,

@@ -86,6 +86,7 @@ unsigned* status_word() {
     auto* e = new ann_ens();
     try {
         e->kind = src.kind;
+        e->basis = src.basis;
         e->N = src.N;
         e->num_samples = src.num_samples;
         e->num_sweeps = src.num_sweeps;
@@ -131,6 +132,11 @@ OpDev ann_op_impl::view() const {
     v.str_coeff = str_coeff.as<double>();
     v.diag_coeff_f = diag_coeff_f.as<float>();
     v.str_coeff_f = str_coeff_f.as<float>();
+    v.n_raw = n_strings;
+    v.raw_a = raw_a.as<uint64_t>();
+    v.raw_b = raw_b.as<uint64_t>();
+    v.raw_coeff = raw_c.as<double>();
+    v.raw_coeff_f = raw_cf.as<float>();
     return v;
 }
 
@@ -138,6 +144,7 @@ void psi_prepare(ann_psi_impl& psi, cudaStream_t st) {
     if(psi.kind == 0) {
         if(psi.precision == 0) rbm_prepare_T<float>(psi, st);
         else rbm_prepare_T<double>(psi, st);
+        if(psi.deep.tab_len) deep_prepare(psi, st);  // also serves Pauli-string ensembles
     } else if(psi.kind == 1) {
         cnn_prepare(psi, st);
     } else {
@@ -147,11 +154,21 @@ void psi_prepare(ann_psi_impl& psi, cudaStream_t st) {
 
 void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t,
                   cudaStream_t st) {
-    if(op && op->max_site > psi.N) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
-    if(ens.kind == 0 && ens.N != psi.N) throw Error(ANN_ERR_INVALID, "exact summation size differs from psi.N");
-    if(psi.kind != 0 && ens.kind == 1 && ens.made && ens.indep_per_sample)
-        throw Error(ANN_ERR_UNSUPPORTED, "the learned proposal is built for the RBM family (PsiRBM, one-layer PsiDeep)");
-    if(psi.kind == 0) {
+    if(op && !ens.basis && op->max_site > psi.N)
+        throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
+    if(ens.kind == 0 && !ens.basis && ens.N != psi.N)
+        throw Error(ANN_ERR_INVALID, "exact summation size differs from psi.N");
+    if((psi.kind != 0 || ens.basis) && ens.kind == 1 && ens.made && ens.indep_per_sample)
+        throw Error(ANN_ERR_UNSUPPORTED, "the learned proposal is built for the RBM family over spins");
+    if(ens.basis == ANN_BASIS_PAULIS) {
+        const unsigned sites = ens.kind == 0 ? ens.N : psi.N / 3u;
+        if(psi.N != 3u * sites)
+            throw Error(ANN_ERR_INVALID, "a wavefunction over Pauli strings needs 3 input units per site");
+        if(op && op->max_site > sites) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the strings");
+        if(ens.kind == 1 && ens.tape_len) throw Error(ANN_ERR_UNSUPPORTED, "no proposal tape over Pauli strings");
+        deep_ensure(psi);
+        deep_run(psi, op, ens, t, st);
+    } else if(psi.kind == 0) {
         if(ens.kind == 0) {
             if(psi.precision == 0) rbm_exact_T<float>(psi, op, ens, t, st);
             else rbm_exact_T<double>(psi, op, ens, t, st);
@@ -178,7 +195,14 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
 }
 
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
-               size_t ldO, cudaStream_t st) {
+               size_t ldO, cudaStream_t st, int basis) {
+    if(basis == ANN_BASIS_PAULIS) {
+        if(psi.N % 3u) throw Error(ANN_ERR_INVALID, "a wavefunction over Pauli strings needs 3 input units per site");
+        if(op && op->max_site > psi.N / 3u) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the strings");
+        deep_ensure(psi);
+        deep_confs(psi, op, confs, n, rows, O, ldO, st, basis);
+        return;
+    }
     if(op && op->max_site > psi.N) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
     if(psi.kind == 0) {
         if(psi.precision == 0) rbm_confs_T<float>(psi, op, confs, n, rows, O, ldO, st);
@@ -186,7 +210,7 @@ void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, 
     } else if(psi.kind == 1) {
         cnn_confs(psi, op, confs, n, rows, O, ldO, st);
     } else {
-        deep_confs(psi, op, confs, n, rows, O, ldO, st);
+        deep_confs(psi, op, confs, n, rows, O, ldO, st, basis);
     }
 }
 
@@ -599,6 +623,22 @@ int ann_op_create_pauli(unsigned n, unsigned nw_in, const uint64_t* a, const uin
             std::vector<float> df(dcoef.begin(), dcoef.end()), sf(scoef.begin(), scoef.end());
             upload(op->diag_coeff_f, df.data(), df.size() * 4);
             upload(op->str_coeff_f, sf.data(), sf.size() * 4);
+            // the strings as given, for the Pauli-string basis (first word: sites < 64)
+            std::vector<uint64_t> ra(n), rb(n);
+            std::vector<double> rc(2 * (size_t)n);
+            std::vector<float> rcf(2 * (size_t)n);
+            for(unsigned k = 0; k < n; k++) {
+                ra[k] = op->a[(size_t)k * nw];
+                rb[k] = op->b[(size_t)k * nw];
+                rc[2 * k] = op->coeff[k].real();
+                rc[2 * k + 1] = op->coeff[k].imag();
+                rcf[2 * k] = (float)rc[2 * k];
+                rcf[2 * k + 1] = (float)rc[2 * k + 1];
+            }
+            upload(op->raw_a, ra.data(), ra.size() * 8);
+            upload(op->raw_b, rb.data(), rb.size() * 8);
+            upload(op->raw_c, rc.data(), rc.size() * 8);
+            upload(op->raw_cf, rcf.data(), rcf.size() * 4);
         } catch(...) {
             delete op;
             throw;
@@ -677,7 +717,20 @@ int ann_ens_destroy(ann_ens* e) {
 int ann_ens_num_steps(const ann_ens* e, unsigned* out) {
     return guard([&] {
         need(e && out, "null argument");
-        *out = e->kind == 0 ? (unsigned)(1u << e->N) : e->num_samples;
+        *out = e->kind == 0 ? e->num_steps() : e->num_samples;
+    });
+}
+int ann_ens_set_basis(ann_ens* e, int basis) {
+    return guard([&] {
+        need(e, "null argument");
+        need(basis == ANN_BASIS_SPINS || basis == ANN_BASIS_PAULIS, "unknown basis");
+        if(basis == ANN_BASIS_PAULIS) {
+            need(e->kind == 1 || e->N <= 14, "exact summation over Pauli strings supports 1..14 sites");
+            need(e->kind == 0 || (e->move == ANN_MOVE_FLIP && e->n_up < 0 && e->tape_len == 0),
+                 "Pauli-string chains take single-site moves only (no exchange, fixed Sz or tape)");
+        }
+        e->basis = basis;
+        e->chains_valid = false;
     });
 }
 int ann_ens_refresh_stats(ann_ens* e, void* stream) {
@@ -896,6 +949,60 @@ int ann_local_energies(ann_psi* psi, ann_op* op, const uint64_t* confs, unsigned
         run_confs(*psi, op, sc.confs.as<uint64_t>(), n, sc.rows2, nullptr, 0, st);
         ANN_CUDA(cudaMemcpyAsync(out, sc.rows2.eloc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
         sync(st);
+        check_status();
+    });
+}
+
+namespace {
+// (a, b) pairs -> device rows, then the explicit-configuration kernels in the Pauli basis
+void paulis_to_rows(const uint64_t* ab, unsigned n, DevBuf& dst, cudaStream_t st) {
+    dst.ensure((size_t)std::max(1u, n) * kMaxWords * 8);
+    ANN_CUDA(cudaMemcpyAsync(dst.p, ab, (size_t)n * kMaxWords * 8, cudaMemcpyHostToDevice, st));
+}
+}  // namespace
+
+int ann_log_psi_paulis(ann_psi* psi, const uint64_t* ab, unsigned n, void* stream, double* out) {
+    return guard([&] {
+        need(psi && ab && out, "null argument");
+        auto& sc = scratch();
+        cudaStream_t st = S(stream);
+        paulis_to_rows(ab, n, sc.confs, st);
+        run_confs(*psi, nullptr, sc.confs.as<uint64_t>(), n, sc.rows2, nullptr, 0, st, ANN_BASIS_PAULIS);
+        ANN_CUDA(cudaMemcpyAsync(out, sc.rows2.log_psi.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        sync(st);
+        check_status();
+    });
+}
+
+int ann_local_energies_paulis(ann_psi* psi, ann_op* op, const uint64_t* ab, unsigned n, void* stream, double* out) {
+    return guard([&] {
+        need(psi && op && ab && out, "null argument");
+        auto& sc = scratch();
+        cudaStream_t st = S(stream);
+        paulis_to_rows(ab, n, sc.confs, st);
+        run_confs(*psi, op, sc.confs.as<uint64_t>(), n, sc.rows2, nullptr, 0, st, ANN_BASIS_PAULIS);
+        ANN_CUDA(cudaMemcpyAsync(out, sc.rows2.eloc.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        sync(st);
+        check_status();
+    });
+}
+
+int ann_psi_O_k_paulis(ann_psi* psi, const uint64_t* ab, double* out) {
+    return guard([&] {
+        need(psi && ab && out, "null argument");
+        auto& sc = scratch();
+        paulis_to_rows(ab, 1, sc.confs, nullptr);
+        const size_t ld = ld_for(psi->Np);
+        sc.O.ensure(ld * psi->elem_bytes());
+        run_confs(*psi, nullptr, sc.confs.as<uint64_t>(), 1, sc.rows2, sc.O.p, ld, nullptr, ANN_BASIS_PAULIS);
+        ANN_CUDA(cudaDeviceSynchronize());
+        if(psi->precision == 1) {
+            ANN_CUDA(cudaMemcpy(out, sc.O.p, (size_t)psi->Np * 16, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> f((size_t)psi->Np * 2);
+            ANN_CUDA(cudaMemcpy(f.data(), sc.O.p, f.size() * 4, cudaMemcpyDeviceToHost));
+            for(size_t k = 0; k < f.size(); k++) out[k] = f[k];
+        }
         check_status();
     });
 }

@@ -54,6 +54,21 @@ struct ChainDraw {
     unsigned tape_pos = 0;
     u32x4 rr = {0, 0, 0, 0};
 
+    // the four words of proposal counter (t, chain, 0); t advances
+    __device__ __forceinline__ void words(const McArgs& a, unsigned chain, int lane, uint32_t& r0, uint32_t& r1,
+                                          uint32_t& r2, uint32_t& r3) {
+        const unsigned k = (unsigned)(t - t0) & 31u;
+        if(k == 0) {
+            const uint64_t tl = t + lane;
+            rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
+        }
+        r0 = __shfl_sync(0xffffffffu, rr.x, k);
+        r1 = __shfl_sync(0xffffffffu, rr.y, k);
+        r2 = __shfl_sync(0xffffffffu, rr.z, k);
+        r3 = __shfl_sync(0xffffffffu, rr.w, k);
+        t++;
+    }
+
     __device__ __forceinline__ void next(const McArgs& a, unsigned chain, unsigned N, int lane, unsigned& i,
                                          unsigned& j, double& u, float& uf) {
         j = 0xFFFFFFFFu;
@@ -64,16 +79,8 @@ struct ChainDraw {
             tape_pos++;
             return;
         }
-        const unsigned k = (unsigned)(t - t0) & 31u;
-        if(k == 0) {
-            const uint64_t tl = t + lane;
-            rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
-        }
-        const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
-        const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
-        const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
-        const uint32_t r3 = __shfl_sync(0xffffffffu, rr.w, k);
-        t++;
+        uint32_t r0, r1, r2, r3;
+        words(a, chain, lane, r0, r1, r2, r3);
         i = mulhi32(r0, N);
         if(a.move_kind == 1) {
             const unsigned bnd = mulhi32(r0, a.n_bonds);

@@ -10,6 +10,11 @@
 // with f_0 the log-cosh polynomial and deeper f the odd polynomial (or log cosh on
 // every layer). Parameters [a | b_0 | W_0 | b_1 | W_1 | ...], W_l entry (i, j) at i*M_l + j.
 //
+// Configurations are spins (bit i = input unit i) or, in the Pauli-string basis, strings of
+// I, X, Y, Z over N/3 sites held as words (a, b) (include/basis/PauliString.hpp); site x
+// feeds three input units, +1 for the one of X, Y, Z it holds and -1 otherwise
+// (network_unit_at, :84-90). Operators act on Pauli strings by the product P x.
+//
 // One warp per chain (or enumerated / explicit configuration). A chain keeps its
 // layer-0 pre-activations; a proposal adds the flipped sites' weight columns (the
 // reference's update_angles, through per-site lists of (i, j) entries) and runs the
@@ -39,7 +44,9 @@ struct DeepDev {
     unsigned rq_off[kDeepMaxLayers];          // list entries q = i*M_l + j
     unsigned tab_len;
     int act, a_in;
-    int dup0;       // a site appears twice in one unit's window: layer 0 recomputed per move
+    int basis;      // 0 spins, 1 Pauli strings (N = 3 x sites input units)
+    unsigned sites; // sites of a Pauli string
+    int dup0;       // an input unit appears twice in one unit's window: layer 0 recomputed per move
     int stage_w;    // weights staged in shared memory
     cplx<T> lp;
     const cplx<T>* w;    // Np
@@ -58,6 +65,42 @@ struct DeepCtx {
     cplx<T>* A;    // U: activations (deltas during back-propagation)
 };
 
+// Pauli type of site x: 0 I, 1 X, 2 Y, 3 Z (a bit | b bit << 1)
+__device__ __forceinline__ unsigned ptype(const Conf<2>& s, unsigned x) {
+    return (unsigned)((s.w[0] >> x) & 1u) | ((unsigned)((s.w[1] >> x) & 1u) << 1);
+}
+
+// input unit u is +1
+template<typename T>
+__device__ __forceinline__ int input_up(const DeepCtx<T>& c, const Conf<2>& s, unsigned u) {
+    if(!c.p->basis) return spin_bit(s, u);
+    const unsigned x = u / 3u;
+    return ptype(s, x) == u - 3u * x + 1u;
+}
+
+// calls f(u) for every input unit whose value differs between s and s2 (warp-uniform)
+template<typename T, typename F>
+__device__ __forceinline__ void for_changed_units(const DeepCtx<T>& c, const Conf<2>& s, const Conf<2>& s2, F f) {
+    if(!c.p->basis) {
+        for(int w = 0; w < 2; w++) {
+            uint64_t d = s.w[w] ^ s2.w[w];
+            while(d) {
+                f(64u * w + (unsigned)(__ffsll((long long)d) - 1));
+                d &= d - 1;
+            }
+        }
+        return;
+    }
+    uint64_t d = (s.w[0] ^ s2.w[0]) | (s.w[1] ^ s2.w[1]);
+    while(d) {
+        const unsigned x = (unsigned)(__ffsll((long long)d) - 1);
+        d &= d - 1;
+        const unsigned to = ptype(s, x), tn = ptype(s2, x);
+        if(to) f(3u * x + to - 1u);
+        if(tn) f(3u * x + tn - 1u);
+    }
+}
+
 template<typename T>
 __device__ __forceinline__ void add_spin(cplx<T>& z, cplx<T> w, int up) {
     if(up) { z.re += w.re; z.im += w.im; }
@@ -72,7 +115,7 @@ __device__ void deep_z0(const DeepCtx<T>& c, const Conf<2>& s, cplx<T>* dst, int
     const uint16_t* cn = c.tab + p.conn_off[0];
     for(unsigned j = lane; j < M; j += 32) {
         cplx<T> z = c.w[p.b_off[0] + j];
-        for(unsigned i = 0; i < p.C[0]; i++) add_spin(z, c.w[p.w_off[0] + i * M + j], spin_bit(s, cn[i * M + j]));
+        for(unsigned i = 0; i < p.C[0]; i++) add_spin(z, c.w[p.w_off[0] + i * M + j], input_up(c, s, cn[i * M + j]));
         dst[j] = z;
     }
 }
@@ -81,19 +124,19 @@ __device__ void deep_z0(const DeepCtx<T>& c, const Conf<2>& s, cplx<T>* dst, int
 template<typename T>
 __device__ cplx<T> deep_as(const DeepCtx<T>& c, const Conf<2>& s, int lane) {
     cplx<T> acc = mk<T>(T(0), T(0));
-    for(unsigned x = lane; x < c.p->N; x += 32) add_spin(acc, c.w[x], spin_bit(s, x));
+    for(unsigned x = lane; x < c.p->N; x += 32) add_spin(acc, c.w[x], input_up(c, s, x));
     return warp_sum(acc);
 }
 
-// Z[0, M_0) += the change of flipping site x of s (update_angles, PsiDeep.hpp:268-281).
-// A site's entries address distinct units (checked on the host), so lanes do not collide.
+// Z[0, M_0) += the change of flipping input unit x of s (update_angles, PsiDeep.hpp:268-307).
+// A unit's entries address distinct first-layer units (checked on the host), so lanes do not collide.
 template<typename T>
 __device__ void deep_flip0(const DeepCtx<T>& c, const Conf<2>& s, unsigned x, int lane) {
     const DeepDev<T>& p = *c.p;
     const uint16_t* rb = c.tab + p.rbeg_off[0];
     const uint16_t* rq = c.tab + p.rq_off[0];
     const unsigned M = p.size[0];
-    const T d = spin_bit(s, x) ? T(-2) : T(2);
+    const T d = input_up(c, s, x) ? T(-2) : T(2);
     for(unsigned e = rb[x] + lane; e < rb[x + 1]; e += 32) {
         const unsigned q = rq[e];
         const cplx<T> wv = c.w[p.w_off[0] + q];
@@ -128,34 +171,28 @@ __device__ cplx<T> deep_forward(const DeepCtx<T>& c, int lane) {
     return warp_sum(acc);
 }
 
-// log psi of s with the sites in `sites` flipped (n sites; s itself for n = 0), from the
-// chain's layer-0 pre-activations th; Z / A hold that configuration afterwards
+// log psi of s2 from the chain's layer-0 pre-activations th of s (the units that differ are
+// moved); Z / A hold s2 afterwards. `as` is a.s of s.
 template<typename T>
-__device__ cplx<T> deep_eval_flips(const DeepCtx<T>& c, const Conf<2>& s, cplx<T> as, const uint16_t* sites,
-                                   unsigned n, unsigned i0, unsigned j0, int lane) {
+__device__ cplx<T> deep_eval_moved(const DeepCtx<T>& c, const Conf<2>& s, const Conf<2>& s2, cplx<T> as, int lane) {
     const DeepDev<T>& p = *c.p;
-    // sites come from a list (operator groups) or from (i0, j0) (proposals)
-    auto site = [&](unsigned k) -> unsigned { return sites ? (unsigned)sites[k] : (k == 0 ? i0 : j0); };
     if(!p.dup0) {
         for(unsigned j = lane; j < p.size[0]; j += 32) c.Z[j] = c.th[j];
         __syncwarp();
-        for(unsigned k = 0; k < n; k++) {
-            deep_flip0(c, s, site(k), lane);
+        for_changed_units(c, s, s2, [&](unsigned u) {
+            deep_flip0(c, s, u, lane);
             __syncwarp();
-        }
+        });
     } else {
-        Conf<2> s2 = s;
-        for(unsigned k = 0; k < n; k++) flip(s2, site(k));
         deep_z0(c, s2, c.Z, lane);
         __syncwarp();
     }
     if(p.a_in)
-        for(unsigned k = 0; k < n; k++) {
-            const unsigned x = site(k);
-            const T d = spin_bit(s, x) ? T(-2) : T(2);
-            as.re += d * c.w[x].re;
-            as.im += d * c.w[x].im;
-        }
+        for_changed_units(c, s, s2, [&](unsigned u) {
+            const T d = input_up(c, s, u) ? T(-2) : T(2);
+            as.re += d * c.w[u].re;
+            as.im += d * c.w[u].im;
+        });
     const cplx<T> f = deep_forward(c, lane);
     return mk<T>(p.lp.re + as.re + f.re, p.lp.im + as.im + f.im);
 }
@@ -179,7 +216,7 @@ __device__ void deep_O_row(const DeepCtx<T>& c, const Conf<2>& s, int lane, cplx
         for(unsigned q = lane; q < C * M; q += 32) {
             const unsigned j = q % M, u = cn[q];
             cplx<T> o;
-            if(l == 0) o = spin_bit(s, u) ? dl[j] : -dl[j];
+            if(l == 0) o = input_up(c, s, u) ? dl[j] : -dl[j];
             else o = dl[j] * c.A[p.uoff[l - 1] + u];
             O[p.w_off[l] + q] = o;
         }
@@ -201,7 +238,7 @@ __device__ void deep_O_row(const DeepCtx<T>& c, const Conf<2>& s, int lane, cplx
             __syncwarp();
         }
     }
-    for(unsigned x = lane; x < p.N; x += 32) O[x] = mk<T>(spin_bit(s, x) ? T(1) : T(-1), T(0));
+    for(unsigned x = lane; x < p.N; x += 32) O[x] = mk<T>(input_up(c, s, x) ? T(1) : T(-1), T(0));
     __syncwarp();
 }
 
@@ -228,9 +265,43 @@ __device__ cplx<double> deep_local_energy(const DeepCtx<T>& c, const OpDev& op, 
             cg.im += (neg & 1) ? -c_im : c_im;
         }
         if(cg.re == T(0) && cg.im == T(0)) continue;
-        const unsigned b0 = op.grp_site_begin[g];
-        const cplx<T> l2 = deep_eval_flips(c, s, as, op.grp_sites + b0, op.grp_site_begin[g + 1] - b0, 0, 0, lane);
+        Conf<2> s2 = s;
+        for(unsigned q = op.grp_site_begin[g]; q < op.grp_site_begin[g + 1]; q++) flip(s2, op.grp_sites[q]);
+        const cplx<T> l2 = deep_eval_moved(c, s, s2, as, lane);
         e += cg * cexp(l2 - lpsi);
+    }
+    return cvt<double>(e);
+}
+
+// local energy over Pauli strings: sum_n c_n phase(P_n, x) psi(P_n x) / psi(x) with the product
+// string P_n ^ x and phase (-1)^{#(XZ, YX, ZY) pairs} (-i)^{n_eps}, n_eps the sites where both
+// are non-trivial and differ (PauliString::apply(PauliString), PauliString.hpp:256-276)
+template<typename T>
+__device__ cplx<double> deep_local_energy_paulis(const DeepCtx<T>& c, const OpDev& op, const Conf<2>& s,
+                                                 cplx<T> lpsi, cplx<T> as, int lane) {
+    const uint64_t xa = s.w[0], xb = s.w[1];
+    const uint64_t xX = xa & ~xb, xY = ~xa & xb, xZ = xa & xb;
+    cplx<T> e = mk<T>(T(0), T(0));
+    for(unsigned n = 0; n < op.n_raw; n++) {
+        const uint64_t pa = op.raw_a[n], pb = op.raw_b[n];
+        const T c_re = raw_coeff<T>(op)[2 * n], c_im = raw_coeff<T>(op)[2 * n + 1];
+        if(!(pa | pb)) {
+            e.re += c_re;
+            e.im += c_im;
+            continue;
+        }
+        const uint64_t pX = pa & ~pb, pY = ~pa & pb, pZ = pa & pb;
+        const int neg = __popcll((pX & xZ) | (pY & xX) | (pZ & xY)) & 1;
+        const int ne = __popcll((pa | pb) & (xa | xb) & ((pa ^ xa) | (pb ^ xb)));
+        // coefficient times (-1)^neg, times -1 if ne % 4 >= 2, times -i if ne is odd
+        T f_re = c_re, f_im = c_im;
+        if(neg ^ ((ne & 3) > 1)) { f_re = -f_re; f_im = -f_im; }
+        if(ne & 1) { const T t = f_re; f_re = f_im; f_im = -t; }
+        Conf<2> s2;
+        s2.w[0] = xa ^ pa;
+        s2.w[1] = xb ^ pb;
+        const cplx<T> l2 = deep_eval_moved(c, s, s2, as, lane);
+        e += mk<T>(f_re, f_im) * cexp(l2 - lpsi);
     }
     return cvt<double>(e);
 }
@@ -244,12 +315,13 @@ __device__ void deep_process_sample(const DeepCtx<T>& c, const OpDev* op, const 
     deep_z0(c, s, c.th, lane);
     __syncwarp();
     const cplx<T> as = c.p->a_in ? deep_as(c, s, lane) : mk<T>(T(0), T(0));
-    const cplx<T> lpsi = deep_eval_flips(c, s, as, nullptr, 0, 0, 0, lane);
+    const cplx<T> lpsi = deep_eval_moved(c, s, s, as, lane);
     if(lpsi_out) *lpsi_out = lpsi;
     if(as_out) *as_out = as;
     if(out.O) deep_O_row(c, s, lane, reinterpret_cast<cplx<T>*>(out.O) + row * out.ldO);
     cplx<double> e = mk(0.0, 0.0);
-    if(op) e = deep_local_energy(c, *op, s, lpsi, as, lane);
+    if(op) e = c.p->basis ? deep_local_energy_paulis(c, *op, s, lpsi, as, lane)
+                          : deep_local_energy(c, *op, s, lpsi, as, lane);
     if(lane == 0) {
         for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = s.w[w];
         const cplx<double> l = cvt<double>(lpsi);
@@ -317,40 +389,63 @@ __global__ void __launch_bounds__(256, 1) deep_mc_kernel(DeepDev<T> p, OpDev op,
     const unsigned N = p.N;
     Conf<2> s;
     ChainDraw dr;
-    chain_start(a, chain, N, s, dr.t);
+    if(p.basis) {
+        // Pauli strings: a fresh string from counter (t, chain, 1), masked to the sites
+        dr.t = a.chain_counter[chain];
+        if(a.do_init) {
+            const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)dr.t, (uint32_t)(dr.t >> 32), chain, 1u});
+            const uint64_t mask = p.sites >= 64u ? ~(uint64_t)0 : (((uint64_t)1 << p.sites) - 1u);
+            s.w[0] = ((uint64_t)r.x | ((uint64_t)r.y << 32)) & mask;
+            s.w[1] = ((uint64_t)r.z | ((uint64_t)r.w << 32)) & mask;
+        } else {
+            for(int w = 0; w < 2; w++) s.w[w] = a.chain_conf[(size_t)chain * kMaxWords + w];
+        }
+    } else {
+        chain_start(a, chain, N, s, dr.t);
+    }
     dr.t0 = dr.t;
     deep_z0(c, s, c.th, lane);
     __syncwarp();
     cplx<T> as = p.a_in ? deep_as(c, s, lane) : mk<T>(T(0), T(0));
-    cplx<T> lpsi = deep_eval_flips(c, s, as, nullptr, 0, 0, 0, lane);
+    cplx<T> lpsi = deep_eval_moved(c, s, s, as, lane);
     unsigned long long n_acc = 0, n_rej = 0;
     auto propose = [&]() {
-        unsigned i, j;
         double u;
         float uf;
-        dr.next(a, chain, N, lane, i, j, u, uf);
-        unsigned n = 1;
-        if(j != kNoSite) {
-            if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
-            n = 2;
+        Conf<2> s2 = s;
+        if(p.basis) {
+            // site mulhi(r0, sites) set to type r1 >> 30 (Update_Policy.hpp:41-57 draws x % sites, x >> 30)
+            uint32_t r0, r1, r2, r3;
+            dr.words(a, chain, lane, r0, r1, r2, r3);
+            const unsigned x = mulhi32(r0, p.sites), type = r1 >> 30;
+            s2.w[0] = (s2.w[0] & ~((uint64_t)1 << x)) | ((uint64_t)(type & 1u) << x);
+            s2.w[1] = (s2.w[1] & ~((uint64_t)1 << x)) | ((uint64_t)(type >> 1) << x);
+            u = u53(r2, r3);
+            uf = __uint2float_rz(r3 >> 8) * 0x1.0p-24f;
+            if(s2.w[0] == s.w[0] && s2.w[1] == s.w[1]) { n_acc++; return; }  // ratio 1
+        } else {
+            unsigned i, j;
+            dr.next(a, chain, N, lane, i, j, u, uf);
+            flip(s2, i);
+            if(j != kNoSite) {
+                if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
+                flip(s2, j);
+            }
         }
-        const cplx<T> l2 = deep_eval_flips(c, s, as, nullptr, n, i, j, lane);
+        const cplx<T> l2 = deep_eval_moved(c, s, s2, as, lane);
         const T ratio = fexp(T(2) * (l2.re - lpsi.re));
         const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
         if(accept) {
             // Z holds the moved configuration's layer-0 pre-activations
             for(unsigned q = lane; q < p.size[0]; q += 32) c.th[q] = c.Z[q];
             __syncwarp();
-            if(p.a_in) {
-                for(unsigned k = 0; k < n; k++) {
-                    const unsigned x = k == 0 ? i : j;
-                    const T d = spin_bit(s, x) ? T(-2) : T(2);
-                    as.re += d * c.w[x].re;
-                    as.im += d * c.w[x].im;
-                }
-            }
-            flip(s, i);
-            if(n == 2) flip(s, j);
+            if(p.a_in)
+                for_changed_units(c, s, s2, [&](unsigned uu) {
+                    const T d = input_up(c, s, uu) ? T(-2) : T(2);
+                    as.re += d * c.w[uu].re;
+                    as.im += d * c.w[uu].im;
+                });
+            s = s2;
             lpsi = l2;
             n_acc++;
         } else {
@@ -384,8 +479,17 @@ __global__ void __launch_bounds__(256, 1) deep_exact_kernel(DeepDev<T> p, OpDev 
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     for(uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n_conf; idx += warps) {
         Conf<2> s;
-        s.w[0] = idx;
-        s.w[1] = 0;
+        if(p.basis) {
+            // base-4 digit x of idx is the type of site x (PauliString::enumerate, PauliString.hpp:30-35)
+            s.w[0] = s.w[1] = 0;
+            for(unsigned x = 0; x < p.sites; x++) {
+                s.w[0] |= ((idx >> (2 * x)) & 1u) << x;
+                s.w[1] |= ((idx >> (2 * x + 1)) & 1u) << x;
+            }
+        } else {
+            s.w[0] = idx;
+            s.w[1] = 0;
+        }
         deep_process_sample(c, with_op ? &op : nullptr, s, lane, idx, out, true);
     }
 }
@@ -414,8 +518,10 @@ __global__ void deep_prepare_kernel(const cplx<double>* __restrict__ params, cpl
 constexpr size_t kDeepSmemCap = 200 * 1024;
 
 template<typename T>
-DeepDev<T> deep_view(const ann_psi_impl& psi) {
+DeepDev<T> deep_view(const ann_psi_impl& psi, int basis) {
     DeepDev<T> p{};
+    p.basis = basis;
+    p.sites = basis ? psi.N / 3u : psi.N;
     const DeepHost& d = psi.deep;
     p.N = psi.N;
     p.L = (unsigned)d.sizes.size();
@@ -485,13 +591,13 @@ void deep_rows(Rows& rows, size_t n) {
 template<typename T>
 void deep_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t,
                 cudaStream_t st) {
-    const DeepDev<T> p = deep_view<T>(psi);
+    const DeepDev<T> p = deep_view<T>(psi, ens.basis);
     const int wpb = deep_warps(p);
     const size_t smem = deep_fixed_bytes(p) + wpb * deep_warp_bytes(p);
     OpDev ov{};
     if(op) ov = op->view();
     if(ens.kind == 0) {
-        const uint64_t n_conf = 1ull << ens.N;
+        const uint64_t n_conf = ens.num_steps();
         deep_rows(*t.rows, n_conf);
         SampleOut out = deep_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
         uint64_t blocks = (n_conf + wpb - 1) / wpb;
@@ -534,8 +640,8 @@ void deep_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, con
 
 template<typename T>
 void deep_confs_T(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
-                  size_t ldO, cudaStream_t st) {
-    const DeepDev<T> p = deep_view<T>(psi);
+                  size_t ldO, cudaStream_t st, int basis) {
+    const DeepDev<T> p = deep_view<T>(psi, basis);
     const int wpb = deep_warps(p);
     const size_t smem = deep_fixed_bytes(p) + wpb * deep_warp_bytes(p);
     OpDev ov{};
@@ -546,6 +652,57 @@ void deep_confs_T(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* conf
     deep_set_smem(deep_confs_kernel<T>, smem);
     deep_confs_kernel<T><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, confs, n, out);
     check_launch("deep_confs_kernel");
+}
+
+// device table of a PsiDeep layer structure: connection blocks | per layer the lists of the
+// units below (rbeg: units below + 1 offsets, rq: C x M entries). The lists follow the reference's
+// compile_rhs_connections_and_weights order (PsiDeep.cu:213-242): units ascending, then
+// connections ascending within a unit.
+void deep_build_tables(ann_psi_impl& p) {
+    DeepHost& h = p.deep;
+    const unsigned L = (unsigned)h.sizes.size();
+    // table: connection blocks | per layer (rbeg: in + 1 entries, rq: C x M entries)
+    std::vector<uint16_t> tab;
+    unsigned coff = 0;
+    h.conn_off.assign(L, 0);
+    h.rbeg_off.assign(L, 0);
+    h.rq_off.assign(L, 0);
+    for(unsigned l = 0; l < L; l++) {
+        const unsigned in = l ? h.sizes[l - 1] : p.N, M = h.sizes[l], C = h.C[l];
+        h.conn_off[l] = (unsigned)tab.size();
+        for(unsigned k = 0; k < C * M; k++) {
+            const unsigned u = h.conn[coff + k];
+            if(u >= in) throw Error(ANN_ERR_INVALID, "connection index out of range");
+            tab.push_back((uint16_t)u);
+        }
+        coff += C * M;
+    }
+    coff = 0;
+    h.dup0 = 0;
+    for(unsigned l = 0; l < L; l++) {
+        const unsigned in = l ? h.sizes[l - 1] : p.N, M = h.sizes[l], C = h.C[l];
+        std::vector<std::vector<uint16_t>> lists(in);
+        for(unsigned j = 0; j < M; j++)
+            for(unsigned i = 0; i < C; i++) lists[h.conn[coff + i * M + j]].push_back((uint16_t)(i * M + j));
+        if(l == 0)
+            for(const auto& li : lists) {
+                std::vector<unsigned> js;
+                for(uint16_t q : li) js.push_back(q % M);
+                std::sort(js.begin(), js.end());
+                if(std::adjacent_find(js.begin(), js.end()) != js.end()) h.dup0 = 1;
+            }
+        h.rbeg_off[l] = (unsigned)tab.size();
+        unsigned acc = 0;
+        for(unsigned u = 0; u <= in; u++) {
+            tab.push_back((uint16_t)acc);
+            if(u < in) acc += (unsigned)lists[u].size();
+        }
+        h.rq_off[l] = (unsigned)tab.size();
+        for(const auto& li : lists) tab.insert(tab.end(), li.begin(), li.end());
+        coff += C * M;
+    }
+    h.tab_len = (unsigned)tab.size();
+    upload(p.deep_tab, tab.data(), tab.size() * sizeof(uint16_t));
 }
 
 }  // namespace
@@ -566,10 +723,23 @@ void deep_run(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     else deep_run_T<double>(psi, op, ens, t, st);
 }
 
+void deep_ensure(ann_psi_impl& psi) {
+    if(psi.kind == 2 || psi.deep.tab_len) return;
+    if(psi.kind != 0 || psi.layout != ANN_LAYOUT_DEEP)
+        throw Error(ANN_ERR_UNSUPPORTED, "Pauli strings are built for PsiDeep (any depth)");
+    psi.deep.sizes = {psi.M};
+    psi.deep.C = {psi.C};
+    psi.deep.conn = psi.conn;
+    deep_build_tables(psi);
+    psi.cnn_w.ensure((size_t)psi.Np * psi.elem_bytes());
+    deep_prepare(psi, nullptr);
+    ANN_CUDA(cudaStreamSynchronize(nullptr));
+}
+
 void deep_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
-                size_t ldO, cudaStream_t st) {
-    if(psi.precision == 0) deep_confs_T<float>(psi, op, confs, n, rows, O, ldO, st);
-    else deep_confs_T<double>(psi, op, confs, n, rows, O, ldO, st);
+                size_t ldO, cudaStream_t st, int basis) {
+    if(psi.precision == 0) deep_confs_T<float>(psi, op, confs, n, rows, O, ldO, st, basis);
+    else deep_confs_T<double>(psi, op, confs, n, rows, O, ldO, st, basis);
 }
 
 }  // namespace ann
@@ -614,48 +784,7 @@ extern "C" int ann_psi_create_deep(const ann_deep_desc* d, ann_psi** out) {
             if(np != d->num_params) throw Error(ANN_ERR_INVALID, "num_params does not match the layer structure");
             p->Np = np;
             h.conn.assign(d->connections, d->connections + total);
-            // table: connection blocks | per layer (rbeg: in + 1 entries, rq: C x M entries)
-            std::vector<uint16_t> tab;
-            unsigned coff = 0;
-            h.conn_off.assign(L, 0);
-            h.rbeg_off.assign(L, 0);
-            h.rq_off.assign(L, 0);
-            for(unsigned l = 0; l < L; l++) {
-                const unsigned in = l ? h.sizes[l - 1] : d->N, M = h.sizes[l], C = h.C[l];
-                h.conn_off[l] = (unsigned)tab.size();
-                for(unsigned k = 0; k < C * M; k++) {
-                    const unsigned u = h.conn[coff + k];
-                    if(u >= in) throw Error(ANN_ERR_INVALID, "connection index out of range");
-                    tab.push_back((uint16_t)u);
-                }
-                coff += C * M;
-            }
-            coff = 0;
-            h.dup0 = 0;
-            for(unsigned l = 0; l < L; l++) {
-                const unsigned in = l ? h.sizes[l - 1] : d->N, M = h.sizes[l], C = h.C[l];
-                std::vector<std::vector<uint16_t>> lists(in);
-                for(unsigned j = 0; j < M; j++)
-                    for(unsigned i = 0; i < C; i++) lists[h.conn[coff + i * M + j]].push_back((uint16_t)(i * M + j));
-                if(l == 0)
-                    for(const auto& li : lists) {
-                        std::vector<unsigned> js;
-                        for(uint16_t q : li) js.push_back(q % M);
-                        std::sort(js.begin(), js.end());
-                        if(std::adjacent_find(js.begin(), js.end()) != js.end()) h.dup0 = 1;
-                    }
-                h.rbeg_off[l] = (unsigned)tab.size();
-                unsigned acc = 0;
-                for(unsigned u = 0; u <= in; u++) {
-                    tab.push_back((uint16_t)acc);
-                    if(u < in) acc += (unsigned)lists[u].size();
-                }
-                h.rq_off[l] = (unsigned)tab.size();
-                for(const auto& li : lists) tab.insert(tab.end(), li.begin(), li.end());
-                coff += C * M;
-            }
-            h.tab_len = (unsigned)tab.size();
-            upload(p->deep_tab, tab.data(), tab.size() * sizeof(uint16_t));
+            deep_build_tables(*p);
             const unsigned ML = h.sizes[L - 1];
             p->fw.assign(ML, zd(0, 0));
             const size_t es = p->elem_bytes();

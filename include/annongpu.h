@@ -175,6 +175,16 @@ int ann_ens_copy(const ann_ens* ens, ann_ens** out);
 int ann_ens_destroy(ann_ens* ens);
 /* num_steps (main.cpp.template:363, 398) */
 int ann_ens_num_steps(const ann_ens* ens, unsigned* out);
+
+#define ANN_BASIS_SPINS 0   /* configurations are spins, bit i = input unit i */
+#define ANN_BASIS_PAULIS 1  /* configurations are Pauli strings (words a, b; include/basis/PauliString.hpp) */
+/* ExactSummationPaulis(num_sites) (main.cpp.template:402-406) = an exact ensemble over num_sites
+   sites switched to ANN_BASIS_PAULIS (4^num_sites strings, PauliString.hpp:26-35);
+   MonteCarloPaulis (main.cpp.template:369-380) = a Monte Carlo ensemble switched to it (moves set
+   one random site to a random Pauli type, Update_Policy.hpp:41-57; single-flip moves only, no
+   tape, no learned proposal). The wavefunction sees 3 input units per site
+   (PauliString::network_unit_at, :84-90): PsiDeep of any depth. */
+int ann_ens_set_basis(ann_ens* ens, int basis);
 /* acceptance_rate of the last sampling call (main.cpp.template:364-366) */
 int ann_ens_acceptance_rate(const ann_ens* ens, double* out);
 /* reads the acceptance counters of the last sampling pass (synchronising `stream`) and
@@ -223,6 +233,11 @@ int ann_log_psi_batch(ann_psi* psi, const uint64_t* confs, unsigned n, void* str
 int ann_local_energies(ann_psi* psi, ann_op* op, const uint64_t* confs, unsigned n, void* stream, double* out);
 /* psi_O_k(psi, Spins) (PsiOkVector.cu.template:40-74) */
 int ann_psi_O_k(ann_psi* psi, const uint64_t* conf, double* out);
+/* the same over Pauli strings (log_psi_s / psi_O_k with a PauliString, PsiVector.cu.template:191-197):
+   `ab` holds (a, b) word pairs, one per string */
+int ann_log_psi_paulis(ann_psi* psi, const uint64_t* ab, unsigned n, void* stream, double* out);
+int ann_psi_O_k_paulis(ann_psi* psi, const uint64_t* ab, double* out);
+int ann_local_energies_paulis(ann_psi* psi, ann_op* op, const uint64_t* ab, unsigned n, void* stream, double* out);
 /* psi_O_k_vector(psi, esum): sum_s O_k(s), unweighted (PsiOkVector.cu.template:8-38) */
 int ann_psi_O_k_vector(ann_psi* psi, ann_ens* ens, void* stream, double* out);
 /* log_psi(psi, ens): sum_s w(s) log psi(s) (PsiVector.cu.template:73-99) */

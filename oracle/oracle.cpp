@@ -8,6 +8,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <memory>
 #include <random>
 #include <vector>
 
@@ -631,6 +632,55 @@ struct DeepChain {
     }
 };
 
+
+// ---- PsiClassical: PsiClassical.hpp:75-133, Operator.hpp:122-133 ----
+struct Classical {
+    const or_classical* p;
+    unsigned K;
+    std::vector<cd> theta;
+    const Deep* ref;
+    cd lp;
+    Classical(const or_classical* p_, const Deep* ref_) : p(p_), K(p_->n_features), ref(ref_) {
+        theta.resize(K);
+        for(unsigned k = 0; k < K; k++) theta[k] = cx(p->params, k);
+        lp = cd(p->lp_re, p->lp_im);
+    }
+    bool with_ref() const { return p->order > 1 && ref; }
+    unsigned np() const { return K + (with_ref() ? ref->np : 0u); }
+    // h_k(s) = sum over the feature's strings of coefficient x <s|P|P s> (Operator::fast_local_energy)
+    cd h(unsigned k, const Conf& s) const {
+        cd r(0.0);
+        for(unsigned q = p->feat_begin[k]; q < p->feat_begin[k + 1]; q++)
+            r += cx(p->coeff, q) * pauli_apply(p->a + (size_t)q * p->nw, p->b + (size_t)q * p->nw, p->nw, s).factor;
+        return r;
+    }
+    cd log_psi(const Conf& s) const {
+        cd r = lp;
+        for(unsigned k = 0; k < K; k++) r += theta[k] * h(k, s);
+        if(with_ref()) r += ref->log_psi(s);
+        return r;
+    }
+    void O_k(const Conf& s, std::vector<cd>& O) const {
+        O.assign(np(), cd(0.0));
+        for(unsigned k = 0; k < K; k++) O[k] = h(k, s);
+        if(with_ref()) {
+            std::vector<cd> Or;
+            ref->O_k(s, Or);
+            for(size_t k = 0; k < Or.size(); k++) O[K + k] = Or[k];
+        }
+    }
+    cd local_energy(const or_op* op, const Conf& s, cd lpsi) const {
+        cd r(0.0);
+        for(unsigned n = 0; n < op->n; n++) {
+            ME me = pauli_apply(op->a + n * op->nw, op->b + n * op->nw, op->nw, s);
+            me.factor *= cx(op->coeff, n);
+            if(me.conf != s) r += me.factor * std::exp(log_psi(me.conf) - lpsi);
+            else r += me.factor;
+        }
+        return r;
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -877,7 +927,8 @@ void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uin
                       n_bonds, init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
         return;
     }
-    // Pauli-string chains: one sweep = N/3 proposals
+    // Pauli-string chains: one sweep = N proposals, N the input units (MonteCarlo.hpp:89-100
+    // counts sweeps in get_num_input_units())
     const unsigned S = psi.sites();
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     uint64_t acc_total = 0, rej_total = 0;
@@ -910,9 +961,9 @@ void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uin
             else rej_total++;
         };
         if(init)
-            for(unsigned k = 0; k < num_therm * S; k++) propose();
+            for(unsigned k = 0; k < num_therm * psi.N; k++) propose();
         for(unsigned st = 0; st < samples_per_chain; st++) {
-            for(unsigned k = 0; k < num_sweeps * S; k++) propose();
+            for(unsigned k = 0; k < num_sweeps * psi.N; k++) propose();
             lp = psi.log_psi(s);
             const size_t row = (size_t)st * n_chains + c;
             if(sconf) { sconf[row * 2] = s[0]; sconf[row * 2 + 1] = s[1]; }
@@ -926,6 +977,121 @@ void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uin
     if(n_accept) *n_accept = acc_total;
     if(n_reject) *n_reject = rej_total;
     if(min_tie) *min_tie = tie;
+}
+
+unsigned or_classical_num_params(const or_classical* p) {
+    if(p->order > 1 && p->ref) return p->n_features + Deep(p->ref).np;
+    return p->n_features;
+}
+
+void or_classical_log_psi(const or_classical* p, const uint64_t* conf, double* out) {
+    std::unique_ptr<Deep> ref(p->ref ? new Deep(p->ref) : nullptr);
+    Classical psi(p, ref.get());
+    put(out, psi.log_psi(load_conf(conf, nwords(p->num_sites))));
+}
+
+void or_classical_O_k(const or_classical* p, const uint64_t* conf, double* out) {
+    std::unique_ptr<Deep> ref(p->ref ? new Deep(p->ref) : nullptr);
+    Classical psi(p, ref.get());
+    std::vector<cd> O;
+    psi.O_k(load_conf(conf, nwords(p->num_sites)), O);
+    for(size_t k = 0; k < O.size(); k++) put(out + 2 * k, O[k]);
+}
+
+void or_classical_local_energy(const or_classical* p, const or_op* op, const uint64_t* conf, double* out) {
+    std::unique_ptr<Deep> ref(p->ref ? new Deep(p->ref) : nullptr);
+    Classical psi(p, ref.get());
+    const Conf s = load_conf(conf, nwords(p->num_sites));
+    put(out, psi.local_energy(op, s, psi.log_psi(s)));
+}
+
+void or_classical_exact(const or_classical* p, const or_op* op, double* E, double* norm,
+                        double* tE, double* tE2, double* tO, double* tF, double* tS) {
+    std::unique_ptr<Deep> ref(p->ref ? new Deep(p->ref) : nullptr);
+    Classical psi(p, ref.get());
+    Accum acc(psi.np());
+    double nrm = 0.0;
+    std::vector<cd> Ok;
+    for(uint64_t idx = 0; idx < ((uint64_t)1 << p->num_sites); idx++) {
+        const Conf s = enumerate(idx);
+        const cd lp = psi.log_psi(s);
+        const double w = std::exp(2.0 * lp.real());
+        const cd eloc = op ? psi.local_energy(op, s, lp) : cd(0.0);
+        psi.O_k(s, Ok);
+        acc.add(w, eloc, Ok, tS != nullptr);
+        nrm += w;
+    }
+    if(E) put(E, acc.E);
+    if(norm) norm[0] = std::sqrt(nrm);
+    acc.finish(nullptr, nullptr, tE, tE2, tO, tF, tS);
+}
+
+void or_kl(const or_classical* pc, const or_deep* pp, const uint64_t* confs, const double* wprime, unsigned n,
+           double threshold, const double* last_mean, double log_psi_scale, double nu,
+           double* value, double* grad, double* noise, double* total_weight, double* mean_deviation) {
+    std::unique_ptr<Deep> ref(pc->ref ? new Deep(pc->ref) : nullptr);
+    Classical psi(pc, ref.get());
+    Deep prime(pp);
+    const unsigned np = prime.np;
+    const cd last(last_mean ? last_mean[0] : 0.0, last_mean ? last_mean[1] : 0.0);
+    const double th2 = threshold * threshold;
+    double W = 0.0, d2 = 0.0;
+    cd mean(0.0), d(0.0);
+    std::vector<cd> Ok(np, 0.0), dOc(np, 0.0), dO(np, 0.0), d2O(np, 0.0), dOk2(np, 0.0);
+    std::vector<double> d2Ok2(np, 0.0), Ok2(np, 0.0);
+    const bool exact = confs == nullptr;
+    const uint64_t rows = exact ? ((uint64_t)1 << prime.N) : n;
+    std::vector<cd> O;
+    for(uint64_t r = 0; r < rows; r++) {
+        const Conf s = exact ? enumerate(r) : load_conf(confs + r * 2, 2);
+        const cd lpp = prime.log_psi(s);
+        const double wp = exact ? std::exp(2.0 * lpp.real()) : wprime[r];
+        const cd lps = log_psi_scale * psi.log_psi(s);
+        const double w = std::exp(2.0 * (lps.real() - lpp.real())) * wp;
+        W += w;
+        mean += w * (lpp - lps);
+        const cd dev = lpp - lps - last;
+        const double dev2 = std::norm(dev);
+        const bool in = dev2 > th2;
+        if(in) { d += w * dev; d2 += w * dev2; }
+        if(!grad) continue;
+        prime.O_k(s, O);
+        for(unsigned k = 0; k < np; k++) {
+            Ok[k] += w * O[k];
+            if(in) dOc[k] += w * dev * std::conj(O[k]);
+            if(noise) {
+                const double o2 = std::norm(O[k]);
+                if(in) {
+                    d2Ok2[k] += w * dev2 * o2;
+                    dO[k] += w * dev * O[k];
+                    dOk2[k] += w * dev * o2;
+                    d2O[k] += w * dev2 * O[k];
+                }
+                Ok2[k] += w * o2;
+            }
+        }
+    }
+    d /= W;
+    d2 /= W;
+    const double val = std::sqrt(std::max(1e-8, d2 - std::norm(d)));
+    if(value) *value = val;
+    if(total_weight) *total_weight = W;
+    if(mean_deviation) put(mean_deviation, mean / W);
+    if(!grad) return;
+    const double factor = std::pow(val, nu);
+    for(unsigned k = 0; k < np; k++) {
+        const cd o = Ok[k] / W, doc = dOc[k] / W;
+        put(grad + 2 * k, (doc - d * std::conj(o)) / factor);
+        if(noise) {
+            const double a = d2Ok2[k] / W, o2 = Ok2[k] / W;
+            const cd b = dO[k] / W, c = dOk2[k] / W, e = d2O[k] / W;
+            const double var = a - std::norm(doc) +
+                2.0 * (b * std::conj(d) * std::conj(o) + 2.0 * std::conj(doc) * d * std::conj(o) - e * std::conj(o) -
+                       c * std::conj(d)).real() +
+                d2 * std::norm(o) + std::norm(d) * o2 - 4.0 * std::norm(d) * std::norm(o);
+            noise[k] = std::sqrt(var / (double)rows) / factor;
+        }
+    }
 }
 
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

@@ -146,13 +146,47 @@ void or_deep_exact(const or_deep* p, const or_op* op, double* E, double* norm,
 // Pauli-string basis (basis = 1; move_kind, bonds and n_up unused): initial string at counter
 // (t, chain, 1): a = r0 | r1 << 32, b = r2 | r3 << 32 masked to N/3 sites; proposal t at
 // (t, chain, 0): site mulhi(r0, N/3) set to type r1 >> 30 (the reference draws x % sites and
-// x >> 30 from one word, Update_Policy.hpp:41-57), u from (r2, r3).
+// x >> 30 from one word, Update_Policy.hpp:41-57), u from (r2, r3); a sweep is N proposals.
 void or_deep_mc_philox(const or_deep* p, const or_op* op, unsigned n_chains, uint64_t seed,
                        unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
                        int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
                        uint64_t* conf, uint64_t* counter,
                        uint64_t* sconf, double* slp, double* seloc,
                        uint64_t* n_accept, uint64_t* n_reject, double* min_tie);
+
+// PsiClassical (vCN, include/quantum_state/PsiClassical.hpp:48-163): features h_k(s) =
+// fast_local_energy of operator k = sum of its strings' c <s|P|s'> (Operator.hpp:122-133);
+// log psi = lp + sum_k params_k h_k(s) (+ log psi_ref(s) for order 2), O_k = (h_k(s), O_ref).
+// params = [params_k | ref params] (PsiClassical.cu:37-60). ref NULL: fully polarized (log psi_ref = 0).
+struct or_classical {
+    unsigned num_sites;
+    unsigned n_features;
+    const unsigned* feat_begin;    // n_features + 1 offsets into the strings
+    unsigned nw;                   // words per string
+    const uint64_t* a;             // strings x nw
+    const uint64_t* b;
+    const double* coeff;           // strings complex
+    const double* params;          // n_features complex
+    double lp_re, lp_im;
+    int order;                     // 1 or 2
+    const or_deep* ref;            // reference network (order 2), or NULL
+};
+unsigned or_classical_num_params(const or_classical* p);
+void or_classical_log_psi(const or_classical* p, const uint64_t* conf, double* out);
+void or_classical_O_k(const or_classical* p, const uint64_t* conf, double* out);
+void or_classical_local_energy(const or_classical* p, const or_op* op, const uint64_t* conf, double* out);
+void or_classical_exact(const or_classical* p, const or_op* op, double* E, double* norm,
+                        double* tE, double* tE2, double* tO, double* tF, double* tS);
+
+// KullbackLeibler (source/network_functions/KullbackLeibler.cu.template:17-329) of psi
+// (classical) against psi_prime over psi_prime's ensemble: rows (conf, w') given, or all 2^N
+// configurations with w' = |psi'(s)|^2 when confs is NULL. w = |psi/psi'|^2 w',
+// d = log psi' - log psi - last_mean (deviations with |d|^2 <= threshold^2 skipped in the
+// deviation sums). Outputs value, gradient (psi_prime's parameters), noise (if non-NULL),
+// total weight and the new mean deviation.
+void or_kl(const or_classical* psi, const or_deep* psi_prime, const uint64_t* confs, const double* wprime,
+           unsigned n, double threshold, const double* last_mean, double log_psi_scale, double nu,
+           double* value, double* grad, double* noise, double* total_weight, double* mean_deviation);
 
 // Pauli application, single string (for KATs).
 void or_pauli_apply(const uint64_t* a, const uint64_t* b, unsigned nw, const uint64_t* conf,

@@ -238,3 +238,115 @@ def test_deep_builder_and_json_roundtrip():
     cp = +psi2
     np.testing.assert_array_equal(cp.params, psi2.params)
     assert abs(ann.log_psi_s(cp, ann.Spins(77, 16)) - ann.log_psi_s(psi2, ann.Spins(77, 16))) < 1e-6
+
+
+# ---- the Pauli-string basis (ExactSummationPaulis / MonteCarloPaulis) ----
+PAULI_FIX = ["deep_pauli_s3_9_6.npz", "deep_pauli_s4_12_6_3.npz"]
+
+
+def pauli_h(S):
+    H = ann.transverse_field_ising_1d(S, 0.7) + 0.3 * ann.sigma_y(0) * ann.sigma_x(1)
+    return H + 0.2 * ann.sigma_z(S - 1) * ann.sigma_y(1) + 0.15 * ann.sigma_y(2) + 0.1
+
+
+@pytest.mark.parametrize("name", PAULI_FIX)
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 5e-5)])
+def test_deep_pauli_matches_reference_fixture(name, precision, tol):
+    g = dict(np.load(os.path.join(GOLD, name)))
+    S, N = int(g["num_sites"]), int(g["N"])
+    sizes = [int(x) for x in g["sizes"]]
+    C = [int(x) for x in g["connectivity"]]
+    blocks, off = [], 0
+    for m, c in zip(sizes, C):
+        blocks.append(g["conn"][off:off + m * c].reshape(c, m))
+        off += m * c
+    a, b, W = split_params(N, sizes, C, g["params"])
+    psi = ann.PsiDeep(S, a, b, blocks, W, g["fw"], g["lp"][0], True, a_in_log_psi=False, precision=precision)
+    strings = [ann.PauliString(int(x), int(y)) for x, y in zip(g["conf_a"], g["conf_b"])]
+    np.testing.assert_allclose(ann.log_psi_batch(psi, strings), g["log_psi"], rtol=tol, atol=tol)
+    for k, p in enumerate(strings):
+        np.testing.assert_allclose(ann.log_psi_s(psi, p), g["log_psi"][k], rtol=tol, atol=tol)
+        np.testing.assert_allclose(ann.psi_O_k(psi, p), g["O_k"][k], rtol=10 * tol,
+                                   atol=10 * tol * np.abs(g["O_k"][k]).max())
+    H = ann.PauliExpression({(int(x), int(y)): c for x, y, c in zip(g["op_a"], g["op_b"], g["op_c"])})
+    op = ann.Operator(H)
+    es = ann.ExactSummationPaulis(S)
+    assert es.num_steps == 4 ** S
+    np.testing.assert_allclose(ann.ExpectationValue()(op, psi, es), g["ex_E"][0], rtol=20 * tol)
+    np.testing.assert_allclose(psi.norm(es), g["ex_norm"][0], rtol=20 * tol)
+    np.testing.assert_allclose(ann.psi_vector(psi, es), g["ex_vec"], rtol=20 * tol, atol=20 * tol)
+    if precision == "fp64":
+        td = ann.TDVP(psi.num_params)
+        td.eval(op, psi, es)
+        np.testing.assert_allclose(td.E_local, g["ex_tE"][0], rtol=1e-10)
+        np.testing.assert_allclose(td.O_k_vector, g["ex_tO"], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(td.F_vector, g["ex_tF"], rtol=1e-9, atol=1e-10 * np.abs(g["ex_tF"]).max())
+        np.testing.assert_allclose(td.S_matrix, g["ex_tS"], rtol=1e-9, atol=1e-10 * np.abs(g["ex_tS"]).max())
+
+
+def test_deep_pauli_one_layer_and_parameter_updates(oracle):
+    """A one-layer PsiDeep (RBM-family kernels over spins) meets Pauli strings: the
+    any-depth kernels take it over, with a.s in log psi, and follow parameter updates."""
+    S = 4
+    N = 3 * S
+    c = Case(N, [24], [6], seed=31, a_in=True, scale=0.12)
+    H = pauli_h(S)
+    op = ann.Operator(H)
+    ref = DeepDesc(N, c.conns, c.params, c.fw, log_prefactor=0.05 - 0.1j, a_in_log_psi=True, paulis=True)
+    r = oracle.deep_exact(ref, H, want_S=True)
+    es = ann.ExactSummationPaulis(S)
+    np.testing.assert_allclose(ann.ExpectationValue()(op, c.gpu, es), r["E"][0], rtol=1e-10)
+    td = ann.TDVP(c.gpu.num_params)
+    td.eval(op, c.gpu, es)
+    np.testing.assert_allclose(td.S_matrix, r["tS"], rtol=1e-9, atol=1e-11 * np.abs(r["tS"]).max())
+    p2 = c.params * (1 + 0.1j)
+    c.gpu.params = p2
+    ref2 = DeepDesc(N, c.conns, p2, c.fw, log_prefactor=0.05 - 0.1j, a_in_log_psi=True, paulis=True)
+    for x, y in [(0, 0), (5, 3), (15, 9)]:
+        np.testing.assert_allclose(ann.log_psi_s(c.gpu, ann.PauliString(x, y)), oracle.deep_log_psi(ref2, (x, y)),
+                                   rtol=1e-11, atol=1e-11)
+    el = ann.local_energies(c.gpu, op, [ann.PauliString(5, 3), ann.PauliString(1, 14)])
+    np.testing.assert_allclose(el, [oracle.deep_local_energy(ref2, H, (5, 3)), oracle.deep_local_energy(ref2, H, (1, 14))],
+                               rtol=1e-9, atol=1e-11)
+
+
+def test_deep_pauli_mc_philox_stream_matches_oracle(oracle):
+    S = 5
+    N = 3 * S
+    c = Case(N, [15, 10], [3, 3], seed=17, a_in=True, scale=0.2)
+    H = pauli_h(S)
+    ref = DeepDesc(N, c.conns, c.params, c.fw, log_prefactor=0.05 - 0.1j, a_in_log_psi=True, paulis=True)
+    n_chains, spc, sw, th, seed = 64, 4, 1, 2, 0x5EED0123
+    mc = ann.MonteCarloPaulis(spc * n_chains, sw, th, n_chains, True, seed=seed, persistent=True)
+    ann.ExpectationValue()(ann.Operator(H), c.gpu, mc)
+    conf, lp, el = mc.samples()
+    r = oracle.deep_mc_philox(ref, H, n_chains, seed, spc, sw, th)
+    assert r["tie"][0] > 1e-11
+    np.testing.assert_array_equal(conf.reshape(-1), r["sconf"])
+    np.testing.assert_allclose(lp, r["slp"], rtol=1e-10)
+    np.testing.assert_allclose(el, r["seloc"], rtol=1e-9, atol=1e-11)
+    ch_conf, ch_ctr = mc.get_chains()
+    np.testing.assert_array_equal(ch_conf.reshape(-1), r["conf"])
+    np.testing.assert_array_equal(ch_ctr, r["counter"])
+    ann.ExpectationValue()(ann.Operator(H), c.gpu, mc)
+    conf2, _, _ = mc.samples()
+    r2 = oracle.deep_mc_philox(ref, H, n_chains, seed, spc, sw, th, init=False, conf=r["conf"], counter=r["counter"])
+    np.testing.assert_array_equal(conf2.reshape(-1), r2["sconf"])
+
+
+def test_deep_pauli_fp32_monte_carlo_energy(oracle):
+    """FP32 chains over Pauli strings: the energy agrees with exact summation within
+    3 standard errors."""
+    S = 5
+    N = 3 * S
+    c = Case(N, [15, 10], [3, 3], seed=2, precision="fp32", scale=0.25)
+    H = pauli_h(S)
+    op = ann.Operator(H)
+    es = ann.ExactSummationPaulis(S)
+    e_exact = ann.ExpectationValue()(op, c.gpu, es) / c.gpu.norm(es) ** 2
+    mc = ann.MonteCarloPaulis(256 * 40, 2, 10, 256, True, seed=3)
+    e = ann.ExpectationValue()(op, c.gpu, mc)
+    _, _, el = mc.samples()
+    se = el.real.reshape(40, 256).mean(axis=0).std(ddof=1) / np.sqrt(256)
+    assert abs(e.real - e_exact.real) < 3 * se + 1e-6, (e, e_exact, se)
+    assert 0.0 < mc.acceptance_rate <= 1.0
