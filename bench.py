@@ -65,6 +65,13 @@ LEARNED_SWEEPS = 1       # local sweeps between samples with the learned proposa
 LEARNED_INDEP = 2        # learned independence moves per sample
 MIN_ACCEPT = 0.1         # the proposal is dropped below this acceptance
 TUNING_FILE = None       # --tuning: load the tuning table instead of autotuning
+# DRAM bytes (read + written) of this workload from a one-pass ncu capture of two precision-form
+# SR steps (dram__bytes_read.sum + dram__bytes_write.sum per kernel, profile window, Np = 8384,
+# 16384 samples): the FP32 factorisation's kernels (trailing updates, panels, inverses, shift
+# conversion) 20.9 GB per factorisation; herk_tc_kernel 7.0 GB per launch
+WORKLOAD_NP_NS = (N_SITES + M_HIDDEN + N_SITES * M_HIDDEN, N_CHAINS)
+FACTOR_DRAM_BYTES = 20.9e9
+HERK_DRAM_BYTES = 7.0e9
 
 
 def init_params(rng):
@@ -554,27 +561,37 @@ def run_ours(args):
         "energy_per_site": energy["energy_per_site"], "energy_check": energy,
         "phase_ms": summary["phase_ms"], "phase_note": "CUDA-event phases of eager steps (the headline times graph replays)",
         "solver": info,
-        "roofline": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
-                     "achieved": s_tflops, "peak": pk.get("bf16_tflops", 1900.0) if f.name == "precision" else None,
-                     "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst", "traffic": None,
-                     "work": "4*Np*(Np+1)*Ns real flops per step"},
+        "roofline_herk": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
+                          "achieved": s_tflops, "peak": pk.get("bf16_tflops", 1900.0) if f.name == "precision" else None,
+                          "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst",
+                          "traffic": HERK_DRAM_BYTES if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision"
+                          else None,
+                          "work": "4*Np*(Np+1)*Ns real flops per step (over the S phase: operand prep + kernel)"},
         "clocks": clk,
         "e2e": {"value": Ns / tau / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": Np * 16,
                 "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e},
         "gpu_launches": int(launches),
     }
-    if out["roofline"]["peak"]:
-        out["roofline"]["frac"] = s_tflops / out["roofline"]["peak"]
+    if out["roofline_herk"]["peak"]:
+        out["roofline_herk"]["frac"] = s_tflops / out["roofline_herk"]["peak"]
     if getattr(f, "t_factor_ms", None):
         # FP32 Cholesky: (4/3) Np^3 real flops of complex factorisation; its trailing
         # updates run as three TF32 products on tcgen05 (TF32 rate = half the BF16 rate)
         chol_tflops = (4.0 / 3.0) * Np ** 3 / (f.t_factor_ms * 1e-3) / 1e12
         tf32x3_peak = pk.get("bf16_tflops", 1900.0) / 2 / 3
-        out["roofline_cholesky"] = {"bound": "tensor", "kernel": "FP32 Cholesky (chol_update_tc + panel path)",
-                                    "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
-                                    "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
-                                    "peak_kind": pk_kind + " bf16 burst / 2 (TF32) / 3 (split products)",
-                                    "work": "(4/3)*Np^3 real flops per factorisation"}
+        # the dominant kernel group of the step: trailing updates + panel path are about half
+        # of the launch list (the S kernel 14 %)
+        out["roofline"] = {"bound": "tensor",
+                           "kernel": "FP32 Cholesky factorisation (chol_update_tc3/tc2 tcgen05 split-TF32 trailing "
+                                     "updates + potrf32/trsm32 panel path)",
+                           "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
+                           "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
+                           "traffic": FACTOR_DRAM_BYTES if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision"
+                           else None,
+                           "peak_kind": pk_kind + " bf16 burst / 2 (TF32) / 3 (split products)",
+                           "work": "(4/3)*Np^3 real flops per factorisation (CUDA events around it)"}
+    else:
+        out["roofline"] = out["roofline_herk"]
     out.update(fp64)
     if ablation:
         out["tau_ablation"] = ablation
