@@ -55,6 +55,12 @@ class OrDeep(ct.Structure):
                 ("a_in_log_psi", ct.c_int), ("activation", ct.c_int), ("basis", ct.c_int)]
 
 
+class OrClassical(ct.Structure):
+    _fields_ = [("num_sites", ct.c_uint), ("n_features", ct.c_uint), ("feat_begin", P), ("nw", ct.c_uint),
+                ("a", P), ("b", P), ("coeff", P), ("params", P), ("lp_re", ct.c_double), ("lp_im", ct.c_double),
+                ("order", ct.c_int), ("ref", P)]
+
+
 def nwords(N):
     return (N + 63) // 64
 
@@ -170,6 +176,37 @@ class DeepDesc:
         return conf_words(conf, self.N)
 
 
+class ClassicalDesc:
+    """PsiClassical for the oracle: ``features`` is a list of Pauli expressions (one operator
+    per feature), ``params`` one complex per feature, ``ref`` a DeepDesc (order 2) or None."""
+
+    def __init__(self, num_sites, features, params, log_prefactor=0j, order=1, ref=None):
+        self.N = int(num_sites)
+        nw = max(1, nwords(self.N))
+        a, b, c, beg = [], [], [], [0]
+        for f in features:
+            fa, fb, fc = f.arrays(nw)
+            a.append(np.asarray(fa, np.uint64).reshape(-1, nw))
+            b.append(np.asarray(fb, np.uint64).reshape(-1, nw))
+            c.append(np.asarray(fc, np.complex128))
+            beg.append(beg[-1] + len(fc))
+        self.a = np.ascontiguousarray(np.concatenate(a))
+        self.b = np.ascontiguousarray(np.concatenate(b))
+        self.c = np.ascontiguousarray(np.concatenate(c))
+        self.beg = np.ascontiguousarray(beg, np.uint32)
+        self.params = np.ascontiguousarray(np.asarray(params, np.complex128))
+        self.ref = ref
+        self.order = int(order)
+        self.lp = complex(log_prefactor)
+        self.struct = OrClassical(self.N, len(features), _ptr(self.beg), nw, _ptr(self.a), _ptr(self.b),
+                                  _ptr(self.c), _ptr(self.params), self.lp.real, self.lp.imag, self.order,
+                                  ct.cast(ct.pointer(ref.struct), P) if ref is not None else None)
+
+    @property
+    def num_params(self):
+        return self.params.size + (self.ref.num_params if self.order > 1 and self.ref is not None else 0)
+
+
 class Oracle:
     def __init__(self):
         self.lib = ct.CDLL(build_oracle())
@@ -184,6 +221,7 @@ class Oracle:
         L.or_activation.argtypes = [ct.c_double, ct.c_double, ct.c_uint, ct.c_int, P, P]
         L.or_deep_num_params.restype = ct.c_uint
         L.or_deep_mc_philox.argtypes = L.or_rbm_mc_philox.argtypes
+        L.or_classical_num_params.restype = ct.c_uint
 
     # ---- RBM family ----
     def log_psi(self, psi: RbmDesc, conf):
@@ -371,6 +409,51 @@ class Oracle:
         return self.mc_philox(psi, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind,
                               bonds, init, n_up, conf, counter, _fn=self.lib.or_deep_mc_philox)
 
+    # ---- PsiClassical and KullbackLeibler ----
+    def classical_log_psi(self, psi: ClassicalDesc, conf):
+        out = np.zeros(1, np.complex128)
+        self.lib.or_classical_log_psi(ct.byref(psi.struct), _ptr(conf_words(conf, psi.N)), _ptr(out))
+        return out[0]
+
+    def classical_O_k(self, psi: ClassicalDesc, conf):
+        out = np.zeros(psi.num_params, np.complex128)
+        self.lib.or_classical_O_k(ct.byref(psi.struct), _ptr(conf_words(conf, psi.N)), _ptr(out))
+        return out
+
+    def classical_local_energy(self, psi: ClassicalDesc, expr, conf):
+        op = OpArrays(expr, psi.N)
+        out = np.zeros(1, np.complex128)
+        self.lib.or_classical_local_energy(ct.byref(psi.struct), ct.byref(op.struct), _ptr(conf_words(conf, psi.N)),
+                                           _ptr(out))
+        return out[0]
+
+    def classical_exact(self, psi: ClassicalDesc, expr, want_S=False):
+        np_ = psi.num_params
+        r = dict(E=np.zeros(1, np.complex128), norm=np.zeros(1), tE=np.zeros(1, np.complex128), tE2=np.zeros(1),
+                 tO=np.zeros(np_, np.complex128), tF=np.zeros(np_, np.complex128),
+                 tS=np.zeros((np_, np_), np.complex128) if want_S else None)
+        op = OpArrays(expr, psi.N)
+        self.lib.or_classical_exact(ct.byref(psi.struct), ct.byref(op.struct),
+                                    *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
+        return r
+
+    def kl(self, psi: ClassicalDesc, psi_prime: DeepDesc, confs=None, wprime=None, threshold=0.0, last_mean=0j,
+           log_psi_scale=1.0, nu=1.0, gradient=True, noise=False):
+        """KullbackLeibler of psi against psi_prime over rows (confs (n, 2) uint64, weights w')
+        of psi_prime's ensemble, or exact summation when confs is None."""
+        np_ = psi_prime.num_params
+        c = None if confs is None else np.ascontiguousarray(np.asarray(confs, np.uint64).reshape(-1, 2))
+        w = None if wprime is None else np.ascontiguousarray(np.asarray(wprime, np.float64))
+        lm = np.array([complex(last_mean).real, complex(last_mean).imag])
+        r = dict(value=np.zeros(1), grad=np.zeros(np_, np.complex128) if gradient else None,
+                 noise=np.zeros(np_) if noise else None, total_weight=np.zeros(1),
+                 mean_deviation=np.zeros(1, np.complex128))
+        self.lib.or_kl(ct.byref(psi.struct), ct.byref(psi_prime.struct), _ptr(c), _ptr(w),
+                       ct.c_uint(0 if c is None else len(c)), ct.c_double(threshold), _ptr(lm),
+                       ct.c_double(log_psi_scale), ct.c_double(nu), _ptr(r["value"]), _ptr(r["grad"]),
+                       _ptr(r["noise"]), _ptr(r["total_weight"]), _ptr(r["mean_deviation"]))
+        return r
+
     def pauli_apply(self, a, b, conf, N):
         nw = max(1, nwords(N))
         aw, bw, cw = conf_words(a, N), conf_words(b, N), conf_words(conf, N)
@@ -409,4 +492,6 @@ class RefHarness:
         self.lib.ref_deepml_O_k.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, P]
         self.lib.ref_deepml_pauli_log_psi_s.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, ct.c_uint64, P]
         self.lib.ref_deepml_pauli_O_k.argtypes = [U, U, P, P, P, P, P, P, ct.c_uint64, ct.c_uint64, P]
+        self.lib.ref_classical_log_psi_s.argtypes = [P, ct.c_uint64, P]
+        self.lib.ref_classical_O_k.argtypes = [P, ct.c_uint64, P]
         self.lib.ref_pauli_apply.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64, U, P, P]

@@ -14,6 +14,10 @@
 //   * PsiCNN kernel                                 include/quantum_state/PsiCNN.hpp:97-266
 //   * MonteCarlo_t::kernel_foreach / mc_update       include/ensembles/MonteCarlo.hpp:55-177
 //   * ExactSummation_t::kernel_foreach               include/ensembles/ExactSummation.hpp:33-72
+//   * PsiClassical kernel (order 1 with the fully polarized reference, order 2 with a
+//     PsiDeep reference)                            include/quantum_state/PsiClassical.hpp:48-163
+//   * KullbackLeibler value / gradient / gradient_with_noise
+//                                                   source/network_functions/KullbackLeibler.cu.template
 //   * ExpectationValue / TDVP / PsiVector / PsiOkVector / PsiNorm bodies
 //     (source/network_functions/*.cu.template, with the "//! begin template"
 //     instantiation blocks stripped at build time by oracle/Makefile).
@@ -30,6 +34,7 @@
 #include "network_functions/PsiVector.hpp"
 #include "network_functions/PsiNorm.hpp"
 #include "network_functions/PsiOkVector.hpp"
+#include "network_functions/KullbackLeibler.hpp"
 
 #include <vector>
 #include <cstdint>
@@ -189,6 +194,7 @@ struct LoggingPolicy : public LoggingPolicyKernel {
 #include "PsiNorm.cu"
 #include "PsiOkVector.cu"
 #include "ensembles/MonteCarlo.cu"
+#include "KullbackLeibler.cu"
 
 using namespace ann_on_gpu;
 
@@ -285,6 +291,80 @@ PsiDeep make_deep_ml(const DeepMLDesc& d) {
     for(auto k = 0u; k < psi.num_params; k++) p[k] = complex_t(d.params[2 * k], d.params[2 * k + 1]);
     psi.set_params(p);
     return psi;
+}
+
+// PsiClassical: the host constructor is __PYTHONCC__-only (PsiClassical.hpp:199-222); this
+// shim fills the kernel fields as PsiClassical_t::init_kernel does (PsiClassical.cu:13-33),
+// with one operator per feature built from HarnessExpr.
+using OpKernel = kernel::StandartOperator<PauliString>;
+
+template<unsigned order, typename RefKernel>
+struct HarnessClassical : public kernel::PsiClassical_t<complex_t, OpKernel, order, false, RefKernel> {
+    using Kernel = kernel::PsiClassical_t<complex_t, OpKernel, order, false, RefKernel>;
+    std::vector<Operator> ops;
+    Array<OpKernel> ops_kernel;
+    Array<complex_t> prm;
+    bool gpu;
+
+    HarnessClassical(unsigned num_sites, const std::vector<HarnessExpr>& feats, const double* params,
+                     const double* lp, const RefKernel& ref, unsigned ref_params)
+        : ops_kernel(feats.size(), false), prm(feats.size(), false), gpu(false) {
+        ops.reserve(feats.size());
+        for(const auto& f : feats) ops.emplace_back(f, false);
+        for(auto k = 0u; k < feats.size(); k++) {
+            ops_kernel[k] = ops[k].kernel();
+            prm[k] = complex_t(params[2 * k], params[2 * k + 1]);
+        }
+        this->params = prm.data();
+        this->num_ops_H = feats.size();
+        this->H_local = ops_kernel.data();
+        this->num_sites = num_sites;
+        this->log_prefactor = complex_t(lp[0], lp[1]);
+        this->psi_ref = ref;
+        this->num_params = feats.size() + (order > 1u ? ref_params : 0u);
+    }
+    HarnessClassical(const HarnessClassical& o)
+        : Kernel(o), ops(), ops_kernel(o.ops_kernel.size(), false), prm(o.prm), gpu(false) {
+        ops.reserve(o.ops.size());
+        for(const auto& op : o.ops) ops.push_back(op);
+        for(auto k = 0u; k < ops.size(); k++) ops_kernel[k] = ops[k].kernel();
+        this->params = prm.data();
+        this->H_local = ops_kernel.data();
+    }
+    Kernel& kernel() { return *this; }
+    const Kernel& kernel() const { return *this; }
+};
+
+// a classical network: features (strings grouped per feature), parameters, order and an
+// optional PsiDeep reference (order 2)
+struct ClassicalDesc {
+    unsigned num_sites, n_features;
+    const unsigned* feat_begin;    // n_features + 1
+    const uint64_t* a;             // strings (one word each)
+    const uint64_t* b;
+    const double* coeff;
+    const double* params;          // n_features complex
+    const double* log_pref;
+    unsigned order;
+    const DeepMLDesc* ref;         // order 2 (may be null: fully polarized)
+};
+
+std::vector<HarnessExpr> features_of(const ClassicalDesc& d) {
+    std::vector<HarnessExpr> f;
+    for(auto k = 0u; k < d.n_features; k++) {
+        const unsigned b0 = d.feat_begin[k], b1 = d.feat_begin[k + 1];
+        f.push_back(HarnessExpr{d.a + b0, d.b + b0, d.coeff + 2 * b0, b1 - b0});
+    }
+    return f;
+}
+
+kernel::PsiFullyPolarized_t<complex_t> fully_polarized(unsigned num_sites) {
+    kernel::PsiFullyPolarized_t<complex_t> r;
+    r.num_sites = num_sites;
+    r.num_params = 0u;
+    r.log_prefactor = complex_t(0.0, 0.0);
+    r.gpu = false;
+    return r;
 }
 
 void put(double* out, const complex_t& z) { out[0] = z.real(); out[1] = z.imag(); }
@@ -449,6 +529,86 @@ void ref_deepml_pauli_exact(unsigned N, unsigned L, const unsigned* sizes, const
     auto psi = make_deep_ml({N, L, sizes, connectivity, conn, params, fw, lp, N / 3u});
     exact_all<PsiDeep, ExactSummationPaulis>(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS,
                                              vec, norm, mlp, O_sum);
+}
+
+// ---- PsiClassical and KullbackLeibler ----
+// (descriptors arrive as void pointers: their types have internal linkage)
+void ref_classical_log_psi_s(const void* dv, uint64_t conf, double* out) {
+    const ClassicalDesc* d = static_cast<const ClassicalDesc*>(dv);
+    if(d->ref) {
+        auto ref = make_deep_ml(*d->ref);
+        HarnessClassical<2u, PsiDeep::Kernel> psi(d->num_sites, features_of(*d), d->params, d->log_pref, ref.kernel(),
+                                                  ref.num_params);
+        psi_log_psi_s(psi, conf, out);
+    } else {
+        HarnessClassical<1u, kernel::PsiFullyPolarized_t<complex_t>> psi(
+            d->num_sites, features_of(*d), d->params, d->log_pref, fully_polarized(d->num_sites), 0u);
+        psi_log_psi_s(psi, conf, out);
+    }
+}
+void ref_classical_O_k(const void* dv, uint64_t conf, double* out) {
+    const ClassicalDesc* d = static_cast<const ClassicalDesc*>(dv);
+    if(d->ref) {
+        auto ref = make_deep_ml(*d->ref);
+        HarnessClassical<2u, PsiDeep::Kernel> psi(d->num_sites, features_of(*d), d->params, d->log_pref, ref.kernel(),
+                                                  ref.num_params);
+        psi_O_k(psi, conf, out);
+    } else {
+        HarnessClassical<1u, kernel::PsiFullyPolarized_t<complex_t>> psi(
+            d->num_sites, features_of(*d), d->params, d->log_pref, fully_polarized(d->num_sites), 0u);
+        psi_O_k(psi, conf, out);
+    }
+}
+void ref_classical_exact(const void* dv, const uint64_t* a, const uint64_t* b, const double* coeff,
+                         unsigned n_strings, double* E, double* fluct, double* grad, double* tE, double* tE2,
+                         double* tO, double* tF, double* tS, double* vec, double* norm, double* mlp, double* O_sum) {
+    const ClassicalDesc* d = static_cast<const ClassicalDesc*>(dv);
+    if(d->ref) {
+        auto ref = make_deep_ml(*d->ref);
+        HarnessClassical<2u, PsiDeep::Kernel> psi(d->num_sites, features_of(*d), d->params, d->log_pref, ref.kernel(),
+                                                  ref.num_params);
+        exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
+    } else {
+        HarnessClassical<1u, kernel::PsiFullyPolarized_t<complex_t>> psi(
+            d->num_sites, features_of(*d), d->params, d->log_pref, fully_polarized(d->num_sites), 0u);
+        exact_all(psi, {a, b, coeff, n_strings}, E, fluct, grad, tE, tE2, tO, tF, tS, vec, norm, mlp, O_sum);
+    }
+}
+// KL of the classical network against psi_prime over ExactSummationSpins: two consecutive
+// value calls (the second subtracts the first's mean deviation), then gradient and
+// gradient_with_noise; out4 = total weight, mean deviation (re, im), second value
+void ref_kl_exact(const void* dv, const void* primev, double threshold, double nu, double* value,
+                  double* grad, double* grad2, double* noise, double* out4) {
+    const ClassicalDesc* d = static_cast<const ClassicalDesc*>(dv);
+    auto pp = make_deep_ml(*static_cast<const DeepMLDesc*>(primev));
+    ExactSummationSpins es(d->num_sites, false);
+    KullbackLeibler kl(pp.num_params, false);
+    auto run = [&](auto& psi) {
+        value[0] = kl.value(psi, pp, es, threshold);
+        out4[0] = kl.total_weight.front();
+        out4[1] = kl.mean_deviation.front().real();
+        out4[2] = kl.mean_deviation.front().imag();
+        out4[3] = kl.value(psi, pp, es, threshold);
+        std::vector<std::complex<double>> g(pp.num_params);
+        value[1] = kl.gradient(g.data(), psi, pp, es, nu, threshold);
+        for(auto k = 0u; k < pp.num_params; k++) put(grad + 2 * k, g[k]);
+        auto r = kl.gradient_with_noise(psi, pp, es, nu, threshold);
+        for(auto k = 0u; k < pp.num_params; k++) {
+            put(grad2 + 2 * k, std::get<0>(r)[k]);
+            noise[k] = std::get<1>(r)[k];
+        }
+        value[2] = std::get<2>(r);
+    };
+    if(d->ref) {
+        auto ref = make_deep_ml(*d->ref);
+        HarnessClassical<2u, PsiDeep::Kernel> psi(d->num_sites, features_of(*d), d->params, d->log_pref, ref.kernel(),
+                                                  ref.num_params);
+        run(psi);
+    } else {
+        HarnessClassical<1u, kernel::PsiFullyPolarized_t<complex_t>> psi(
+            d->num_sites, features_of(*d), d->params, d->log_pref, fully_polarized(d->num_sites), 0u);
+        run(psi);
+    }
 }
 
 // ---- PsiRBM (no biases) ----

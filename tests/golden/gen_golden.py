@@ -6,7 +6,7 @@ stores inputs and outputs as .npz files. The fixtures pin the FP64 oracle
 (oracle/oracle.cpp) and, through it, the CUDA path. The reference checkout is
 needed only to regenerate them:
 
-    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml | deep_pauli]
+    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml | deep_pauli | classical]
 """
 
 import ctypes as ct
@@ -258,6 +258,98 @@ def gen_deep_pauli(ref, rng, name, num_sites, M, C):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
+class _DeepML(ct.Structure):
+    _fields_ = [("N", ct.c_uint), ("L", ct.c_uint), ("sizes", ct.c_void_p), ("connectivity", ct.c_void_p),
+                ("conn", ct.c_void_p), ("params", ct.c_void_p), ("final_w", ct.c_void_p), ("log_pref", ct.c_void_p),
+                ("num_sites", ct.c_uint)]
+
+
+class _Classical(ct.Structure):
+    _fields_ = [("num_sites", ct.c_uint), ("n_features", ct.c_uint), ("feat_begin", ct.c_void_p),
+                ("a", ct.c_void_p), ("b", ct.c_void_p), ("coeff", ct.c_void_p), ("params", ct.c_void_p),
+                ("log_pref", ct.c_void_p), ("order", ct.c_uint), ("ref", ct.c_void_p)]
+
+
+def _deep_arrays(rng, N, M, C, scale):
+    blocks = builder_connections(N, M, C)
+    np_ = N + sum(m * (1 + c) for m, c in zip(M, C))
+    d = dict(sizes=np.array(M, np.uint32), connectivity=np.array(C, np.uint32),
+             conn=np.ascontiguousarray(np.concatenate([b.reshape(-1) for b in blocks])),
+             params=cplx(rng, np_, scale), fw=(1.0 + cplx(rng, M[-1], 0.1)).astype(np.complex128),
+             lp=np.array([0.02 + 0.1j]))
+    st = _DeepML(N, len(M), P(d["sizes"]), P(d["connectivity"]), P(d["conn"]), P(d["params"]), P(d["fw"]),
+                 P(d["lp"]), 0)
+    return d, st
+
+
+def gen_classical_kl(ref, rng, name, S, features, order, ref_shape, threshold):
+    """PsiClassical (features = one Pauli expression each; order 2 with a PsiDeep reference)
+    and KullbackLeibler against a PsiDeep psi_prime, through the reference's own kernels."""
+    beg, fa, fb, fc = [0], [], [], []
+    for f in features:
+        a, b, c, n = op_arrays(f)
+        fa.append(a)
+        fb.append(b)
+        fc.append(c)
+        beg.append(beg[-1] + n)
+    beg = np.array(beg, np.uint32)
+    fa, fb, fc = (np.ascontiguousarray(np.concatenate(x)) for x in (fa, fb, fc))
+    K = len(features)
+    theta = cplx(rng, K, 0.2)
+    lp = np.array([0.1 - 0.2j])
+    out = {"num_sites": S, "order": order, "feat_begin": beg, "feat_a": fa, "feat_b": fb, "feat_c": fc,
+           "theta": theta, "lp": lp, "threshold": np.array([threshold])}
+    refst = None
+    if ref_shape is not None:
+        rd, refst = _deep_arrays(rng, S, *ref_shape, 0.1)
+        out.update({"ref_" + k: v for k, v in rd.items()})
+    cd = _Classical(S, K, P(beg), P(fa), P(fb), P(fc), P(theta), P(lp), order,
+                    ct.cast(ct.pointer(refst), ct.c_void_p) if refst is not None else None)
+    np_ = K + (int(rd["params"].size) if refst is not None else 0)
+    lps, oks = [], []
+    for s in range(1 << S):
+        r = np.zeros(1, np.complex128)
+        ref.lib.ref_classical_log_psi_s(ct.byref(cd), ct.c_uint64(s), P(r))
+        lps.append(r[0])
+        o = np.zeros(np_, np.complex128)
+        ref.lib.ref_classical_O_k(ct.byref(cd), ct.c_uint64(s), P(o))
+        oks.append(o)
+    out["log_psi"] = np.array(lps)
+    out["O_k"] = np.array(oks)
+    H = transverse_field_ising_1d(S, h=0.8) + 0.3 * sigma_y(0) * sigma_y(1)
+    a, b, c, n = op_arrays(H)
+    out.update({"op_a": a, "op_b": b, "op_c": c})
+    ex = exact_outputs(np_, S)
+    ref.lib.ref_classical_exact(ct.byref(cd), P(a), P(b), P(c), ct.c_uint(n), *[P(ex[k]) for k in KEYS])
+    out.update({"ex_" + k: v for k, v in ex.items()})
+    pd, pst = _deep_arrays(rng, S, [2 * S], [3], 0.15)
+    out.update({"prime_" + k: v for k, v in pd.items()})
+    npp = int(pd["params"].size)
+    val = np.zeros(3)
+    g = np.zeros(npp, np.complex128)
+    g2 = np.zeros(npp, np.complex128)
+    nz = np.zeros(npp)
+    o4 = np.zeros(4)
+    ref.lib.ref_kl_exact(ct.byref(cd), ct.byref(pst), ct.c_double(threshold), ct.c_double(1.0), P(val), P(g), P(g2),
+                         P(nz), P(o4))
+    out.update({"kl_value": val, "kl_grad": g, "kl_grad_noise_call": g2, "kl_noise": nz, "kl_out4": o4})
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def gen_classical_all(ref):
+    from annongpu_gb300.expression import PauliExpression
+
+    def terms(expr):
+        a, b, c = expr.arrays(1)
+        return [PauliExpression({(int(a[k, 0]), int(b[k, 0])): c[k]}) for k in range(len(c))]
+    rng = np.random.default_rng(20261206)
+    # the reference test suite's classical-network shapes (test/conftest.py)
+    gen_classical_kl(ref, rng, "classical_s4_order2_deep", 4, terms(sigma_z(0) * sigma_y(1) + 1.1 * sigma_x(0)), 2,
+                     ([4], [4]), 0.0)
+    gen_classical_kl(ref, rng, "classical_s6_order1", 6,
+                     terms(sigma_z(0) * sigma_x(1) * sigma_z(2) + sigma_y(0) + sigma_x(0) * sigma_x(1)), 1, None, 0.05)
+
+
 def gen_kats(ref, rng):
     zs = cplx(rng, 24, 0.6)
     f = np.zeros((2, 24), np.complex128)
@@ -292,6 +384,9 @@ def main(only=None):
     if only == "deep_pauli":
         gen_deep_pauli_all(ref)
         return
+    if only == "classical":
+        gen_classical_all(ref)
+        return
     rng = np.random.default_rng(20261203)
     gen_kats(ref, rng)
     gen_rbm(ref, rng)
@@ -303,6 +398,7 @@ def main(only=None):
     gen_cnn(ref, rng)
     gen_deep_ml_all(ref)
     gen_deep_pauli_all(ref)
+    gen_classical_all(ref)
     print("fixtures written to", HERE)
 
 

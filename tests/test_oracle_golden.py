@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from pyoracle import CnnDesc, DeepDesc, RbmDesc
+from pyoracle import ClassicalDesc, CnnDesc, DeepDesc, RbmDesc
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -166,6 +166,56 @@ def test_deep_pauli_string_basis(oracle, name):
     close(r["tO"], g["ex_tO"])
     close(r["tF"], g["ex_tF"], rtol=1e-9, atol=1e-10)
     close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-10)
+
+
+def classical_from(g):
+    """(classical psi, psi_prime) of a classical-network fixture for the oracle."""
+    S = int(g["num_sites"])
+    beg = g["feat_begin"]
+    feats = [_Expr(g["feat_a"][beg[k]:beg[k + 1]], g["feat_b"][beg[k]:beg[k + 1]], g["feat_c"][beg[k]:beg[k + 1]])
+             for k in range(len(beg) - 1)]
+
+    def deep(prefix):
+        blocks, off = [], 0
+        for m, c in zip(g[prefix + "sizes"], g[prefix + "connectivity"]):
+            blocks.append(g[prefix + "conn"][off:off + int(m) * int(c)].reshape(int(c), int(m)))
+            off += int(m) * int(c)
+        return DeepDesc(S, blocks, g[prefix + "params"], g[prefix + "fw"], log_prefactor=g[prefix + "lp"][0],
+                        a_in_log_psi=False)
+    ref = deep("ref_") if "ref_params" in g else None
+    psi = ClassicalDesc(S, feats, g["theta"], log_prefactor=g["lp"][0], order=int(g["order"]), ref=ref)
+    return psi, deep("prime_"), ref
+
+
+@pytest.mark.parametrize("name", ["classical_s4_order2_deep.npz", "classical_s6_order1.npz"])
+def test_classical_network_and_kullback_leibler(oracle, name):
+    """PsiClassical (order 1, and order 2 over a PsiDeep reference) and KullbackLeibler value,
+    gradient and gradient_with_noise (with the carried mean deviation) against the reference."""
+    g = load(name)
+    psi, prime, ref = classical_from(g)
+    S = int(g["num_sites"])
+    for s in range(1 << S):
+        close(oracle.classical_log_psi(psi, s), g["log_psi"][s])
+        close(oracle.classical_O_k(psi, s), g["O_k"][s])
+    r = oracle.classical_exact(psi, _Expr(g["op_a"], g["op_b"], g["op_c"]), want_S=True)
+    for k in ("E", "norm", "tE", "tO"):
+        close(r[k], g["ex_" + k])
+    close(r["tF"], g["ex_tF"], rtol=1e-9, atol=1e-11)
+    close(r["tS"], g["ex_tS"], rtol=1e-9, atol=1e-11)
+    th = float(g["threshold"][0])
+    r1 = oracle.kl(psi, prime, threshold=th, gradient=False)
+    close(r1["value"][0], g["kl_value"][0])
+    close(r1["total_weight"][0], g["kl_out4"][0])
+    close(r1["mean_deviation"][0], g["kl_out4"][1] + 1j * g["kl_out4"][2])
+    r2 = oracle.kl(psi, prime, threshold=th, last_mean=r1["mean_deviation"][0], gradient=False)
+    close(r2["value"][0], g["kl_out4"][3])
+    r3 = oracle.kl(psi, prime, threshold=th, last_mean=r2["mean_deviation"][0], nu=1.0)
+    close(r3["value"][0], g["kl_value"][1])
+    close(r3["grad"], g["kl_grad"], rtol=1e-9, atol=1e-12)
+    r4 = oracle.kl(psi, prime, threshold=th, last_mean=r3["mean_deviation"][0], nu=1.0, noise=True)
+    close(r4["value"][0], g["kl_value"][2])
+    close(r4["grad"], g["kl_grad_noise_call"], rtol=1e-9, atol=1e-12)
+    close(r4["noise"], g["kl_noise"], rtol=1e-8, atol=1e-12)
 
 
 def test_deep_one_layer_equals_rbm_family(oracle):
