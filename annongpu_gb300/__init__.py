@@ -17,7 +17,9 @@ from .api import (MADE, Batch, ExactSummationPaulis, ExactSummationSpins, Expect
                   local_energies, log_psi_s, log_psi_vector, psi_O_k, psi_O_k_vector, psi_vector, setDevice, start_profiling,
                   stop_profiling)
 from .api import autotune, load_tuning, save_tuning, set_tuning, tuning_table  # noqa: F401
-from .builders import new_RBM, new_convolutional_network, new_deep_neural_network  # noqa: F401
+from .api import (KullbackLeibler, PsiClassical, PsiClassicalANN_1, PsiClassicalANN_2, PsiClassicalFP_1,  # noqa: F401
+                  PsiClassicalFP_2, PsiFullyPolarized)
+from .builders import new_RBM, new_classical_network, new_convolutional_network, new_deep_neural_network  # noqa: F401
 from ._lib import AnnError, launch_count  # noqa: F401
 
 __version__ = "1.0.0"

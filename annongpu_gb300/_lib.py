@@ -60,6 +60,11 @@ class DeepDesc(ct.Structure):
                 ("a_in_log_psi", I), ("activation", I), ("precision", I)]
 
 
+class ClassicalDesc(ct.Structure):
+    _fields_ = [("num_sites", U), ("n_features", U), ("feature_begin", P), ("num_words", U), ("a", P), ("b", P),
+                ("coeff", P), ("params", P), ("log_prefactor", D * 2), ("order", U), ("ref", P), ("precision", I)]
+
+
 class McDesc(ct.Structure):
     _fields_ = [("num_samples", U), ("num_sweeps", U), ("num_thermalization_sweeps", U),
                 ("num_markov_chains", U), ("move", I), ("bonds", P), ("n_bonds", U), ("n_up", I),
@@ -78,6 +83,14 @@ _SIGS = {
     "ann_psi_create_cnn": ([P, P], I),
     "ann_psi_create_deep": ([P, P], I),
     "ann_ens_set_basis": ([P, I], I),
+    "ann_psi_create_classical": ([P, P], I),
+    "ann_psi_ref_log_prefactor": ([P, P, P], I),
+    "ann_kl_create": ([U, P], I),
+    "ann_kl_destroy": ([P], I),
+    "ann_kl_log_psi_scale": ([P, P, P], I),
+    "ann_kl_value": ([P, P, P, P, D, P, P], I),
+    "ann_kl_gradient": ([P, P, P, P, D, D, P, P, P, P], I),
+    "ann_kl_stats": ([P, P, P], I),
     "ann_log_psi_paulis": ([P, P, U, P, P], I),
     "ann_psi_O_k_paulis": ([P, P, P], I),
     "ann_local_energies_paulis": ([P, P, P, U, P, P], I),

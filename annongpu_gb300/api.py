@@ -966,6 +966,176 @@ class HilbertSpaceDistance:
 
 
 # ----------------------------------------------------------------------------------
+class PsiFullyPolarized:
+    """The trivial reference of a classical network: log psi = 0, no parameters
+    (include/quantum_state/PsiFullyPolarized.hpp:16-120)."""
+
+    def __init__(self, num_sites, log_prefactor=0.0):
+        self.num_sites = int(num_sites)
+        self.log_prefactor = complex(log_prefactor)
+        self.num_params = 0
+        self.params = np.zeros(0, np.complex128)
+
+
+def _feature_strings(H_local, nw):
+    """(feature_begin, a, b, coeff) of a list of operators / Pauli expressions."""
+    beg, A, B, C = [0], [], [], []
+    for h in H_local:
+        expr = h.expr if isinstance(h, Operator) else h
+        if not isinstance(expr, PauliExpression):
+            expr = PauliExpression({(int(a), int(b)): c for (a, b), c in expr})
+        a, b, c = expr.arrays(nw)
+        A.append(np.asarray(a, np.uint64).reshape(-1, nw))
+        B.append(np.asarray(b, np.uint64).reshape(-1, nw))
+        C.append(np.asarray(c, np.complex128))
+        beg.append(beg[-1] + len(C[-1]))
+    cat = lambda xs, shape: np.ascontiguousarray(np.concatenate(xs) if xs else np.zeros(shape))
+    return (np.ascontiguousarray(beg, np.uint32), cat(A, (0, nw)).astype(np.uint64), cat(B, (0, nw)).astype(np.uint64),
+            cat(C, 0).astype(np.complex128))
+
+
+class PsiClassical(_Psi):
+    """Variational classical network (vCN; include/quantum_state/PsiClassical.hpp:48-260):
+    log psi(s) = log_prefactor + sum_k params_k h_k(s) (+ log psi_ref(s) for order 2), with
+    h_k(s) = fast_local_energy of the k-th operator of H_local (Operator.hpp:122-133).
+    ``params`` are [classical params | reference params]; psi_ref is a PsiDeep (any depth,
+    copied at construction) or PsiFullyPolarized. Runs on the PsiDeep kernels."""
+
+    def __init__(self, num_sites, H_local, params, psi_ref, log_prefactor=0.0, gpu=True, *, order=1,
+                 precision="fp64"):
+        self.num_sites = int(num_sites)
+        self.N = self.num_sites
+        self.order = int(order)
+        self.H_local = list(H_local)
+        p = c128(params).reshape(-1)
+        if p.size != len(self.H_local):
+            raise ValueError("params needs one value per operator of H_local")
+        self._ref = psi_ref
+        nw = 2 if self.num_sites > 64 else 1
+        beg, A, B, C = _feature_strings(self.H_local, nw)
+        self._keep = (beg, A, B, C, p)
+        ref = psi_ref if (self.order > 1 and isinstance(psi_ref, _Psi)) else None
+        self.precision = ref.precision if ref is not None else precision
+        lp = complex(log_prefactor)
+        d = L.ClassicalDesc(self.num_sites, len(self.H_local), ptr(beg), nw, ptr(A), ptr(B), ptr(C), ptr(p),
+                            (ct.c_double * 2)(lp.real, lp.imag), self.order,
+                            None if ref is None else ref.handle, _PREC[self.precision])
+        _Handle.__init__(self)
+        call("ann_psi_create_classical", ct.byref(d), ct.byref(self._h))
+        self._init_common(gpu)
+
+    @property
+    def ref_log_prefactor(self) -> complex:
+        out = np.zeros(2)
+        call("ann_psi_ref_log_prefactor", self._h, None, ptr(out))
+        return complex(out[0], out[1])
+
+    @ref_log_prefactor.setter
+    def ref_log_prefactor(self, value):
+        v = np.array([complex(value).real, complex(value).imag])
+        call("ann_psi_ref_log_prefactor", self._h, ptr(v), None)
+
+    @property
+    def psi_ref(self):
+        """The reference with this network's current reference parameters (a copy)."""
+        if not isinstance(self._ref, _Psi):
+            return self._ref
+        r = +self._ref
+        if self.order > 1:
+            r.params = self.params[len(self.H_local):]
+            r.log_prefactor = self.ref_log_prefactor
+        return r
+
+    def calibrate(self, ensemble):
+        if type(ensemble).__name__.startswith("ExactSummation"):
+            _Psi.calibrate(self, ensemble)
+            return
+        # main.cpp.template:253-260: the reference part first, then the whole
+        if self.order > 1 and isinstance(self._ref, _Psi):
+            self.ref_log_prefactor -= log_psi(self.psi_ref, ensemble)
+        self.log_prefactor -= log_psi(self, ensemble)
+
+
+def _classical_factory(name, order, ann):
+    def init(self, num_sites, H_local, params, psi_ref, log_prefactor=0.0, gpu=True, **kwargs):
+        if ann and not isinstance(psi_ref, _Psi):
+            raise ValueError(name + " needs a PsiDeep reference")
+        PsiClassical.__init__(self, num_sites, H_local, params, psi_ref, log_prefactor, gpu, order=order, **kwargs)
+    return type(name, (PsiClassical,), {"__init__": init, "__doc__": f"PsiClassical of order {order} "
+                                         f"({'PsiDeep' if ann else 'fully polarized'} reference)."})
+
+
+PsiClassicalFP_1 = _classical_factory("PsiClassicalFP_1", 1, False)
+PsiClassicalFP_2 = _classical_factory("PsiClassicalFP_2", 2, False)
+PsiClassicalANN_1 = _classical_factory("PsiClassicalANN_1", 1, True)
+PsiClassicalANN_2 = _classical_factory("PsiClassicalANN_2", 2, True)
+
+
+class KullbackLeibler(_Handle):
+    """Kullback-Leibler-type divergence of psi (a classical network) from psi_prime over
+    psi_prime's ensemble, its gradient in psi_prime's parameters and the gradient's noise
+    (source/network_functions/KullbackLeibler.cu.template:17-329; binding
+    main.cpp.template:445-461). The mean deviation of a call is subtracted in the next."""
+
+    _destroy = "ann_kl_destroy"
+
+    def __init__(self, num_params, gpu=True, stream=None):
+        _Handle.__init__(self)
+        self.num_params = int(num_params)
+        self.gpu = bool(gpu)
+        self.stream = stream
+        call("ann_kl_create", self.num_params, ct.byref(self._h))
+
+    def __call__(self, psi, psi_prime, ensemble, threshold=0.0) -> float:
+        out = np.zeros(1)
+        call("ann_kl_value", self._h, psi.handle, psi_prime.handle, ensemble.handle, float(threshold),
+             stream_ptr(self.stream), ptr(out))
+        return float(out[0])
+
+    def gradient(self, psi, psi_prime, ensemble, nu=1.0, threshold=0.0):
+        """(gradient, value), as gradient_py (KullbackLeibler.hpp:100-112)."""
+        grad = cbuf(psi_prime.num_params)
+        v = np.zeros(1)
+        call("ann_kl_gradient", self._h, psi.handle, psi_prime.handle, ensemble.handle, float(nu), float(threshold),
+             stream_ptr(self.stream), ptr(grad), None, ptr(v))
+        return grad, float(v[0])
+
+    def gradient_with_noise(self, psi, psi_prime, ensemble, nu=1.0, threshold=0.0):
+        """(gradient, noise, value)."""
+        grad = cbuf(psi_prime.num_params)
+        noise = np.zeros(psi_prime.num_params)
+        v = np.zeros(1)
+        call("ann_kl_gradient", self._h, psi.handle, psi_prime.handle, ensemble.handle, float(nu), float(threshold),
+             stream_ptr(self.stream), ptr(grad), ptr(noise), ptr(v))
+        return grad, noise, float(v[0])
+
+    def _stats(self):
+        w = np.zeros(1)
+        m = np.zeros(2)
+        call("ann_kl_stats", self._h, ptr(w), ptr(m))
+        return float(w[0]), complex(m[0], m[1])
+
+    @property
+    def total_weight(self) -> float:
+        return self._stats()[0]
+
+    @property
+    def mean_deviation(self) -> complex:
+        return self._stats()[1]
+
+    @property
+    def log_psi_scale(self) -> float:
+        out = np.zeros(1)
+        call("ann_kl_log_psi_scale", self._h, None, ptr(out))
+        return float(out[0])
+
+    @log_psi_scale.setter
+    def log_psi_scale(self, value):
+        v = np.array([float(value)])
+        call("ann_kl_log_psi_scale", self._h, ptr(v), None)
+
+
+# ----------------------------------------------------------------------------------
 class Batch(_Handle):
     """Many (psi, operator, Monte Carlo ensemble[, TDVP]) instances of uneven size in one
     persistent sampling launch, with per-instance SR solves (this project's addition)."""

@@ -10,7 +10,9 @@ import math
 
 import numpy as np
 
-from .api import PsiCNN, PsiDeep, PsiRBM
+from .api import (PsiCNN, PsiClassicalANN_1, PsiClassicalANN_2, PsiClassicalFP_1, PsiClassicalFP_2, PsiDeep,
+                  PsiFullyPolarized, PsiRBM)
+from .expression import PauliExpression
 
 
 def _noise(rng, shape, scale, complex_=True):
@@ -127,3 +129,27 @@ def new_convolutional_network(L, layers, initial_value=(0.01 + 1j * math.pi / 4)
                     w = w + math.sqrt(6 / (vol * prev + vol * ch)) * (2 * rng.random(vol) - 1)
                 params.extend(w)
     return PsiCNN(L, channels, conns, symmetry_classes, np.array(params), final_factor, 0.0, gpu, **kwargs)
+
+
+def new_classical_network(num_sites, order, H_local, symmetric=False, distance="max", params=0,
+                          psi_ref="fully polarized", use_super_operator=False, gpu=True, **kwargs):
+    """Classical network (pyANNonGPU/new_classical_network.py:6-66): one parameter per operator
+    of ``H_local`` (a list, or a Pauli expression whose terms become the operators), zero
+    initial parameters, log_prefactor log(2^(-N/2)) over the fully polarized reference or 0 over
+    a PsiDeep reference (copied; its parameters join the variational ones at order 2)."""
+    if order not in (1, 2):
+        raise ValueError("order must be 1 or 2")
+    if symmetric or use_super_operator:
+        raise NotImplementedError("symmetric classical networks and super-operator features are not built")
+    if isinstance(H_local, PauliExpression):
+        H_local = [PauliExpression({k: c}) for k, c in H_local.terms.items()]
+    H_local = list(H_local)
+    if isinstance(params, (int, float)) and params == 0:
+        params = np.zeros(len(H_local), dtype=complex)
+    if isinstance(psi_ref, str):
+        lp = math.log(1 / 2 ** (num_sites / 2))
+        cls = PsiClassicalFP_1 if order == 1 else PsiClassicalFP_2
+        return cls(num_sites, H_local, params, PsiFullyPolarized(num_sites, lp), lp, gpu, **kwargs)
+    cls = PsiClassicalANN_1 if order == 1 else PsiClassicalANN_2
+    return cls(num_sites, H_local, params, psi_ref, 0.0, gpu, **kwargs)
+

@@ -56,6 +56,9 @@ struct DeepHost {
     std::vector<unsigned> conn_off, rbeg_off, rq_off;  // offsets into the device table (u16 entries)
     unsigned tab_len = 0;
     int dup0 = 0;   // a site appears twice in one first-layer window
+    unsigned na = 0;        // input-unit parameters a (N; 0 for a classical network without reference)
+    unsigned K = 0;         // classical features (PsiClassical), parameters [theta | network]
+    zd lp_ref{0.0, 0.0};    // log prefactor of the reference network (PsiClassical)
 };
 
 struct ann_psi_impl {
@@ -81,6 +84,11 @@ struct ann_psi_impl {
     // multi-layer PsiDeep (final weights in fw / fwd)
     DeepHost deep;
     DevBuf deep_tab;
+    DevBuf feat_beg, feat_zy, feat_c, feat_cf;   // classical features (u32 offsets, Z|Y masks, FP64 / FP32 coefficients)
+    std::vector<unsigned> feat_beg_h;
+    std::vector<uint64_t> feat_a_h, feat_b_h;     // feature strings as given (one word each)
+    std::vector<zd> feat_coeff_h;
+    int order = 0;                                 // PsiClassical order (0: not a classical network)
     size_t elem_bytes() const { return precision ? 16 : 8; }
 };
 

@@ -161,6 +161,7 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
     if((psi.kind != 0 || ens.basis) && ens.kind == 1 && ens.made && ens.indep_per_sample)
         throw Error(ANN_ERR_UNSUPPORTED, "the learned proposal is built for the RBM family over spins");
     if(ens.basis == ANN_BASIS_PAULIS) {
+        if(psi.deep.K) throw Error(ANN_ERR_UNSUPPORTED, "classical networks are built over spins");
         const unsigned sites = ens.kind == 0 ? ens.N : psi.N / 3u;
         if(psi.N != 3u * sites)
             throw Error(ANN_ERR_INVALID, "a wavefunction over Pauli strings needs 3 input units per site");
@@ -197,6 +198,7 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
                size_t ldO, cudaStream_t st, int basis) {
     if(basis == ANN_BASIS_PAULIS) {
+        if(psi.deep.K) throw Error(ANN_ERR_UNSUPPORTED, "classical networks are built over spins");
         if(psi.N % 3u) throw Error(ANN_ERR_INVALID, "a wavefunction over Pauli strings needs 3 input units per site");
         if(op && op->max_site > psi.N / 3u) throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the strings");
         deep_ensure(psi);
@@ -470,6 +472,15 @@ int ann_psi_copy(const ann_psi* src, ann_psi** out) {
             clone(p->cnn_w, src->cnn_w);
             clone(p->cnn_meta, src->cnn_meta);
             clone(p->deep_tab, src->deep_tab);
+            clone(p->feat_beg, src->feat_beg);
+            clone(p->feat_zy, src->feat_zy);
+            clone(p->feat_c, src->feat_c);
+            clone(p->feat_cf, src->feat_cf);
+            p->feat_beg_h = src->feat_beg_h;
+            p->feat_a_h = src->feat_a_h;
+            p->feat_b_h = src->feat_b_h;
+            p->feat_coeff_h = src->feat_coeff_h;
+            p->order = src->order;
         } catch(...) {
             delete p;
             throw;

@@ -21,6 +21,11 @@
 // deeper layers in full. O_k rows back-propagate through the same per-unit lists.
 // Weights, connection blocks and lists sit in shared memory when they fit, the per-warp
 // pre-activations Z and activations A (reused for the deltas) always do.
+//
+// The same kernels carry PsiClassical (include/quantum_state/PsiClassical.hpp:48-163): K
+// classical features h_k(s) = fast_local_energy of operator k (Operator.hpp:122-133) enter
+// log psi as sum_k theta_k h_k(s), their parameters first; the network above is its reference
+// (order 2, with no layers when the reference is fully polarized).
 #include <algorithm>
 
 #include "ann_internal.hpp"
@@ -52,6 +57,11 @@ struct DeepDev {
     const cplx<T>* w;    // Np
     const cplx<T>* fw;   // M_{L-1}
     const uint16_t* tab; // tab_len
+    unsigned a_off, na;  // input-unit parameters a: first index, count (0: none)
+    unsigned K;                  // classical features; their parameters are w[0, K)
+    const uint32_t* feat_beg;    // K + 1 offsets into the strings
+    const uint64_t* feat_zy;     // [strings][2]: sites holding Z or Y
+    const cplx<T>* feat_c;       // strings: coefficient x (-i)^{n_y}
 };
 
 template<typename T>
@@ -124,7 +134,29 @@ __device__ void deep_z0(const DeepCtx<T>& c, const Conf<2>& s, cplx<T>* dst, int
 template<typename T>
 __device__ cplx<T> deep_as(const DeepCtx<T>& c, const Conf<2>& s, int lane) {
     cplx<T> acc = mk<T>(T(0), T(0));
-    for(unsigned x = lane; x < c.p->N; x += 32) add_spin(acc, c.w[x], input_up(c, s, x));
+    for(unsigned x = lane; x < c.p->na; x += 32) add_spin(acc, c.w[c.p->a_off + x], input_up(c, s, x));
+    return warp_sum(acc);
+}
+
+// h_k(s) = sum over feature k's strings of c <s|P|P s> = c (-i)^{n_y} (-1)^{#(Z or Y on a down spin)}
+template<typename T>
+__device__ __forceinline__ cplx<T> feat_h(const DeepCtx<T>& c, const Conf<2>& s, unsigned k) {
+    const DeepDev<T>& p = *c.p;
+    cplx<T> r = mk<T>(T(0), T(0));
+    for(unsigned q = p.feat_beg[k]; q < p.feat_beg[k + 1]; q++) {
+        const int neg = (__popcll(~s.w[0] & p.feat_zy[2 * q]) + __popcll(~s.w[1] & p.feat_zy[2 * q + 1])) & 1;
+        const cplx<T> cq = p.feat_c[q];
+        r.re += neg ? -cq.re : cq.re;
+        r.im += neg ? -cq.im : cq.im;
+    }
+    return r;
+}
+
+// sum_k theta_k h_k(s) (every lane holds the sum)
+template<typename T>
+__device__ cplx<T> classical_term(const DeepCtx<T>& c, const Conf<2>& s, int lane) {
+    cplx<T> acc = mk<T>(T(0), T(0));
+    for(unsigned k = lane; k < c.p->K; k += 32) cmac(acc, c.w[k], feat_h(c, s, k));
     return warp_sum(acc);
 }
 
@@ -150,6 +182,7 @@ __device__ void deep_flip0(const DeepCtx<T>& c, const Conf<2>& s, unsigned x, in
 template<typename T>
 __device__ cplx<T> deep_forward(const DeepCtx<T>& c, int lane) {
     const DeepDev<T>& p = *c.p;
+    if(p.L == 0) return mk<T>(T(0), T(0));
     for(unsigned j = lane; j < p.size[0]; j += 32) c.A[j] = act_f(c.Z[j], p.act, 0);
     __syncwarp();
     for(unsigned l = 1; l < p.L; l++) {
@@ -176,24 +209,25 @@ __device__ cplx<T> deep_forward(const DeepCtx<T>& c, int lane) {
 template<typename T>
 __device__ cplx<T> deep_eval_moved(const DeepCtx<T>& c, const Conf<2>& s, const Conf<2>& s2, cplx<T> as, int lane) {
     const DeepDev<T>& p = *c.p;
-    if(!p.dup0) {
+    if(p.L && !p.dup0) {
         for(unsigned j = lane; j < p.size[0]; j += 32) c.Z[j] = c.th[j];
         __syncwarp();
         for_changed_units(c, s, s2, [&](unsigned u) {
             deep_flip0(c, s, u, lane);
             __syncwarp();
         });
-    } else {
+    } else if(p.L) {
         deep_z0(c, s2, c.Z, lane);
         __syncwarp();
     }
-    if(p.a_in)
+    if(p.a_in && p.na)
         for_changed_units(c, s, s2, [&](unsigned u) {
             const T d = input_up(c, s, u) ? T(-2) : T(2);
-            as.re += d * c.w[u].re;
-            as.im += d * c.w[u].im;
+            as.re += d * c.w[p.a_off + u].re;
+            as.im += d * c.w[p.a_off + u].im;
         });
-    const cplx<T> f = deep_forward(c, lane);
+    cplx<T> f = deep_forward(c, lane);
+    if(p.K) f += classical_term(c, s2, lane);
     return mk<T>(p.lp.re + as.re + f.re, p.lp.im + as.im + f.im);
 }
 
@@ -202,7 +236,8 @@ template<typename T>
 __device__ void deep_O_row(const DeepCtx<T>& c, const Conf<2>& s, int lane, cplx<T>* O) {
     const DeepDev<T>& p = *c.p;
     const unsigned L = p.L;
-    {
+    for(unsigned k = lane; k < p.K; k += 32) O[k] = feat_h(c, s, k);
+    if(L) {
         const unsigned top = p.uoff[L - 1];
         for(unsigned j = lane; j < p.size[L - 1]; j += 32)
             c.A[top + j] = c.fw[j] * act_df(c.Z[top + j], p.act, (int)(L - 1));
@@ -238,7 +273,7 @@ __device__ void deep_O_row(const DeepCtx<T>& c, const Conf<2>& s, int lane, cplx
             __syncwarp();
         }
     }
-    for(unsigned x = lane; x < p.N; x += 32) O[x] = mk<T>(input_up(c, s, x) ? T(1) : T(-1), T(0));
+    for(unsigned x = lane; x < p.na; x += 32) O[p.a_off + x] = mk<T>(input_up(c, s, x) ? T(1) : T(-1), T(0));
     __syncwarp();
 }
 
@@ -332,12 +367,18 @@ __device__ void deep_process_sample(const DeepCtx<T>& c, const OpDev* op, const 
     }
 }
 
+// units of the top layer (0 without layers)
+template<typename T>
+__host__ __device__ __forceinline__ unsigned deep_top(const DeepDev<T>& p) {
+    return p.L ? p.size[p.L - 1] : 0u;
+}
+
 // shared-memory layout: [weights (if staged) | fw | tables | per-warp th, Z, A]
 template<typename T>
 __host__ __device__ size_t deep_fixed_bytes(const DeepDev<T>& p) {
     size_t b = 0;
     if(p.stage_w) b += ((size_t)p.Np * sizeof(cplx<T>) + 15) & ~(size_t)15;
-    b += ((size_t)p.size[p.L - 1] * sizeof(cplx<T>) + 15) & ~(size_t)15;
+    b += ((size_t)deep_top(p) * sizeof(cplx<T>) + 15) & ~(size_t)15;
     b += ((size_t)p.tab_len * sizeof(uint16_t) + 15) & ~(size_t)15;
     return b;
 }
@@ -364,9 +405,9 @@ __device__ DeepCtx<T> deep_stage(const DeepDev<T>& p, unsigned char* smem) {
         c.w = p.w;
     }
     cplx<T>* fw = reinterpret_cast<cplx<T>*>(q);
-    for(unsigned k = threadIdx.x; k < p.size[p.L - 1]; k += blockDim.x) fw[k] = p.fw[k];
+    for(unsigned k = threadIdx.x; k < deep_top(p); k += blockDim.x) fw[k] = p.fw[k];
     c.fw = fw;
-    q += ((size_t)p.size[p.L - 1] * sizeof(cplx<T>) + 15) & ~(size_t)15;
+    q += ((size_t)deep_top(p) * sizeof(cplx<T>) + 15) & ~(size_t)15;
     uint16_t* tab = reinterpret_cast<uint16_t*>(q);
     for(unsigned k = threadIdx.x; k < p.tab_len; k += blockDim.x) tab[k] = p.tab[k];
     c.tab = tab;
@@ -439,11 +480,11 @@ __global__ void __launch_bounds__(256, 1) deep_mc_kernel(DeepDev<T> p, OpDev op,
             // Z holds the moved configuration's layer-0 pre-activations
             for(unsigned q = lane; q < p.size[0]; q += 32) c.th[q] = c.Z[q];
             __syncwarp();
-            if(p.a_in)
+            if(p.a_in && p.na)
                 for_changed_units(c, s, s2, [&](unsigned uu) {
                     const T d = input_up(c, s, uu) ? T(-2) : T(2);
-                    as.re += d * c.w[uu].re;
-                    as.im += d * c.w[uu].im;
+                    as.re += d * c.w[p.a_off + uu].re;
+                    as.im += d * c.w[p.a_off + uu].im;
                 });
             s = s2;
             lpsi = l2;
@@ -526,7 +567,13 @@ DeepDev<T> deep_view(const ann_psi_impl& psi, int basis) {
     p.N = psi.N;
     p.L = (unsigned)d.sizes.size();
     p.Np = psi.Np;
-    unsigned off = psi.N, u = 0;
+    p.K = d.K;
+    p.a_off = d.K;
+    p.na = d.na;
+    p.feat_beg = psi.feat_beg.as<uint32_t>();
+    p.feat_zy = psi.feat_zy.as<uint64_t>();
+    p.feat_c = psi.precision ? reinterpret_cast<const cplx<T>*>(psi.feat_c.p) : reinterpret_cast<const cplx<T>*>(psi.feat_cf.p);
+    unsigned off = d.K + d.na, u = 0;
     for(unsigned l = 0; l < p.L; l++) {
         p.size[l] = d.sizes[l];
         p.C[l] = d.C[l];
@@ -545,7 +592,7 @@ DeepDev<T> deep_view(const ann_psi_impl& psi, int basis) {
     p.act = psi.act;
     p.a_in = psi.a_in;
     p.dup0 = d.dup0;
-    p.lp = mk<T>((T)psi.lp.real(), (T)psi.lp.imag());
+    p.lp = mk<T>((T)(psi.lp.real() + d.lp_ref.real()), (T)(psi.lp.imag() + d.lp_ref.imag()));
     p.w = psi.cnn_w.as<cplx<T>>();
     p.fw = psi.fwd.as<cplx<T>>();
     p.tab = psi.deep_tab.as<uint16_t>();
@@ -730,6 +777,7 @@ void deep_ensure(ann_psi_impl& psi) {
     psi.deep.sizes = {psi.M};
     psi.deep.C = {psi.C};
     psi.deep.conn = psi.conn;
+    psi.deep.na = psi.N;
     deep_build_tables(psi);
     psi.cnn_w.ensure((size_t)psi.Np * psi.elem_bytes());
     deep_prepare(psi, nullptr);
@@ -784,6 +832,7 @@ extern "C" int ann_psi_create_deep(const ann_deep_desc* d, ann_psi** out) {
             if(np != d->num_params) throw Error(ANN_ERR_INVALID, "num_params does not match the layer structure");
             p->Np = np;
             h.conn.assign(d->connections, d->connections + total);
+            h.na = d->N;
             deep_build_tables(*p);
             const unsigned ML = h.sizes[L - 1];
             p->fw.assign(ML, zd(0, 0));

@@ -39,6 +39,7 @@ typedef struct ann_ens ann_ens;
 typedef struct ann_tdvp ann_tdvp;
 typedef struct ann_made ann_made;
 typedef struct ann_batch ann_batch;
+typedef struct ann_kl ann_kl;
 
 const char* ann_last_error(void);
 int ann_version(void);
@@ -331,6 +332,52 @@ int ann_hsd_distance(ann_psi* psi, ann_psi* psi_prime, ann_op* op, int is_unitar
                      double* distance);
 int ann_hsd_gradient(ann_psi* psi, ann_psi* psi_prime, ann_op* op, int is_unitary, ann_ens* ens, double nu,
                      void* stream, double* grad, double* distance);
+
+/* ---------------------------------------------------------------------------------
+ * PsiClassical, the variational classical network (PsiClassicalFP_1/_2, PsiClassicalANN_1/_2;
+ * include/quantum_state/PsiClassical.hpp:48-260, main.cpp.template:207-268):
+ * log psi(s) = log_prefactor + sum_k params_k h_k(s) (+ log psi_ref(s) for order 2), with
+ * h_k(s) = sum over the strings of operator k of coeff <s|P|P s> (Operator::fast_local_energy,
+ * Operator.hpp:122-133) and O_k = (h_k(s), O_ref(s)); params = [params_k | reference params].
+ * The reference network (a PsiDeep of any depth) is copied; NULL = fully polarized (log psi_ref = 0).
+ * ------------------------------------------------------------------------------ */
+typedef struct {
+    unsigned num_sites;              /* spins, <= 128 */
+    unsigned n_features;             /* operators H_local, one feature each */
+    const unsigned* feature_begin;   /* n_features + 1 offsets into the strings */
+    unsigned num_words;              /* words per string, 1 or 2 */
+    const uint64_t* a;               /* strings x num_words, Pauli (a, b) encoding as ann_op_create_pauli */
+    const uint64_t* b;
+    const double* coeff;             /* strings, interleaved complex */
+    const double* params;            /* n_features complex */
+    double log_prefactor[2];
+    unsigned order;                  /* 1 or 2 */
+    const ann_psi* ref;              /* order 2: reference PsiDeep (copied), or NULL */
+    int precision;                   /* ANN_PREC_* without a reference (with one: the reference's) */
+} ann_classical_desc;
+int ann_psi_create_classical(const ann_classical_desc* desc, ann_psi** out);
+/* log_prefactor of the reference part (ref_log_prefactor, main.cpp.template:224-231); either pointer may be NULL */
+int ann_psi_ref_log_prefactor(ann_psi* psi, const double* set2, double* get2);
+
+/* ---------------------------------------------------------------------------------
+ * KullbackLeibler (KullbackLeibler(num_params, gpu), main.cpp.template:445-461;
+ * source/network_functions/KullbackLeibler.cu.template:17-329) of psi (classical) against
+ * psi_prime over psi_prime's ensemble: w = |psi/psi'|^2 w', d = log psi' - log psi - the mean
+ * deviation of the previous call; deviations with |d|^2 <= threshold^2 are left out of the
+ * deviation sums. value = sqrt(max(1e-8, <|d|^2> - |<d>|^2)); gradient (psi_prime's parameters)
+ * = (<d conj(O)> - <d> conj(<O>)) / value^nu; noise as gradient_with_noise.
+ * ------------------------------------------------------------------------------ */
+int ann_kl_create(unsigned num_params, ann_kl** out);
+int ann_kl_destroy(ann_kl* kl);
+/* log_psi_scale (read / write property): log psi is scaled by it; either pointer may be NULL */
+int ann_kl_log_psi_scale(ann_kl* kl, const double* set, double* get);
+int ann_kl_value(ann_kl* kl, ann_psi* psi, ann_psi* psi_prime, ann_ens* ens, double threshold, void* stream,
+                 double* value);
+/* grad: num_params(psi_prime) complex; noise (num_params doubles) may be NULL */
+int ann_kl_gradient(ann_kl* kl, ann_psi* psi, ann_psi* psi_prime, ann_ens* ens, double nu, double threshold,
+                    void* stream, double* grad, double* noise, double* value);
+/* total_weight and mean_deviation (2 doubles) of the last call */
+int ann_kl_stats(const ann_kl* kl, double* total_weight, double* mean_deviation2);
 
 /* ---------------------------------------------------------------------------------
  * Autotuner (no counterpart in the reference, whose launch shape is fixed: one CTA
