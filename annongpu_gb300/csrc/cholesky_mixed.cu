@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(1024) diag_inv_kernel(const cf* __restrict__ A
 
 constexpr unsigned kTrsmRows = 16;  // rows per CTA: many short CTAs, the panel is on the critical path
 
-// rows below the diagonal block: X <- X L_kk^{-H} by substitution, one warp per row,
+// rows below the diagonal block: X <- X L_kk^{-H} by substitution, one warp per two rows,
 // lane owning columns lane and lane + 32: for c = 0..63 the owner finalises
 //   x_c = (x_c - sum_{p<c} x_p conj(L_cp)) / L_cc,
 // broadcasts it, and the lanes subtract x_c conj(L_qc) from their columns q > c.
@@ -193,34 +193,64 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
     __syncthreads();
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t row0 = (size_t)kb + NB + (size_t)blockIdx.x * kTrsmRows;
-    for(unsigned rr = warp; rr < kTrsmRows; rr += 8) {
-        const size_t row = row0 + rr;
-        if(row >= n) break;
-        cf* X = A + row * n + kb;
-        cf x0 = X[lane], x1 = X[lane + 32];
-        for(unsigned c = 0; c < 32; c++) {
-            cf xc;
-            xc.re = __shfl_sync(0xffffffffu, x0.re, c);
-            xc.im = __shfl_sync(0xffffffffu, x0.im, c);
-            xc = inv_d[c] * xc;
-            if(lane == c) x0 = xc;
-            else if(lane > c) cmac_conj(x0, Lt[c][lane], -xc);  // -= x_c conj(L_qc)
-            cmac_conj(x1, Lt[c][lane + 32], -xc);
+    // each warp solves its two rows (warp, warp + 8) side by side: two independent chains
+    static_assert(kTrsmRows == 16, "two rows per warp of eight");
+    const size_t ra = row0 + warp, rb = row0 + warp + 8;
+    if(ra >= n) return;
+    const bool has_b = rb < n;
+    cf* Xa = A + ra * n + kb;
+    cf* Xb = A + (has_b ? rb : ra) * n + kb;
+    cf a0 = Xa[lane], a1 = Xa[lane + 32], b0 = Xb[lane], b1 = Xb[lane + 32];
+    for(unsigned c = 0; c < 32; c++) {
+        cf xa, xb;
+        xa.re = __shfl_sync(0xffffffffu, a0.re, c);
+        xa.im = __shfl_sync(0xffffffffu, a0.im, c);
+        xb.re = __shfl_sync(0xffffffffu, b0.re, c);
+        xb.im = __shfl_sync(0xffffffffu, b0.im, c);
+        const float id = inv_d[c];
+        xa = id * xa;
+        xb = id * xb;
+        const cf l0 = Lt[c][lane], l1 = Lt[c][lane + 32];
+        if(lane == c) {
+            a0 = xa;
+            b0 = xb;
+        } else if(lane > c) {
+            cmac_conj(a0, l0, -xa);  // -= x_c conj(L_qc)
+            cmac_conj(b0, l0, -xb);
         }
-        for(unsigned c = 32; c < NB; c++) {
-            cf xc;
-            xc.re = __shfl_sync(0xffffffffu, x1.re, c - 32);
-            xc.im = __shfl_sync(0xffffffffu, x1.im, c - 32);
-            xc = inv_d[c] * xc;
-            if(lane + 32 == c) x1 = xc;
-            else if(lane + 32 > c) cmac_conj(x1, Lt[c][lane + 32], -xc);
+        cmac_conj(a1, l1, -xa);
+        cmac_conj(b1, l1, -xb);
+    }
+    for(unsigned c = 32; c < NB; c++) {
+        cf xa, xb;
+        xa.re = __shfl_sync(0xffffffffu, a1.re, c - 32);
+        xa.im = __shfl_sync(0xffffffffu, a1.im, c - 32);
+        xb.re = __shfl_sync(0xffffffffu, b1.re, c - 32);
+        xb.im = __shfl_sync(0xffffffffu, b1.im, c - 32);
+        const float id = inv_d[c];
+        xa = id * xa;
+        xb = id * xb;
+        const cf l1 = Lt[c][lane + 32];
+        if(lane + 32 == c) {
+            a1 = xa;
+            b1 = xb;
+        } else if(lane + 32 > c) {
+            cmac_conj(a1, l1, -xa);
+            cmac_conj(b1, l1, -xb);
         }
-        X[lane] = x0;
-        X[lane + 32] = x1;
+    }
+    Xa[lane] = a0;
+    Xa[lane + 32] = a1;
+    if(PT) {
+        put_tf32(PT, ra - (kb + NB), lane, a0);
+        put_tf32(PT, ra - (kb + NB), lane + 32, a1);
+    }
+    if(has_b) {
+        Xb[lane] = b0;
+        Xb[lane + 32] = b1;
         if(PT) {
-            const size_t i = row - (kb + NB);
-            put_tf32(PT, i, lane, x0);
-            put_tf32(PT, i, lane + 32, x1);
+            put_tf32(PT, rb - (kb + NB), lane, b0);
+            put_tf32(PT, rb - (kb + NB), lane + 32, b1);
         }
     }
 }
