@@ -541,8 +541,19 @@ __global__ void __launch_bounds__(256) ir_residual_kernel(const zc* __restrict__
         const size_t i = (size_t)blockIdx.x * 8 + warp;
         if(i < n) {
             const zc* Si = S + i * n;
-            zc acc = mk(0.0, 0.0);
-            for(unsigned j = lane; j < n; j += 32) cmac(acc, Si[j], x[j]);
+            // four independent accumulators: four 16-byte loads in flight per lane
+            zc a0 = mk(0.0, 0.0), a1 = a0, a2 = a0, a3 = a0;
+            unsigned j = lane;
+            for(; j + 96 < n; j += 128) {
+                const zc s0 = Si[j], s1 = Si[j + 32], s2 = Si[j + 64], s3 = Si[j + 96];
+                const zc x0 = x[j], x1 = x[j + 32], x2 = x[j + 64], x3 = x[j + 96];
+                cmac(a0, s0, x0);
+                cmac(a1, s1, x1);
+                cmac(a2, s2, x2);
+                cmac(a3, s3, x3);
+            }
+            for(; j < n; j += 32) cmac(a0, Si[j], x[j]);
+            zc acc = (a0 + a1) + (a2 + a3);
             acc = warp_sum(acc);
             if(lane == 0) {
                 const zc ri = F[i] - acc - shift * x[i];

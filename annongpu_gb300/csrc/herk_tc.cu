@@ -240,9 +240,9 @@ void herk_tc(ann_tdvp_impl& td, const double* wts, double w0, bool split, cudaSt
     const size_t ns_pad = (td.n_rows + kBK - 1) / kBK * kBK;
     const size_t ldx = split ? 2 * ns_pad : ns_pad;
     td.herk_in.ensure(rows_x * ldx * sizeof(__nv_bfloat16));
-    // padding rows / samples must read as zero
-    ANN_CUDA(cudaMemsetAsync(td.herk_in.p, 0, rows_x * ldx * sizeof(__nv_bfloat16), st));
-    dim3 pg((Np + 63) / 64, (unsigned)(ns_pad / 64));
+    // the grid covers every parameter slot of the nblk blocks and every padded sample, so
+    // the padding (parameters >= Np, samples >= rows) is written as zero by the kernel
+    dim3 pg(2 * nblk, (unsigned)(ns_pad / 64));
     auto* XT = td.herk_in.as<__nv_bfloat16>();
     if(td.O_precision == 0)
         herk_prep_kernel<float><<<pg, 256, 0, st>>>(td.O.as<cplx<float>>(), td.n_rows, td.ldO, Np, wts, w0,
