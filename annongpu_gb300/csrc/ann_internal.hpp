@@ -281,6 +281,7 @@ std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_slab(size_t rows, unsigned Np);
 std::string key_chol_update(unsigned n);
+std::string key_chol_reserve(unsigned n);
 
 // PsiCNN (cnn.cu)
 void deep_prepare(ann_psi_impl& psi, cudaStream_t st);

@@ -18,6 +18,8 @@
 // Every mbarrier wait is bounded (globaltimer deadline): a timeout raises
 // kStatusTimeout, all roles leave their loops, the producer waits (bounded) for its
 // copies in flight and the tensor memory is freed before the CTA returns.
+#include <algorithm>
+
 #include "ann_internal.hpp"
 #include "tcgen05.cuh"
 
@@ -669,8 +671,12 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
             ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         }
         if(tiles > (unsigned)sms) {
-            // more than a wave: persistent CTAs, the epilogue of one tile under the MMAs of the next
-            chol_update_tc3_kernel<<<(unsigned)sms, 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
+            // more than a wave: persistent CTAs, the epilogue of one tile under the MMAs of the
+            // next. A few SMs stay free for the next panel (potrf32 / trsm32 on the side stream),
+            // which otherwise only gets the resources left beside the persistent CTAs and runs
+            // several times slower; the panel is the critical path of the factorisation.
+            const int reserve = std::min(tuning_get(key_chol_reserve(n), 32), sms / 2);
+            chol_update_tc3_kernel<<<(unsigned)(sms - reserve), 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
             check_launch("chol_update_tc3_kernel");
         } else {
             // up to a wave: one tile per CTA, two CTAs per SM

@@ -10,6 +10,7 @@
 //   stats.slab      rows per FP32 slab of the <O> / F reductions: 128, 256, 512
 //   chol.update     trailing update of the FP32 Cholesky: 128 x 128 tcgen05 tiles
 //                   (split TF32) or 64 x 64 FP32 SIMT tiles
+//   chol.reserve    SMs the persistent tcgen05 update leaves free for the next panel: 0, 16, 32, 48, 64
 // The sampler is timed on a copy of the ensemble, so the caller's chains do not move.
 // The reference has no tuning layer (its launch shape is fixed: one CTA per chain,
 // blockDim = hidden width, include/ensembles/MonteCarlo.hpp:223-228).
@@ -101,6 +102,12 @@ std::string key_slab(size_t rows, unsigned Np) {
 std::string key_chol_update(unsigned n) {
     std::ostringstream o;
     o << "chol.update/n" << ((n + 1023) / 1024) * 1024;
+    return o.str();
+}
+
+std::string key_chol_reserve(unsigned n) {
+    std::ostringstream o;
+    o << "chol.reserve/n" << ((n + 1023) / 1024) * 1024;
     return o.str();
 }
 
@@ -247,6 +254,19 @@ int ann_autotune(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, double dia
                     if(ms < best) { best = ms; best_m = m; }
                 }
                 tuning_set(key, best_m);
+                // SMs left to the panel beside the persistent tensor-core update
+                if(best_m == 1) {
+                    const std::string kr = key_chol_reserve(t->Np);
+                    double best_r_ms = 1e300;
+                    int best_r = 32;
+                    for(int r : {0, 16, 32, 48, 64}) {
+                        tuning_set(kr, r);
+                        const double ms = time_ms([&] { sr_solve_any(*t, diag_shift, status_word(), st); }, 2, st);
+                        record(4, r, ms);
+                        if(ms < best_r_ms) { best_r_ms = ms; best_r = r; }
+                    }
+                    tuning_set(kr, best_r);
+                }
             }
         } catch(...) {
             ann_ens_destroy(e2);
