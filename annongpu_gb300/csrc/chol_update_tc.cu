@@ -268,160 +268,24 @@ chol_update_tc_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_con
     if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
-// The same update with Re and Im of the tile accumulated directly (N = 128 MMAs, the
-// negate-A bit giving -Re_I . Im_J^T), so a CTA holds 256 TMEM columns; one 64 KB pipeline
-// stage and a double-buffered 16 KB epilogue chunk keep its shared memory under half an
-// SM's, so two CTAs share an SM and one's epilogue overlaps the other's loads and MMAs:
+// The update with Re and Im of the tile accumulated directly (N = 128 MMAs, the
+// negate-A bit giving -Re_I . Im_J^T), 256 TMEM columns per tile:
 //   Re C (TMEM cols   0..127) += Re_I . Re_J^T + Im_I . Im_J^T
 //   Im C (TMEM cols 128..255) += Im_I . Re_J^T - Re_I . Im_J^T
 // The epilogue streams C in eight 16-column chunks through the swizzled buffer into bulk
 // tensor reduce-adds (A's row pitch must be 16-byte aligned: n even).
-constexpr int kStage2Bytes = 2 * kRows * kBK * 4;  // one stage: A block + B block (64 KB)
+constexpr int kStageBytesN = 2 * kRows * kBK * 4;  // one stage: A block + B block (64 KB)
 constexpr int kChunkBytes = kBM * 128;             // 128 rows x 16 complex
-constexpr int kSmem2Bytes = kStage2Bytes + 2 * kChunkBytes + 1024 + 256;
-
-__global__ void __launch_bounds__(128, 2)
-chol_update_tc2_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap amap, UpdArgs a) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* chunks = base + kStage2Bytes;
-    unsigned char* tail = chunks + 2 * kChunkBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(tail);
-    uint64_t* empty = full + 1;
-    uint64_t* done = empty + 1;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned I, J;
-    if(a.col_only) {
-        I = blockIdx.x;
-        J = 0;
-    } else {
-        unsigned b = blockIdx.x;
-        I = 0;
-        while(b > I) { b -= I + 1; I++; }
-        J = b + 1;
-        I += 1;
-    }
-    if(threadIdx.x == 0) {
-        mbar_init(smem_u32(full), 1);
-        mbar_init(smem_u32(empty), 1);
-        mbar_init(smem_u32(done), 1);
-        *abort_flag = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncwarp();
-    if(warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *tmem_slot;
-
-    constexpr unsigned total = kSegments * kStepsPerSeg;
-    int issued = 0;
-    if(warp == 0 && lane == 0) {
-        // ---- TMA producer (one stage) ----
-        for(unsigned kt = 0; kt < total; kt++) {
-            if(!mbar_wait(smem_u32(empty), (kt & 1u) ^ 1u, abort_flag, a.status)) break;
-            const unsigned seg = kt / kStepsPerSeg, k = kt % kStepsPerSeg;
-            const int xa = (int)(k * kBK + (seg == 2 ? kPanel : 0u));
-            const int xb = (int)(k * kBK + (seg == 1 ? kPanel : 0u));
-            mbar_expect_tx(smem_u32(full), kStage2Bytes);
-            tma_load_2d(smem_u32(base), &tmap, xa, (int)(I * kRows), smem_u32(full));
-            tma_load_2d(smem_u32(base + kRows * kBK * 4), &tmap, xb, (int)(J * kRows), smem_u32(full));
-            issued++;
-        }
-    } else if(warp == 1 && lane == 0) {
-        // ---- MMA issuer ----
-        constexpr uint32_t idesc = idesc_tf32(128, 128);
-        constexpr uint32_t idesc_neg = idesc | (1u << 13);  // negate A
-        const uint32_t sa = smem_u32(base), sb = sa + kRows * kBK * 4;
-        bool ok = true;
-        for(unsigned kt = 0; kt < total && ok; kt++) {
-            if(!mbar_wait(smem_u32(full), kt & 1u, abort_flag, a.status)) { ok = false; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for(int kk = 0; kk < kBK / 8; kk++) {
-                const int acc = (kt > 0 || kk > 0) ? 1 : 0;
-                const uint64_t are = sw128_desc(sa + kk * 32), aim = sw128_desc(sa + kBM * 128 + kk * 32);
-                const uint64_t bre = sw128_desc(sb + kk * 32), bim = sw128_desc(sb + kBM * 128 + kk * 32);
-                mma_tf32(tmem, are, bre, idesc, acc);            // Re C += Re_I Re_J^T
-                mma_tf32(tmem, aim, bim, idesc, 1);              //      + Im_I Im_J^T
-                mma_tf32(tmem + 128, aim, bre, idesc, acc);      // Im C += Im_I Re_J^T
-                mma_tf32(tmem + 128, are, bim, idesc_neg, 1);    //      - Re_I Im_J^T
-            }
-            mma_commit(smem_u32(empty));
-        }
-        mma_commit(smem_u32(done));
-    }
-    __syncwarp();
-
-    // ---- epilogue: four warps, TMEM lane = row of the tile ----
-    bool ok = mbar_wait(smem_u32(done), 0, abort_flag, a.status) && !*abort_flag;
-    ok = __all_sync(0xffffffffu, ok);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    ok = __syncthreads_and(ok ? 1 : 0) != 0;
-    if(ok) {
-        const unsigned i = warp * 32 + lane;
-        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-        const bool diag = I == J;
-        const int y = (int)(a.t0 + I * kBM);
-        for(int c = 0; c < kBM / 16; c++) {
-            unsigned char* buf = chunks + (c & 1) * kChunkBytes;
-            if(c >= 2) {
-                // the reduce of chunk c - 2 has finished reading this buffer
-                if(threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-                __syncthreads();
-            }
-            float re[16], im[16];
-            tmem_ld16(lane_addr + c * 16, re);
-            tmem_ld16(lane_addr + 128 + c * 16, im);
-            unsigned char* row = buf + (size_t)i * 128;
-#pragma unroll
-            for(int u = 0; u < 8; u++) {
-                const int q0 = 2 * u, q1 = 2 * u + 1;
-                const bool z0 = diag && (unsigned)(c * 16 + q0) > i, z1 = diag && (unsigned)(c * 16 + q1) > i;
-                float4 v;
-                v.x = z0 ? 0.f : -re[q0];
-                v.y = z0 ? 0.f : -im[q0];
-                v.z = z1 ? 0.f : -re[q1];
-                v.w = z1 ? 0.f : -im[q1];
-                *reinterpret_cast<float4*>(row + ((u ^ (i & 7u)) << 4)) = v;
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if(threadIdx.x == 0) {
-                tma_reduce_add_2d(&amap, (int)(2 * (a.t0 + J * kBM) + 32 * c), y, smem_u32(buf));
-                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            }
-        }
-        if(threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-    } else if(warp == 0 && lane == 0) {
-        for(int q = 0; q < issued; q++) {
-            const unsigned long long t0 = gtime();
-            while(!mbar_try(smem_u32(full), q & 1u) && gtime() - t0 < kWaitNs) {}
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
-}
-
-// Persistent form for the large launches: one CTA per SM walks the tiles i, i + G, ...
-// with the roles split over warps (warp 0: TMA producer, warp 1: MMA issuer, warps 4-7:
-// epilogue, TMEM lane quarter = warp % 4). Two 256-column TMEM accumulators (Re | Im, the
-// N = 128 MMAs of chol_update_tc2_kernel) let the MMAs of the next tile run while the
-// epilogue drains the previous one; loads go through a two-stage ring of 64 KB, the
-// epilogue through a double-buffered 16 KB chunk into bulk tensor reduce-adds.
+// Persistent kernel: CTA g walks the tiles g, g + G, ... (one tile per CTA for launches of
+// up to a wave) with the roles split over warps (warp 0: TMA producer, warp 1: MMA issuer,
+// warps 4-7: epilogue, TMEM lane quarter = warp % 4). Two 256-column TMEM accumulators
+// (Re | Im) let the MMAs of the next tile run while the epilogue drains the previous one;
+// loads go through a two-stage ring of 64 KB, the epilogue through a double-buffered 16 KB
+// chunk into bulk tensor reduce-adds.
 // Barriers: full/empty (stage ring), acc_full (MMA -> epilogue), acc_empty (epilogue ->
 // MMA), all waits bounded; a timeout raises kStatusTimeout and every role leaves.
 constexpr int kStages3 = 2;
-constexpr int kSmem3Bytes = kStages3 * kStage2Bytes + 2 * kChunkBytes + 1024 + 256;
+constexpr int kSmem3Bytes = kStages3 * kStageBytesN + 2 * kChunkBytes + 1024 + 256;
 constexpr unsigned kEpiThreads = 128;
 
 __global__ void __launch_bounds__(256, 1)
@@ -429,7 +293,7 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
                        unsigned n_tiles) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* chunks = base + kStages3 * kStage2Bytes;
+    unsigned char* chunks = base + kStages3 * kStageBytesN;
     uint64_t* full = reinterpret_cast<uint64_t*>(chunks + 2 * kChunkBytes);
     uint64_t* empty = full + kStages3;
     uint64_t* accf = empty + kStages3;
@@ -490,8 +354,8 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
                 const unsigned seg = kt / kStepsPerSeg, k = kt % kStepsPerSeg;
                 const int xa = (int)(k * kBK + (seg == 2 ? kPanel : 0u));
                 const int xb = (int)(k * kBK + (seg == 1 ? kPanel : 0u));
-                unsigned char* st = base + s * kStage2Bytes;
-                mbar_expect_tx(smem_u32(&full[s]), kStage2Bytes);
+                unsigned char* st = base + s * kStageBytesN;
+                mbar_expect_tx(smem_u32(&full[s]), kStageBytesN);
                 tma_load_2d(smem_u32(st), &tmap, xa, (int)(I * kRows), smem_u32(&full[s]));
                 tma_load_2d(smem_u32(st + kRows * kBK * 4), &tmap, xb, (int)(J * kRows), smem_u32(&full[s]));
                 issued++;
@@ -518,7 +382,7 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
                 const unsigned g = lt * ksteps + kt, s = g % kStages3, ph = (g / kStages3) & 1u;
                 if(!mbar_wait(smem_u32(&full[s]), ph, abort_flag, a.status)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t sa = smem_u32(base + s * kStage2Bytes), sb = sa + kRows * kBK * 4;
+                const uint32_t sa = smem_u32(base + s * kStageBytesN), sb = sa + kRows * kBK * 4;
 #pragma unroll
                 for(int kk = 0; kk < kBK / 8; kk++) {
                     const int acc = (kt > 0 || kk > 0) ? 1 : 0;
@@ -619,11 +483,6 @@ void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
     if(!attr) {
         ANN_CUDA(cudaFuncSetAttribute(chol_update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       kSmemBytes));
-        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kSmem2Bytes));
-        // the whole unified L1 / shared array as shared memory, so that two CTAs fit per SM
-        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc2_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                      cudaSharedmemCarveoutMaxShared));
         ANN_CUDA(cudaFuncSetAttribute(chol_update_tc3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       kSmem3Bytes));
         attr = true;
@@ -670,19 +529,15 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
             ANN_CUDA(cudaGetDevice(&dev));
             ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         }
-        if(tiles > (unsigned)sms) {
-            // more than a wave: persistent CTAs, the epilogue of one tile under the MMAs of the
-            // next. A few SMs stay free for the next panel (potrf32 / trsm32 on the side stream),
-            // which otherwise only gets the resources left beside the persistent CTAs and runs
-            // several times slower; the panel is the critical path of the factorisation.
-            const int reserve = std::min(tuning_get(key_chol_reserve(n), 32), sms / 2);
-            chol_update_tc3_kernel<<<(unsigned)(sms - reserve), 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
-            check_launch("chol_update_tc3_kernel");
-        } else {
-            // up to a wave: one tile per CTA, two CTAs per SM
-            chol_update_tc2_kernel<<<tiles, 128, kSmem2Bytes, st>>>(pmap, amap, a);
-            check_launch("chol_update_tc2_kernel");
-        }
+        // More than a wave: persistent CTAs, the epilogue of one tile under the MMAs of the
+        // next; a few SMs stay free for the next panel (potrf32 / trsm32 on the side stream),
+        // which otherwise only gets the resources left beside the persistent CTAs and runs
+        // several times slower (the panel is the critical path of the factorisation). Up to
+        // a wave: one tile per CTA, still with the two-stage pipeline.
+        const int reserve = std::min(tuning_get(key_chol_reserve(n), 32), sms / 2);
+        const unsigned grid = tiles > (unsigned)sms ? (unsigned)(sms - reserve) : tiles;
+        chol_update_tc3_kernel<<<grid, 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
+        check_launch("chol_update_tc3_kernel");
         return;
     }
     chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(pmap, amap, a);
