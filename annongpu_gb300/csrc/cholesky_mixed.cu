@@ -327,69 +327,69 @@ struct IrState {
     double last;     // ... after the last one
 };
 
-// y_k = Dk b_k for the diagonal block (Dk = Dinv or DinvH of block kb): output c by one
-// warp with the 64-term dot split over lanes
-__device__ __forceinline__ void block_apply(const cf* __restrict__ Dk, const cf* __restrict__ bk, cf* y,
-                                            unsigned nb) {
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for(unsigned c = warp; c < NB; c += nw) {
-        cf acc = mk(0.f, 0.f);
-        cmac(acc, Dk[c * NB + lane], bk[lane]);
-        cmac(acc, Dk[c * NB + lane + 32], bk[lane + 32]);
-        acc = warp_sum(acc);
-        if(lane == 0) y[c] = c < nb ? acc : mk(0.f, 0.f);
-    }
-}
-
-// vectors that other CTAs of the solve update are read and written through L2
-__device__ __forceinline__ cf ld_l2(const cf* p) {
-    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
-    return mk(v.x, v.y);
-}
-__device__ __forceinline__ void st_l2(cf* p, cf v) { __stcg(reinterpret_cast<float2*>(p), make_float2(v.re, v.im)); }
-
 __device__ __forceinline__ unsigned long long gtime() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
 
-constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait on a ready flag
+constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s per wait on a solution block
 constexpr int kSolveThreads = 512;
+constexpr size_t kSolveSyncHead = 16;  // abort flag, padded to the 16-byte alignment of the tagged blocks
 
-// Waits (thread 0 of the CTA) until flag != 0. Bounded: after kWaitNs it raises
-// kStatusTimeout and the abort flag; every CTA of the solve then stops waiting.
-// Returns false when the solve is being abandoned.
-__device__ bool wait_flag(const int* flag, int* abort_flag, unsigned* status) {
-    __shared__ int ok;
-    if(threadIdx.x == 0) {
-        ok = 1;
-        const volatile int* vf = flag;
-        const volatile int* va = abort_flag;
-        const unsigned long long t0 = gtime();
-        while(*vf == 0) {
-            if(*va) { ok = 0; break; }
-            if(gtime() - t0 > kWaitNs) {
-                atomicExch(abort_flag, 1);
-                atomicOr(status, kStatusTimeout);
-                ok = 0;
-                break;
+// Solution blocks pass between the CTAs of a solve as self-validating words: one
+// 64-bit word per float holds its bits in the low half and a ready tag in the high
+// half (the "low-latency" protocol of NCCL's LL transport). A 64-bit access is
+// single-copy atomic, so a reader that sees the tag also sees the value: a block
+// reaches its consumers in one L2 round trip, with no fence and no separate flag
+// to poll. The buffers are zeroed (tag 0) before every launch.
+constexpr unsigned long long kReadyTag = 1ull << 32;
+
+__device__ __forceinline__ void st_ll(ulonglong2* p, cf v) {
+    const unsigned long long w0 = kReadyTag | __float_as_uint(v.re);
+    const unsigned long long w1 = kReadyTag | __float_as_uint(v.im);
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(w0), "l"(w1) : "memory");
+}
+
+__device__ __forceinline__ bool ld_ll(const ulonglong2* p, cf& v) {
+    unsigned long long w0, w1;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(p) : "memory");
+    v = mk(__uint_as_float((unsigned)w0), __uint_as_float((unsigned)w1));
+    return (w0 >> 32) == 1ull && (w1 >> 32) == 1ull;
+}
+
+// Thread t < NB reads entry t of a published solution block into v[t], waiting until
+// it carries the ready tag. Bounded: after kWaitNs the thread raises kStatusTimeout
+// and the abort flag, and every CTA of the solve gives up at its next wait. Returns
+// false, for the whole CTA, when the solve is being abandoned; on true, v is
+// visible to every thread of the CTA.
+__device__ bool wait_block(const ulonglong2* blk, cf* v, int* abort_flag, unsigned* status) {
+    int bad = 0;
+    const unsigned t = threadIdx.x;
+    if(t < NB) {
+        cf val;
+        if(!ld_ll(blk + t, val)) {
+            const unsigned long long t0 = gtime();
+            for(unsigned it = 1;; it++) {
+                if(ld_ll(blk + t, val)) break;
+                if((it & 15u) == 0) {
+                    if(*(volatile int*)abort_flag) { bad = 1; break; }
+                    if(gtime() - t0 > kWaitNs) {
+                        atomicExch(abort_flag, 1);
+                        atomicOr(status, kStatusTimeout);
+                        bad = 1;
+                        break;
+                    }
+                }
             }
         }
-        __threadfence();
+        v[t] = val;
     }
-    __syncthreads();
-    return ok != 0;
+    return __syncthreads_or(bad) == 0;
 }
 
-// publishes a block of the solution: the CTA's stores, then its ready flag
-__device__ __forceinline__ void set_flag(int* flag) {
-    __threadfence();
-    __syncthreads();
-    if(threadIdx.x == 0) atomicExch(flag, 1);
-}
-
-// y = D x for a diagonal block held in shared memory (D[c][p], row-major)
+// y = D x for a diagonal block held in shared memory (D[c][p], row-major): output c
+// by one warp with the 64-term dot split over lanes
 __device__ __forceinline__ void block_apply_sm(const cf (*D)[NB], const cf* __restrict__ x, cf* y, unsigned nb) {
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for(unsigned c = warp; c < NB; c += nw) {
@@ -403,25 +403,26 @@ __device__ __forceinline__ void block_apply_sm(const cf (*D)[NB], const cf* __re
 
 // b <- (L L^H)^{-1} b in one cooperative launch without grid barriers. CTA g owns the
 // block rows j = g, g + G, ... (G CTAs, all resident). Forward: y_j = L_jj^{-1} (b_j -
-// sum_{k<j} L_jk y_k), adding each y_k as soon as its ready flag is set. Backward:
+// sum_{k<j} L_jk y_k), adding each y_k as soon as it is published. Backward:
 // x_j = L_jj^{-H} (y_j - sum_{k>j} L_kj^H x_k), blocks taken from the last. Every
 // thread adds its contributions in a fixed order, so the result is bit-reproducible.
-// The critical path is the chain of ready flags, so everything that does not depend
-// on the awaited block (the next L block, the inverted diagonal block) is loaded
-// before the wait.
-// flags: [nblk] forward ready, [nblk] backward ready, [1] abort; zero on entry.
+// The critical path is the chain of published blocks, so everything that does not
+// depend on the awaited block (the next L block, the inverted diagonal block) is
+// loaded before the wait; the awaited block lands in one of two shared buffers in
+// turn, so one barrier per block suffices.
+// ll: [nblk * NB] forward blocks y, then [nblk * NB] backward blocks x, as tagged
+// words; abort_flag: one int. All zero on entry. Entries past n are published as 0.
 __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __restrict__ A,
                                                                    const cf* __restrict__ Dinv,
                                                                    const cf* __restrict__ DinvH, unsigned n, cf* b,
-                                                                   cf* y, const IrState* irs, int* flags,
-                                                                   unsigned* status) {
+                                                                   ulonglong2* ll, const IrState* irs,
+                                                                   int* abort_flag, unsigned* status) {
     if(irs->done) return;
-    __shared__ cf v[NB], z[NB], red[8][NB];
+    __shared__ cf v[2][NB], w[NB], z[NB], red[8][NB];
     __shared__ cf D[NB][NB];
     const unsigned nblk = (n + NB - 1) / NB;
-    int* fwd_ready = flags;
-    int* bwd_ready = flags + nblk;
-    int* abort_flag = flags + 2 * nblk;
+    ulonglong2* yl = ll;
+    ulonglong2* xl = ll + (size_t)nblk * NB;
     const unsigned t = threadIdx.x;
     // forward: thread t sums row r = t / 8 of the block, columns 8 (t % 8) .. + 7 of each L_jk
     for(unsigned j = blockIdx.x; j < nblk; j += gridDim.x) {
@@ -443,14 +444,12 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
 #pragma unroll
                 for(int q = 0; q < 8; q++) Ln[q] = Lrow[(k + 1) * NB + q];
             }
-            if(!wait_flag(fwd_ready + k, abort_flag, status)) return;
-            if(t < NB) v[t] = ld_l2(y + k * NB + t);
-            __syncthreads();
+            cf* vk = v[k & 1u];
+            if(!wait_block(yl + (size_t)k * NB, vk, abort_flag, status)) return;
             if(r < nbj) {
 #pragma unroll
-                for(int q = 0; q < 8; q++) cmac(acc, Lc[q], v[s8 + q]);
+                for(int q = 0; q < 8; q++) cmac(acc, Lc[q], vk[s8 + q]);
             }
-            __syncthreads();
         }
         // the 8 partial sums of row r are in lanes 8 (r % 4) .. + 7 of one warp
 #pragma unroll
@@ -458,17 +457,17 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
             acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
             acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
         }
-        if((t & 7u) == 0 && r < NB) v[r] = r < nbj ? b[jb + r] - acc : mk(0.f, 0.f);
+        if((t & 7u) == 0 && r < NB) w[r] = r < nbj ? b[jb + r] - acc : mk(0.f, 0.f);
         __syncthreads();
-        block_apply_sm(D, v, z, nbj);
+        block_apply_sm(D, w, z, nbj);
         __syncthreads();
-        if(t < nbj) st_l2(y + jb + t, z[t]);
-        set_flag(fwd_ready + j);
+        if(t < NB) st_ll(yl + jb + t, z[t]);
     }
     // backward: thread t sums column c = t % 64 of L_kj^H over rows q = 8 (t / 64) .. + 7
     for(int jj = (int)nblk - 1 - (int)blockIdx.x; jj >= 0; jj -= (int)gridDim.x) {
         const unsigned j = (unsigned)jj, jb = j * NB, nbj = min((unsigned)NB, n - jb);
         const unsigned c = t & 63u, q8 = (t >> 6) * 8u;
+        __syncthreads();  // the previous block's reads of D, w and red are done
         for(unsigned q = t; q < NB * NB; q += blockDim.x) D[q / NB][q % NB] = DinvH[(size_t)j * NB * NB + q];
         cf acc = mk(0.f, 0.f);
         // L[kb + q8 + q][jb + c] of block k, rows past n read as zero
@@ -485,28 +484,28 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
 #pragma unroll
             for(int q = 0; q < 8; q++) Lc[q] = Ln[q];
             if(k - 1 > j) load_col(k - 1, Ln);
-            if(!wait_flag(bwd_ready + k, abort_flag, status)) return;
-            const unsigned kb = k * NB, nbk = min((unsigned)NB, n - kb);
-            if(t < NB) v[t] = t < nbk ? ld_l2(b + kb + t) : mk(0.f, 0.f);
-            __syncthreads();
+            cf* vk = v[k & 1u];
+            if(!wait_block(xl + (size_t)k * NB, vk, abort_flag, status)) return;
 #pragma unroll
-            for(int q = 0; q < 8; q++) cmac_conj(acc, Lc[q], v[q8 + q]);
-            __syncthreads();
+            for(int q = 0; q < 8; q++) cmac_conj(acc, Lc[q], vk[q8 + q]);
         }
         red[t >> 6][c] = acc;
-        // y_j is final once the forward pass published it
-        if(!wait_flag(fwd_ready + j, abort_flag, status)) return;
+        // y_j, published by the forward pass (w as the landing buffer: its last reader,
+        // the block_apply of the forward pass or of the previous block, is past a barrier)
+        if(!wait_block(yl + jb, w, abort_flag, status)) return;
         if(t < NB) {
             cf sum = mk(0.f, 0.f);
 #pragma unroll
             for(int g = 0; g < 8; g++) sum += red[g][t];
-            v[t] = t < nbj ? ld_l2(y + jb + t) - sum : mk(0.f, 0.f);
+            z[t] = t < nbj ? w[t] - sum : mk(0.f, 0.f);
         }
         __syncthreads();
-        block_apply_sm(D, v, z, nbj);
+        block_apply_sm(D, z, w, nbj);
         __syncthreads();
-        if(t < nbj) st_l2(b + jb + t, z[t]);
-        set_flag(bwd_ready + j);
+        if(t < NB) {
+            st_ll(xl + jb + t, w[t]);
+            if(t < nbj) b[jb + t] = w[t];
+        }
     }
 }
 
@@ -673,10 +672,10 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
     check_launch("diag_inv_kernel");
 }
 
-// b <- (L L^H)^{-1} b; tmp (n entries) holds y = L^{-1} b; flags (2 nblk + 1 ints) are
-// cleared before the launch
-void solve32(const cf* A, const cf* Dinv, const cf* DinvH, unsigned n, cf* b, cf* tmp, const IrState* irs,
-             int* flags, unsigned* status, cudaStream_t st) {
+// b <- (L L^H)^{-1} b; sync holds the abort flag (16 bytes) and the tagged solution
+// blocks (2 nblk NB 16-byte entries), cleared before the launch
+void solve32(const cf* A, const cf* Dinv, const cf* DinvH, unsigned n, cf* b, const IrState* irs, int* sync,
+             unsigned* status, cudaStream_t st) {
     static int resident = 0;  // CTAs of trsv_flags_kernel that fit on the GPU at once
     if(!resident) {
         int dev = 0, sms = 0, per_sm = 0;
@@ -688,18 +687,19 @@ void solve32(const cf* A, const cf* Dinv, const cf* DinvH, unsigned n, cf* b, cf
     }
     const unsigned nblk = (n + NB - 1) / NB;
     const unsigned grid = std::min<unsigned>(nblk, (unsigned)resident);
-    ANN_CUDA(cudaMemsetAsync(flags, 0, (2 * (size_t)nblk + 1) * sizeof(int), st));
+    ANN_CUDA(cudaMemsetAsync(sync, 0, kSolveSyncHead + 2 * (size_t)nblk * NB * sizeof(ulonglong2), st));
+    ulonglong2* ll = reinterpret_cast<ulonglong2*>(reinterpret_cast<char*>(sync) + kSolveSyncHead);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kSolveThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident: the flag waits can be met
+    attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident: the waits can be met
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    ANN_CUDA(cudaLaunchKernelEx(&cfg, trsv_flags_kernel, A, Dinv, DinvH, n, b, tmp, irs, flags, status));
+    ANN_CUDA(cudaLaunchKernelEx(&cfg, trsv_flags_kernel, A, Dinv, DinvH, n, b, ll, irs, sync, status));
     check_launch("trsv_flags_kernel");
 }
 
@@ -715,9 +715,11 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     td.Dinv32.ensure(2 * (size_t)nblk * NB * NB * sizeof(cf));
     td.delta.ensure(n * sizeof(zc));
     td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
-    td.c32.ensure(2 * (size_t)n * sizeof(cf));
+    td.c32.ensure((size_t)n * sizeof(cf));
     const unsigned res_blocks = (n + 7) / 8;
-    td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double) + (2 * (size_t)nblk + 2) * sizeof(int));
+    static_assert(sizeof(IrState) % 16 == 0, "the solve's tagged blocks need 16-byte alignment");
+    td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double) + kSolveSyncHead +
+                 2 * (size_t)nblk * NB * sizeof(ulonglong2));
     cf* A = td.L32.as<cf>();
     cf* Dinv = td.Dinv32.as<cf>();
     cf* DinvH = Dinv + (size_t)nblk * NB * NB;
@@ -726,7 +728,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     cf* c = td.c32.as<cf>();
     IrState* irs = td.ir.as<IrState>();
     double* part = reinterpret_cast<double*>(irs + 1);
-    int* flags = reinterpret_cast<int*>(part + 2 * (size_t)res_blocks);
+    int* sync = reinterpret_cast<int*>(part + 2 * (size_t)res_blocks);
     const zc* S = td.S.as<zc>();
     const zc* F = td.F.as<zc>();
 
@@ -743,7 +745,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     cholesky32(td, A, n, Dinv, DinvH, pivots_to_status ? status : &irs->notpd, st);
     solve_mark(1, st);
     for(unsigned it = 0; it < max_iter; it++) {
-        solve32(A, Dinv, DinvH, n, c, c + n, irs, flags, status, st);
+        solve32(A, Dinv, DinvH, n, c, irs, sync, status, st);
         ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs);
         check_launch("ir_axpy_kernel");
         ir_residual_kernel<<<res_blocks, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs);
