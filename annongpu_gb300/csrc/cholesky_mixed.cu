@@ -47,23 +47,22 @@ __global__ void cvt_shift_kernel(const zc* __restrict__ S, cf* __restrict__ A, u
 
 // Cholesky of the nb x nb diagonal block at (kb, kb), factor only (the critical path of
 // the factorisation; the inverses of the diagonal blocks are formed afterwards by
-// diag_inv_kernel). Right-looking on the block in shared memory with the pivots left
-// unscaled: per column j every lower entry (r, c), j < c <= r, takes
-//   a_rc -= a_rj conj(a_cj) / a_jj,
-// the entries enumerated column-major so that the work of column j is one contiguous
-// suffix split evenly over the threads; one barrier per column. At the end
-// L_rc = a_rc / sqrt(a_cc) (r > c), L_cc = sqrt(a_cc).
-constexpr int kPotrfThreads = 512;
-constexpr int kTri = NB * (NB + 1) / 2;  // lower-triangle entries of a block
+// diag_inv_kernel). Blocked in four 16-column panels on the block held in shared
+// memory. A panel (rows kk.. of columns kk..kk+15) is factorised in registers with
+// one row per lane: lanes 0-15 of every warp hold the 16 diagonal rows (each warp
+// factorises them redundantly, so no warp waits on another) and lanes 16-31 hold 16 of
+// the rows below. Column j of the panel is then
+//   l_jj = sqrt(a_jj), l_rj = a_rj / l_jj, a_rc -= l_rj conj(l_cj) (c = j+1..15),
+// with l_cj broadcast by shuffle from lane c. The 16-column trailing update of the rest
+// of the block runs on all threads in 2 x 2 register tiles; two barriers per panel.
+constexpr int kPotrfThreads = 256;
+constexpr int kPw = 16;  // panel width
 
 __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
                                                                 unsigned* status) {
     __shared__ cf a[NB][NB + 1];
-    __shared__ uint16_t pr[kTri];      // (c << 8) | r, column-major
-    __shared__ unsigned short off[NB + 1];
-    __shared__ float piv[NB];
     const unsigned nb = min((unsigned)NB, n - kb);
-    const unsigned tid = threadIdx.x;
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     {
         cf v[NB * NB / kPotrfThreads];
 #pragma unroll
@@ -77,34 +76,76 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__
             a[t / NB][t % NB] = v[q];
         }
     }
-    if(tid <= NB) off[tid] = (unsigned short)(tid * NB - tid * (tid - 1) / 2);  // first entry of column tid
-    if(tid < NB) {
-        const unsigned c = tid, o = c * NB - c * (c - 1) / 2;
-        for(unsigned r = c; r < NB; r++) pr[o + r - c] = (uint16_t)((c << 8) | r);
-    }
     __syncthreads();
-    for(unsigned j = 0; j < NB; j++) {
-        float d = a[j][j].re;
-        if(!(d > 0.f) || !isfinite(d)) {
-            if(tid == 0) atomicOr(status, kStatusNotPosDef);
-            d = 1.f;
-        }
-        if(tid == 0) piv[j] = d;
-        const float id = 1.f / d;
-        for(unsigned t = off[j + 1] + tid; t < (unsigned)kTri; t += kPotrfThreads) {
-            const unsigned c = pr[t] >> 8, r = pr[t] & 255u;
-            cf v = a[r][c];
-            cmac_conj(v, a[c][j], -(id * a[r][j]));  // -= a_rj conj(a_cj) / a_jj
-            a[r][c] = v;
+#pragma unroll 1
+    for(unsigned kk = 0; kk < NB; kk += kPw) {
+        const unsigned below = NB - kk - kPw;                       // rows under the panel's diagonal block
+        const unsigned nwp = below ? (below + kPw - 1) / kPw : 1u;  // warps on the panel
+        if(warp < nwp) {
+            // lane < 16: diagonal row kk + lane; lane >= 16: row kk + 16 + 16 warp + lane - 16
+            const bool diag = lane < kPw;
+            const unsigned r = diag ? kk + lane : kk + kPw + warp * kPw + (lane - kPw);
+            const bool live = r < NB;
+            cf x[kPw];
+#pragma unroll
+            for(int c = 0; c < kPw; c++) x[c] = live ? a[r][kk + c] : mk(0.f, 0.f);
+#pragma unroll
+            for(int j = 0; j < kPw; j++) {
+                float d = __shfl_sync(0xffffffffu, x[j].re, j);
+                if(!(d > 0.f) || !isfinite(d)) {
+                    if(tid == 0) atomicOr(status, kStatusNotPosDef);
+                    d = 1.f;
+                }
+                const float s = sqrtf(d), inv = __frcp_rn(s);
+                if(diag && lane == (unsigned)j) x[j] = mk(s, 0.f);
+                else x[j] = inv * x[j];
+#pragma unroll
+                for(int c = 1; c < kPw; c++) {  // constant bounds, so that both loops unroll
+                    if(c <= j) continue;
+                    cf l;
+                    l.re = __shfl_sync(0xffffffffu, x[j].re, c);
+                    l.im = __shfl_sync(0xffffffffu, x[j].im, c);
+                    if(!diag || lane >= (unsigned)c) cmac_conj(x[c], l, -x[j]);  // -= l_rj conj(l_cj)
+                }
+            }
+            if(live && (!diag || warp == 0)) {
+#pragma unroll
+                for(int c = 0; c < kPw; c++)
+                    if(!diag || (unsigned)c <= lane) a[r][kk + c] = x[c];
+            }
         }
         __syncthreads();
-    }
-    for(unsigned t = tid; t < (unsigned)kTri; t += kPotrfThreads) {
-        const unsigned c = pr[t] >> 8, r = pr[t] & 255u;
-        if(r < nb) {
-            const float sc = sqrtf(piv[c]);
-            A[(size_t)(kb + r) * n + kb + c] = r == c ? mk(sc, 0.f) : (1.f / sc) * a[r][c];
+        if(below) {
+            // a_rc -= sum_p l_rp conj(l_cp) for kk + 16 <= c <= r < NB, in 2 x 2 tiles
+            const unsigned t2 = below / 2, tiles = t2 * (t2 + 1) / 2, base = kk + kPw;
+            for(unsigned q = tid; q < tiles; q += kPotrfThreads) {
+                // tile q -> (ti, tj), tj <= ti, row-major over the lower triangle of tiles
+                unsigned ti = (unsigned)((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
+                while(ti * (ti + 1) / 2 > q) ti--;
+                while((ti + 1) * (ti + 2) / 2 <= q) ti++;
+                const unsigned tj = q - ti * (ti + 1) / 2;
+                const unsigned r0 = base + 2 * ti, c0 = base + 2 * tj;
+                cf s00 = mk(0.f, 0.f), s01 = s00, s10 = s00, s11 = s00;
+#pragma unroll
+                for(int p = 0; p < kPw; p++) {
+                    const cf xr0 = a[r0][kk + p], xr1 = a[r0 + 1][kk + p];
+                    const cf xc0 = a[c0][kk + p], xc1 = a[c0 + 1][kk + p];
+                    cmac_conj(s00, xc0, xr0);
+                    cmac_conj(s01, xc1, xr0);
+                    cmac_conj(s10, xc0, xr1);
+                    cmac_conj(s11, xc1, xr1);
+                }
+                a[r0][c0] = a[r0][c0] - s00;
+                if(ti != tj) a[r0][c0 + 1] = a[r0][c0 + 1] - s01;
+                a[r0 + 1][c0] = a[r0 + 1][c0] - s10;
+                a[r0 + 1][c0 + 1] = a[r0 + 1][c0 + 1] - s11;
+            }
+            __syncthreads();
         }
+    }
+    for(unsigned t = tid; t < NB * NB; t += kPotrfThreads) {
+        const unsigned r = t / NB, c = t % NB;
+        if(r < nb && c <= r) A[(size_t)(kb + r) * n + kb + c] = a[r][c];
     }
 }
 
