@@ -582,7 +582,7 @@ def run_ours(args):
         # the dominant kernel group of the step: trailing updates + panel path are about half
         # of the launch list (the S kernel 14 %)
         out["roofline"] = {"bound": "tensor",
-                           "kernel": "FP32 Cholesky factorisation (chol_update_tc3/tc2 tcgen05 split-TF32 trailing "
+                           "kernel": "FP32 Cholesky factorisation (chol_update_tc3 tcgen05 split-TF32 trailing "
                                      "updates + potrf32/trsm32 panel path)",
                            "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
                            "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
