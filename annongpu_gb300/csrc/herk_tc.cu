@@ -38,7 +38,8 @@ constexpr int kRowsPerBlock = 2 * kBM;      // Re + Im rows of one parameter blo
 constexpr int kBK = 64;                     // samples per K step (128 bytes of BF16)
 constexpr int kStages = 3;
 constexpr int kStageBytes = 2 * kRowsPerBlock * kBK * 2;  // A block + B block
-constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr int kTailBytes = 128 + kBM * 8;  // mbarriers, TMEM slot, abort flag | mu_J in FP32
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + kTailBytes;
 struct HerkArgs {
     unsigned Np;            // parameters
     unsigned nblk;          // parameter blocks of 128
@@ -50,6 +51,30 @@ struct HerkArgs {
     cplx<double>* S;
     unsigned* status;
 };
+
+// Exact FP32 -> FP64 widening in integer arithmetic (sign, exponent rebias 127 -> 1023,
+// mantissa shifted to 52 bits; subnormals renormalised; infinities and NaNs kept).
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    uint64_t bits;
+    if(e != 0u && e != 0xFFu) {
+        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    } else if(e == 0xFFu) {
+        bits = sign | (0x7FFull << 52) | ((uint64_t)m << 29);
+    } else if(m == 0u) {
+        bits = sign;
+    } else {
+        const uint32_t p = 31u - __clz(m);  // top set bit: value = 1.f * 2^(p - 149)
+        bits = sign | ((uint64_t)(p + 874u) << 52) | ((uint64_t)(m ^ (1u << p)) << (52u - p));
+    }
+    return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ void store_widened(cplx<double>* p, float re, float im) {
+    *reinterpret_cast<double2*>(p) = make_double2(widen(re), widen(im));
+}
 
 // lower block triangle (I >= J) from the linear CTA index
 __device__ __forceinline__ void tile_of(unsigned b, unsigned& I, unsigned& J) {
@@ -69,6 +94,7 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
     uint64_t* done = empty + kStages;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    cplx<float>* obar_j = reinterpret_cast<cplx<float>*>(tail + 128);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned I, J;
@@ -83,6 +109,11 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    {
+        // Obar of the tile's columns in FP32 for the epilogue (its only use there)
+        const unsigned l = J * kBM + threadIdx.x;
+        obar_j[threadIdx.x] = l < a.Np ? cvt<float>(a.Obar[l]) : mk(0.f, 0.f);
     }
     __syncwarp();
     if(warp == 0) {
@@ -141,13 +172,17 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
     ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if(ok) {
+        // FP32 arithmetic and an integer widening to FP64: the FP64 pipe (1/64 of the FP32
+        // rate on this GPU) would otherwise hold the SM for a third of the tile's time.
+        // The accumulators are FP32 sums of K products, so rounding Re S = rr + ii once
+        // more in FP32 is below their own rounding.
         const double W = a.stats->W;
         const double corr = 1.0 / W - 1.0;
         const unsigned i = warp * 32 + lane;  // TMEM lane = row of the tile
         const unsigned k = I * kBM + i;       // parameter of the row
         const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
         const bool row_ok = k < a.Np;
-        const cplx<double> ok_conj = row_ok ? conj(a.Obar[k]) : mk(0.0, 0.0);
+        const cplx<float> ok_c = row_ok ? cvt<float>(corr * conj(a.Obar[k])) : mk(0.f, 0.f);
         for(int c0 = 0; c0 < kBM; c0 += 16) {
             float rr[16], ri[16], ir[16], ii[16];
             tmem_ld16(lane_addr + c0, rr);
@@ -159,10 +194,14 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
             for(int q = 0; q < 16; q++) {
                 const unsigned l = J * kBM + c0 + q;
                 if(l >= a.Np) continue;
-                cplx<double> v = mk((double)rr[q] + (double)ii[q], (double)ri[q] - (double)ir[q]);
-                v = v + corr * (ok_conj * a.Obar[l]);
-                a.S[(size_t)k * a.Np + l] = v;
-                if(I != J) a.S[(size_t)l * a.Np + k] = conj(v);
+                const cplx<float> ob = obar_j[c0 + q];
+                float vr = rr[q] + ii[q], vi = ri[q] - ir[q];
+                vr = fmaf(ok_c.re, ob.re, vr);
+                vr = fmaf(-ok_c.im, ob.im, vr);
+                vi = fmaf(ok_c.re, ob.im, vi);
+                vi = fmaf(ok_c.im, ob.re, vi);
+                store_widened(a.S + (size_t)k * a.Np + l, vr, vi);
+                if(I != J) store_widened(a.S + (size_t)l * a.Np + k, vr, -vi);
             }
         }
     } else if(warp == 0 && lane == 0) {
