@@ -160,6 +160,39 @@ __host__ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
 
 // ---------------------------------------------------------------------------------
 // warp reductions (xor butterflies leave the bit-identical sum in every lane)
+// Round-to-nearest-even FP64 -> FP32 in integer arithmetic (subnormal results rounded
+// at their own precision, overflow to infinity, NaN kept as NaN): the same value as
+// cvt.rn.f32.f64, without the FP64 pipe, which runs at 1/64 of the FP32 rate on GB300.
+__device__ __forceinline__ float narrow(double d) {
+    const uint64_t b = (uint64_t)__double_as_longlong(d);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint32_t E = (uint32_t)(b >> 52) & 0x7FFu;
+    const uint64_t M = b & 0xFFFFFFFFFFFFFull;
+    uint32_t r;
+    if(E == 0x7FFu) {
+        r = 0x7F800000u | (M ? (0x400000u | (uint32_t)(M >> 29)) : 0u);
+    } else {
+        const int e = (int)E - 1023;
+        if(e > 127) {
+            r = 0x7F800000u;
+        } else if(e >= -126) {
+            const uint32_t m23 = (uint32_t)(M >> 29), rem = (uint32_t)(M & 0x1FFFFFFFu);
+            r = ((uint32_t)(e + 127) << 23) | m23;
+            r += (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) ? 1u : 0u;  // carries into the exponent
+        } else {
+            const int sh = -97 - e;  // bits of the 53-bit significand below the subnormal's last place
+            if(sh > 54 || E == 0u) {
+                r = 0u;
+            } else {
+                const uint64_t sig = M | (1ull << 52);
+                const uint64_t q = sig >> sh, rm = sig & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+                r = (uint32_t)q + ((rm > half || (rm == half && (q & 1ull))) ? 1u : 0u);
+            }
+        }
+    }
+    return __uint_as_float(r | sign);
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

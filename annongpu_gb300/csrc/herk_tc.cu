@@ -20,6 +20,8 @@
 // Every wait on an mbarrier is bounded (globaltimer deadline); a timeout sets
 // kStatusTimeout, makes all roles leave their loops, waits (bounded) for the
 // copies in flight and frees the tensor memory before returning.
+#include <algorithm>
+
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -217,25 +219,33 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
     if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
+// Per-sample sqrt(w_s) and per-parameter mu_k = Obar_k / W, once per S in FP64 and rounded
+// to FP32 (the values the operand prep used to form per CTA, where the FP64 square root and
+// division, at 1/64 of the FP32 rate, cost more than the tile's loads). Entries past the
+// samples / parameters are zero.
+__global__ void herk_consts_kernel(size_t rows, size_t ns_pad, unsigned Np, unsigned np_pad,
+                                   const double* __restrict__ wts, double w0, const cplx<double>* __restrict__ Obar,
+                                   const Stats* __restrict__ stats, float* __restrict__ sw_all,
+                                   cplx<float>* __restrict__ mu_all) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < ns_pad) sw_all[i] = i < rows ? (float)sqrt(wts ? wts[i] : w0) : 0.f;
+    if(i < np_pad) mu_all[i] = i < Np ? cvt<float>((1.0 / stats->W) * Obar[i]) : mk(0.f, 0.f);
+}
+
 // XT[row][col] (BF16): row = 256 * (k / 128) + (k % 128) for Re, + 128 for Im;
 // col = sample (hi copy) and lo_offset + sample (lo copy, split mode).
 template<typename T>
 __global__ void __launch_bounds__(256)
-herk_prep_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned Np, const double* __restrict__ wts,
-                 double w0, const cplx<double>* __restrict__ Obar, const Stats* __restrict__ stats,
-                 __nv_bfloat16* __restrict__ XT, size_t ldx, unsigned lo_offset, int split) {
+herk_prep_kernel(const cplx<T>* __restrict__ O, size_t rows, size_t ld, unsigned Np, const float* __restrict__ sw_all,
+                 const cplx<float>* __restrict__ mu_all, __nv_bfloat16* __restrict__ XT, size_t ldx,
+                 unsigned lo_offset, int split) {
     __shared__ cplx<float> tile[64][65];
     __shared__ float sw[64];          // sqrt(w_s) of the tile's rows
     __shared__ cplx<float> mu[64];    // Obar_k / W of the tile's columns
     const size_t s0 = (size_t)blockIdx.y * 64;
     const unsigned k0 = blockIdx.x * 64;
-    if(threadIdx.x < 64) {
-        const size_t s = s0 + threadIdx.x;
-        sw[threadIdx.x] = s < rows ? (float)sqrt(wts ? wts[s] : w0) : 0.f;
-    } else if(threadIdx.x < 128) {
-        const unsigned c = threadIdx.x - 64, k = k0 + c;
-        mu[c] = k < Np ? cvt<float>((1.0 / stats->W) * Obar[k]) : mk(0.f, 0.f);
-    }
+    if(threadIdx.x < 64) sw[threadIdx.x] = sw_all[s0 + threadIdx.x];
+    else if(threadIdx.x < 128) mu[threadIdx.x - 64] = mu_all[k0 + threadIdx.x - 64];
     __syncthreads();
     // per element in FP32: the centring and scaling feed BF16 operands
     for(int q = threadIdx.x; q < 64 * 64; q += 256) {
@@ -278,17 +288,24 @@ void herk_tc(ann_tdvp_impl& td, const double* wts, double w0, bool split, cudaSt
     const size_t rows_x = (size_t)nblk * kRowsPerBlock;
     const size_t ns_pad = (td.n_rows + kBK - 1) / kBK * kBK;
     const size_t ldx = split ? 2 * ns_pad : ns_pad;
-    td.herk_in.ensure(rows_x * ldx * sizeof(__nv_bfloat16));
+    // operand XT, then sqrt(w) per padded sample and mu per parameter slot (FP32)
+    const size_t np_pad = (size_t)nblk * kBM;
+    const size_t xt_bytes = rows_x * ldx * sizeof(__nv_bfloat16);  // a multiple of 128
+    td.herk_in.ensure(xt_bytes + ns_pad * sizeof(float) + np_pad * sizeof(cplx<float>));
+    auto* XT = td.herk_in.as<__nv_bfloat16>();
+    float* sw_all = reinterpret_cast<float*>(td.herk_in.as<unsigned char>() + xt_bytes);
+    auto* mu_all = reinterpret_cast<cplx<float>*>(sw_all + ns_pad);  // ns_pad is a multiple of 64
+    if(td.O_precision != 0) throw Error(ANN_ERR_UNSUPPORTED, "tensor-core S takes complex64 rows");
+    const size_t nc = std::max(ns_pad, np_pad);
+    herk_consts_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(td.n_rows, ns_pad, Np, (unsigned)np_pad, wts, w0,
+                                                                       td.Obar.as<cplx<double>>(),
+                                                                       td.stats.as<Stats>(), sw_all, mu_all);
+    check_launch("herk_consts_kernel");
     // the grid covers every parameter slot of the nblk blocks and every padded sample, so
     // the padding (parameters >= Np, samples >= rows) is written as zero by the kernel
     dim3 pg(2 * nblk, (unsigned)(ns_pad / 64));
-    auto* XT = td.herk_in.as<__nv_bfloat16>();
-    if(td.O_precision == 0)
-        herk_prep_kernel<float><<<pg, 256, 0, st>>>(td.O.as<cplx<float>>(), td.n_rows, td.ldO, Np, wts, w0,
-                                                     td.Obar.as<cplx<double>>(), td.stats.as<Stats>(), XT, ldx,
-                                                     (unsigned)ns_pad, split ? 1 : 0);
-    else
-        throw Error(ANN_ERR_UNSUPPORTED, "tensor-core S takes complex64 rows");
+    herk_prep_kernel<float><<<pg, 256, 0, st>>>(td.O.as<cplx<float>>(), td.n_rows, td.ldO, Np, sw_all, mu_all, XT,
+                                                 ldx, (unsigned)ns_pad, split ? 1 : 0);
     check_launch("herk_prep_kernel");
 
     CUtensorMap map;
