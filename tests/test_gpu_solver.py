@@ -72,6 +72,34 @@ def test_mixed_solver_matches_numpy_on_gpu_S(N, M, update):
     np.testing.assert_allclose(d_mixed, d_fp64, rtol=1e-8, atol=1e-9 * np.abs(d_fp64).max())
 
 
+def test_mixed_solver_more_block_rows_than_resident_ctas():
+    """Np = 80 + 120 + 9600 = 9800: 154 block rows of 64, more than the triangular
+    solves' cooperative launch holds at one CTA per SM on a 152-SM GPU, so CTAs own
+    several block rows (the hand-off of solution blocks between rounds). The residual is
+    checked on the host in FP64 as well as on the device, and the solution against the
+    FP64 Cholesky solve."""
+    N, M = 80, 120
+    rng = np.random.default_rng(5)
+    a, b, W = cplx(rng, N, 0.01), cplx(rng, M, 0.01), cplx(rng, (N, M), 0.01)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    assert psi.num_params == 9800
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(16384, 2, 8, 16384, True, seed=13)
+    # the refinement count depends on the conditioning; the point here is the solves
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed", max_iter=10)
+    td.eval(op, psi, mc)
+    shift = 1e-3
+    d_mixed = td.solve(shift)
+    info = td.solver_info
+    assert not info["fell_back"] and info["residual_last"] <= 1e-12, info
+    S, F = td.S_matrix, td.F_vector
+    r = F - (S @ d_mixed + shift * d_mixed)
+    assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(F)
+    td.set_solver("fp64")
+    d_fp64 = td.solve(shift)
+    np.testing.assert_allclose(d_mixed, d_fp64, rtol=1e-8, atol=1e-9 * np.abs(d_fp64).max())
+
+
 def test_mixed_solver_stall_falls_back_to_fp64():
     """One FP32 solve cannot reach a residual of 1e-15: the eager solve is redone
     with the FP64 Cholesky and gives exactly its answer."""
