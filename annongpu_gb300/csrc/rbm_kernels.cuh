@@ -376,8 +376,10 @@ __device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, con
 
 // ---------------------------------------------------------------------------------
 // Metropolis sampler: one warp per chain.
+// complex64 chains with up to 128 hidden units: registers capped for three 8-warp CTAs per
+// SM (the sampler is latency-bound; the cap costs a few spilled words to L1)
 template<typename T, int NW, int U>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && U <= 4) ? 3 : 1)
 rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
