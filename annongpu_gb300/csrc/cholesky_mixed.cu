@@ -450,17 +450,22 @@ __device__ bool wait_block(const ulonglong2* blk, cf* v, int* abort_flag, unsign
     return __syncthreads_or(bad) == 0;
 }
 
-// y = D x for a diagonal block held in shared memory (D[c][p], row-major): output c
-// by one warp with the 64-term dot split over lanes
-__device__ __forceinline__ void block_apply_sm(const cf (*D)[NB], const cf* __restrict__ x, cf* y, unsigned nb) {
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for(unsigned c = warp; c < NB; c += nw) {
-        cf acc = mk(0.f, 0.f);
-        cmac(acc, D[c][lane], x[lane]);
-        cmac(acc, D[c][lane + 32], x[lane + 32]);
-        acc = warp_sum(acc);
-        if(lane == 0) y[c] = c < nb ? acc : mk(0.f, 0.f);
+// y = D x for a diagonal block held in shared memory (D[c][p], rows padded to kDs):
+// output c by eight threads (t = 8 c + part), part summing columns part, part + 8, ...,
+// then three shuffle levels; 512 threads. The padding (kDs = NB + 8) puts the two rows a
+// half-warp reads on different banks.
+constexpr int kDs = NB + 8;
+__device__ __forceinline__ void block_apply_sm(const cf (*D)[kDs], const cf* __restrict__ x, cf* y, unsigned nb) {
+    const unsigned c = threadIdx.x >> 3, part = threadIdx.x & 7u;
+    cf acc = mk(0.f, 0.f);
+#pragma unroll
+    for(int q = 0; q < NB / 8; q++) cmac(acc, D[c][part + 8 * q], x[part + 8 * q]);
+#pragma unroll
+    for(int o = 1; o < 8; o <<= 1) {
+        acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+        acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
     }
+    if(part == 0) y[c] = c < nb ? acc : mk(0.f, 0.f);
 }
 
 // b <- (L L^H)^{-1} b in one cooperative launch without grid barriers. CTA g owns the
@@ -481,7 +486,8 @@ __global__ void __launch_bounds__(kSolveThreads) trsv_flags_kernel(const cf* __r
                                                                    int* abort_flag, unsigned* status) {
     if(irs->done) return;
     __shared__ cf v[2][NB], w[NB], z[NB], red[8][NB];
-    __shared__ cf D[NB][NB];
+    __shared__ cf D[NB][kDs];
+    static_assert(kSolveThreads == 8 * NB, "block_apply_sm: eight threads per output");
     const unsigned nblk = (n + NB - 1) / NB;
     ulonglong2* yl = ll;
     ulonglong2* xl = ll + (size_t)nblk * NB;
