@@ -364,6 +364,23 @@ def timed_steps(form, args, stream, dist):
     return ms, phase, launches
 
 
+def whole_job(ms, ms_e2e, samples, tau, dist):
+    """Whole-job figures over the ranks (independent replicas, weak scaling): the step
+    times are the maximum over ranks, the effective samples per step the sum of each
+    rank's samples / tau_int. Returns (ms, ms_e2e, value, e2e_value)."""
+    eff = samples / tau
+    if dist:
+        import torch
+        import torch.distributed as td
+        dev = "cuda" if td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([ms, ms_e2e], dtype=torch.float64, device=dev)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        e = torch.tensor([eff], dtype=torch.float64, device=dev)
+        td.all_reduce(e, op=td.ReduceOp.SUM)
+        ms, ms_e2e, eff = float(t[0].item()), float(t[1].item()), float(e[0].item())
+    return ms, ms_e2e, eff / (ms * 1e-3), eff / (ms_e2e * 1e-3)
+
+
 def form_summary(form, ms, phase, tau, acc):
     Ns = N_CHAINS
     d = {"ms_per_step": ms, "ms_per_step_eager": getattr(form, "ms_eager", None), "sr_steps_per_s": 1e3 / ms,
@@ -549,8 +566,9 @@ def run_ours(args):
     flops_S = 4.0 * Np * (Np + 1) * Ns  # algorithmic HERK count per step
     s_tflops = flops_S / (phase[2] * 1e-3) / 1e12
     summary = form_summary(f, ms, phase, tau, acc)
+    ms, ms_e2e, value, e2e_value = whole_job(ms, ms_e2e, Ns, tau, dist)
     out = {
-        "metric": METRIC, "value": summary["effective_samples_per_s"], "unit": UNIT, "n_gpus": args.gpus,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": ("c64 sampling + learned proposal / bf16 S (fp32 acc) / fp32 Cholesky + f64 refinement"
@@ -568,7 +586,7 @@ def run_ours(args):
                           else None,
                           "work": "4*Np*(Np+1)*Ns real flops per step (over the S phase: operand prep + kernel)"},
         "clocks": clk,
-        "e2e": {"value": Ns / tau / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": Np * 16,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": Np * 16,
                 "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e},
         "gpu_launches": int(launches),
     }
