@@ -1266,7 +1266,8 @@ def activation_function(z, layer=0, activation="poly") -> complex:
 
 # ----------------------------------------------------------------------------------
 # autotuner (tuning.cu; this project's addition)
-_KNOBS = {0: "rbm_mc.wpb", 1: "stats.slab", 2: "chol.update", 3: "rbm_mc.wsmem", 4: "chol.reserve"}
+_KNOBS = {0: "rbm_mc.wpb", 1: "stats.slab", 2: "chol.update", 3: "rbm_mc.wsmem", 4: "chol.reserve",
+          5: "chol.pair"}
 
 
 def autotune(operator, psi, ensemble, tdvp, diag_shift=1e-3, stream=None):

@@ -179,6 +179,7 @@ struct ann_tdvp_impl {
     DevBuf chol_pt;             // TF32 hi/lo panel operands (two buffers) of the tensor-core update
     unsigned chol_pt_n = 0;
     alignas(64) unsigned char chol_map[2][128];  // TMA descriptors of its two buffers (CUtensorMap)
+    alignas(64) unsigned char chol_pmap[2][128]; // the same buffers in the panel-pair layout (K = 128)
     alignas(64) unsigned char chol_amap[128]; // TMA descriptor of the FP32 factor (reduce-add epilogue)
     int chol_reduce = 0;                      // chol_amap is bound (n even)
     DevBuf herk_in;             // BF16 operand for the tensor-core HERK
@@ -260,6 +261,9 @@ void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n);
 bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n);
 // operand buffer 0 / 1 (panel k uses k % 2), written by the panel solve
 float* chol_update_tc_operand(ann_tdvp_impl& td, unsigned buf);
+float* chol_update_tc_pair_operand(ann_tdvp_impl& td, unsigned buf);
+void chol_update_tc_pair(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned pb, bool col_only, unsigned* status,
+                         cudaStream_t st);
 void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, bool col_only, unsigned* status,
                     cudaStream_t st);
 // the look-ahead side stream of the Cholesky factorisations (high priority)
@@ -282,6 +286,7 @@ std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_slab(size_t rows, unsigned Np);
 std::string key_chol_update(unsigned n);
 std::string key_chol_reserve(unsigned n);
+std::string key_chol_pair(unsigned n);
 
 // PsiCNN (cnn.cu)
 void deep_prepare(ann_psi_impl& psi, cudaStream_t st);

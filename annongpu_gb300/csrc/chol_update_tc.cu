@@ -288,9 +288,13 @@ constexpr int kStages3 = 2;
 constexpr int kSmem3Bytes = kStages3 * kStageBytesN + 2 * kChunkBytes + 1024 + 256;
 constexpr unsigned kEpiThreads = 128;
 
+// P = K of the update: 64 (one panel) or 128 (two panels, rows [hi (128) | lo (128)])
+template<int P>
 __global__ void __launch_bounds__(256, 1)
 chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap amap, UpdArgs a,
                        unsigned n_tiles) {
+    static_assert(P % kBK == 0, "K steps of 32 TF32 values");
+    constexpr unsigned kSteps = P / kBK;  // K steps per segment
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* chunks = base + kStages3 * kStageBytesN;
@@ -339,7 +343,7 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    constexpr unsigned ksteps = kSegments * kStepsPerSeg;
+    constexpr unsigned ksteps = kSegments * kSteps;
 
     if(warp == 0 && lane == 0) {
         // ---- TMA producer ----
@@ -351,9 +355,9 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
             for(unsigned kt = 0; kt < ksteps; kt++) {
                 const unsigned g = lt * ksteps + kt, s = g % kStages3, ph = (g / kStages3) & 1u;
                 if(!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag, a.status)) { ok = false; break; }
-                const unsigned seg = kt / kStepsPerSeg, k = kt % kStepsPerSeg;
-                const int xa = (int)(k * kBK + (seg == 2 ? kPanel : 0u));
-                const int xb = (int)(k * kBK + (seg == 1 ? kPanel : 0u));
+                const unsigned seg = kt / kSteps, k = kt % kSteps;
+                const int xa = (int)(k * kBK + (seg == 2 ? (unsigned)P : 0u));  // lo of I in segment lo.hi
+                const int xb = (int)(k * kBK + (seg == 1 ? (unsigned)P : 0u));  // lo of J in segment hi.lo
                 unsigned char* st = base + s * kStageBytesN;
                 mbar_expect_tx(smem_u32(&full[s]), kStageBytesN);
                 tma_load_2d(smem_u32(st), &tmap, xa, (int)(I * kRows), smem_u32(&full[s]));
@@ -457,34 +461,45 @@ chol_update_tc3_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_co
 
 }  // namespace
 
-// two operand buffers (panel k uses buffer k % 2), each with its TMA descriptor; rows
-// past the trailing matrix only reach outputs past n, which are never written
-size_t pt_bytes(unsigned n) { return (size_t)((n + kBM - 1) / kBM) * kRows * kRowFloats * sizeof(float); }
+// Operand buffers: two (panel k uses buffer k % 2), each with its TMA descriptor, in the
+// layout of one panel (rows [hi (64) | lo (64)], chol_map) or of a panel pair (rows
+// [hi (128) | lo (128)], chol_pmap); a factorisation uses one layout, so both views share
+// the memory. Rows past the trailing matrix only reach outputs past n, never written.
+size_t pt_bytes_w(unsigned n, unsigned P) {
+    return (size_t)((n + kBM - 1) / kBM) * kRows * (2 * P) * sizeof(float);
+}
+size_t pt_bytes(unsigned n) { return pt_bytes_w(n, kPanel); }
+
+static void encode_pt(unsigned char* map, unsigned char* base, size_t bytes, unsigned P) {
+    const size_t rows = bytes / (2 * P * sizeof(float));
+    const cuuint64_t dims[2] = {(cuuint64_t)(2 * P), (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(2 * P * sizeof(float))};
+    const cuuint32_t box[2] = {kBK, kRows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims,
+                                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
+}
 
 void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
-    const size_t bytes = pt_bytes(n);
-    const size_t rows = bytes / (kRowFloats * sizeof(float));
-    if(td.chol_pt.bytes >= 2 * bytes && td.chol_pt_n == n) return;
-    td.chol_pt.ensure(2 * bytes);
-    ANN_CUDA(cudaMemset(td.chol_pt.p, 0, 2 * bytes));
+    const size_t b1 = pt_bytes_w(n, kPanel), b2 = pt_bytes_w(n, 2 * kPanel);
+    if(td.chol_pt.bytes >= 2 * b2 && td.chol_pt_n == n) return;
+    td.chol_pt.ensure(2 * b2);
+    ANN_CUDA(cudaMemset(td.chol_pt.p, 0, 2 * b2));
     td.chol_pt_n = n;
     for(int b = 0; b < 2; b++) {
-        const cuuint64_t dims[2] = {(cuuint64_t)kRowFloats, (cuuint64_t)rows};
-        const cuuint64_t strides[1] = {(cuuint64_t)(kRowFloats * sizeof(float))};
-        const cuuint32_t box[2] = {kBK, kRows};
-        const cuuint32_t estr[2] = {1, 1};
-        const CUresult r = encode_fn()(reinterpret_cast<CUtensorMap*>(td.chol_map[b]), CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
-                                       2, td.chol_pt.as<unsigned char>() + b * bytes, dims, strides, box, estr,
-                                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
+        encode_pt(td.chol_map[b], td.chol_pt.as<unsigned char>() + b * b1, b1, kPanel);
+        encode_pt(td.chol_pmap[b], td.chol_pt.as<unsigned char>() + b * b2, b2, 2 * kPanel);
     }
     static bool attr = false;
     if(!attr) {
         ANN_CUDA(cudaFuncSetAttribute(chol_update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       kSmemBytes));
-        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc3_kernel<kPanel>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       kSmem3Bytes));
+        ANN_CUDA(cudaFuncSetAttribute(chol_update_tc3_kernel<2 * kPanel>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem3Bytes));
         attr = true;
     }
 }
@@ -508,7 +523,32 @@ bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n) {
 }
 
 float* chol_update_tc_operand(ann_tdvp_impl& td, unsigned buf) {
-    return reinterpret_cast<float*>(td.chol_pt.as<unsigned char>() + buf * pt_bytes(td.chol_pt_n));
+    return reinterpret_cast<float*>(td.chol_pt.as<unsigned char>() + buf * pt_bytes_w(td.chol_pt_n, kPanel));
+}
+
+float* chol_update_tc_pair_operand(ann_tdvp_impl& td, unsigned buf) {
+    return reinterpret_cast<float*>(td.chol_pt.as<unsigned char>() + buf * pt_bytes_w(td.chol_pt_n, 2 * kPanel));
+}
+
+// Persistent launch of the reduce-add update (n even). More than a wave: persistent CTAs,
+// the epilogue of one tile under the MMAs of the next; a few SMs stay free for the next
+// panel (potrf32 / trsm32 on the side stream), which otherwise only gets the resources
+// left beside the persistent CTAs and runs several times slower (the panel is the
+// critical path of the factorisation). Up to a wave: one tile per CTA, still with the
+// two-stage pipeline.
+template<int P>
+static void launch_tc3(const CUtensorMap& pmap, const CUtensorMap& amap, const UpdArgs& a, unsigned tiles, unsigned n,
+                       cudaStream_t st) {
+    static int sms = 0;
+    if(!sms) {
+        int dev = 0;
+        ANN_CUDA(cudaGetDevice(&dev));
+        ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int reserve = std::min(tuning_get(key_chol_reserve(n), 32), sms / 2);
+    const unsigned grid = tiles > (unsigned)sms ? (unsigned)(sms - reserve) : tiles;
+    chol_update_tc3_kernel<P><<<grid, 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
+    check_launch("chol_update_tc3_kernel");
 }
 
 // A22 -= X X^H on tiles (I, 0) (col_only) or (I, J >= 1) of the trailing matrix of panel kb
@@ -523,25 +563,27 @@ void chol_update_tc(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned kb, 
     const CUtensorMap& pmap = *reinterpret_cast<const CUtensorMap*>(td.chol_map[(kb / kPanel) & 1u]);
     const CUtensorMap& amap = *reinterpret_cast<const CUtensorMap*>(td.chol_amap);
     if(td.chol_reduce) {
-        static int sms = 0;
-        if(!sms) {
-            int dev = 0;
-            ANN_CUDA(cudaGetDevice(&dev));
-            ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        }
-        // More than a wave: persistent CTAs, the epilogue of one tile under the MMAs of the
-        // next; a few SMs stay free for the next panel (potrf32 / trsm32 on the side stream),
-        // which otherwise only gets the resources left beside the persistent CTAs and runs
-        // several times slower (the panel is the critical path of the factorisation). Up to
-        // a wave: one tile per CTA, still with the two-stage pipeline.
-        const int reserve = std::min(tuning_get(key_chol_reserve(n), 32), sms / 2);
-        const unsigned grid = tiles > (unsigned)sms ? (unsigned)(sms - reserve) : tiles;
-        chol_update_tc3_kernel<<<grid, 256, kSmem3Bytes, st>>>(pmap, amap, a, tiles);
-        check_launch("chol_update_tc3_kernel");
+        launch_tc3<kPanel>(pmap, amap, a, tiles, n, st);
         return;
     }
     chol_update_tc_kernel<<<tiles, 128, kSmemBytes, st>>>(pmap, amap, a);
     check_launch("chol_update_tc_kernel");
+}
+
+// The same with K = 128 from the panel pair at columns pb .. pb + 127 (operand buffer
+// (pb / 128) % 2); the reduce-add epilogue only (n even)
+void chol_update_tc_pair(ann_tdvp_impl& td, cplx<float>* A, unsigned n, unsigned pb, bool col_only, unsigned* status,
+                         cudaStream_t st) {
+    if(!td.chol_reduce) throw Error(ANN_ERR_INVALID, "panel-pair update needs the reduce-add epilogue (n even)");
+    const unsigned t0 = pb + 2 * kPanel;
+    if(t0 >= n) return;
+    const unsigned T = (n - t0 + kBM - 1) / kBM;
+    const unsigned tiles = col_only ? T : T * (T - 1) / 2;
+    if(tiles == 0) return;
+    UpdArgs a{A, n, t0, col_only ? 1 : 0, 1, status};
+    const CUtensorMap& pmap = *reinterpret_cast<const CUtensorMap*>(td.chol_pmap[(pb / (2 * kPanel)) & 1u]);
+    const CUtensorMap& amap = *reinterpret_cast<const CUtensorMap*>(td.chol_amap);
+    launch_tc3<2 * kPanel>(pmap, amap, a, tiles, n, st);
 }
 
 }  // namespace ann

@@ -228,22 +228,28 @@ __device__ __forceinline__ float tf32_round(float x) {
 }
 
 // The panel rows are also the operand of the next tensor-core trailing update: with
-// PT != null each row is written there as well, split into TF32 hi and lo (the layout
-// of chol_update_tc.cu: per 128-row block of the rows below the panel,
-// [Re rows ; Im rows], each row [hi (64) | lo (64)] floats).
-__device__ __forceinline__ void put_tf32(float* PT, size_t i, unsigned p, cf v) {
+// PT != null each row from global row pt_row0 on is written there as well, split into
+// TF32 hi and lo (the layout of chol_update_tc.cu: per 128-row block of the rows from
+// pt_row0, [Re rows ; Im rows], each row [hi (w/2) | lo (w/2)] floats; the panel's 64
+// columns at pt_col0 of each half: w = 128 for one panel, 256 for a panel pair).
+struct PtDst {
+    float* PT;
+    unsigned row0, col0, w;
+};
+
+__device__ __forceinline__ void put_tf32(const PtDst& d, size_t i, unsigned p, cf v) {
     const size_t blk = i / 128, r = i % 128;
-    float* re = PT + (blk * 256 + r) * 128;
-    float* im = PT + (blk * 256 + 128 + r) * 128;
+    float* re = d.PT + (blk * 256 + r) * d.w + d.col0;
+    float* im = d.PT + (blk * 256 + 128 + r) * d.w + d.col0;
+    const unsigned lo = d.w / 2;
     const float hr = tf32_round(v.re), hi = tf32_round(v.im);
     re[p] = hr;
-    re[64 + p] = tf32_round(v.re - hr);
+    re[lo + p] = tf32_round(v.re - hr);
     im[p] = hi;
-    im[64 + p] = tf32_round(v.im - hi);
+    im[lo + p] = tf32_round(v.im - hi);
 }
 
-__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
-                                                     float* __restrict__ PT) {
+__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb, PtDst pt) {
     __shared__ cf Lt[NB][NB + 1];
     __shared__ float inv_d[NB];
     for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
@@ -303,16 +309,16 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
     }
     Xa[lane] = a0;
     Xa[lane + 32] = a1;
-    if(PT) {
-        put_tf32(PT, ra - (kb + NB), lane, a0);
-        put_tf32(PT, ra - (kb + NB), lane + 32, a1);
+    if(pt.PT && ra >= pt.row0) {
+        put_tf32(pt, ra - pt.row0, lane, a0);
+        put_tf32(pt, ra - pt.row0, lane + 32, a1);
     }
     if(has_b) {
         Xb[lane] = b0;
         Xb[lane + 32] = b1;
-        if(PT) {
-            put_tf32(PT, rb - (kb + NB), lane, b0);
-            put_tf32(PT, rb - (kb + NB), lane + 32, b1);
+        if(pt.PT && rb >= pt.row0) {
+            put_tf32(pt, rb - pt.row0, lane, b0);
+            put_tf32(pt, rb - pt.row0, lane + 32, b1);
         }
     }
 }
@@ -673,15 +679,28 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
 }
 
 // diagonal block, then the rows below it (and, for the tensor-core update, its operand)
-void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, float* PT, cudaStream_t st) {
+void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, PtDst pt, cudaStream_t st) {
     potrf32_kernel<<<1, kPotrfThreads, 0, st>>>(A, n, kb, status);
     check_launch("potrf32_kernel");
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned below = n - kb - nb;
     if(below) {
-        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb, PT);
+        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb, pt);
         check_launch("trsm32_kernel");
     }
+}
+
+// the panel pair at columns pb .. pb + 127: panel pb, its rank-64 update of the second
+// panel's 64 columns (FP32 SIMT, rows below pb + 64), then the second panel. The rows
+// from pb + 128 on of both panels go to PT (pair layout: K = 128, rows [hi | lo] of 256
+// floats) for the pair's tensor-core update of the rest.
+void panel_pair32(cf* A, unsigned n, unsigned pb, unsigned* status, float* PT, cudaStream_t st) {
+    panel32(A, n, pb, status, PtDst{PT, pb + 2 * NB, 0, 4 * NB}, st);
+    if(n - pb <= (unsigned)NB) return;
+    const unsigned below = n - pb - NB;
+    herk32_kernel<<<(below + UT - 1) / UT, 256, 2 * NB * (UT + 1) * sizeof(cf), st>>>(A, n, pb, NB, 1);
+    check_launch("herk32_kernel");
+    panel32(A, n, pb + NB, status, PtDst{PT, pb + 2 * NB, NB, 4 * NB}, st);
 }
 
 void set_smem_attrs() {
@@ -708,9 +727,32 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         chol_update_tc_bind(td, A, n);
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
+    if(tc && td.chol_reduce && tuning_get(key_chol_pair(n), 1) != 0) {
+        // Panel pairs (128 columns): the tensor-core update of the rest is one rank-128
+        // update per pair, half the passes over the trailing matrix and half the launches
+        // of one update per panel. Pair p's rows go to operand buffer p % 2: pair p+1 (side
+        // stream, after the update of the tile column holding it) fills the other buffer
+        // while the rest of update p still reads this one.
+        auto ppt = [&](unsigned pb) { return chol_update_tc_pair_operand(td, (pb / (2 * NB)) & 1u); };
+        panel_pair32(A, n, 0, status, ppt(0), st);
+        for(unsigned pb = 0; pb + 2 * NB < n; pb += 2 * NB) {
+            chol_update_tc_pair(td, A, n, pb, true, status, st);
+            ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
+            ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
+            panel_pair32(A, n, pb + 2 * NB, status, ppt(pb + 2 * NB), td.side);
+            ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
+            chol_update_tc_pair(td, A, n, pb, false, status, st);
+            ANN_CUDA(cudaStreamWaitEvent(st, td.side_ev[1], 0));
+        }
+        diag_inv_kernel<<<(n + NB - 1) / NB, 1024, 2 * NB * (NB + 1) * sizeof(cf), st>>>(A, n, Dinv, DinvH);
+        check_launch("diag_inv_kernel");
+        return;
+    }
     // panel k's rows go to operand buffer k % 2: panel k+1 (side stream) fills the other
     // buffer while the rest of update k still reads this one
-    auto pt = [&](unsigned kb) { return tc ? chol_update_tc_operand(td, (kb / NB) & 1u) : nullptr; };
+    auto pt = [&](unsigned kb) {
+        return PtDst{tc ? chol_update_tc_operand(td, (kb / NB) & 1u) : nullptr, kb + NB, 0, 2 * NB};
+    };
     panel32(A, n, 0, status, pt(0), st);
     for(unsigned kb = 0; kb < n; kb += NB) {
         const unsigned nb = min((unsigned)NB, n - kb);

@@ -11,6 +11,7 @@
 //   chol.update     trailing update of the FP32 Cholesky: 128 x 128 tcgen05 tiles
 //                   (split TF32) or 64 x 64 FP32 SIMT tiles
 //   chol.reserve    SMs the persistent tcgen05 update leaves free for the next panel: 0, 16, 32, 48, 64
+//   chol.pair       tcgen05 trailing updates of rank 64 per panel (0) or rank 128 per panel pair (1)
 // The sampler is timed on a copy of the ensemble, so the caller's chains do not move.
 // The reference has no tuning layer (its launch shape is fixed: one CTA per chain,
 // blockDim = hidden width, include/ensembles/MonteCarlo.hpp:223-228).
@@ -108,6 +109,12 @@ std::string key_chol_update(unsigned n) {
 std::string key_chol_reserve(unsigned n) {
     std::ostringstream o;
     o << "chol.reserve/n" << ((n + 1023) / 1024) * 1024;
+    return o.str();
+}
+
+std::string key_chol_pair(unsigned n) {
+    std::ostringstream o;
+    o << "chol.pair/n" << ((n + 1023) / 1024) * 1024;
     return o.str();
 }
 
@@ -254,6 +261,20 @@ int ann_autotune(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, double dia
                     if(ms < best) { best = ms; best_m = m; }
                 }
                 tuning_set(key, best_m);
+                // one rank-64 update per panel or one rank-128 update per panel pair (the
+                // pair form needs the reduce-add epilogue: n even)
+                if(best_m == 1 && t->Np % 2 == 0) {
+                    const std::string kp = key_chol_pair(t->Np);
+                    double best_p_ms = 1e300;
+                    int best_p = 1;
+                    for(int pr : {1, 0}) {
+                        tuning_set(kp, pr);
+                        const double ms = time_ms([&] { sr_solve_any(*t, diag_shift, status_word(), st); }, 2, st);
+                        record(5, pr, ms);
+                        if(ms < best_p_ms) { best_p_ms = ms; best_p = pr; }
+                    }
+                    tuning_set(kp, best_p);
+                }
                 // SMs left to the panel beside the persistent tensor-core update
                 if(best_m == 1) {
                     const std::string kr = key_chol_reserve(t->Np);

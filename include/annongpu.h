@@ -391,6 +391,8 @@ int ann_kl_stats(const ann_kl* kl, double* total_weight, double* mean_deviation2
  *           (mixed / FP32 solvers without an explicit ann_tdvp_set_chol_update)
  *   knob 3  sampler weights W staged in shared memory (1) or read through L1 (0)
  *   knob 4  SMs the persistent tcgen05 trailing update leaves to the next panel: 0, 16, 32, 48, 64
+ *   knob 5  tcgen05 trailing updates of rank 64 per panel (0) or rank 128 per pair of panels (1;
+ *           n even)
  * report (3 doubles per timed candidate: knob, candidate, median ms) may be NULL;
  * n_report receives the number of rows. Table keys are "dev<ordinal>/<knob>/<shape>". */
 int ann_autotune(ann_tdvp* tdvp, ann_op* op, ann_psi* psi, ann_ens* ens, double diag_shift, void* stream,
