@@ -68,7 +68,8 @@ TUNING_FILE = None       # --tuning: load the tuning table instead of autotuning
 # DRAM bytes (read + written) of this workload from a one-pass ncu capture of two precision-form
 # SR steps (dram__bytes_read.sum + dram__bytes_write.sum per kernel, profile window, Np = 8384,
 # 16384 samples): the FP32 factorisation's kernels (trailing updates, panels, inverses, shift
-# conversion) 20.9 GB per factorisation; herk_tc_kernel 7.0 GB per launch
+# conversion) 20.9 GB per factorisation with one rank-64 trailing update per panel (the
+# panel-pair form was not captured); herk_tc_kernel 7.0 GB per launch
 WORKLOAD_NP_NS = (N_SITES + M_HIDDEN + N_SITES * M_HIDDEN, N_CHAINS)
 FACTOR_DRAM_BYTES = 20.9e9
 HERK_DRAM_BYTES = 7.0e9
@@ -597,6 +598,8 @@ def run_ours(args):
         # updates run as three TF32 products on tcgen05 (TF32 rate = half the BF16 rate)
         chol_tflops = (4.0 / 3.0) * Np ** 3 / (f.t_factor_ms * 1e-3) / 1e12
         tf32x3_peak = pk.get("bf16_tflops", 1900.0) / 2 / 3
+        # the autotuned form of the trailing updates; the DRAM capture is of the per-panel form
+        pair = any("/chol.pair/" in k and v == 1 for k, v in ann.tuning_table().items())
         # the dominant kernel group of the step: trailing updates + panel path are about half
         # of the launch list (the S kernel 14 %)
         out["roofline"] = {"bound": "tensor",
@@ -604,8 +607,9 @@ def run_ours(args):
                                      "updates + potrf32/trsm32 panel path)",
                            "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
                            "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
-                           "traffic": FACTOR_DRAM_BYTES if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision"
-                           else None,
+                           "traffic": FACTOR_DRAM_BYTES
+                           if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision" and not pair else None,
+                           "update_form": "rank 128 per panel pair" if pair else "rank 64 per panel",
                            "peak_kind": pk_kind + " bf16 burst / 2 (TF32) / 3 (split products)",
                            "work": "(4/3)*Np^3 real flops per factorisation (CUDA events around it)"}
     else:
