@@ -495,3 +495,4 @@ class RefHarness:
         self.lib.ref_classical_log_psi_s.argtypes = [P, ct.c_uint64, P]
         self.lib.ref_classical_O_k.argtypes = [P, ct.c_uint64, P]
         self.lib.ref_pauli_apply.argtypes = [ct.c_uint64, ct.c_uint64, ct.c_uint64, U, P, P]
+        self.lib.ref_deep_hsd_exact.argtypes = [U, U, U, P, P, P, P, P, P, P, P, P, P, U, ct.c_int, D, P, P]

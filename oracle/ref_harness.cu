@@ -18,6 +18,7 @@
 //     PsiDeep reference)                            include/quantum_state/PsiClassical.hpp:48-163
 //   * KullbackLeibler value / gradient / gradient_with_noise
 //                                                   source/network_functions/KullbackLeibler.cu.template
+//   * HilbertSpaceDistance distance / gradient       source/network_functions/HilbertSpaceDistance.cu.template
 //   * ExpectationValue / TDVP / PsiVector / PsiOkVector / PsiNorm bodies
 //     (source/network_functions/*.cu.template, with the "//! begin template"
 //     instantiation blocks stripped at build time by oracle/Makefile).
@@ -35,6 +36,7 @@
 #include "network_functions/PsiNorm.hpp"
 #include "network_functions/PsiOkVector.hpp"
 #include "network_functions/KullbackLeibler.hpp"
+#include "network_functions/HilbertSpaceDistance.hpp"
 
 #include <vector>
 #include <cstdint>
@@ -195,6 +197,7 @@ struct LoggingPolicy : public LoggingPolicyKernel {
 #include "PsiOkVector.cu"
 #include "ensembles/MonteCarlo.cu"
 #include "KullbackLeibler.cu"
+#include "HilbertSpaceDistance.cu"
 
 using namespace ann_on_gpu;
 
@@ -479,6 +482,26 @@ unsigned ref_deep_mc(unsigned N, unsigned M, unsigned C, const unsigned* conn, c
     auto psi = make_deep({N, M, C, conn, params, fw, lp});
     return mc_trace(psi, {a, b, coeff, n_strings}, num_samples, num_sweeps, num_therm,
                     sconf, slp, seloc, pconf, psite, max_props, mc_energy);
+}
+
+// HilbertSpaceDistance between psi_prime and U psi over ExactSummationSpins, both
+// one-hidden-layer PsiDeep of the same shape: distance() and gradient(nu) with respect to
+// psi_prime's parameters (HilbertSpaceDistance.cu.template:104-165); dist[0] from distance(),
+// dist[1] from gradient()
+void ref_deep_hsd_exact(unsigned N, unsigned M, unsigned C, const unsigned* conn,
+                        const double* params, const double* fw, const double* lp,
+                        const double* params_p, const double* fw_p, const double* lp_p,
+                        const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                        int unitary, double nu, double* dist, double* grad) {
+    auto psi = make_deep({N, M, C, conn, params, fw, lp});
+    auto psi_p = make_deep({N, M, C, conn, params_p, fw_p, lp_p});
+    Operator op(HarnessExpr{a, b, coeff, n_strings}, false);
+    ExactSummationSpins es(N, false);
+    HilbertSpaceDistance hsd(psi_p.num_params, false);
+    dist[0] = hsd.distance(psi, psi_p, op, unitary != 0, es);
+    std::vector<std::complex<double>> g(psi_p.num_params);
+    dist[1] = hsd.gradient(g.data(), psi, psi_p, op, unitary != 0, es, (float)nu);
+    for(auto k = 0u; k < psi_p.num_params; k++) put(grad + 2 * k, g[k]);
 }
 
 // ---- PsiDeep (several hidden layers) ----

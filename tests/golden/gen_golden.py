@@ -6,7 +6,7 @@ stores inputs and outputs as .npz files. The fixtures pin the FP64 oracle
 (oracle/oracle.cpp) and, through it, the CUDA path. The reference checkout is
 needed only to regenerate them:
 
-    make -C oracle ref && python tests/golden/gen_golden.py [deep_ml | deep_pauli | classical]
+    make -C oracle ref REF=<reference checkout> && python tests/golden/gen_golden.py [deep_ml | deep_pauli | classical | hsd]
 """
 
 import ctypes as ct
@@ -387,6 +387,9 @@ def main(only=None):
     if only == "classical":
         gen_classical_all(ref)
         return
+    if only == "hsd":
+        gen_hsd_all(ref)
+        return
     rng = np.random.default_rng(20261203)
     gen_kats(ref, rng)
     gen_rbm(ref, rng)
@@ -399,7 +402,46 @@ def main(only=None):
     gen_deep_ml_all(ref)
     gen_deep_pauli_all(ref)
     gen_classical_all(ref)
+    gen_hsd_all(ref)
     print("fixtures written to", HERE)
+
+
+def gen_hsd(ref, rng, name, N, M):
+    """HilbertSpaceDistance of psi' to U psi over all 2^N configurations, both one-hidden-layer
+    PsiDeep with full connectivity, in the unitary form (U = 1 + i t H) and the exponential
+    form (operator i t H): distance() and gradient() for nu = 1 and nu = 0.5."""
+    C = N
+    np_ = N + M + C * M
+
+    def draw(scale):
+        return np.concatenate([cplx(rng, N, 0.05), cplx(rng, M, 0.05), cplx(rng, C * M, scale)])
+
+    params, params_p = draw(0.1), draw(0.12)
+    fw = (1.0 + cplx(rng, M, 0.1)).astype(np.complex128)
+    fw_p = (1.0 + cplx(rng, M, 0.1)).astype(np.complex128)
+    lp, lp_p = np.array([0.02 - 0.1j]), np.array([-0.03 + 0.2j])
+    H = mixed_hamiltonian(N)
+    t = 1e-2
+    out = {"N": N, "M": M, "C": C, "params": params, "fw": fw, "lp": lp, "params_p": params_p, "fw_p": fw_p,
+           "lp_p": lp_p, "t": np.array([t])}
+    from annongpu_gb300.expression import identity
+    for form, expr, unitary in (("unitary", identity() + 1j * t * H, 1), ("exponential", 1j * t * H, 0)):
+        a, b, c, n = op_arrays(expr)
+        out[f"{form}_op_a"], out[f"{form}_op_b"], out[f"{form}_op_c"] = a, b, c
+        for nu in (1.0, 0.5):
+            dist = np.zeros(2)
+            grad = np.zeros(np_, np.complex128)
+            ref.lib.ref_deep_hsd_exact(N, M, C, None, P(params), P(fw), P(lp), P(params_p), P(fw_p), P(lp_p),
+                                       P(a), P(b), P(c), n, unitary, nu, P(dist), P(grad))
+            tag = f"{form}_nu{nu:g}"
+            out[f"{tag}_dist"] = dist
+            out[f"{tag}_grad"] = grad
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def gen_hsd_all(ref):
+    rng = np.random.default_rng(20261206)
+    gen_hsd(ref, rng, "hsd_n8_m8", 8, 8)
 
 
 def gen_deep_ml_all(ref):

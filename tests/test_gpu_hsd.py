@@ -7,6 +7,8 @@ Monte Carlo estimate against the exact value.
 Tolerances: FP64 kernels vs the oracle rtol 1e-10 (distance) and 1e-8 of the largest
 gradient entry; finite differences as the reference: rtol 1e-3, atol 1e-4."""
 
+import os
+
 import numpy as np
 import pytest
 
@@ -116,3 +118,32 @@ def test_hsd_monte_carlo_matches_exact():
     mc = ann.MonteCarloSpins(1 << 18, 2, 20, 4096, True, seed=9)
     d_mc = hsd(psi, psi_p, op, True, mc)
     assert abs(d_mc - d_ex) < 0.05 * d_ex, (d_mc, d_ex)
+
+
+@pytest.mark.parametrize("form", ["unitary", "exponential"])
+@pytest.mark.parametrize("nu", [1.0, 0.5])
+def test_hsd_matches_reference_fixture(form, nu):
+    """Distance and gradient on the GPU (FP64 kernels, exact summation) against the
+    reference's own HilbertSpaceDistance run on the same PsiDeep pair
+    (tests/golden/hsd_n8_m8.npz; source/network_functions/HilbertSpaceDistance.cu.template:16-168).
+    The reference's log psi omits a.s, so both networks take a_in_log_psi=False."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "hsd_n8_m8.npz")))
+    N, M = int(g["N"]), int(g["M"])
+    conn = np.array([[i] * M for i in range(N)], np.uint32)
+
+    def make(p, fw, lp):
+        return ann.PsiDeep(N, p[:N], [p[N:N + M]], [conn], [p[N + M:].reshape(N, M)], fw, lp[0], True,
+                           a_in_log_psi=False, precision="fp64")
+    psi = make(g["params"], g["fw"], g["lp"])
+    psi_p = make(g["params_p"], g["fw_p"], g["lp_p"])
+    a, b, c = g[f"{form}_op_a"], g[f"{form}_op_b"], g[f"{form}_op_c"]
+    expr = ann.PauliExpression({(int(ai), int(bi)): complex(ci) for ai, bi, ci in zip(a, b, c)})
+    op = ann.Operator(expr)
+    es = ann.ExactSummationSpins(N)
+    hsd = ann.HilbertSpaceDistance(psi_p.num_params)
+    tag = f"{form}_nu{nu:g}"
+    d = hsd(psi, psi_p, op, form == "unitary", es)
+    grad, d2 = hsd.gradient(psi, psi_p, op, form == "unitary", es, nu)
+    np.testing.assert_allclose(d, g[f"{tag}_dist"][0], rtol=1e-10)
+    np.testing.assert_allclose(d2, g[f"{tag}_dist"][1], rtol=1e-10)
+    assert np.abs(grad - g[f"{tag}_grad"]).max() <= 1e-9 * np.abs(g[f"{tag}_grad"]).max()

@@ -293,3 +293,29 @@ def test_hsd_restatement_distance_and_gradient():
                   o.hsd_exact(make(p0), make(p1 - dp), op, False)[0]) / (2 * eps)
             g_ref[k] += unit * fd
     np.testing.assert_allclose(g, g_ref, rtol=1e-4, atol=1e-7)
+
+
+def hsd_pair_from(g):
+    """psi and psi' of an HSD fixture as oracle descriptors (reference semantics: no a.s)."""
+    N, M = int(g["N"]), int(g["M"])
+
+    def one(p, fw, lp):
+        return RbmDesc(N, M, p[N + M:], a=p[:N], b=p[N:N + M], fw=fw, log_prefactor=lp[0], layout=1,
+                       a_in_log_psi=False)
+    return one(g["params"], g["fw"], g["lp"]), one(g["params_p"], g["fw_p"], g["lp_p"])
+
+
+@pytest.mark.parametrize("form", ["unitary", "exponential"])
+@pytest.mark.parametrize("nu", [1.0, 0.5])
+def test_hsd_exact_matches_reference(oracle, form, nu):
+    """The oracle's HilbertSpaceDistance (distance and gradient in psi', exact summation)
+    against the reference's own HilbertSpaceDistance::distance / gradient run on the same
+    PsiDeep pair (source/network_functions/HilbertSpaceDistance.cu.template:16-168)."""
+    g = load("hsd_n8_m8.npz")
+    psi, psi_p = hsd_pair_from(g)
+    expr = _Expr(g[f"{form}_op_a"], g[f"{form}_op_b"], g[f"{form}_op_c"])
+    d, grad = oracle.hsd_exact(psi, psi_p, expr, form == "unitary", nu=nu)
+    tag = f"{form}_nu{nu:g}"
+    close(d, g[f"{tag}_dist"][0])
+    close(d, g[f"{tag}_dist"][1])
+    close(grad, g[f"{tag}_grad"], rtol=1e-9, atol=1e-12)
