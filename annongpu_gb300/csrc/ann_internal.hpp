@@ -81,6 +81,8 @@ struct ann_psi_impl {
     unsigned ncls = 1;
     double final_factor = 1.0;
     DevBuf cnn_w, cnn_meta;  // kernel-precision weights (CNN, multi-layer PsiDeep); packed CNN metadata
+    DevBuf cnn_scratch;      // CNN: per resident warp, pre-activations of both layers and two work buffers
+    unsigned cnn_x0 = 0, cnn_x1 = 0;  // CNN: most layer-0 / layer-1 sites a move of one or two flips changes
     // multi-layer PsiDeep (final weights in fw / fwd)
     DeepHost deep;
     DevBuf deep_tab;
@@ -126,7 +128,8 @@ struct ann_ens_impl {
     const ann_made_impl* made = nullptr;
     unsigned indep_per_sample = 0;
     double made_min_acceptance = 0.0;
-    bool made_dropped = false;
+    bool made_dropped = false;     // host copy of the device flag, read back by the bookkeeping
+    DevBuf made_on;                // int on the device: the sampler runs the learned moves while 1
     unsigned long long last_made_acc = 0, last_made_rej = 0;
     // ring buffer of recent sample configurations (training data for the proposal)
     DevBuf hist, hist_posd;        // rows; device write position (advanced by every pass)

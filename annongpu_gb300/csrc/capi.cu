@@ -111,6 +111,7 @@ unsigned* status_word() {
         clone(e->chain_conf, src.chain_conf);
         clone(e->chain_counter, src.chain_counter);
         clone(e->acc_rej, src.acc_rej);
+        clone(e->made_on, src.made_on);
     } catch(...) {
         delete e;
         throw;
@@ -158,6 +159,9 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
         throw Error(ANN_ERR_INVALID, "operator acts on sites beyond the wavefunction");
     if(ens.kind == 0 && !ens.basis && ens.N != psi.N)
         throw Error(ANN_ERR_INVALID, "exact summation size differs from psi.N");
+    if(ens.kind == 1 && ens.move == ANN_MOVE_EXCHANGE_BONDS)
+        for(const uint32_t site : ens.bonds)
+            if(site >= psi.N) throw Error(ANN_ERR_INVALID, "a bond names a site beyond the wavefunction");
     if((psi.kind != 0 || ens.basis) && ens.kind == 1 && ens.made && ens.indep_per_sample)
         throw Error(ANN_ERR_UNSUPPORTED, "the learned proposal is built for the RBM family over spins");
     if(ens.basis == ANN_BASIS_PAULIS) {
@@ -332,9 +336,14 @@ void mc_bookkeeping(ann_ens_impl& ens, cudaStream_t st) {
     ens.last_made_acc = ar[2];
     ens.last_made_rej = ar[3];
     // the learned proposal is dropped (local Metropolis continues alone) when its
-    // acceptance falls below the set rate
-    const unsigned long long tot = ar[2] + ar[3];
-    if(ens.made && tot > 0 && (double)ar[2] / (double)tot < ens.made_min_acceptance) ens.made_dropped = true;
+    // acceptance falls below the set rate: the sampling pass's drop-rule kernel cleared the
+    // device flag; the host copy follows it
+    if(ens.made && ens.made_on.p) {
+        int on = 1;
+        ANN_CUDA(cudaMemcpyAsync(&on, ens.made_on.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        sync(st);
+        ens.made_dropped = on == 0;
+    }
 }
 
 Stats fetch_stats(const DevBuf& b, cudaStream_t st) {
@@ -781,6 +790,9 @@ int ann_ens_set_proposal(ann_ens* e, const ann_made* m, unsigned indep_per_sampl
         e->indep_per_sample = m ? indep_per_sample : 0;
         e->made_min_acceptance = min_acceptance;
         e->made_dropped = false;
+        const int on = 1;
+        e->made_on.ensure(sizeof(int));
+        ANN_CUDA(cudaMemcpy(e->made_on.p, &on, sizeof(int), cudaMemcpyHostToDevice));
     });
 }
 int ann_ens_proposal_stats(const ann_ens* e, double* acceptance, int* dropped) {

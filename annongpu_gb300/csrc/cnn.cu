@@ -11,12 +11,19 @@
 // layer semantics (layer 0: polynomial log cosh, deeper: odd polynomial) or
 // log cosh on every layer.
 //
-// One warp per chain (or enumerated / explicit configuration). Layer-0 activations
-// and back-propagated deltas live in per-warp shared memory; the weights and the
-// neighbour tables (site x, window offset k) -> x + k and its inverse are shared by
-// the CTA. Proposals are evaluated by a full forward pass of the proposed
-// configuration (the reference also recomputes fully, PsiCNN.hpp:177-181).
+// One warp per chain (or enumerated / explicit configuration); a persistent grid whose
+// warps take chains in turn. Each warp keeps its chain's pre-activations z^0 and z^1 in a
+// slab of global memory (L1 / L2 resident: one slab per resident warp). A move that
+// flips one or two sites changes z^0 only on the sites whose layer-0 window holds a
+// flipped site (3 x 3 = 9 sites per flip for 3 x 3 windows) and z^1 only on the sites
+// whose layer-1 window holds one of those (the 5 x 5 cone): the proposal evaluates
+// those entries alone, from lists of the changed sites in per-warp shared memory, and
+// an accepted move writes them back. The reference recomputes the full forward pass for
+// every proposal (PsiCNN.hpp:177-181); samples here recompute it once, which also
+// removes the rounding the increments accumulate. Weights and neighbour tables
+// (site x, window offset k) -> x + k and its inverse are shared by the CTA.
 #include <algorithm>
+#include <set>
 
 #include "ann_internal.hpp"
 #include "chain.cuh"
@@ -26,6 +33,8 @@ namespace ann {
 namespace {
 
 constexpr int kCnnMaxLayers = 2;
+constexpr unsigned kCnnMaxSites = 128;   // site indices are stored as bytes
+constexpr unsigned kCnnMaxMoveFlips = 2;  // moves and flip groups with more sites take a full forward pass
 
 template<typename T>
 struct CnnDev {
@@ -40,10 +49,9 @@ struct CnnDev {
     const uint16_t* inv;     // [L][N][vol_l] site x whose window offset k lands on y
     unsigned nbr_off[kCnnMaxLayers];
     unsigned tab_len;        // entries of nbr (= inv)
-};
-
-struct CnnSmem {
-    unsigned w_bytes, tab_bytes, per_warp_bytes;
+    unsigned x0max, x1max;   // capacity of the changed-site lists (layer 0, layer 1)
+    cplx<T>* slab;           // per resident warp: z0 [ch0 N] | z1 [ch1 N] | work A [ch0 N] | work B [ch1 N]
+    size_t slab_len;         // complex entries per warp
 };
 
 template<typename T>
@@ -53,8 +61,20 @@ struct CnnCtx {
     const uint8_t* cls;
     const uint16_t* nbr;
     const uint16_t* inv;
-    cplx<T>* bufA;   // ch[0] x N
-    cplx<T>* bufB;   // ch[1] x N (two layers)
+    // this warp's slab (global)
+    cplx<T>* z0;     // ch0 x N pre-activations of the current configuration
+    cplx<T>* z1;     // ch1 x N (two layers)
+    cplx<T>* bufA;   // ch0 x N work buffer (activations, deltas)
+    cplx<T>* bufB;   // ch1 x N work buffer
+    // this warp's move lists (shared)
+    cplx<T>* da0;    // x0max x ch0: f0(z0 new) - f0(z0 old) on the changed layer-0 sites
+    cplx<T>* z0n;    // x0max x ch0: new z0 there
+    cplx<T>* z1n;    // x1max x ch1: new z1 on the changed layer-1 sites
+    uint8_t* pos0;   // kCnnMaxSites: position of a site in list0, 0xFF if absent
+    uint8_t* mark;   // kCnnMaxSites
+    uint8_t* list0;  // x0max changed layer-0 sites
+    uint8_t* list1;  // x1max changed layer-1 sites
+    unsigned n0, n1;
 };
 
 template<typename T>
@@ -68,9 +88,9 @@ __device__ __forceinline__ T spin_v(const Conf<2>& s, unsigned i) {
     return spin_bit(s, i) ? T(1) : T(-1);
 }
 
-// layer-0 pre-activation z^0_c(x)
+// layer-0 pre-activation z^0_c(x) from the spins
 template<typename T>
-__device__ __forceinline__ cplx<T> z0(const CnnCtx<T>& c, const Conf<2>& s, unsigned ch, unsigned x) {
+__device__ __forceinline__ cplx<T> z0_of(const CnnCtx<T>& c, const Conf<2>& s, unsigned ch, unsigned x) {
     const CnnDev<T>& p = *c.p;
     const uint16_t* nb = c.nbr + p.nbr_off[0] + x * p.vol[0];
     const cplx<T>* wr = c.w + p.woff[0] + (ch * p.ncls + c.cls[x]) * p.vol[0];
@@ -83,81 +103,202 @@ __device__ __forceinline__ cplx<T> z0(const CnnCtx<T>& c, const Conf<2>& s, unsi
     return z;
 }
 
-// layer-1 pre-activation z^1_d(x) from layer-0 activations in bufA
+// layer-1 pre-activation z^1_d(x) from the layer-0 activations in a (ch0 x N)
 template<typename T>
-__device__ __forceinline__ cplx<T> z1(const CnnCtx<T>& c, unsigned d, unsigned x) {
+__device__ __forceinline__ cplx<T> z1_of(const CnnCtx<T>& c, const cplx<T>* a, unsigned d, unsigned x) {
     const CnnDev<T>& p = *c.p;
     const uint16_t* nb = c.nbr + p.nbr_off[1] + x * p.vol[1];
     cplx<T> z = mk<T>(T(0), T(0));
     for(unsigned ci = 0; ci < p.ch[0]; ci++) {
         const cplx<T>* wr = c.w + p.woff[1] + ((ci * p.ch[1] + d) * p.ncls + c.cls[x]) * p.vol[1];
-        const cplx<T>* a = c.bufA + ci * p.N;
-        for(unsigned k = 0; k < p.vol[1]; k++) z += wr[k] * a[nb[k]];
+        const cplx<T>* ac = a + ci * p.N;
+        for(unsigned k = 0; k < p.vol[1]; k++) cmac(z, wr[k], ac[nb[k]]);
     }
     return z;
 }
 
-// full forward pass, warp-cooperative; returns log psi in every lane
 template<typename T>
-__device__ cplx<T> cnn_log_psi(const CnnCtx<T>& c, const Conf<2>& s, int lane) {
-    const CnnDev<T>& p = *c.p;
-    cplx<T> acc = mk<T>(T(0), T(0));
-    if(p.L == 1) {
-        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
-            const unsigned ch = e / p.N, x = e % p.N;
-            acc += act_f(z0(c, s, ch, x), p.act, 0);
-        }
-    } else {
-        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
-            const unsigned ch = e / p.N, x = e % p.N;
-            c.bufA[e] = act_f(z0(c, s, ch, x), p.act, 0);
-        }
-        __syncwarp();
-        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
-            const unsigned d = e / p.N, x = e % p.N;
-            acc += act_f(z1(c, d, x), p.act, 1);
-        }
-        __syncwarp();
-    }
-    acc = warp_sum(acc);
+__device__ __forceinline__ cplx<T> scaled_lp(const CnnDev<T>& p, cplx<T> acc) {
     return mk<T>((T)(p.ff * (double)acc.re) + p.lp.re, (T)(p.ff * (double)acc.im) + p.lp.im);
 }
 
-// O_k row (back-propagation, PsiCNN.hpp:183-266); forward state is recomputed
+// Full forward pass of s into the warp's slab (z0, z1; layer-0 activations left in bufA);
+// returns log psi in every lane.
+template<typename T>
+__device__ cplx<T> cnn_forward_state(const CnnCtx<T>& c, const Conf<2>& s, int lane) {
+    const CnnDev<T>& p = *c.p;
+    cplx<T> acc = mk<T>(T(0), T(0));
+    for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+        const unsigned ch = e / p.N, x = e % p.N;
+        const cplx<T> z = z0_of(c, s, ch, x);
+        c.z0[e] = z;
+        const cplx<T> f = act_f(z, p.act, 0);
+        if(p.L == 1) acc += f;
+        else c.bufA[e] = f;
+    }
+    __syncwarp();
+    if(p.L > 1) {
+        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
+            const unsigned d = e / p.N, x = e % p.N;
+            const cplx<T> z = z1_of(c, c.bufA, d, x);
+            c.z1[e] = z;
+            acc += act_f(z, p.act, 1);
+        }
+        __syncwarp();
+    }
+    return scaled_lp(p, warp_sum(acc));
+}
+
+// log psi of s without touching the slab's pre-activations (bufA as scratch)
+template<typename T>
+__device__ cplx<T> cnn_log_psi_scratch(const CnnCtx<T>& c, const Conf<2>& s, int lane) {
+    const CnnDev<T>& p = *c.p;
+    cplx<T> acc = mk<T>(T(0), T(0));
+    for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
+        const unsigned ch = e / p.N, x = e % p.N;
+        const cplx<T> f = act_f(z0_of(c, s, ch, x), p.act, 0);
+        if(p.L == 1) acc += f;
+        else c.bufA[e] = f;
+    }
+    __syncwarp();
+    if(p.L > 1) {
+        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
+            const unsigned d = e / p.N, x = e % p.N;
+            acc += act_f(z1_of(c, c.bufA, d, x), p.act, 1);
+        }
+        __syncwarp();
+    }
+    return scaled_lp(p, warp_sum(acc));
+}
+
+// Sites set in mark[] -> ascending list (and their positions in pos, when given); clears
+// the marks. Returns the count; entries beyond cap are dropped and flagged.
+__device__ unsigned compact_marks(uint8_t* mark, uint8_t* list, uint8_t* pos, unsigned N, unsigned cap, int lane,
+                                  unsigned* status) {
+    __syncwarp();
+    unsigned n = 0;
+    for(unsigned base = 0; base < N; base += 32) {
+        const unsigned x = base + lane;
+        const bool m = x < N && mark[x];
+        const unsigned b = __ballot_sync(0xffffffffu, m);
+        if(m) {
+            const unsigned q = n + __popc(b & ((1u << lane) - 1u));
+            if(q < cap) {
+                list[q] = (uint8_t)x;
+                if(pos) pos[x] = (uint8_t)q;
+            } else {
+                atomicOr(status, kStatusBadInput);
+            }
+            mark[x] = 0;
+        }
+        n += __popc(b);
+    }
+    __syncwarp();
+    return n < cap ? n : cap;
+}
+
+// Change of log psi when the nF <= 2 sites F flip, from the changed pre-activations
+// alone; leaves the new pre-activations in the move lists for cnn_commit.
+template<typename T>
+__device__ cplx<T> cnn_delta(CnnCtx<T>& c, const Conf<2>& s, const unsigned* F, unsigned nF, int lane,
+                             unsigned* status) {
+    const CnnDev<T>& p = *c.p;
+    const unsigned N = p.N, C0 = p.ch[0], v0 = p.vol[0];
+    // layer-0 sites whose window holds a flipped site
+    for(unsigned q = lane; q < nF * v0; q += 32) c.mark[c.inv[p.nbr_off[0] + F[q / v0] * v0 + q % v0]] = 1;
+    c.n0 = compact_marks(c.mark, c.list0, c.pos0, N, p.x0max, lane, status);
+    const unsigned n0 = c.n0;
+    const uint16_t* nb0 = c.nbr + p.nbr_off[0];
+    const T m2s0 = spin_bit(s, F[0]) ? T(-2) : T(2);  // s' - s at the flipped sites
+    const T m2s1 = nF > 1 ? (spin_bit(s, F[1]) ? T(-2) : T(2)) : T(0);
+    const unsigned f1 = nF > 1 ? F[1] : 0xFFFFFFFFu;
+    cplx<T> acc = mk<T>(T(0), T(0));
+    for(unsigned e = lane; e < n0 * C0; e += 32) {
+        const unsigned u = e / C0, ch = e % C0, x = c.list0[u];
+        const cplx<T>* wr = c.w + p.woff[0] + (ch * p.ncls + c.cls[x]) * v0;
+        cplx<T> dz = mk<T>(T(0), T(0));
+        for(unsigned k = 0; k < v0; k++) {
+            const unsigned y = nb0[x * v0 + k];
+            const T m = y == F[0] ? m2s0 : (y == f1 ? m2s1 : T(0));
+            dz.re += m * wr[k].re;
+            dz.im += m * wr[k].im;
+        }
+        const cplx<T> zo = c.z0[ch * N + x], zn = zo + dz;
+        c.z0n[e] = zn;
+        const cplx<T> df = act_f(zn, p.act, 0) - act_f(zo, p.act, 0);
+        if(p.L == 1) acc += df;
+        else c.da0[e] = df;
+    }
+    c.n1 = 0;
+    if(p.L > 1) {
+        const unsigned C1 = p.ch[1], v1 = p.vol[1];
+        // layer-1 sites whose window holds a changed layer-0 site
+        for(unsigned q = lane; q < n0 * v1; q += 32)
+            c.mark[c.inv[p.nbr_off[1] + c.list0[q / v1] * v1 + q % v1]] = 1;
+        c.n1 = compact_marks(c.mark, c.list1, nullptr, N, p.x1max, lane, status);
+        const uint16_t* nb1 = c.nbr + p.nbr_off[1];
+        const unsigned cstride = C1 * p.ncls * v1;  // weight stride between input channels
+        for(unsigned e = lane; e < c.n1 * C1; e += 32) {
+            const unsigned v = e / C1, d = e % C1, x = c.list1[v];
+            const cplx<T>* wr = c.w + p.woff[1] + (d * p.ncls + c.cls[x]) * v1;
+            cplx<T> dz = mk<T>(T(0), T(0));
+            for(unsigned k = 0; k < v1; k++) {
+                const unsigned u = c.pos0[nb1[x * v1 + k]];
+                if(u == 0xFFu) continue;
+                const cplx<T>* da = c.da0 + u * C0;
+                for(unsigned ci = 0; ci < C0; ci++) cmac(dz, wr[ci * cstride + k], da[ci]);
+            }
+            const cplx<T> zo = c.z1[d * N + x], zn = zo + dz;
+            c.z1n[e] = zn;
+            acc += act_f(zn, p.act, 1) - act_f(zo, p.act, 1);
+        }
+    }
+    __syncwarp();
+    for(unsigned u = lane; u < n0; u += 32) c.pos0[c.list0[u]] = 0xFFu;
+    __syncwarp();
+    acc = warp_sum(acc);
+    const T ff = (T)p.ff;
+    return mk<T>(ff * acc.re, ff * acc.im);
+}
+
+// the accepted move: its new pre-activations into the slab
+template<typename T>
+__device__ void cnn_commit(const CnnCtx<T>& c, int lane) {
+    const CnnDev<T>& p = *c.p;
+    for(unsigned e = lane; e < c.n0 * p.ch[0]; e += 32) c.z0[(e % p.ch[0]) * p.N + c.list0[e / p.ch[0]]] = c.z0n[e];
+    if(p.L > 1)
+        for(unsigned e = lane; e < c.n1 * p.ch[1]; e += 32)
+            c.z1[(e % p.ch[1]) * p.N + c.list1[e / p.ch[1]]] = c.z1n[e];
+    __syncwarp();
+}
+
+// O_k row (back-propagation, PsiCNN.hpp:183-266) from the slab's pre-activations
 template<typename T>
 __device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T>* O) {
     const CnnDev<T>& p = *c.p;
     const T ff = (T)p.ff;
     if(p.L == 1) {
         // dlogpsi/dz0 = ff f0'(z0); O[w0[0,c][cls,k]] = sum_{x in cls} ff f0'(z0_c(x)) s(x+k)
-        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
-            const unsigned ch = e / p.N, x = e % p.N;
-            c.bufA[e] = ff * act_df(z0(c, s, ch, x), p.act, 0);
-        }
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) c.bufA[e] = ff * act_df(c.z0[e], p.act, 0);
         __syncwarp();
     } else {
-        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) {
-            const unsigned ch = e / p.N, x = e % p.N;
-            c.bufA[e] = act_f(z0(c, s, ch, x), p.act, 0);
-        }
-        __syncwarp();
-        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
-            const unsigned d = e / p.N, x = e % p.N;
-            c.bufB[e] = ff * act_df(z1(c, d, x), p.act, 1);
-        }
+        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) c.bufA[e] = act_f(c.z0[e], p.act, 0);
+        for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) c.bufB[e] = ff * act_df(c.z1[e], p.act, 1);
         __syncwarp();
         // layer-1 parameters: O[(ci, d), cls, k] = sum_{x: cls(x)=cls} delta1_d(x) a0_ci(x + k)
         const unsigned n1 = p.ch[0] * p.ch[1] * p.ncls * p.vol[1];
+        const uint16_t* nb = c.nbr + p.nbr_off[1];
         for(unsigned q = lane; q < n1; q += 32) {
             const unsigned k = q % p.vol[1];
             const unsigned cl = (q / p.vol[1]) % p.ncls;
             const unsigned link = q / (p.vol[1] * p.ncls);
             const unsigned ci = link / p.ch[1], d = link % p.ch[1];
             cplx<T> o = mk<T>(T(0), T(0));
-            const uint16_t* nb = c.nbr + p.nbr_off[1];
+            const cplx<T>* dl = c.bufB + d * p.N;
+            const cplx<T>* ac = c.bufA + ci * p.N;
             for(unsigned x = 0; x < p.N; x++) {
                 if(c.cls[x] != cl) continue;
-                o += c.bufB[d * p.N + x] * c.bufA[ci * p.N + nb[x * p.vol[1] + k]];
+                cmac(o, dl[x], ac[nb[x * p.vol[1] + k]]);
             }
             O[p.woff[1] + q] = o;
         }
@@ -170,34 +311,38 @@ __device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T
             for(unsigned d = 0; d < p.ch[1]; d++)
                 for(unsigned k = 0; k < p.vol[1]; k++) {
                     const unsigned x = iv[k];
-                    g += wgt(c, 1, ci, d, c.cls[x], k) * c.bufB[d * p.N + x];
+                    cmac(g, wgt(c, 1, ci, d, c.cls[x], k), c.bufB[d * p.N + x]);
                 }
             // bufA[e] (the activation a0) is read by no other lane from here on
-            c.bufA[e] = g * act_df(z0(c, s, ci, y), p.act, 0);
+            c.bufA[e] = g * act_df(c.z0[e], p.act, 0);
         }
         __syncwarp();
     }
     // layer-0 parameters: O[(0, c), cls, k] = sum_{x: cls(x)=cls} delta0_c(x) s(x + k)
     const unsigned n0 = p.ch[0] * p.ncls * p.vol[0];
+    const uint16_t* nb = c.nbr + p.nbr_off[0];
     for(unsigned q = lane; q < n0; q += 32) {
         const unsigned k = q % p.vol[0];
         const unsigned cl = (q / p.vol[0]) % p.ncls;
         const unsigned ch = q / (p.vol[0] * p.ncls);
         cplx<T> o = mk<T>(T(0), T(0));
-        const uint16_t* nb = c.nbr + p.nbr_off[0];
+        const cplx<T>* dl = c.bufA + ch * p.N;
         for(unsigned x = 0; x < p.N; x++) {
             if(c.cls[x] != cl) continue;
-            o += spin_v<T>(s, nb[x * p.vol[0] + k]) * c.bufA[ch * p.N + x];
+            const T sv = spin_v<T>(s, nb[x * p.vol[0] + k]);
+            o.re += sv * dl[x].re;
+            o.im += sv * dl[x].im;
         }
         O[p.woff[0] + q] = o;
     }
     __syncwarp();
 }
 
-// local energy with one full forward pass per off-diagonal group (Operator.hpp:36-121)
+// local energy (Operator.hpp:36-121): one psi ratio per off-diagonal flip group, from the
+// changed pre-activations for groups of one or two sites, a full forward pass otherwise
 template<typename T>
-__device__ cplx<double> cnn_local_energy(const CnnCtx<T>& c, const OpDev& op, const Conf<2>& s, cplx<T> lpsi,
-                                         int lane) {
+__device__ cplx<double> cnn_local_energy(CnnCtx<T>& c, const OpDev& op, const Conf<2>& s, cplx<T> lpsi, int lane,
+                                         unsigned* status) {
     T dre = T(0), dim = T(0);
     for(unsigned n = lane; n < op.n_diag; n += 32) {
         int neg = 0;
@@ -217,20 +362,28 @@ __device__ cplx<double> cnn_local_energy(const CnnCtx<T>& c, const OpDev& op, co
             cg.im += (neg & 1) ? -c_im : c_im;
         }
         if(cg.re == T(0) && cg.im == T(0)) continue;
-        Conf<2> s2 = s;
-        for(unsigned q = op.grp_site_begin[g]; q < op.grp_site_begin[g + 1]; q++) flip(s2, op.grp_sites[q]);
-        const cplx<T> l2 = cnn_log_psi(c, s2, lane);
-        e += cg * cexp(l2 - lpsi);
+        const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
+        cplx<T> d;
+        if(se - sb <= kCnnMaxMoveFlips) {
+            unsigned F[kCnnMaxMoveFlips];
+            for(unsigned q = 0; q < se - sb; q++) F[q] = op.grp_sites[sb + q];
+            d = cnn_delta(c, s, F, se - sb, lane, status);
+        } else {
+            Conf<2> s2 = s;
+            for(unsigned q = sb; q < se; q++) flip(s2, op.grp_sites[q]);
+            d = cnn_log_psi_scratch(c, s2, lane) - lpsi;
+        }
+        e += cg * cexp(d);
     }
     return cvt<double>(e);
 }
 
 template<typename T>
-__device__ void cnn_process_sample(const CnnCtx<T>& c, const OpDev* op, const Conf<2>& s, int lane, size_t row,
+__device__ void cnn_process_sample(CnnCtx<T>& c, const OpDev* op, const Conf<2>& s, int lane, size_t row,
                                    const SampleOut& out, bool exact_weight) {
-    const cplx<T> lpsi = cnn_log_psi(c, s, lane);
+    const cplx<T> lpsi = cnn_forward_state(c, s, lane);
     cplx<double> e = mk(0.0, 0.0);
-    if(op) e = cnn_local_energy(c, *op, s, lpsi, lane);
+    if(op) e = cnn_local_energy(c, *op, s, lpsi, lane, out.status);
     if(lane == 0) {
         for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = s.w[w];
         const cplx<double> l = cvt<double>(lpsi);
@@ -242,7 +395,14 @@ __device__ void cnn_process_sample(const CnnCtx<T>& c, const OpDev* op, const Co
     if(out.O) cnn_O_row(c, s, lane, reinterpret_cast<cplx<T>*>(out.O) + row * out.ldO);
 }
 
-// stages weights and tables in shared memory, carves the per-warp buffers
+__host__ __device__ inline size_t cnn_warp_smem(unsigned x0max, unsigned x1max, unsigned ch0, unsigned ch1,
+                                                size_t elem) {
+    const size_t cplx_bytes = ((size_t)2 * x0max * ch0 + (size_t)x1max * ch1) * elem;
+    const size_t byte_bytes = 2 * kCnnMaxSites + x0max + x1max;
+    return (cplx_bytes + byte_bytes + 15) & ~(size_t)15;
+}
+
+// stages weights and tables in shared memory, carves this warp's move lists and slab
 template<typename T>
 __device__ CnnCtx<T> cnn_stage(const CnnDev<T>& p, unsigned char* smem) {
     CnnCtx<T> c;
@@ -260,67 +420,87 @@ __device__ CnnCtx<T> cnn_stage(const CnnDev<T>& p, unsigned char* smem) {
     uint8_t* cl = q;
     for(unsigned k = threadIdx.x; k < p.N; k += blockDim.x) cl[k] = p.cls[k];
     q += (p.N + 15) & ~15u;
-    const unsigned per_warp = (p.ch[0] + (p.L > 1 ? p.ch[1] : 0)) * p.N;
-    cplx<T>* buf = reinterpret_cast<cplx<T>*>(q) + (size_t)(threadIdx.x >> 5) * per_warp;
+    const unsigned warp = threadIdx.x >> 5;
+    const unsigned ch1 = p.L > 1 ? p.ch[1] : 0u;
+    q += warp * cnn_warp_smem(p.x0max, p.x1max, p.ch[0], ch1, sizeof(cplx<T>));
+    c.da0 = reinterpret_cast<cplx<T>*>(q);
+    c.z0n = c.da0 + (size_t)p.x0max * p.ch[0];
+    c.z1n = c.z0n + (size_t)p.x0max * p.ch[0];
+    uint8_t* b = reinterpret_cast<uint8_t*>(c.z1n + (size_t)p.x1max * ch1);
+    c.pos0 = b;
+    c.mark = b + kCnnMaxSites;
+    c.list0 = b + 2 * kCnnMaxSites;
+    c.list1 = c.list0 + p.x0max;
+    const int lane = threadIdx.x & 31;
+    for(unsigned k = lane; k < kCnnMaxSites; k += 32) {
+        c.pos0[k] = 0xFFu;
+        c.mark[k] = 0;
+    }
+    c.n0 = c.n1 = 0;
+    cplx<T>* slab = p.slab + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.slab_len;
+    c.z0 = slab;
+    c.z1 = c.z0 + (size_t)p.ch[0] * p.N;
+    c.bufA = c.z1 + (size_t)ch1 * p.N;
+    c.bufB = c.bufA + (size_t)p.ch[0] * p.N;
     c.w = w;
     c.nbr = nb;
     c.inv = iv;
     c.cls = cl;
-    c.bufA = buf;
-    c.bufB = buf + p.ch[0] * p.N;
     __syncthreads();
     return c;
 }
 
+// Metropolis chains (MonteCarlo.hpp:55-177 with the sampler's Philox contract); each warp
+// runs chains warp, warp + total warps, ...
 template<typename T>
 __global__ void __launch_bounds__(256) cnn_mc_kernel(CnnDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
     const int lane = threadIdx.x & 31;
-    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if(chain >= a.n_chains) return;
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
     const unsigned N = p.N;
-    Conf<2> s;
-    ChainDraw dr;
-    chain_start(a, chain, N, s, dr.t);
-    dr.t0 = dr.t;
-    cplx<T> lpsi = cnn_log_psi(c, s, lane);
-    unsigned long long n_acc = 0, n_rej = 0;
-    auto propose = [&]() {
-        unsigned i, j;
-        double u;
-        float uf;
-        dr.next(a, chain, N, lane, i, j, u, uf);
-        Conf<2> s2 = s;
-        flip(s2, i);
-        if(j != 0xFFFFFFFFu) {
-            if(spin_bit(s, i) == spin_bit(s, j)) { n_rej++; return; }
-            flip(s2, j);
+    for(unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); chain < a.n_chains; chain += warps) {
+        Conf<2> s;
+        ChainDraw dr;
+        chain_start(a, chain, N, s, dr.t);
+        dr.t0 = dr.t;
+        cnn_forward_state(c, s, lane);
+        unsigned long long n_acc = 0, n_rej = 0;
+        auto propose = [&]() {
+            unsigned F[2];
+            double u;
+            float uf;
+            dr.next(a, chain, N, lane, F[0], F[1], u, uf);
+            unsigned nF = 1;
+            if(F[1] != 0xFFFFFFFFu) {
+                if(spin_bit(s, F[0]) == spin_bit(s, F[1])) { n_rej++; return; }
+                nF = 2;
+            }
+            const cplx<T> d = cnn_delta(c, s, F, nF, lane, out.status);
+            const T ratio = fexp(T(2) * d.re);
+            const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
+            if(accept) {
+                cnn_commit(c, lane);
+                for(unsigned q = 0; q < nF; q++) flip(s, F[q]);
+                n_acc++;
+            } else {
+                n_rej++;
+            }
+        };
+        if(a.do_init || a.tape_site)
+            for(unsigned k = 0; k < a.num_therm * N; k++) propose();
+        for(unsigned st = 0; st < a.samples_per_chain; st++) {
+            for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
+            cnn_process_sample(c, with_op ? &op : nullptr, s, lane, (size_t)st * a.n_chains + chain, out, false);
         }
-        const cplx<T> l2 = cnn_log_psi(c, s2, lane);
-        const T ratio = fexp(T(2) * (l2.re - lpsi.re));
-        const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
-        if(accept) {
-            s = s2;
-            lpsi = l2;
-            n_acc++;
-        } else {
-            n_rej++;
+        if(lane == 0) {
+            if(!a.tape_site) {
+                for(int w = 0; w < kMaxWords; w++) a.chain_conf[(size_t)chain * kMaxWords + w] = s.w[w];
+                a.chain_counter[chain] = dr.t;
+            }
+            atomicAdd(&a.acc_rej[0], n_acc);
+            atomicAdd(&a.acc_rej[1], n_rej);
         }
-    };
-    if(a.do_init || a.tape_site)
-        for(unsigned k = 0; k < a.num_therm * N; k++) propose();
-    for(unsigned st = 0; st < a.samples_per_chain; st++) {
-        for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
-        cnn_process_sample(c, with_op ? &op : nullptr, s, lane, (size_t)st * a.n_chains + chain, out, false);
-    }
-    if(lane == 0) {
-        if(!a.tape_site) {
-            for(int w = 0; w < kMaxWords; w++) a.chain_conf[(size_t)chain * kMaxWords + w] = s.w[w];
-            a.chain_counter[chain] = dr.t;
-        }
-        atomicAdd(&a.acc_rej[0], n_acc);
-        atomicAdd(&a.acc_rej[1], n_rej);
     }
 }
 
@@ -328,7 +508,7 @@ template<typename T>
 __global__ void __launch_bounds__(256) cnn_exact_kernel(CnnDev<T> p, OpDev op, int with_op, uint64_t n_conf,
                                                          SampleOut out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
     const int lane = threadIdx.x & 31;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     for(uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n_conf; idx += warps) {
@@ -343,14 +523,15 @@ template<typename T>
 __global__ void __launch_bounds__(256) cnn_confs_kernel(CnnDev<T> p, OpDev op, int with_op, const uint64_t* confs,
                                                          uint64_t n, SampleOut out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
+    CnnCtx<T> c = cnn_stage<T>(p, smem_raw);
     const int lane = threadIdx.x & 31;
-    const uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if(idx >= n) return;
-    Conf<2> s;
-    s.w[0] = confs[idx * kMaxWords];
-    s.w[1] = confs[idx * kMaxWords + 1];
-    cnn_process_sample(c, with_op ? &op : nullptr, s, lane, idx, out, true);
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for(uint64_t idx = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n; idx += warps) {
+        Conf<2> s;
+        s.w[0] = confs[idx * kMaxWords];
+        s.w[1] = confs[idx * kMaxWords + 1];
+        cnn_process_sample(c, with_op ? &op : nullptr, s, lane, idx, out, true);
+    }
 }
 
 template<typename T>
@@ -385,20 +566,23 @@ CnnDev<T> cnn_view(const ann_psi_impl& psi) {
     p.nbr = reinterpret_cast<const uint16_t*>(meta);
     p.inv = p.nbr + tab;
     p.cls = meta + 4 * tab;
+    p.x0max = psi.cnn_x0;
+    p.x1max = p.L > 1 ? psi.cnn_x1 : 0u;
+    p.slab_len = (size_t)2 * (p.ch[0] + (p.L > 1 ? p.ch[1] : 0u)) * p.N;
     return p;
 }
 
 template<typename T>
 size_t cnn_smem(const CnnDev<T>& p, int warps) {
-    const size_t per_warp = (size_t)(p.ch[0] + (p.L > 1 ? p.ch[1] : 0)) * p.N * sizeof(cplx<T>);
+    const unsigned ch1 = p.L > 1 ? p.ch[1] : 0u;
     return ((p.Np * sizeof(cplx<T>) + 15) & ~(size_t)15) + ((2 * p.tab_len * 2 + 15) & ~(size_t)15) +
-           ((p.N + 15) & ~(size_t)15) + warps * per_warp;
+           ((p.N + 15) & ~(size_t)15) + warps * cnn_warp_smem(p.x0max, p.x1max, p.ch[0], ch1, sizeof(cplx<T>));
 }
 
 template<typename T>
 int cnn_warps(const CnnDev<T>& p) {
     int w = 8;
-    while(w > 1 && cnn_smem(p, w) > 200 * 1024) w >>= 1;
+    while(w > 1 && cnn_smem(p, w) > 100 * 1024) w >>= 1;
     if(cnn_smem(p, w) > 220 * 1024) throw Error(ANN_ERR_INVALID, "PsiCNN too large for shared memory");
     return w;
 }
@@ -406,6 +590,25 @@ int cnn_warps(const CnnDev<T>& p) {
 template<typename K>
 void cnn_set_smem(K k, size_t bytes) {
     if(bytes > 48 * 1024) ANN_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+// Persistent grid: at most the CTAs resident at once (and no more than the work needs);
+// binds one slab per warp of it.
+template<typename T, typename K>
+unsigned cnn_grid(K kernel, ann_psi_impl& psi, CnnDev<T>& p, int wpb, size_t smem, uint64_t work) {
+    cnn_set_smem(kernel, smem);
+    int dev = 0, sms = 0, per_sm = 0;
+    ANN_CUDA(cudaGetDevice(&dev));
+    ANN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    ANN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, wpb * 32, smem));
+    if(per_sm < 1) throw Error(ANN_ERR_INVALID, "PsiCNN kernel does not fit on an SM");
+    uint64_t grid = (uint64_t)sms * per_sm;
+    const uint64_t need = (work + wpb - 1) / wpb;
+    if(need < grid) grid = need;
+    if(grid < 1) grid = 1;
+    psi.cnn_scratch.ensure((size_t)grid * wpb * p.slab_len * sizeof(cplx<T>));
+    p.slab = psi.cnn_scratch.as<cplx<T>>();
+    return (unsigned)grid;
 }
 
 SampleOut cnn_out(Rows& rows, void* O, size_t ldO, bool want_eloc) {
@@ -430,7 +633,7 @@ void cnn_rows(Rows& rows, size_t n) {
 
 template<typename T>
 void cnn_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t, cudaStream_t st) {
-    const CnnDev<T> p = cnn_view<T>(psi);
+    CnnDev<T> p = cnn_view<T>(psi);
     const int wpb = cnn_warps(p);
     const size_t smem = cnn_smem(p, wpb);
     OpDev ov{};
@@ -439,16 +642,14 @@ void cnn_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, cons
         const uint64_t n_conf = 1ull << ens.N;
         cnn_rows(*t.rows, n_conf);
         SampleOut out = cnn_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
-        uint64_t blocks = (n_conf + wpb - 1) / wpb;
-        if(blocks > 152ull * 16) blocks = 152ull * 16;
-        cnn_set_smem(cnn_exact_kernel<T>, smem);
-        cnn_exact_kernel<T><<<(unsigned)blocks, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, n_conf, out);
+        const unsigned grid = cnn_grid(cnn_exact_kernel<T>, psi, p, wpb, smem, n_conf);
+        cnn_exact_kernel<T><<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, n_conf, out);
         check_launch("cnn_exact_kernel");
         return;
     }
     const unsigned spc = ens.num_samples / ens.n_chains;
     cnn_rows(*t.rows, (size_t)spc * ens.n_chains);
-    McArgs a;
+    McArgs a{};
     a.n_chains = ens.n_chains;
     a.samples_per_chain = spc;
     a.num_sweeps = ens.num_sweeps;
@@ -471,8 +672,8 @@ void cnn_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, cons
                                  cudaMemcpyDeviceToDevice, st));
     ANN_CUDA(cudaMemsetAsync(ens.acc_rej.p, 0, 2 * sizeof(unsigned long long), st));
     SampleOut out = cnn_out(*t.rows, t.O, t.ldO, t.want_eloc && op);
-    cnn_set_smem(cnn_mc_kernel<T>, smem);
-    cnn_mc_kernel<T><<<(ens.n_chains + wpb - 1) / wpb, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out);
+    const unsigned grid = cnn_grid(cnn_mc_kernel<T>, psi, p, wpb, smem, ens.n_chains);
+    cnn_mc_kernel<T><<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out);
     check_launch("cnn_mc_kernel");
     ens.chains_valid = true;
 }
@@ -480,15 +681,15 @@ void cnn_run_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, cons
 template<typename T>
 void cnn_confs_T(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,
                  size_t ldO, cudaStream_t st) {
-    const CnnDev<T> p = cnn_view<T>(psi);
+    CnnDev<T> p = cnn_view<T>(psi);
     const int wpb = cnn_warps(p);
     const size_t smem = cnn_smem(p, wpb);
     OpDev ov{};
     if(op) ov = op->view();
     cnn_rows(rows, n);
     SampleOut out = cnn_out(rows, O, ldO, op != nullptr);
-    cnn_set_smem(cnn_confs_kernel<T>, smem);
-    cnn_confs_kernel<T><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, confs, n, out);
+    const unsigned grid = cnn_grid(cnn_confs_kernel<T>, psi, p, wpb, smem, n);
+    cnn_confs_kernel<T><<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, confs, n, out);
     check_launch("cnn_confs_kernel");
 }
 
@@ -588,6 +789,25 @@ extern "C" int ann_psi_create_cnn(const ann_cnn_desc* d, ann_psi** out) {
             std::memcpy(meta.data() + 2 * nbr.size(), inv.data(), 2 * inv.size());
             for(unsigned x = 0; x < N; x++) meta[4 * nbr.size() + x] = (unsigned char)p->sym[x];
             upload(p->cnn_meta, meta.data(), meta.size());
+            // capacities of the move lists: the most layer-0 sites one flip reaches (its inverse
+            // window) and the most layer-1 sites reached through those, times the flips of a move
+            {
+                const unsigned v0 = p->layers[0].vol;
+                unsigned cone0 = 0, cone1 = 0;
+                for(unsigned y = 0; y < N; y++) {
+                    std::set<unsigned> s0, s1;
+                    for(unsigned k = 0; k < v0; k++) s0.insert(inv[y * v0 + k]);
+                    if(p->layers.size() > 1) {
+                        const unsigned v1 = p->layers[1].vol;
+                        for(unsigned x : s0)
+                            for(unsigned k = 0; k < v1; k++) s1.insert(inv[N * v0 + x * v1 + k]);
+                    }
+                    cone0 = std::max<unsigned>(cone0, (unsigned)s0.size());
+                    cone1 = std::max<unsigned>(cone1, (unsigned)s1.size());
+                }
+                p->cnn_x0 = std::min(N, 2 * cone0);
+                p->cnn_x1 = std::min(N, 2 * cone1);
+            }
             upload(p->params, d->params, (size_t)p->Np * 16);
             p->cnn_w.ensure((size_t)p->Np * p->elem_bytes());
             psi_prepare(*p, nullptr);

@@ -633,6 +633,25 @@ struct DeepChain {
 };
 
 
+// PsiCNN: full forward passes (the reference recomputes fully, PsiCNN.hpp:177-181)
+struct CnnChain {
+    const Cnn& psi;
+    cd lp{0.0}, lp2{0.0};
+    explicit CnnChain(const Cnn& p) : psi(p) {}
+    void reset(const Conf& s) { lp = psi.log_psi(s); }
+    double dre(const Conf&, const Conf& nx) {
+        lp2 = psi.log_psi(nx);
+        return lp2.real() - lp.real();
+    }
+    void accept() { lp = lp2; }
+    cd sample(const Conf& s, const or_op* op, cd* eloc) {
+        lp = psi.log_psi(s);
+        if(op && eloc) *eloc = psi.local_energy(op, s, lp);
+        return lp;
+    }
+};
+
+
 // ---- PsiClassical: PsiClassical.hpp:75-133, Operator.hpp:122-133 ----
 struct Classical {
     const or_classical* p;
@@ -854,6 +873,18 @@ void or_cnn_exact(const or_cnn* p, const or_op* op, double* E, double* norm,
     if(E) put(E, acc.E);
     if(norm) norm[0] = std::sqrt(nrm);
     acc.finish(nullptr, nullptr, tE, tE2, tO, tF, tS);
+}
+
+void or_cnn_mc_philox(const or_cnn* p, const or_op* op, unsigned n_chains, uint64_t seed,
+                      unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
+                      int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
+                      uint64_t* conf, uint64_t* counter,
+                      uint64_t* sconf, double* slp, double* seloc,
+                      uint64_t* n_accept, uint64_t* n_reject, double* min_tie) {
+    Cnn psi(p);
+    CnnChain m(psi);
+    philox_chains(m, psi.N, op, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind, bonds, n_bonds,
+                  init, n_up, conf, counter, sconf, slp, seloc, n_accept, n_reject, min_tie);
 }
 
 void or_rbm_tdvp_samples(const or_rbm* p, const or_op* op, const uint64_t* confs, unsigned n, double weight,

@@ -135,6 +135,13 @@ void or_cnn_O_k(const or_cnn* p, const uint64_t* conf, double* out);
 void or_cnn_local_energy(const or_cnn* p, const or_op* op, const uint64_t* conf, double* out);
 void or_cnn_exact(const or_cnn* p, const or_op* op, double* E, double* norm,
                   double* tE, double* tE2, double* tO, double* tF, double* tS);
+// counter-based chains (same contract as or_rbm_mc_philox); dlogpsi from full forward passes
+void or_cnn_mc_philox(const or_cnn* p, const or_op* op, unsigned n_chains, uint64_t seed,
+                      unsigned samples_per_chain, unsigned num_sweeps, unsigned num_therm,
+                      int move_kind, const uint32_t* bonds, unsigned n_bonds, int init, int n_up,
+                      uint64_t* conf, uint64_t* counter,
+                      uint64_t* sconf, double* slp, double* seloc,
+                      uint64_t* n_accept, uint64_t* n_reject, double* min_tie);
 
 unsigned or_deep_num_params(const or_deep* p);
 void or_deep_log_psi(const or_deep* p, const uint64_t* conf, double* out);

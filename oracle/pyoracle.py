@@ -404,6 +404,11 @@ class Oracle:
                                *[_ptr(r[k]) for k in ("E", "norm", "tE", "tE2", "tO", "tF", "tS")])
         return r
 
+    def cnn_mc_philox(self, psi: CnnDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
+                      move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None):
+        return self.mc_philox(psi, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind,
+                              bonds, init, n_up, conf, counter, _fn=self.lib.or_cnn_mc_philox)
+
     def deep_mc_philox(self, psi: DeepDesc, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm,
                        move_kind=0, bonds=None, init=True, n_up=-1, conf=None, counter=None):
         return self.mc_philox(psi, expr, n_chains, seed, samples_per_chain, num_sweeps, num_therm, move_kind,
