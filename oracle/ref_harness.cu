@@ -662,6 +662,20 @@ unsigned ref_rbm_mc(unsigned N, unsigned M, const double* W, const double* fw, c
                     sconf, slp, seloc, pconf, psite, max_props, mc_energy);
 }
 
+// TDVP (E, E2, <O>, F, S) over the reference's own host Monte Carlo with one chain (the
+// host path runs chain 0 alone, MonteCarlo.hpp:69-71): TDVP::eval, TDVP.cu.template:181-302.
+// Used to time the reference's CPU path against the oracle's restatement of it.
+void ref_rbm_tdvp_mc(unsigned N, unsigned M, const double* W, const double* fw, const double* lp,
+                     const uint64_t* a, const uint64_t* b, const double* coeff, unsigned n_strings,
+                     unsigned num_samples, unsigned num_sweeps, unsigned num_therm, double* tE) {
+    HarnessRBM psi(N, M, W, fw, lp);
+    Operator op(HarnessExpr{a, b, coeff, n_strings}, false);
+    MonteCarloSpins mc(num_samples, num_sweeps, num_therm, 1u, Update_Policy<Spins>(), false);
+    TDVP tdvp(psi.num_params, false);
+    tdvp.eval(op, psi, mc, false_t());
+    put(tE, tdvp.E_local.front());
+}
+
 // ---- PsiCNN ----
 void ref_cnn_log_psi_s(const unsigned* extent, unsigned L, const unsigned* ch, const unsigned* conn,
                        const unsigned* cls, const double* p, unsigned np, double ff, const double* lp,
