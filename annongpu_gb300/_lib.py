@@ -149,6 +149,7 @@ _SIGS = {
     "ann_tdvp_S_dot_vector": ([P, P, P, P], I),
     "ann_tdvp_set_solver": ([P, I, U, D], I),
     "ann_tdvp_solver_info": ([P, P], I),
+    "ann_tdvp_solver_form": ([P, P], I),
     "ann_tdvp_set_chol_update": ([P, I], I),
     "ann_autotune": ([P, P, P, P, D, P, P, U, P], I),
     "ann_hsd_distance": ([P, P, P, I, P, P, P], I),

@@ -825,11 +825,16 @@ class TDVP(_Handle):
 
     @property
     def solver_info(self):
-        """{'solves', 'residual_first', 'residual_last', 'fell_back'} of the last SR solve."""
+        """{'solves', 'residual_first', 'residual_last', 'fell_back', 'update_form'} of the last
+        SR solve; update_form names the FP32 factorisation's trailing-update form."""
         out = np.zeros(4)
         call("ann_tdvp_solver_info", self._h, ptr(out))
+        form = ct.c_int()
+        call("ann_tdvp_solver_form", self._h, ct.byref(form))
         return {"solves": int(out[0]), "residual_first": float(out[1]), "residual_last": float(out[2]),
-                "fell_back": bool(out[3])}
+                "fell_back": bool(out[3]),
+                "update_form": {0: None, 1: "FP32 SIMT", 2: "tensor core, rank 64 per panel",
+                                3: "tensor core, rank 128 per panel pair"}[form.value]}
 
     @property
     def s_mode(self):

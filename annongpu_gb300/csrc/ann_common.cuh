@@ -273,6 +273,7 @@ struct McArgs {
     unsigned long long* acc_rej;  // [4]: local accepted, rejected; learned accepted, rejected
     MadeDev made;                 // learned independence proposal (made.N == 0: none)
     unsigned indep_per_sample;    // independence proposals after the local sweeps of each sample
+    const int* made_on;           // device flag: 0 while the drop rule holds the proposal off (null: on)
 };
 
 struct SampleOut {

@@ -178,6 +178,7 @@ struct ann_tdvp_impl {
     bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
     int chol_tc = 1;            // FP32 Cholesky trailing update: 1 tcgen05 (split TF32), 0 FP32 SIMT
+    int chol_form = 0;          // ANN_CHOL_FORM_* of the last FP32 factorisation
     bool chol_tc_set = false;   // chosen explicitly (ann_tdvp_set_chol_update): the tuning table is not read
     DevBuf chol_pt;             // TF32 hi/lo panel operands (two buffers) of the tensor-core update
     unsigned chol_pt_n = 0;

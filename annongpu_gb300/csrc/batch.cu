@@ -71,6 +71,9 @@ RbmDev<float> view_f32(const ann_psi_impl& psi) {
     p.fw = psi.fwd.as<cplx<float>>();
     p.conn = psi.connd.as<uint16_t>();
     p.lp = mk<float>((float)psi.lp.real(), (float)psi.lp.imag());
+    p.fw_real = 1;
+    for(const zd& f : psi.fw)
+        if(f.imag() != 0.0) p.fw_real = 0;
     return p;
 }
 
@@ -145,6 +148,7 @@ void batch_table(ann_batch_impl& b) {
         a.acc_rej = ens.acc_rej.as<unsigned long long>();
         a.made = MadeDev{};
         a.indep_per_sample = 0;
+        a.made_on = nullptr;
         SampleTargets tg{&ens.rows, nullptr, 0, true};
         if(b.tdvps[i]) tg = tdvp_prepare(*b.tdvps[i], psi, ens);
         const size_t rows = (size_t)spc * ens.n_chains;

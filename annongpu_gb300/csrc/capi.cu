@@ -1375,6 +1375,13 @@ int ann_tdvp_solver_info(ann_tdvp* t, double* out4) {
     });
 }
 
+int ann_tdvp_solver_form(const ann_tdvp* t, int* form) {
+    return guard([&] {
+        need(t && form, "null argument");
+        *form = t->solver == ANN_SOLVER_FP64 ? ANN_CHOL_FORM_NONE : t->chol_form;
+    });
+}
+
 int ann_sr_update(ann_tdvp* t, ann_psi* psi, double lr, void* stream) {
     return guard([&] {
         need(t && psi && t->delta.p, "no solved delta");

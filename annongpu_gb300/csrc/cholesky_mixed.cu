@@ -727,7 +727,9 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         chol_update_tc_bind(td, A, n);
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
-    if(tc && td.chol_reduce && tuning_get(key_chol_pair(n), 1) != 0) {
+    const bool pair = tc && td.chol_reduce && tuning_get(key_chol_pair(n), 1) != 0;
+    td.chol_form = pair ? ANN_CHOL_FORM_TC_PAIR : (tc ? ANN_CHOL_FORM_TC_PANEL : ANN_CHOL_FORM_SIMT);
+    if(pair) {
         // Panel pairs (128 columns): the tensor-core update of the rest is one rank-128
         // update per pair, half the passes over the trailing matrix and half the launches
         // of one update per panel. Pair p's rows go to operand buffer p % 2: pair p+1 (side

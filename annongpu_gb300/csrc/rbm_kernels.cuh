@@ -32,20 +32,54 @@ struct RbmDev {
     const cplx<T>* fw;   // Mpad (zero padded)
     const uint16_t* conn;// C x M: input site of connection (c, j)
     cplx<T> lp;          // log prefactor
+    int fw_real;         // every final weight is real: Re(fw f) = Re fw Re f
 };
 
+// Per lane: the angles of units lane, lane + 32, ... and the real parts of their
+// log-psi terms. A Metropolis decision needs only Re(log psi' - log psi), so proposals
+// evaluate the real part of the activation alone; the complex terms are formed when a
+// sample is taken.
 template<typename T, int U>
 struct Lane {
     cplx<T> th[U];   // angles
-    cplx<T> ft[U];   // fw_j * f(theta_j)
+    T fr[U];         // Re(fw_j f(theta_j))
+    T fwr[U];        // Re fw_j (registers: read by every proposal when the final weights are real)
 };
+
+// Re f(z) of the first-layer activation: the polynomial's real part from z^2 and z^4
+// (Re z^6 = Re z^4 Re z^2 - Im z^4 Im z^2), or Re log cosh z = Re w + log|1 + e^{-2w}| - log 2
+template<typename T>
+__device__ __forceinline__ T act_f_re(cplx<T> z, int act) {
+    if(act == kPoly) {
+        const T x2r = z.re * z.re - z.im * z.im, x2i = T(2) * z.re * z.im;
+        const T x4r = x2r * x2r - x2i * x2i, x4i = T(2) * x2r * x2i;
+        const T x6r = x4r * x2r - x4i * x2i;
+        return T(0.5) * x2r - T(1.0 / 12.0) * x4r + T(1.0 / 45.0) * x6r;
+    }
+    const cplx<T> w = z.re >= T(0) ? z : -z;
+    const cplx<T> e = cexp(T(-2) * w);
+    return w.re + T(0.5) * flog(norm2(mk<T>(T(1) + e.re, e.im))) - T(0.69314718055994530942);
+}
+
+// Re(fw_j f(z)) of unit j = u * 32 + lane (complex final weights are read from memory)
+template<typename T, int U>
+__device__ __forceinline__ T fw_f_re(const RbmDev<T>& p, const Lane<T, U>& L, int u, int lane, cplx<T> z) {
+    if(p.fw_real) return L.fwr[u] * act_f_re(z, p.act);
+    const cplx<T> fw = p.fw[u * 32 + lane];
+    const cplx<T> f = act_f(z, p.act, 0);
+    return fw.re * f.re - fw.im * f.im;
+}
 
 // theta_j = b_j + sum_i s_i Wd[i][j] from scratch
 template<typename T, int NW, int U>
 __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
                                           const Conf<NW>& s, Lane<T, U>& L, int lane) {
 #pragma unroll
-    for(int u = 0; u < U; u++) L.th[u] = (unsigned)u < p.Uact ? p.b[u * 32 + lane] : mk<T>(T(0), T(0));
+    for(int u = 0; u < U; u++) {
+        const bool on = (unsigned)u < p.Uact;
+        L.th[u] = on ? p.b[u * 32 + lane] : mk<T>(T(0), T(0));
+        L.fwr[u] = on ? p.fw[u * 32 + lane].re : T(0);
+    }
     for(unsigned i = 0; i < p.N; i++) {
         const T si = spin_bit(s, i) ? T(1) : T(-1);
         const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
@@ -58,15 +92,57 @@ __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __r
         }
     }
 #pragma unroll
+    for(int u = 0; u < U; u++) L.fr[u] = (unsigned)u < p.Uact ? fw_f_re(p, L, u, lane, L.th[u]) : T(0);
+}
+
+// complex terms fw_j f(theta_j) of the lane's units (sample time)
+template<typename T, int U>
+__device__ __forceinline__ void lane_terms(const RbmDev<T>& p, const Lane<T, U>& L, int lane, cplx<T>* ft) {
+#pragma unroll
     for(int u = 0; u < U; u++)
-        L.ft[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
+        ft[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
+}
+
+// Re(log psi(s') - log psi(s)) summed over the warp for the flip of `sites`; leaves the
+// angle changes in dth and the new real terms in fnew for an accepted move
+template<typename T, int NW, int U>
+__device__ __forceinline__ T delta_re(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const Conf<NW>& s,
+                                      const Lane<T, U>& L, int lane, const uint16_t* sites, unsigned nsites,
+                                      cplx<T>* dth, T* fnew) {
+#pragma unroll
+    for(int u = 0; u < U; u++) dth[u] = mk<T>(T(0), T(0));
+    T dvis = T(0);
+    for(unsigned q = 0; q < nsites; q++) {
+        const unsigned i = sites[q];
+        const T m2s = spin_bit(s, i) ? T(-2) : T(2);  // s'_i - s_i
+        const cplx<T>* row = Wd + (size_t)i * p.Mpad + lane;
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            if((unsigned)u >= p.Uact) break;
+            const cplx<T> w = row[u * 32];
+            dth[u].re += m2s * w.re;
+            dth[u].im += m2s * w.im;
+        }
+        if(p.a_in_log_psi) dvis += m2s * p.a[i].re;
+    }
+    T d = T(0);
+#pragma unroll
+    for(int u = 0; u < U; u++) {
+        if((unsigned)u >= p.Uact) {
+            fnew[u] = T(0);
+            continue;
+        }
+        fnew[u] = fw_f_re(p, L, u, lane, L.th[u] + dth[u]);
+        d += fnew[u] - L.fr[u];
+    }
+    return warp_sum(d) + dvis;
 }
 
 // sum over the warp of fw_j (f(theta_j + dtheta_j) - f(theta_j)) for the sites in `sites`
 template<typename T, int NW, int U>
 __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
-                                                 const Conf<NW>& s, const Lane<T, U>& L, int lane,
-                                                 const uint16_t* sites, unsigned nsites,
+                                                 const Conf<NW>& s, const Lane<T, U>& L, const cplx<T>* ft,
+                                                 int lane, const uint16_t* sites, unsigned nsites,
                                                  cplx<T>* dth, cplx<T>* fnew) {
 #pragma unroll
     for(int u = 0; u < U; u++) dth[u] = mk<T>(T(0), T(0));
@@ -92,7 +168,7 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
             continue;
         }
         fnew[u] = p.fw[u * 32 + lane] * act_f(L.th[u] + dth[u], p.act, 0);
-        d += fnew[u] - L.ft[u];
+        d += fnew[u] - ft[u];
     }
     d = warp_sum(d);
     return d + dvis;
@@ -101,7 +177,7 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
 // local energy of configuration s (Operator.hpp:86-121 semantics)
 template<typename T, int NW, int U>
 __device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op,
-                                     const Conf<NW>& s, const Lane<T, U>& L, int lane) {
+                                     const Conf<NW>& s, const Lane<T, U>& L, const cplx<T>* ft, int lane) {
     // arithmetic in the kernel precision T (coefficients are stored in FP64 and
     // rounded once); the FP64 pipe is reserved for the final conversion
     // diagonal strings, split over lanes
@@ -130,7 +206,7 @@ __device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restri
         }
         if(cg.re == T(0) && cg.im == T(0)) continue;
         const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
-        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, op.grp_sites + sb, se - sb, dth, fnew);
+        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, ft, lane, op.grp_sites + sb, se - sb, dth, fnew);
         e += cg * cexp(d);
     }
     return cvt<double>(e);
@@ -141,15 +217,17 @@ template<typename T, int NW, int U>
 __device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev* op,
                                const Conf<NW>& s, const Lane<T, U>& L, int lane, size_t row,
                                const SampleOut& out, bool exact_weight) {
+    cplx<T> ft[U];
+    lane_terms<T, U>(p, L, lane, ft);
     cplx<T> lsum = mk<T>(T(0), T(0));
 #pragma unroll
-    for(int u = 0; u < U; u++) lsum += L.ft[u];
+    for(int u = 0; u < U; u++) lsum += ft[u];
     if(p.a_in_log_psi)
         for(unsigned i = lane; i < p.N; i += 32) lsum += (spin_bit(s, i) ? T(1) : T(-1)) * p.a[i];
     lsum = warp_sum(lsum);
     const cplx<double> lpsi = cvt<double>(lsum) + cvt<double>(p.lp);
     cplx<double> e = mk<double>(0.0, 0.0);
-    if(op) e = local_energy<T, NW, U>(p, Wd, *op, s, L, lane);
+    if(op) e = local_energy<T, NW, U>(p, Wd, *op, s, L, ft, lane);
     if(lane == 0) {
         for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = w < NW ? s.w[w] : 0;
         out.log_psi[row] = lpsi;
@@ -202,7 +280,7 @@ __device__ __forceinline__ const cplx<T>* stage_Wd(const RbmDev<T>& p, int w_sme
 // One chain: thermalisation (when drawing fresh configurations), then per sample
 // the local sweeps, the learned independence moves, and the sample bookkeeping.
 template<typename T, int NW, int U>
-__device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op, int with_op,
+__device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op, int with_op,
                          const McArgs& a, const SampleOut& out, unsigned chain, int lane, bool use_made,
                          const MadeSm& ms, float* mh) {
     const unsigned N = p.N;
@@ -251,7 +329,8 @@ __device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, con
     uint64_t rr_base = 0;
     bool rr_valid = false;
     u32x4 rr = {0, 0, 0, 0};
-    cplx<T> dth[U], fnew[U];
+    cplx<T> dth[U];
+    T fnew[U];
     float lq_cur = 0.f;
     bool lq_stale = true;
 
@@ -297,8 +376,8 @@ __device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, con
             sites[1] = (uint16_t)j;
             ns = 2;
         }
-        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, lane, sites, ns, dth, fnew);
-        const T ratio = fexp(T(2) * d.re);
+        const T d = delta_re<T, NW, U>(p, Wd, s, L, lane, sites, ns, dth, fnew);
+        const T ratio = fexp(T(2) * d);
         // MonteCarlo.hpp:158-160: accept if ratio > 1 or u <= ratio; u < 1 makes
         // the first clause redundant.
         // complex64 chains compare in FP32 (GB300's FP64 rate is 1/64 of FP32):
@@ -306,7 +385,7 @@ __device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, con
         const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
         if(accept) {
 #pragma unroll
-            for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.ft[q] = fnew[q]; }
+            for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.fr[q] = fnew[q]; }
             for(unsigned q = 0; q < ns; q++) flip(s, sites[q]);
             n_acc++;
             lq_stale = true;
@@ -327,17 +406,17 @@ __device__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, con
         }
         Lane<T, U> L2;
         recompute<T, NW, U>(p, Wd, s2, L2, lane);
-        cplx<T> d = mk<T>(T(0), T(0));
+        T d = T(0);
 #pragma unroll
-        for(int q = 0; q < U; q++) d += L2.ft[q] - L.ft[q];
+        for(int q = 0; q < U; q++) d += L2.fr[q] - L.fr[q];
         if(p.a_in_log_psi)
             for(unsigned i = lane; i < p.N; i += 32) {
                 const int b1 = spin_bit(s2, i), b0 = spin_bit(s, i);
-                if(b1 != b0) d += (b1 ? T(2) : T(-2)) * p.a[i];
+                if(b1 != b0) d += (b1 ? T(2) : T(-2)) * p.a[i].re;
             }
         d = warp_sum(d);
         const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tq, (uint32_t)(tq >> 32), chain, 0u});
-        const float lr = 2.f * (float)d.re + lq_cur - lq2;
+        const float lr = 2.f * (float)d + lq_cur - lq2;
         const float uf = __uint2float_rz(r.w >> 8) * 0x1.0p-24f;
         if(uf <= expf(lr)) {
             s = s2;
@@ -383,8 +462,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && U <= 4) ? 3 : 1)
 rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
-    // learned-proposal weights after Wd, then one H-float scratch per warp
-    const bool use_made = a.made.N != 0;
+    // learned-proposal weights after Wd, then one H-float scratch per warp; the drop rule
+    // switches the moves off through a device flag (graph replays see it change)
+    const bool use_made = a.made.N != 0 && (a.made_on == nullptr || *a.made_on != 0);
     MadeSm ms{};
     float* mh = nullptr;
     if(use_made) {
@@ -396,7 +476,16 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
     const int lane = threadIdx.x & 31;
     const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if(chain >= a.n_chains) return;
-    mc_chain<T, NW, U>(p, Wd, op, with_op, a, out, chain, lane, use_made, ms, mh);
+    RbmDev<T> q = p;
+    q.Uact = U;  // the padded width is exactly 32 U here: the per-slot guards fold away
+    mc_chain<T, NW, U>(q, Wd, op, with_op, a, out, chain, lane, use_made, ms, mh);
+}
+
+// Drop rule of the learned proposal, on the device after each sampling pass: the flag
+// goes to 0 when the pass's learned-move acceptance is below min_acceptance.
+static __global__ void made_drop_rule_kernel(const unsigned long long* acc_rej, double min_acceptance, int* made_on) {
+    const unsigned long long acc = acc_rej[2], tot = acc_rej[2] + acc_rej[3];
+    if(tot > 0 && (double)acc < min_acceptance * (double)tot) *made_on = 0;
 }
 
 // ---------------------------------------------------------------------------------

@@ -28,6 +28,9 @@ RbmDev<T> rbm_view(const ann_psi_impl& psi) {
     p.fw = psi.fwd.as<cplx<T>>();
     p.conn = psi.connd.as<uint16_t>();
     p.lp = mk<T>((T)psi.lp.real(), (T)psi.lp.imag());
+    p.fw_real = 1;
+    for(const zd& f : psi.fw)
+        if(f.imag() != 0.0) p.fw_real = 0;
     return p;
 }
 
@@ -131,13 +134,17 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     a.acc_rej = ens.acc_rej.as<unsigned long long>();
     a.made = MadeDev{};
     a.indep_per_sample = 0;
-    const bool learned = ens.made && !ens.made_dropped && ens.indep_per_sample > 0 && !a.tape_site;
+    a.made_on = nullptr;
+    // the learned moves are launched whenever a proposal is set; the device flag (the drop
+    // rule) decides in the kernel whether they run
+    const bool learned = ens.made && ens.indep_per_sample > 0 && !a.tape_site;
     if(learned) {
         if(ens.made->N != psi.N) throw Error(ANN_ERR_INVALID, "learned proposal size differs from psi.N");
         if(ens.made->H > 256) throw Error(ANN_ERR_INVALID, "learned proposals in the sampler need H <= 256");
         if(ens.move != 0) throw Error(ANN_ERR_UNSUPPORTED, "learned proposals combine with single-flip moves");
         a.made = made_view(*ens.made);
         a.indep_per_sample = ens.indep_per_sample;
+        a.made_on = ens.made_on.as<int>();
     }
     if(a.tape_site) {
         // replay starts from the recorded initial configurations every call
@@ -165,6 +172,11 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
         k<<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out, w_smem);
     });
     check_launch("rbm_mc_kernel");
+    if(learned) {
+        made_drop_rule_kernel<<<1, 1, 0, st>>>(ens.acc_rej.as<unsigned long long>(), ens.made_min_acceptance,
+                                               ens.made_on.as<int>());
+        check_launch("made_drop_rule_kernel");
+    }
     ens.chains_valid = true;
 }
 

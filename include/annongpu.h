@@ -406,6 +406,15 @@ int ann_tuning_clear(void);
    after the last solve, 1 if the FP64 solve replaced a stalled mixed solve}
    (ANN_SOLVER_FP64: {1, residual before refinement, after, 0}) */
 int ann_tdvp_solver_info(ann_tdvp* tdvp, double* out4);
+/* the factorisation form of the last FP32 Cholesky: 0 none (ANN_SOLVER_FP64 or no solve
+   yet), 1 FP32 SIMT trailing updates, 2 tensor-core trailing update per 64-column panel,
+   3 tensor-core trailing update per pair of panels (rank 128). No counterpart in the
+   reference, which has no solver (source/network_functions/TDVP.cu.template:181-302). */
+#define ANN_CHOL_FORM_NONE 0
+#define ANN_CHOL_FORM_SIMT 1
+#define ANN_CHOL_FORM_TC_PANEL 2
+#define ANN_CHOL_FORM_TC_PAIR 3
+int ann_tdvp_solver_form(const ann_tdvp* tdvp, int* form);
 /* SR solve: (S + shift I) delta = F on the GPU with the configured solver; writes delta
    (num_params complex) if out != NULL and the relative residuals ||F - (S + shift I) x|| /
    ||F|| of the first and the final solution to info2 if info2 != NULL. */

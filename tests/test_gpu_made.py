@@ -152,3 +152,36 @@ def test_proposal_dropped_below_acceptance_threshold():
     # the next call runs local Metropolis alone
     ann.ExpectationValue()(ann.Operator(ann.transverse_field_ising_1d(N)), psi, mc)
     assert mc.acceptance_rate > 0.0
+
+
+def test_drop_rule_acts_inside_graph_replays_and_rearms():
+    """The drop rule runs on the device after each sampling pass (a flag the sampler
+    reads), so it also acts in replays of a captured SR step; set_proposal re-arms the
+    proposal (the bench does so after each retraining)."""
+    import torch
+    N = 12
+    psi = bimodal_rbm(N)
+    es = ann.ExactSummationSpins(N)
+    psi.normalize(es)
+    p = np.abs(ann.psi_vector(psi, es)) ** 2
+    p /= p.sum()
+    train = np.random.default_rng(2).choice(1 << N, size=16384, p=p).astype(np.uint64)
+    made = ann.MADE(N, 64, seed=4)
+    made.train(train, steps=800, batch=2048, lr=1e-2)
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloSpins(256, 1, 5, 256, True, seed=1, persistent=True)
+    # accepted learned moves fall short of a 99 % threshold: dropped after the first pass
+    mc.set_proposal(made, indep_per_sample=2, min_acceptance=0.99)
+    st = torch.cuda.Stream()
+    td = ann.TDVP(psi.num_params, s_mode="fp32", solver="fp64", stream=st)
+    td.capture_sr_step(op, psi, mc, 1e-3, 0.0, st)  # one eager step (the proposal runs), then capture
+    mc.refresh_stats(st)
+    assert mc.proposal_dropped and mc.proposal_acceptance > 0.1
+    td.launch_sr_step(st)
+    mc.refresh_stats(st)
+    assert mc.proposal_dropped and mc.proposal_acceptance == 0.0  # the replay ran local moves only
+    mc.set_proposal(made, indep_per_sample=2, min_acceptance=0.99)
+    assert not mc.proposal_dropped
+    td.launch_sr_step(st)
+    mc.refresh_stats(st)
+    assert mc.proposal_dropped and mc.proposal_acceptance > 0.1  # re-armed: learned moves ran once more

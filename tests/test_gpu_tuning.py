@@ -86,3 +86,40 @@ def test_autotune_fills_table_and_choices_keep_results():
         assert not td.solver_info["fell_back"]
         np.testing.assert_allclose(x, d[1], rtol=1e-8, atol=1e-8 * np.abs(d[1]).max())
     ann.set_tuning({}, clear=True)
+
+
+def test_panel_pair_update_alone_matches_per_panel():
+    """The rank-128 update per panel pair against one rank-64 update per panel with no
+    refinement to hide a wrong factor (solver "fp32": one FP32 Cholesky solve): on the
+    same S both unrefined solutions have the FP32 factorisation's residual and agree to
+    its bound; in the mixed solver both forms need the same number of refinement solves.
+    Np = 560 ends in a partial pair (560 = 4 pairs + one panel of 64 + 48)."""
+    ann.set_tuning({}, clear=True)
+    psi, op, mc, td = workload()
+    assert psi.num_params == 560
+    td.eval(op, psi, mc)
+    ann.autotune(op, psi, mc, td)  # times the knobs on its own evaluations: S and F move
+    td.eval(op, psi, mc)
+    ref = td.solve(1e-3)  # mixed: refined to ||r|| / ||F|| <= 1e-12
+    table = ann.tuning_table()
+    ckey = next(k for k in table if "/chol.update/" in k)
+    pkey = ckey.replace("/chol.update/", "/chol.pair/")
+    unrefined, iters = {}, {}
+    for pair in (0, 1):
+        ann.set_tuning({ckey: 1, pkey: pair})
+        td.set_solver("fp32")
+        unrefined[pair] = td.solve(1e-3)
+        info = td.solver_info
+        assert info["update_form"] == ("tensor core, rank 128 per panel pair" if pair else
+                                       "tensor core, rank 64 per panel"), info
+        assert info["residual_first"] < 1e-4, info
+        td.set_solver("mixed", 6, 1e-12)
+        x = td.solve(1e-3)
+        iters[pair] = td.solver_info["solves"]
+        np.testing.assert_allclose(x, ref, rtol=1e-8, atol=1e-8 * np.abs(ref).max())
+    scale = np.abs(ref).max()
+    for pair in (0, 1):
+        assert np.abs(unrefined[pair] - ref).max() <= 1e-3 * scale
+    assert np.abs(unrefined[0] - unrefined[1]).max() <= 2e-3 * scale
+    assert iters[0] == iters[1], iters
+    ann.set_tuning({}, clear=True)
