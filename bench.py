@@ -1,28 +1,32 @@
-"""Benchmark of the SR step of the VMC inner loop on the 2-D TFIM 8x8 workload,
-plain FP32 form against the precision form on the same GPU in the same run.
+"""Benchmark of the VMC inner loop's SR step on the 2-D TFIM 8x8 workload (the headline),
+plain FP32 form against the precision form on the same GPU in the same run, plus the
+other workloads of the path (learned proposal at alpha = 4, CNN on the 10x10 J1-J2
+model, batched uneven instances) as legs of the same JSON line.
 
-Workload (square lattice 8 x 8, periodic, J = 1, h = 3.04): complex RBM with
-visible bias a(64), hidden bias b(128) and W(64 x 128), Np = 8384, entries
-iid N(0, 0.01^2) in real and imaginary parts (seeded). 16384 Markov chains,
-one sample per chain per SR step (N_s = 16384), diagonal shift 1e-3, lr 0.01.
-One step = sampling + local energies + O rows + <O>, F + S + solve + update.
+Headline workload (square lattice 8 x 8, periodic, J = 1, h = 3.04): complex RBM with
+visible bias a(64), hidden bias b(128) and W(64 x 128), Np = 8384, entries iid
+N(0, 0.01^2) in real and imaginary parts (seeded). 16384 Markov chains, 64 single-flip
+sweeps between samples in both forms, one sample per chain per SR step (N_s = 16384),
+diagonal shift 1e-3, lr 0.01. One step = sampling + local energies + O rows + <O>, F +
+S + solve + update. Both forms first run 300 SR steps from the same initial parameters;
+the timed steps continue from there.
 
-  plain:     64 single-flip sweeps between samples; S in FP32 (SIMT); one FP32
-             Cholesky solve with FP32 SIMT trailing updates.
-  precision: learned MADE independence moves between samples (N -> 256 -> N,
-             retrained every 10 SR steps on the last 65536 chain configurations,
-             Adam lr 1e-3, batch 4096; dropped below 10 % acceptance); S from centred
-             O in BF16 on tcgen05 with FP32 accumulation; FP32 Cholesky refined with
-             FP64 residuals against the FP64 S to ||r|| / ||F|| <= 1e-12; launch and
-             tile shapes from the autotuner, run on this workload before timing.
+  plain:     S in FP32 (SIMT); one FP32 Cholesky solve with FP32 SIMT trailing updates.
+  precision: two learned MADE independence moves per sample after the 64 sweeps
+             (N -> 256 -> N, retrained every 10 SR steps on the last 65536 chain
+             configurations, Adam lr 1e-3, batch 4096; dropped below 10 % acceptance and
+             re-armed after each retraining); S from centred O in BF16 on tcgen05 with
+             FP32 accumulation; FP32 Cholesky refined with FP64 residuals against the
+             FP64 S to ||r|| / ||F|| <= 1e-12; launch and tile shapes from the autotuner,
+             run on this workload before timing.
 
-metric: effective samples/s with E_loc = N_s / tau_int / (seconds per SR step),
-tau_int from the Sokal automatic-window estimator (c = 5) on per-chain local
-energy series of a separate sampling run with the same moves and parameters.
+metric: effective samples/s with E_loc = N_s / tau_int / (seconds per SR step), tau_int
+from the Sokal automatic-window estimator (c = 5) on per-chain local-energy series of
+200 samples per chain (4096 chains) with each form's own moves at the trained psi.
 `value` is the precision form's; `forms` and `vs_plain` carry both forms.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--form both|precision|plain]
+                       [--form both|precision|plain] [--train-steps T] [--no-legs]
 """
 
 import argparse
@@ -47,12 +51,14 @@ UNIT = "samples/s"
 L, H_FIELD, ALPHA = 8, 3.04, 2
 N_SITES = L * L
 M_HIDDEN = ALPHA * N_SITES
+NP_C2 = N_SITES + M_HIDDEN + N_SITES * M_HIDDEN
 N_CHAINS = 16384
 SWEEPS = 64
 THERM = 64
 SHIFT = 1e-3
 LR = 0.01
 SEED = 1234
+TRAIN_STEPS = 300
 # learned proposal of the precision form: MADE N -> 256 -> N, Adam lr 1e-3, batch 4096,
 # retrained every 10 SR steps on the last 65536 chain configurations
 MADE_H = 256
@@ -61,34 +67,28 @@ MADE_BATCH = 4096
 HISTORY = 65536
 RETRAIN_EVERY = 10
 MADE_FIRST_EPOCHS = 4
-LEARNED_SWEEPS = 1       # local sweeps between samples with the learned proposal on
 LEARNED_INDEP = 2        # learned independence moves per sample
-MIN_ACCEPT = 0.1         # the proposal is dropped below this acceptance
+MIN_ACCEPT = 0.1         # the proposal is dropped below this acceptance (re-armed after retraining)
+TAU_T, TAU_CHAINS = 200, 4096
 TUNING_FILE = None       # --tuning: load the tuning table instead of autotuning
-# DRAM bytes (read + written) of this workload from a one-pass ncu capture of two precision-form
-# SR steps (dram__bytes_read.sum + dram__bytes_write.sum per kernel, profile window, Np = 8384,
-# 16384 samples): the FP32 factorisation's kernels (trailing updates, panels, inverses, shift
-# conversion) 20.9 GB per factorisation with one rank-64 trailing update per panel (the
-# panel-pair form was not captured); herk_tc_kernel 7.0 GB per launch
-WORKLOAD_NP_NS = (N_SITES + M_HIDDEN + N_SITES * M_HIDDEN, N_CHAINS)
-FACTOR_DRAM_BYTES = 20.9e9
-HERK_DRAM_BYTES = 7.0e9
+
+
+def init_rbm(rng, N, M, s=0.01):
+    c = lambda *sh: s * (rng.standard_normal(sh) + 1j * rng.standard_normal(sh))  # noqa: E731
+    return c(N), c(M), c(N, M)
 
 
 def init_params(rng):
-    s = 0.01
-    a = s * (rng.standard_normal(N_SITES) + 1j * rng.standard_normal(N_SITES))
-    b = s * (rng.standard_normal(M_HIDDEN) + 1j * rng.standard_normal(M_HIDDEN))
-    W = s * (rng.standard_normal((N_SITES, M_HIDDEN)) + 1j * rng.standard_normal((N_SITES, M_HIDDEN)))
-    return a, b, W
+    return init_rbm(rng, N_SITES, M_HIDDEN)
 
 
 def config_dict(form, extra=None):
-    d = {"workload": f"2D TFIM {L}x{L} PBC h={H_FIELD}, complex RBM alpha={ALPHA} (Np=8384), "
+    d = {"workload": f"2D TFIM {L}x{L} PBC h={H_FIELD}, complex RBM alpha={ALPHA} (Np={NP_C2}), "
                      f"{N_CHAINS} chains, {SWEEPS} sweeps between samples, 1 sample/chain/SR step",
-         "form": form, "N": N_SITES, "M": M_HIDDEN, "num_params": N_SITES + M_HIDDEN + N_SITES * M_HIDDEN,
-         "chains": N_CHAINS, "sweeps_between_samples": SWEEPS, "samples_per_step": N_CHAINS,
-         "diag_shift": SHIFT, "lr": LR,
+         "form": form, "N": N_SITES, "M": M_HIDDEN, "num_params": NP_C2,
+         "chains": N_CHAINS, "sweeps_between_samples": SWEEPS,
+         "learned_moves_per_sample": LEARNED_INDEP if form == "precision" else 0,
+         "samples_per_step": N_CHAINS, "diag_shift": SHIFT, "lr": LR, "train_steps_before_timing": TRAIN_STEPS,
          "l2": "inputs larger than L2 (O rows 1.1 GB, S 1.1 GB per step)"}
     if extra:
         d.update(extra)
@@ -168,21 +168,38 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def fp32_simt_peak_tflops():
+    """FP32 FMA peak of the SIMT pipes (128 lanes x 2 flops per SM per clock) at the SM
+    clock the device reports; MEASURED_PEAKS.json has no SIMT figure."""
+    import torch
+    p = torch.cuda.get_device_properties(0)
+    mhz = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=10).stdout.split()
+        mhz = float(out[0])
+    except (OSError, ValueError, IndexError, subprocess.TimeoutExpired):
+        pass
+    return p.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def cuda_ms(fn, stream):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
 # ----------------------------------------------------------------------------------
 class Form:
-    """One form of the SR step on the 8x8 workload.
-
-    plain:     complex64 sampling with single-flip Metropolis (64 sweeps between
-               samples), S in FP32 on SIMT cores, one FP32 Cholesky solve.
-    precision: complex64 sampling with learned MADE independence moves (retrained every
-               10 SR steps on the last 65536 chain configurations), S from centred O in
-               BF16 on tcgen05 (FP32 accumulation), FP32 Cholesky + refinement against
-               the FP64 S to ||r||/||F|| <= 1e-12 (FP64 Cholesky when it stalls)."""
+    """One form of the SR step on the 8x8 workload (see the module docstring)."""
 
     def __init__(self, ann, name, rank):
         self.ann, self.name = ann, name
-        rng = np.random.default_rng(SEED)
-        a, b, W = init_params(rng)
+        a, b, W = init_params(np.random.default_rng(SEED))
         self.H = ann.transverse_field_ising_2d(L, L, h=H_FIELD)
         self.op = ann.Operator(self.H)
         self.psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
@@ -193,38 +210,34 @@ class Form:
         self.n_steps = 0
         self.tuning = None
         self.t_factor_ms = None
+        self.energy = []
+        self.drops = 0
+        self.sweeps = SWEEPS
         if name == "plain":
-            self.sweeps, self.indep = SWEEPS, 0
+            self.indep = 0
             self.tdvp = ann.TDVP(self.Np, s_mode="fp32", solver="fp32")
             self.tdvp.chol_update = "simt"  # FP32 SIMT arithmetic throughout
         else:
-            self.sweeps, self.indep = LEARNED_SWEEPS, LEARNED_INDEP
+            self.indep = LEARNED_INDEP
             self.tdvp = ann.TDVP(self.Np, s_mode="bf16", solver="mixed", max_iter=6, tol=1e-12)
             self.made = ann.MADE(N_SITES, MADE_H, seed=SEED + rank)
-        self.mc = self._ensemble(N_CHAINS, SEED + 17 * rank)
-
-    def _ensemble(self, n_samples, seed):
-        mc = self.ann.MonteCarloLoop(n_samples, self.sweeps, THERM, N_CHAINS, True, seed=seed, persistent=True)
+        self.mc = ann.MonteCarloLoop(N_CHAINS, self.sweeps, THERM, N_CHAINS, True, seed=SEED + 17 * rank,
+                                     persistent=True)
         if self.made is not None:
-            mc.set_history(HISTORY)
-        return mc
+            self.mc.set_history(HISTORY)
 
     def prepare(self, stream):
         """Thermalises the chains; the precision form fills its history with chain
-        configurations (local moves), trains the proposal and switches it on."""
+        configurations, trains the proposal, switches it on and autotunes."""
         self.tdvp.stream = stream
-        if self.made is None:
-            return
-        # first training set: 65536 configurations of thermalised chains, one local sweep apart
-        prep = self.ann.MonteCarloLoop(N_CHAINS, 1, THERM, N_CHAINS, True, seed=SEED + 5 + 17 * self.rank,
-                                       persistent=True)
-        prep.set_history(HISTORY)
         ev = self.ann.ExpectationValue(stream=stream)
+        if self.made is None:
+            ev(self.op, self.psi, self.mc)
+            return
         for _ in range((HISTORY + N_CHAINS - 1) // N_CHAINS):
-            ev(self.op, self.psi, prep)
-        self.made.train_on_samples(prep, steps=MADE_FIRST_EPOCHS * HISTORY // MADE_BATCH, batch=MADE_BATCH,
+            ev(self.op, self.psi, self.mc)
+        self.made.train_on_samples(self.mc, steps=MADE_FIRST_EPOCHS * HISTORY // MADE_BATCH, batch=MADE_BATCH,
                                    lr=MADE_LR, stream=stream)
-        self.mc.set_chains(*prep.get_chains())
         self.mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=MIN_ACCEPT)
         # launch and tile shapes for this workload (outside the timed region), or a table
         # saved by an earlier run (profiling runs: ncu serialises and slows every launch)
@@ -235,18 +248,15 @@ class Form:
             self.tuning = self.ann.autotune(self.op, self.psi, self.mc, self.tdvp, SHIFT, stream)
 
     def retrain(self, stream):
-        import torch
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        self.made.train_on_samples(self.mc, steps=HISTORY // MADE_BATCH, batch=MADE_BATCH, lr=MADE_LR,
-                                   stream=stream)
-        e1.record(stream)
-        e1.synchronize()
-        self.retrain_ms.append(e0.elapsed_time(e1))
-        self.mc.refresh_stats(stream)  # the drop rule for the learned proposal
+        """Retrains the proposal on the history ring and re-arms it (the drop rule decides
+        again on the next sampling pass)."""
+        self.mc.refresh_stats(stream)
+        self.drops += int(self.mc.proposal_dropped)
+        self.retrain_ms.append(cuda_ms(lambda: self.made.train_on_samples(
+            self.mc, steps=HISTORY // MADE_BATCH, batch=MADE_BATCH, lr=MADE_LR, stream=stream), stream))
+        self.mc.set_proposal(self.made, indep_per_sample=self.indep, min_acceptance=MIN_ACCEPT)
 
     def step(self, stream):
-        # the proposal is retrained every RETRAIN_EVERY SR steps after its first training
         if self.made is not None and self.n_steps > 0 and self.n_steps % RETRAIN_EVERY == 0:
             self.retrain(stream)
         self.tdvp.sr_step(self.op, self.psi, self.mc, SHIFT, LR)
@@ -263,31 +273,39 @@ class Form:
         self.tdvp.launch_sr_step(stream)
         self.n_steps += 1
 
-    def tau(self, sweeps=None, indep=None):
-        """tau_int of the local energy from T samples per chain of a separate run with
-        the same moves (fresh chains, thermalised with local sweeps)."""
-        T = 24
-        sweeps = self.sweeps if sweeps is None else sweeps
-        indep = self.indep if indep is None else indep
-        mc = self.ann.MonteCarloLoop(N_CHAINS * T, sweeps, THERM, N_CHAINS, True, seed=SEED + 99,
-                                     persistent=True)
+    def train(self, n, stream):
+        """n SR steps as graph replays, recording the energy per site of every step."""
+        self.capture(stream)
+        self.energy.append(self.tdvp.E_local.real / N_SITES)
+        for _ in range(n - 1):
+            self.graph_step(stream)
+            self.energy.append(self.tdvp.E_local.real / N_SITES)
+
+    def tau_run(self, sweeps, indep, T=TAU_T, chains=TAU_CHAINS):
+        """tau_int, acceptance and cost per sample of chains with `sweeps` local sweeps and
+        `indep` learned moves per sample, continuing from the form's chains at the current
+        psi; T samples per chain."""
+        import torch
+        conf, ctr = self.mc.get_chains()
+        mc = self.ann.MonteCarloLoop(chains * T, sweeps, 0, chains, True, seed=SEED + 99, persistent=True)
+        mc.set_chains(conf[:chains], ctr[:chains])
         if self.made is not None and indep:
             mc.set_proposal(self.made, indep_per_sample=indep, min_acceptance=0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         self.ann.ExpectationValue()(self.op, self.psi, mc)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
         _, _, el = mc.samples()
+        x = el.real.reshape(T, chains)
+        tau = tau_int_sokal(x)
         acc = {"local": mc.acceptance_rate}
         if self.made is not None and indep:
             acc["learned"] = mc.proposal_acceptance
-        return tau_int_sokal(el.real.reshape(T, N_CHAINS)), acc
-
-    def tau_ablation(self):
-        """tau_int with the learned moves alone, the local sweeps alone, and both."""
-        out = {}
-        for name, sw, ind in (("learned_only", 0, self.indep), ("local_only", self.sweeps, 0),
-                              ("local_and_learned", self.sweeps, self.indep)):
-            t, a = self.tau(sw, ind)
-            out[name] = {"sweeps": sw, "learned_moves": ind, "tau_int": t, "acceptance": a}
-        return out
+        se = float(x.std() * np.sqrt(tau / x.size) / N_SITES)
+        return {"sweeps": sweeps, "learned_moves": indep, "tau_int": tau, "acceptance": acc,
+                "ms_per_sample_pass": ms / T, "energy_per_site": float(x.mean() / N_SITES), "se_per_site": se,
+                "effective_samples_per_s_sampler": chains / tau / (ms / T * 1e-3)}
 
     def energy_check(self):
         """Per-site energy of the last step's 16384 sample configurations with the current
@@ -302,6 +320,36 @@ class Form:
                 "abs_diff_per_site_vs_fp64": float(abs(el32.mean() - el64.mean()) / N_SITES),
                 "max_abs_diff_per_sample_per_site": float(np.abs(el32 - el64).max() / N_SITES)}
 
+    def fp64_errors(self, stream):
+        """E, F, S and the SR update delta of one eager evaluation of this form against a
+        full FP64 evaluation on the same 16384 sample configurations: complex128 log psi,
+        local energies and O rows, S from FP64 HERK, delta from the FP64 Cholesky solve of
+        (S + shift) delta = F. Relative Frobenius / 2-norm errors."""
+        ann = self.ann
+        self.tdvp.eval(self.op, self.psi, self.mc)
+        stream.synchronize()
+        S, F, E = self.tdvp.S_matrix, self.tdvp.F_vector, self.tdvp.E_local
+        d = self.tdvp.solve(SHIFT)
+        conf, _, _ = self.mc.samples()
+        psi64 = ann.PsiRBM(self.psi.W, 1.0, 0.0, True, a=self.psi.a, b=self.psi.b, precision="fp64")
+        psi64.params = self.psi.params
+        n = len(conf)
+        replay = ann.MonteCarloLoop(n, 0, 0, n, True, persistent=True)
+        replay.set_tape(conf[:, 0], np.zeros((n, 1), np.uint32), np.zeros((n, 1)))
+        td64 = ann.TDVP(self.Np, s_mode="fp32", solver="fp64", stream=stream)
+        td64.eval(self.op, psi64, replay)
+        c64, _, _ = replay.samples()
+        assert (c64[:, 0] == conf[:, 0]).all()
+        S64, F64, E64 = td64.S_matrix, td64.F_vector, td64.E_local
+        d64 = td64.solve(SHIFT)
+        rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))  # noqa: E731
+        out = {"energy_abs_diff_per_site": float(abs(E - E64) / N_SITES), "F_rel_err": rel(F, F64),
+               "S_rel_err_fro": rel(S, S64), "delta_rel_err": rel(d, d64),
+               "S_max_abs_err_rel_to_max": float(np.abs(S - S64).max() / np.abs(S64).max()),
+               "samples": n, "reference": "complex128 kernels + FP64 HERK + FP64 Cholesky on the same samples"}
+        del S, S64
+        return out
+
 
 def eager_phases(form, stream, n=3):
     """CUDA-event phase times (sampling, reductions, S, solve, update) and the time of the
@@ -310,14 +358,8 @@ def eager_phases(form, stream, n=3):
     ann._lib.call("ann_set_phase_timing", 1)
     phase = np.zeros(5)
     t_factor, ms_eager = [], []
-    import torch
     for _ in range(n):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        form.step(stream)
-        e1.record(stream)
-        e1.synchronize()
-        ms_eager.append(e0.elapsed_time(e1))
+        ms_eager.append(cuda_ms(lambda: form.step(stream), stream))
         ph = np.zeros(5, np.float32)
         ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
         phase += ph
@@ -338,7 +380,8 @@ def timed_steps(form, args, stream, dist):
     import annongpu_gb300 as ann
     phase = eager_phases(form, stream)
     form.capture(stream)
-    form.graph_step(stream)  # one replay before the timed region
+    for _ in range(args.warmup):
+        form.graph_step(stream)
     stream.synchronize()
     if args.profile_window:
         ann.start_profiling()  # ncu --profile-from-start off captures the timed steps only
@@ -357,10 +400,6 @@ def timed_steps(form, args, stream, dist):
     if args.profile_window:
         ann.stop_profiling()
     ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     launches = ann.launch_count() - lc0
     return ms, phase, launches
 
@@ -382,35 +421,205 @@ def whole_job(ms, ms_e2e, samples, tau, dist):
     return ms, ms_e2e, eff / (ms * 1e-3), eff / (ms_e2e * 1e-3)
 
 
-def form_summary(form, ms, phase, tau, acc):
+def form_summary(form, ms, phase, tau_rec):
     Ns = N_CHAINS
+    tau = tau_rec["tau_int"]
+    e = np.asarray(form.energy[-20:])
     d = {"ms_per_step": ms, "ms_per_step_eager": getattr(form, "ms_eager", None), "sr_steps_per_s": 1e3 / ms,
          "effective_samples_per_s": Ns / tau / (ms * 1e-3),
          "sampler_effective_samples_per_s": Ns / tau / (phase[0] * 1e-3),
-         "tau_int": tau, "acceptance": acc,
+         "tau_int": tau, "tau_samples_per_chain": TAU_T, "acceptance": tau_rec["acceptance"],
          "phase_ms": {"sample_eloc_O": phase[0], "reductions": phase[1], "S": phase[2], "solve": phase[3],
                       "update": phase[4]},
-         "sweeps_between_samples": form.sweeps, "learned_moves_per_sample": form.indep}
+         "sweeps_between_samples": form.sweeps, "learned_moves_per_sample": form.indep,
+         "energy_per_site_after_training": {"steps": len(form.energy), "mean_last_20": float(e.mean()),
+                                            "se_last_20": float(e.std(ddof=1) / np.sqrt(len(e))) if len(e) > 1
+                                            else None,
+                                            "trajectory_every_50": [round(float(x), 6) for x in form.energy[::50]]},
+         "energy_per_site_trained_psi": {"value": tau_rec["energy_per_site"], "se": tau_rec["se_per_site"],
+                                         "samples": TAU_T * TAU_CHAINS}}
     if form.retrain_ms:
         d["proposal_retrain_ms"] = float(np.mean(form.retrain_ms))
+        d["proposal_dropped_at_retrains"] = form.drops
     if form.tuning:
         d["autotune_ms"] = {k: {str(c): round(ms, 4) for c, ms in v.items()} for k, v in form.tuning.items()}
     return d
 
 
 # ----------------------------------------------------------------------------------
-# Batched uneven instances (BASELINE config 5): 96 1-D TFIM chains, L uniform on
-# {12, 16, ..., 48}, h uniform on [0.5, 1.5], J = 1, complex RBM with alpha from
-# {1, 2, 4} and a per-instance seed; chains 512 .. 8192 in proportion to Np.
+# Learned proposal at alpha = 4: 1-D TFIM N = 64, h = 1.0 and 2-D TFIM 8 x 8, h = 3.04,
+# complex RBM alpha = 4 (M = 256, Np = 16704), 16384 chains; the psi is trained by SR with
+# the learned moves on, then local Metropolis and the learned moves are compared there.
+C4_TRAIN = 200
+C4_SWEEP_SETS = [(1, 0), (2, 0), (4, 0), (8, 0), (0, 2), (0, 4), (1, 2), (1, 4)]
+C4_RETRAIN_EPOCHS = 4    # passes over the 65536 configurations per retraining (every 10 SR steps)
+C4_FINAL_EPOCHS = 16     # before the move sets are compared at the trained psi
+
+
+def learned_proposal_leg(ann, st, name, H, train_steps=C4_TRAIN):
+    import torch
+    a, b, W = init_rbm(np.random.default_rng(SEED + 4), 64, 256)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    op = ann.Operator(H)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed", max_iter=6, tol=1e-12, stream=st)
+    made = ann.MADE(64, MADE_H, seed=SEED + 5)
+    mc = ann.MonteCarloLoop(N_CHAINS, 1, THERM, N_CHAINS, True, seed=SEED + 6, persistent=True)
+    mc.set_history(HISTORY)
+    ev = ann.ExpectationValue(stream=st)
+    for _ in range(HISTORY // N_CHAINS):
+        ev(op, psi, mc)
+    made.train_on_samples(mc, steps=MADE_FIRST_EPOCHS * HISTORY // MADE_BATCH, batch=MADE_BATCH, lr=MADE_LR,
+                          stream=st)
+    mc.set_proposal(made, indep_per_sample=LEARNED_INDEP, min_acceptance=MIN_ACCEPT)
+    energy, acc_hist, drops, retrain = [], [], 0, []
+    td.capture_sr_step(op, psi, mc, SHIFT, LR, st)
+    t0 = time.perf_counter()
+    for k in range(1, train_steps):
+        if k % RETRAIN_EVERY == 0:
+            mc.refresh_stats(st)
+            drops += int(mc.proposal_dropped)
+            acc_hist.append(round(mc.proposal_acceptance, 4))
+            retrain.append(cuda_ms(lambda: made.train_on_samples(mc, steps=C4_RETRAIN_EPOCHS * HISTORY // MADE_BATCH,
+                                                                 batch=MADE_BATCH, lr=MADE_LR, stream=st), st))
+            mc.set_proposal(made, indep_per_sample=LEARNED_INDEP, min_acceptance=MIN_ACCEPT)
+        td.launch_sr_step(st)
+        energy.append(td.E_local.real / 64)
+    torch.cuda.synchronize()
+    ms_step = (time.perf_counter() - t0) * 1e3 / max(train_steps - 1, 1)
+    # the proposal retrained at the trained psi, then each move set from the same chains
+    made.train_on_samples(mc, steps=C4_FINAL_EPOCHS * HISTORY // MADE_BATCH, batch=MADE_BATCH, lr=MADE_LR, stream=st)
+    conf, ctr = mc.get_chains()
+    rows = []
+    for sw, ind in C4_SWEEP_SETS:
+        m = ann.MonteCarloLoop(TAU_CHAINS * TAU_T, sw, 0, TAU_CHAINS, True, seed=SEED + 99, persistent=True)
+        m.set_chains(conf[:TAU_CHAINS], ctr[:TAU_CHAINS])
+        if ind:
+            m.set_proposal(made, indep_per_sample=ind, min_acceptance=0.0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ann.ExpectationValue()(op, psi, m)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t1) * 1e3 / TAU_T
+        _, _, el = m.samples()
+        x = el.real.reshape(TAU_T, TAU_CHAINS)
+        tau = tau_int_sokal(x)
+        acc = {"local": round(m.acceptance_rate, 4)}
+        if ind:
+            acc["learned"] = round(m.proposal_acceptance, 4)
+        rows.append({"sweeps": sw, "learned_moves": ind, "tau_int": tau, "acceptance": acc,
+                     "ms_per_sample_pass": ms, "effective_samples_per_s_sampler": TAU_CHAINS / tau / (ms * 1e-3),
+                     "energy_per_site": float(x.mean() / 64), "se_per_site": float(x.std() * np.sqrt(tau / x.size) / 64)})
+    best_local = max((r for r in rows if r["learned_moves"] == 0), key=lambda r: r["effective_samples_per_s_sampler"])
+    best_learned = max((r for r in rows if r["learned_moves"] > 0), key=lambda r: r["effective_samples_per_s_sampler"])
+    e = np.asarray(energy[-20:])
+    return {"workload": name, "num_params": psi.num_params, "chains": N_CHAINS, "train_steps": train_steps,
+            "ms_per_sr_step": ms_step, "sr_step": "1 local sweep + 2 learned moves per sample, BF16 tcgen05 S, "
+                                                  "mixed solve, graph replays (retraining included)",
+            "energy_per_site_last_20": float(e.mean()) if len(e) else None,
+            "energy_trajectory_every_20": [round(float(x), 6) for x in energy[::20]],
+            "proposal": {"acceptance_at_retrains": acc_hist, "dropped_at_retrains": drops,
+                         "retrain_ms": float(np.mean(retrain)) if retrain else None,
+                         "retrain_epochs": C4_RETRAIN_EPOCHS, "final_epochs": C4_FINAL_EPOCHS,
+                         "note": "acceptance of the last pass before each retraining (0 after a drop: the "
+                                 "learned moves are off until re-armed by the retraining)"},
+            "move_sets_at_trained_psi": rows,
+            "learned_gain_effective_samples_per_s": best_learned["effective_samples_per_s_sampler"] /
+            best_local["effective_samples_per_s_sampler"],
+            "best_local": [best_local["sweeps"], 0], "best_learned": [best_learned["sweeps"],
+                                                                     best_learned["learned_moves"]]}
+
+
+# ----------------------------------------------------------------------------------
+# CNN on the 2-D J1-J2 Heisenberg model: 10 x 10 periodic, J1 = 1, J2 = 0.5, Sz = 0
+# (50 up spins), two periodic 3 x 3 conv layers (16 then 8 channels), log cosh, sum
+# pooling, kernels N(0, 0.02^2), 32768 chains with exchange moves over the J1 and J2
+# bonds (one sweep of 100 proposals between samples), S from centred O with split hi+lo
+# BF16 products, FP64 Cholesky solve with diagonal shift 1e-4.
+C3_CHAINS, C3_SWEEPS, C3_SHIFT = 32768, 1, 1e-4
+
+
+def cnn_leg(ann, st, steps=3, warm=2):
+    import torch
+    rng = np.random.default_rng(SEED + 3)
+    np_ = 16 * 9 + 16 * 8 * 9
+    params = 0.02 * (rng.standard_normal(np_) + 1j * rng.standard_normal(np_))
+    psi = ann.PsiCNN([1, 10, 10], [16, 8], [[1, 3, 3], [1, 3, 3]], np.zeros(100, np.uint32), params, 1.0, 0.0,
+                     True, activation="logcosh", precision="fp32")
+    op = ann.Operator(ann.heisenberg_j1j2_2d(10, 10, 1.0, 0.5))
+    nn, nnn = ann.square_lattice_bonds(10, 10, diagonal=True)
+    mc = ann.MonteCarloSpins(C3_CHAINS, C3_SWEEPS, 8, C3_CHAINS, True, move="exchange",
+                             bonds=np.array(nn + nnn, np.uint32), n_up=50, seed=SEED + 7, persistent=True)
+    td = ann.TDVP(np_, s_mode="bf16_split", solver="fp64", stream=st)
+    for _ in range(warm):
+        td.sr_step(op, psi, mc, C3_SHIFT, LR)
+    ann._lib.call("ann_set_phase_timing", 1)
+    phase = np.zeros(5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        td.sr_step(op, psi, mc, C3_SHIFT, LR)
+        ph = np.zeros(5, np.float32)
+        ann._lib.call("ann_get_phase_times", ann._lib.ptr(ph))
+        phase += ph
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    ann._lib.call("ann_set_phase_timing", 0)
+    phase /= steps
+    mc.refresh_stats(st)
+    conf, _, _ = mc.samples()
+    pop = np.array([bin(int(x)).count("1") + bin(int(y)).count("1") for x, y in conf[:256]])
+    o_bytes = 8.0 * np_ * C3_CHAINS
+    return {"workload": "2D J1-J2 10x10 PBC J2=0.5, Sz=0, PsiCNN 3x3 16 -> 8 channels log cosh (Np=1296), "
+                        f"{C3_CHAINS} chains, exchange moves over J1+J2 bonds, {C3_SWEEPS} sweep (100 proposals) "
+                        "between samples, hi+lo BF16 S, FP64 Cholesky, shift 1e-4",
+            "ms_per_sr_step": ms, "sr_steps_per_s": 1e3 / ms,
+            "phase_ms": {"sample_eloc_O": phase[0], "reductions": phase[1], "S": phase[2], "solve": phase[3],
+                         "update": phase[4]},
+            "samples_per_s": C3_CHAINS / (ms * 1e-3), "acceptance": mc.acceptance_rate,
+            "sz_sector_kept": bool((pop == 50).all()), "energy_per_site": td.E_local.real / 100,
+            "O_rows_hbm_gbs": o_bytes / (phase[0] * 1e-3) / 1e9,
+            "note": "synchronous eager steps; the sampler phase is SIMT-bound (psi ratios of 400 bond "
+                    "pairs per sample from the 3x3 / 5x5 cones), O rows are 8 * Np bytes per sample"}
+
+
+def cnn_cpu_seconds_per_sample():
+    """The FP64 oracle's restatement (not the reference: it caps N at 64 and channels at
+    6) on one 10x10 sample: one exchange sweep of full forward passes, the J1-J2 local
+    energy and the O_k row."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import CnnDesc, Oracle
+    ex = _expression_module()
+    rng = np.random.default_rng(SEED + 3)
+    np_ = 16 * 9 + 16 * 8 * 9
+    params = 0.02 * (rng.standard_normal(np_) + 1j * rng.standard_normal(np_))
+    ref = CnnDesc([1, 10, 10], [16, 8], [[1, 3, 3], [1, 3, 3]], np.zeros(100, np.uint32), params, 1.0,
+                  activation=1)
+    o = Oracle()
+    nn, nnn = ex.square_lattice_bonds(10, 10, diagonal=True)
+    H = ex.heisenberg_j1j2_2d(10, 10, 1.0, 0.5)
+    t0 = time.perf_counter()
+    r = o.cnn_mc_philox(ref, H, 1, SEED, 1, 1, 0, move_kind=1, bonds=np.array(nn + nnn, np.uint32), n_up=50)
+    o.cnn_O_k(ref, int(r["sconf"][0]) | (int(r["sconf"][1]) << 64))
+    return time.perf_counter() - t0
+
+
+# ----------------------------------------------------------------------------------
+# Batched uneven instances: 96 1-D TFIM chains, L uniform on {12, 16, ..., 48}, h uniform
+# on [0.5, 1.5], J = 1, complex RBM with alpha from {1, 2, 4} and a per-instance seed;
+# chains 512 .. 8192 in proportion to Np; per-instance FP64 Cholesky SR solves.
 N_INST = 96
 BATCH_SWEEPS = 4
+BATCH_MADE_H = 64
+BATCH_HISTORY_PASSES = 4
+BATCH_MADE_STEPS = 64
 
 
 def batched_instances(ann, st, steps):
-    """One persistent sampling + E_loc launch for all instances, per-instance S (BF16
-    tcgen05) and mixed solves on a stream pool, the whole step one CUDA graph; against the
-    same instances stepped one after another (one CUDA graph each). Energies of the
-    instances with L <= 20 against exact summation."""
+    """One persistent sampling + E_loc launch for all instances (local sweeps and each
+    instance's learned proposal), per-instance S (BF16 tcgen05) and FP64 Cholesky solves on
+    a stream pool, the whole step one CUDA graph; against the same instances stepped one
+    after another (one CUDA graph each). Energies of the instances with L <= 20 against
+    exact summation."""
     import torch
     rng = np.random.default_rng(SEED + 5)
     specs = [(int(rng.choice(np.arange(12, 49, 4))), float(rng.uniform(0.5, 1.5)), int(rng.choice([1, 2, 4])))
@@ -426,8 +635,26 @@ def batched_instances(ann, st, steps):
         psi = ann.PsiRBM(c(L, al * L), 1.0, 0.0, True, a=c(L), b=c(al * L), precision="fp32")
         op = ann.Operator(ann.transverse_field_ising_1d(L, h))
         mc = ann.MonteCarloLoop(chains[k], BATCH_SWEEPS, 16, chains[k], True, seed=SEED + 2000 + k, persistent=True)
-        td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed", stream=st)
+        mc.set_history(BATCH_HISTORY_PASSES * chains[k])
+        td = ann.TDVP(psi.num_params, s_mode="bf16", solver="fp64", stream=st)
         return psi, op, mc, td
+
+    def arm_proposals(inst, batch=None):
+        """Fills each instance's history with BATCH_HISTORY_PASSES sampling passes, trains its
+        MADE (L -> 64 -> L) on them and switches the learned moves on."""
+        for _ in range(BATCH_HISTORY_PASSES):
+            if batch is not None:
+                batch.sample()
+            else:
+                for psi, op, mc, _ in inst:
+                    ann.ExpectationValue(stream=st)(op, psi, mc)
+        mades = []
+        for k, (psi, op, mc, _) in enumerate(inst):
+            made = ann.MADE(psi.N, BATCH_MADE_H, seed=SEED + 3000 + k)
+            made.train_on_samples(mc, steps=BATCH_MADE_STEPS, batch=1024, lr=MADE_LR, stream=st)
+            mc.set_proposal(made, indep_per_sample=LEARNED_INDEP, min_acceptance=MIN_ACCEPT)
+            mades.append(made)
+        return mades
 
     def timed(fn, n):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -439,15 +666,24 @@ def batched_instances(ann, st, steps):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n
 
-    # batched: one graph per step
     inst = [make(k) for k in range(N_INST)]
     batch = ann.Batch(*[list(x) for x in zip(*inst)], stream=st)
-    batch.capture_sr_step(SHIFT, LR, st)  # runs one eager step (thermalises) first
+    mades = arm_proposals(inst, batch)  # noqa: F841 (kept alive with the ensembles)
+    batch.capture_sr_step(SHIFT, LR, st)  # runs one eager step first
     batch.launch_sr_step(st)
     ms_batched = timed(lambda: batch.launch_sr_step(st), steps)
-    # energies after the timed steps (persistent, equilibrated chains)
+    # the same step with the mixed-precision solve per instance (FP32 Cholesky on the tensor
+    # cores + FP64 refinement to ||r|| / ||F|| <= 1e-12), for comparison
+    for _, _, _, td in inst:
+        td.set_solver("mixed", 6, 1e-12)
+    batch.capture_sr_step(SHIFT, LR, st)
+    ms_batched_mixed = timed(lambda: batch.launch_sr_step(st), steps)
     batch.sample()
     E = batch.energies()
+    acc = []
+    for _, _, mc, _ in inst:
+        mc.refresh_stats(st)
+        acc.append(mc.proposal_acceptance)
     checks = []
     for k, (L, h, al) in enumerate(specs):
         if L <= 20:
@@ -460,17 +696,24 @@ def batched_instances(ann, st, steps):
             checks.append({"L": L, "alpha": al, "h": round(h, 4), "E_mc": float(E[k].real), "E_exact": float(e_ex),
                            "abs_diff_per_site": float(abs(E[k].real - e_ex) / L),
                            "diff_in_se": float(abs(E[k].real - e_ex) / se)})
-    del batch, inst
+    del batch, inst, mades
     torch.cuda.empty_cache()
-    # one instance after another: a captured SR step per instance, launched in turn
     seq = [make(k) for k in range(N_INST)]
+    mades = arm_proposals(seq)  # noqa: F841
     for psi, op, mc, td in seq:
         td.capture_sr_step(op, psi, mc, SHIFT, LR, st)
     ms_seq = timed(lambda: [td.launch_sr_step(st) for (_, _, _, td) in seq], steps)
     samples = sum(chains)
     return {"instances": N_INST, "samples_per_step": samples, "num_params_range": [lo, hi],
             "chains_range": [min(chains), max(chains)], "sweeps_between_samples": BATCH_SWEEPS,
+            "solver": "per-instance FP64 Cholesky + 1 refinement step",
+            "learned_proposal": {"made": f"L -> {BATCH_MADE_H} -> L per instance, trained on "
+                                         f"{BATCH_HISTORY_PASSES} sampling passes", "moves_per_sample": LEARNED_INDEP,
+                                 "acceptance_mean": float(np.mean(acc)), "acceptance_min": float(np.min(acc)),
+                                 "dropped": int(sum(a < MIN_ACCEPT for a in acc))},
+            "form": "BF16 tcgen05 S + learned proposal + one batched sampling launch (the combined form)",
             "ms_per_step_batched": ms_batched, "ms_per_step_one_by_one": ms_seq,
+            "ms_per_step_batched_mixed_solver": ms_batched_mixed,
             "speedup": ms_seq / ms_batched, "samples_per_s_batched": samples / (ms_batched * 1e-3),
             "exact_summation_checks": checks,
             "max_diff_in_standard_errors": max(c["diff_in_se"] for c in checks) if checks else None}
@@ -485,14 +728,49 @@ def hsd_timing(ann, f, st):
     op = ann.Operator(ann.identity() + 0.01j * f.H)
     hsd = ann.HilbertSpaceDistance(psi_p.num_params, stream=st)
     hsd.gradient(f.psi, psi_p, op, True, f.mc, 1.0)
-    reps = 5
+    reps = 3
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
         _, d = hsd.gradient(f.psi, psi_p, op, True, f.mc, 1.0)
     ms = (time.perf_counter() - t0) * 1e3 / reps
     return {"ms_per_gradient_call": ms, "samples": N_CHAINS, "distance": d,
-            "note": "host-synchronous calls (the gradient returns to the host), sampling included"}
+            "note": "host-synchronous calls (the gradient returns to the host), 64-sweep sampling included"}
+
+
+def roofline_objects(f, ms, phase, pk, pk_kind):
+    """The dominant kernel of the precision step (the sampler at 64 sweeps) and the other
+    two large kernel groups, each with its algorithmic work per launch."""
+    Np, Ns = f.Np, N_CHAINS
+    props = Ns * (SWEEPS * N_SITES)
+    simt_peak = fp32_simt_peak_tflops()
+    flops_sampler = 34.0 * M_HIDDEN * props  # 34 M flops per proposal (the 64-sweep part alone)
+    sampler = {"bound": "fp32_simt", "kernel": "rbm_mc_kernel<float,1,4> (sampling + E_loc + O rows)",
+               "achieved": flops_sampler / (phase[0] * 1e-3) / 1e12, "peak": simt_peak, "unit": "TFLOP/s",
+               "frac": flops_sampler / (phase[0] * 1e-3) / 1e12 / simt_peak, "ms": phase[0],
+               "traffic": None,
+               "work": f"34*M flops per single-flip proposal x {props} proposals per step (16384 chains x 64 "
+                       "sweeps x 64 sites); E_loc and the O-row writes (1.1 GB) are not credited",
+               "peak_kind": "nominal FP32 FMA rate (SMs x 128 lanes x 2 flops x max SM clock): "
+                            "MEASURED_PEAKS.json holds no SIMT figure"}
+    flops_S = 4.0 * Np * (Np + 1) * Ns
+    herk = {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
+            "achieved": flops_S / (phase[2] * 1e-3) / 1e12, "peak": pk.get("bf16_tflops", 1900.0),
+            "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst", "ms": phase[2], "traffic": None,
+            "work": "4*Np*(Np+1)*Ns real flops per step (over the S phase: operand prep + kernel)"}
+    herk["frac"] = herk["achieved"] / herk["peak"]
+    out = {"roofline": sampler, "roofline_herk": herk}
+    if f.t_factor_ms:
+        chol = (4.0 / 3.0) * Np ** 3 / (f.t_factor_ms * 1e-3) / 1e12
+        peak = pk.get("bf16_tflops", 1900.0)
+        out["roofline_factorisation"] = {
+            "bound": "tensor", "kernel": "FP32 Cholesky factorisation (tcgen05 split-TF32 trailing updates + "
+                                        "potrf32/trsm32 panel path)",
+            "achieved": chol, "peak": peak, "unit": "TFLOP/s", "frac": chol / peak, "ms": f.t_factor_ms,
+            "traffic": None, "update_form": f.tdvp.solver_info.get("update_form"),
+            "peak_kind": pk_kind + " bf16 burst (no credit for the three split products)",
+            "work": "(4/3)*Np^3 real flops per factorisation (CUDA events around it)"}
+    return out
 
 
 def run_ours(args):
@@ -511,12 +789,14 @@ def run_ours(args):
     clocks = ClockSampler()
     clk = None
     forms = ["plain", "precision"] if args.form == "both" else [args.form]
+    t_train = {}
     for name in forms:
         f = Form(ann, name, rank)
         f.prepare(st)
-        for _ in range(args.warmup):
-            f.step(st)
-        st.synchronize()
+        t0 = time.perf_counter()
+        f.train(args.train_steps, st)
+        torch.cuda.synchronize()
+        t_train[name] = time.perf_counter() - t0
         if name == "precision" or len(forms) == 1:
             clocks.start()
         ms, phase, launches = timed_steps(f, args, st, dist)
@@ -524,36 +804,20 @@ def run_ours(args):
             clk = clocks.stop()
         f.mc.refresh_stats(st)
         info = f.tdvp.solver_info
-        tau, acc = f.tau()
-        results[name] = (f, ms, phase, launches, tau, acc, info)
+        tau_rec = f.tau_run(f.sweeps, f.indep)
+        results[name] = (f, ms, phase, launches, tau_rec, info)
 
     main = results["precision"] if "precision" in results else results[forms[0]]
-    f, ms, phase, launches, tau, acc, info = main
+    f, ms, phase, launches, tau_rec, info = main
+    tau = tau_rec["tau_int"]
     Np, Ns = f.Np, N_CHAINS
     energy = f.energy_check()
-    ablation = f.tau_ablation() if f.made is not None else None
-
-    # the same step with the FP64 Cholesky solver (and the solve error of the mixed solver)
-    fp64 = {}
-    if f.name == "precision":
-        d_mixed = f.tdvp.solve(SHIFT)
-        f.tdvp.set_solver("fp64")
-        d_fp64 = f.tdvp.solve(SHIFT)  # same S and F
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        f.step(st)
-        e1.record(st)
-        e1.synchronize()
-        f.tdvp.set_solver("mixed", 6, 1e-12)
-        fp64 = {"ms_per_step_fp64_cholesky": e0.elapsed_time(e1),
-                "solve_rel_err_vs_fp64_cholesky": float(np.linalg.norm(d_mixed - d_fp64) / np.linalg.norm(d_fp64))}
+    summary = {name: form_summary(r[0], r[1], r[2], r[4]) for name, r in results.items()}
 
     # end to end through the public API: parameters from pinned host memory in, the
     # step's energy out, every step
     host_params = torch.from_numpy(f.psi.params.view(np.float64).copy()).pin_memory()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    f.capture(st)  # the parameters may have changed: recapture, then replay
+    f.capture(st)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -564,71 +828,73 @@ def run_ours(args):
     ms_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
 
     pk, pk_kind = peaks()
-    flops_S = 4.0 * Np * (Np + 1) * Ns  # algorithmic HERK count per step
-    s_tflops = flops_S / (phase[2] * 1e-3) / 1e12
-    summary = form_summary(f, ms, phase, tau, acc)
-    ms, ms_e2e, value, e2e_value = whole_job(ms, ms_e2e, Ns, tau, dist)
+    ms_w, ms_e2e_w, value, e2e_value = whole_job(ms, ms_e2e, Ns, tau, dist)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_w, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": ("c64 sampling + learned proposal / bf16 S (fp32 acc) / fp32 Cholesky + f64 refinement"
                   if f.name == "precision" else "c64 sampling / fp32 S / fp32 Cholesky"),
-        "data": "synthetic (seeded random-init RBM, 2D TFIM)",
+        "data": "synthetic (seeded random-init RBM trained by SR, 2D TFIM)",
         "config": config_dict(f.name),
-        "sr_steps_per_s": 1e3 / ms, "ms_per_step_eager": f.ms_eager, "tau_int": tau, "acceptance": acc,
+        "sr_steps_per_s": 1e3 / ms_w, "ms_per_step_eager": f.ms_eager, "tau_int": tau,
+        "tau_samples_per_chain": TAU_T, "acceptance": tau_rec["acceptance"],
         "energy_per_site": energy["energy_per_site"], "energy_check": energy,
-        "phase_ms": summary["phase_ms"], "phase_note": "CUDA-event phases of eager steps (the headline times graph replays)",
-        "solver": info,
-        "roofline_herk": {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
-                          "achieved": s_tflops, "peak": pk.get("bf16_tflops", 1900.0) if f.name == "precision" else None,
-                          "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst",
-                          "traffic": HERK_DRAM_BYTES if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision"
-                          else None,
-                          "work": "4*Np*(Np+1)*Ns real flops per step (over the S phase: operand prep + kernel)"},
+        "phase_ms": summary[f.name]["phase_ms"],
+        "phase_note": "CUDA-event phases of eager steps (the headline times graph replays)",
+        "solver": info, "train_seconds": t_train,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": Np * 16,
-                "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e},
+                "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e_w},
         "gpu_launches": int(launches),
     }
-    if out["roofline_herk"]["peak"]:
-        out["roofline_herk"]["frac"] = s_tflops / out["roofline_herk"]["peak"]
-    if getattr(f, "t_factor_ms", None):
-        # FP32 Cholesky: (4/3) Np^3 real flops of complex factorisation; its trailing
-        # updates run as three TF32 products on tcgen05 (TF32 rate = half the BF16 rate)
-        chol_tflops = (4.0 / 3.0) * Np ** 3 / (f.t_factor_ms * 1e-3) / 1e12
-        tf32x3_peak = pk.get("bf16_tflops", 1900.0) / 2 / 3
-        # the autotuned form of the trailing updates; the DRAM capture is of the per-panel form
-        pair = any("/chol.pair/" in k and v == 1 for k, v in ann.tuning_table().items())
-        # the dominant kernel group of the step: trailing updates + panel path are about half
-        # of the launch list (the S kernel 14 %)
-        out["roofline"] = {"bound": "tensor",
-                           "kernel": "FP32 Cholesky factorisation (chol_update_tc3 tcgen05 split-TF32 trailing "
-                                     "updates + potrf32/trsm32 panel path)",
-                           "achieved": chol_tflops, "peak": tf32x3_peak, "unit": "TFLOP/s",
-                           "frac": chol_tflops / tf32x3_peak, "ms": f.t_factor_ms,
-                           "traffic": FACTOR_DRAM_BYTES
-                           if (Np, Ns) == WORKLOAD_NP_NS and f.name == "precision" and not pair else None,
-                           "update_form": "rank 128 per panel pair" if pair else "rank 64 per panel",
-                           "peak_kind": pk_kind + " bf16 burst / 2 (TF32) / 3 (split products)",
-                           "work": "(4/3)*Np^3 real flops per factorisation (CUDA events around it)"}
-    else:
-        out["roofline"] = out["roofline_herk"]
-    out.update(fp64)
-    if ablation:
-        out["tau_ablation"] = ablation
-    out["forms"] = {name: form_summary(r[0], r[1], r[2], r[4], r[5]) for name, r in results.items()}
+    out.update(roofline_objects(f, ms, phase, pk, pk_kind))
+    out["forms"] = summary
     if "plain" in results and "precision" in results:
-        p, q = out["forms"]["plain"], out["forms"]["precision"]
+        p, q = summary["plain"], summary["precision"]
         out["vs_plain"] = {k: q[k] / p[k] for k in ("sr_steps_per_s", "effective_samples_per_s",
                                                     "sampler_effective_samples_per_s")}
+        ep, eq = p["energy_per_site_trained_psi"], q["energy_per_site_trained_psi"]
+        out["matched_energy"] = {"plain": ep["value"], "precision": eq["value"],
+                                 "abs_diff_per_site": abs(ep["value"] - eq["value"]),
+                                 "combined_se_per_site": float(np.hypot(ep["se"], eq["se"])),
+                                 "note": "each form's psi after the same 300 SR steps from the same initial "
+                                         "parameters, sampled with its own moves (200 x 4096 samples)"}
         out["forms"]["plain"]["energy_check"] = results["plain"][0].energy_check()
-    if f.name == "precision":
-        out["hilbert_space_distance"] = hsd_timing(ann, f, st)
-    if not args.no_batched and f.name == "precision":
-        out["batched_instances"] = batched_instances(ann, st, max(2, args.steps // 5))
+    if not args.no_legs:
+        # error against FP64 of each result (same samples), then the ablation of the moves
+        out["fp64_errors"] = {name: r[0].fp64_errors(st) for name, r in results.items()}
+        if f.made is not None:
+            out["tau_ablation_trained_psi"] = [f.tau_run(sw, ind) for sw, ind in
+                                               ((1, 0), (4, 0), (16, 0), (64, 0), (0, 2), (1, 2), (64, 2))]
+        if f.name == "precision":
+            d_mixed = f.tdvp.solve(SHIFT)
+            f.tdvp.set_solver("fp64")
+            d_fp64 = f.tdvp.solve(SHIFT)
+            out["ms_per_step_fp64_cholesky"] = cuda_ms(lambda: f.step(st), st)
+            f.tdvp.set_solver("mixed", 6, 1e-12)
+            out["solve_rel_err_vs_fp64_cholesky"] = float(np.linalg.norm(d_mixed - d_fp64) / np.linalg.norm(d_fp64))
+            out["hilbert_space_distance"] = hsd_timing(ann, f, st)
+        del results
+        torch.cuda.empty_cache()
+        c4_train = min(C4_TRAIN, max(args.train_steps, 2))
+        out["learned_proposal_alpha4"] = [
+            learned_proposal_leg(ann, st, "1D TFIM N=64 PBC h=1.0, complex RBM alpha=4 (M=256)",
+                                 ann.transverse_field_ising_1d(64, 1.0), c4_train),
+            learned_proposal_leg(ann, st, "2D TFIM 8x8 PBC h=3.04, complex RBM alpha=4 (M=256)",
+                                 ann.transverse_field_ising_2d(8, 8, h=3.04), c4_train)]
+        torch.cuda.empty_cache()
+        out["cnn_j1j2_10x10"] = cnn_leg(ann, st)
+        if rank == 0 and not args.no_cpu:
+            t_cpu = cnn_cpu_seconds_per_sample()
+            out["cnn_j1j2_10x10"]["cpu_oracle"] = {"seconds_per_sample": t_cpu, "cores": 1,
+                                                   "kind": "port (not the reference: it caps N at 64, channels at 6)",
+                                                   "samples_per_s": 1.0 / t_cpu}
+        torch.cuda.empty_cache()
+        out["batched_instances"] = batched_instances(ann, st, 2)
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(*init_params(np.random.default_rng(SEED)), f.H, tau, cores=1)
+        out["cpu_baseline"] = cpu_baseline(*init_params(np.random.default_rng(SEED)),
+                                           _expression_module().transverse_field_ising_2d(L, L, h=H_FIELD), tau)
     if rank == 0:
         print(json.dumps(out))
     if dist:
@@ -636,11 +902,12 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------------
-def cpu_step_seconds(a, b, W, H, n_samples=4, chains=None):
-    """Time the FP64 oracle (a restatement of the reference's host path) on a
-    bounded sample of one SR step and scale to the full step: per-sample work
-    (64 sweeps of single-flip Metropolis, local energy, O_k, S accumulation)
-    times N_s, plus a Cholesky solve timed at n = 2048 and scaled by (Np/2048)^3."""
+def cpu_step_seconds(a, b, W, H, n_samples=4, with_chol=True):
+    """The FP64 oracle (a restatement of the reference's host path, which runs one chain on
+    one core) on a bounded sample of one SR step: per sample 64 sweeps of single-flip
+    Metropolis, the local energy, the O_k row and its S/F accumulation; plus a complex
+    Cholesky solve timed at n = 2048. Returns (seconds per sample of MC, of TDVP, seconds
+    of the n = 2048 Cholesky or None)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from pyoracle import Oracle, RbmDesc
     o = Oracle()
@@ -651,22 +918,27 @@ def cpu_step_seconds(a, b, W, H, n_samples=4, chains=None):
     t0 = time.perf_counter()
     o.tdvp_samples(psi, H, r["sconf"], 1.0 / n_samples, want_S=True)
     t_tdvp = (time.perf_counter() - t0) / n_samples
+    if not with_chol:
+        return t_mc, t_tdvp, None
     n = 2048
     A = np.random.default_rng(0).standard_normal((n, n)) + 1j * np.random.default_rng(1).standard_normal((n, n))
     A = A @ A.conj().T + n * np.eye(n)
     t0 = time.perf_counter()
     np.linalg.cholesky(A)
-    t_chol = (time.perf_counter() - t0) * ((N_SITES + M_HIDDEN + N_SITES * M_HIDDEN) / n) ** 3
-    return N_CHAINS * (t_mc + t_tdvp) + t_chol, t_mc, t_tdvp, t_chol
+    t_chol = time.perf_counter() - t0
+    return t_mc, t_tdvp, t_chol
 
 
 def cpu_baseline(a, b, W, H, tau, cores=1):
-    step_s, t_mc, t_tdvp, t_chol = cpu_step_seconds(a, b, W, H)
+    t_mc, t_tdvp, t_chol = cpu_step_seconds(a, b, W, H)
+    t_chol_full = t_chol * (NP_C2 / 2048) ** 3
+    step_s = N_CHAINS * (t_mc + t_tdvp) + t_chol_full
     return {"value": N_CHAINS / tau / step_s, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"4 chains x 1 sample (64 sweeps, E_loc, O_k, S rows) timed and scaled to {N_CHAINS} "
-                      f"samples; Cholesky timed at n=2048 and scaled by n^3 to Np=8384; tau_int from the GPU run",
+            "sample": f"4 samples (64 sweeps, E_loc, O_k, S rows) timed; the SR step's time = {N_CHAINS} x that "
+                      f"per-sample time + the Cholesky of n=8384 (timed at n=2048, scaled by n^3); tau_int from the "
+                      "GPU run",
             "seconds_per_step": step_s, "s_per_sample_mc": t_mc, "s_per_sample_tdvp": t_tdvp,
-            "s_cholesky": t_chol}
+            "s_cholesky_n2048": t_chol}
 
 
 def _expression_module():
@@ -679,42 +951,61 @@ def _expression_module():
     return mod
 
 
-def _cpu_worker(q):
-    rng = np.random.default_rng(SEED)
-    a, b, W = init_params(rng)
+REF_SAMPLES_PER_PROC = 2
+
+
+def _cpu_worker(_):
+    a, b, W = init_params(np.random.default_rng(SEED))
     H = _expression_module().transverse_field_ising_2d(L, L, h=H_FIELD)
-    q.put(cpu_step_seconds(a, b, W, H, n_samples=2)[0])
+    t_mc, t_tdvp, _ = cpu_step_seconds(a, b, W, H, n_samples=REF_SAMPLES_PER_PROC, with_chol=False)
+    return t_mc, t_tdvp
 
 
 def run_reference(args):
+    """The reference's CPU path for this workload, restated in the FP64 oracle (the
+    reference's own host build is x86-only here and is not on the GPU machine): each step is a
+    bounded sample of the SR step, timed in full: P worker processes (all host cores) each
+    run REF_SAMPLES_PER_PROC samples (64 sweeps, E_loc, O_k row, S/F accumulation), plus
+    the samples' share of the n = 8384 Cholesky (a numpy solve timed at n = 1024 once,
+    scaled by n^3). value = samples / seconds of the bounded step (tau_int = 1)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import multiprocessing as mp
     P = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    times = []
     t_start = time.perf_counter()
-    for _ in range(max(1, args.steps)):
-        q = ctx.Queue()
-        procs = [ctx.Process(target=_cpu_worker, args=(q,)) for _ in range(P)]
-        for p in procs:
-            p.start()
-        vals = [q.get() for _ in procs]
-        for p in procs:
-            p.join()
-        # P independent processes split the samples of one step
-        times.append(float(np.median(vals)) / P)
-    step_s = float(np.median(times))
-    tau = 1.0  # not measured on the CPU: taking 1 makes this an upper bound of the CPU effective rate
-    value = N_CHAINS / tau / step_s
+    n = 1024
+    A = np.random.default_rng(0).standard_normal((n, n)) + 1j * np.random.default_rng(1).standard_normal((n, n))
+    A = A @ A.conj().T + n * np.eye(n)
+    t0 = time.perf_counter()
+    np.linalg.cholesky(A)
+    t_chol_full = (time.perf_counter() - t0) * (NP_C2 / n) ** 3
+    steps = []
+    with ctx.Pool(P) as pool:
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            vals = pool.map(_cpu_worker, range(P), chunksize=1)
+            wall = time.perf_counter() - t0
+            samples = P * REF_SAMPLES_PER_PROC
+            # the Cholesky share of these samples (one solve per 16384 samples)
+            step_s = wall + t_chol_full * samples / N_CHAINS
+            if k >= args.warmup:
+                steps.append((step_s, samples, vals))
+    step_s = float(np.mean([s for s, _, _ in steps]))
+    samples = steps[0][1]
+    value = samples / step_s
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded random-init RBM, 2D TFIM)",
            "config": config_dict("precision" if args.form == "both" else args.form), "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": P, "kind": "port",
-                            "sample": f"{P} processes x 2 chains x 1 sample timed per step and scaled to "
-                                      f"{N_CHAINS} samples; Cholesky scaled from n=2048; tau_int = 1 assumed"},
+                            "sample": f"per step {P} worker processes (one pool, started before the warm-up "
+                                      f"steps) x {REF_SAMPLES_PER_PROC} samples of the SR step (64 sweeps, E_loc, "
+                                      "O_k, S/F rows), the step's wall time measured in full, plus the samples' "
+                                      f"share of the n=8384 Cholesky (timed at n={n}, scaled by n^3); tau_int = 1 "
+                                      "assumed",
+                            "seconds_per_sample_per_core": float(np.mean([sum(v) for _, _, vs in steps for v in vs]))},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "wall_s": time.perf_counter() - t_start}
     print(json.dumps(out))
@@ -726,43 +1017,29 @@ def run_profile_case(solver="fp64"):
     samples, BF16 tensor-core S, SR solve by `solver` (fp64 / mixed / fp32)."""
     import annongpu_gb300 as ann
     rng = np.random.default_rng(0)
-    N, M = 32, 64
-    a = 0.01 * (rng.standard_normal(N) + 1j * rng.standard_normal(N))
-    b = 0.01 * (rng.standard_normal(M) + 1j * rng.standard_normal(M))
-    W = 0.01 * (rng.standard_normal((N, M)) + 1j * rng.standard_normal((N, M)))
+    a, b, W = init_rbm(rng, 32, 64)
     psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
-    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    op = ann.Operator(ann.transverse_field_ising_1d(32, 1.0))
     mc = ann.MonteCarloLoop(16384, 4, 8, 16384, True, seed=1, persistent=True)
     td = ann.TDVP(psi.num_params, s_mode="bf16", solver=solver)
     for _ in range(2):
         td.sr_step(op, psi, mc, 1e-3, 0.01)
-    print("profile case: E/N =", td.E_local / N)
+    print("profile case: E/N =", td.E_local / 32)
 
 
-def run_profile_case_learned():
-    """Small case for ncu captures of the sampler with learned moves: the 8x8 workload's
-    shapes (N = 64, M = 128, h = 3.04) with 4096 chains (O rows 275 MB), one local sweep
-    and two learned independence moves per sample, the proposal trained on 16384
-    configurations first; two SR steps (BF16 tensor-core S, mixed solver)."""
+def run_profile_case_sampler():
+    """Small case for ncu captures of the sampler: the 8x8 workload's shapes (N = 64,
+    M = 128, h = 3.04) with 4096 chains (O rows 275 MB), 8 sweeps between samples, two
+    sampling passes with E_loc and O rows (TDVP evaluations, BF16 S)."""
     import annongpu_gb300 as ann
-    rng = np.random.default_rng(SEED)
-    a, b, W = init_params(rng)
+    a, b, W = init_params(np.random.default_rng(SEED))
     op = ann.Operator(ann.transverse_field_ising_2d(L, L, h=H_FIELD))
     psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
-    chains = 4096
-    prep = ann.MonteCarloLoop(chains, 1, THERM, chains, True, seed=5, persistent=True)
-    prep.set_history(4 * chains)
-    for _ in range(4):
-        ann.ExpectationValue()(op, psi, prep)
-    made = ann.MADE(N_SITES, MADE_H, seed=1)
-    made.train_on_samples(prep, steps=16, batch=MADE_BATCH, lr=MADE_LR)
-    mc = ann.MonteCarloLoop(chains, LEARNED_SWEEPS, THERM, chains, True, seed=6, persistent=True)
-    mc.set_chains(*prep.get_chains())
-    mc.set_proposal(made, indep_per_sample=LEARNED_INDEP, min_acceptance=0.0)
+    mc = ann.MonteCarloLoop(4096, 8, 8, 4096, True, seed=6, persistent=True)
     td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
     for _ in range(2):
-        td.sr_step(op, psi, mc, SHIFT, LR)
-    print("profile case (learned): E/N =", td.E_local / N_SITES)
+        td.eval(op, psi, mc)
+    print("profile case (sampler): E/N =", td.E_local / N_SITES)
 
 
 def main():
@@ -770,21 +1047,25 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--train-steps", type=int, default=TRAIN_STEPS,
+                    help="SR steps of each form before the timed steps (the workload's 300)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="both", choices=["both", "precision", "plain"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances measurement")
+    ap.add_argument("--no-legs", action="store_true", help="headline only: skip the FP64 checks and other workloads")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
-    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "learned"],
-                    help="SR solver of the small profile case; 'learned': the learned-proposal sampler case")
+    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "sampler"],
+                    help="SR solver of the small profile case; 'sampler': the sampler case")
     ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
     ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
     ap.add_argument("--profile-window", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     args = ap.parse_args()
+    if args.warmup < 1 or args.steps < 1:
+        ap.error("--steps and --warmup must be at least 1")
     if args.profile_case:
-        if args.profile_solver == "learned":
-            run_profile_case_learned()
+        if args.profile_solver == "sampler":
+            run_profile_case_sampler()
         else:
             run_profile_case(args.profile_solver)
         return
