@@ -251,6 +251,7 @@ struct MadeDev {
     const float* b1;           // H
     const __nv_bfloat16* W2t;  // H x N
     const float* b2;           // N
+    const __nv_bfloat16* W2;   // N x H (the sampler's layout, read through L1)
 };
 
 struct McArgs {
@@ -274,6 +275,7 @@ struct McArgs {
     MadeDev made;                 // learned independence proposal (made.N == 0: none)
     unsigned indep_per_sample;    // independence proposals after the local sweeps of each sample
     const int* made_on;           // device flag: 0 while the drop rule holds the proposal off (null: on)
+    int made_smem;                // 1: the weights are staged in shared memory; 0: read through L1
 };
 
 struct SampleOut {

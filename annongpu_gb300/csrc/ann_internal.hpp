@@ -149,6 +149,7 @@ struct ann_made_impl {
     uint64_t seed = 0;
     DevBuf W1, b1, W2, b2;            // FP32 master weights (W1: H x N, W2: N x H)
     DevBuf W1t, W2t;                  // BF16 transposed copies read by the kernels
+    DevBuf W2b;                       // BF16 copy of W2 as stored (N x H): read through L1 by the samplers
     DevBuf deg;                       // hidden-unit degrees (u16)
     DevBuf mW1, vW1, mb1, vb1, mW2, vW2, mb2, vb2;  // Adam moments
     DevBuf gW1, gb1, gW2, gb2;        // gradients
@@ -218,6 +219,8 @@ void psi_prepare(ann_psi_impl& psi, cudaStream_t st);
 // runs the ensemble (MC sampling or exact enumeration) over psi
 void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const SampleTargets& t,
                   cudaStream_t st);
+// appends n sample configurations (rows of conf) to the ensemble's history ring (capi.cu)
+void hist_append(ann_ens_impl& ens, const uint64_t* conf, size_t n, cudaStream_t st);
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs_dev, size_t n, Rows& rows,
                void* O, size_t ldO, cudaStream_t st, int basis = ANN_BASIS_SPINS);
 

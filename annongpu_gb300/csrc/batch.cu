@@ -32,7 +32,7 @@ struct BatchInst {
 
 __global__ void __launch_bounds__(kBatchWarps * 32)
 rbm_mc_batch_kernel(const BatchInst* __restrict__ insts, const uint2* __restrict__ items, unsigned n_items,
-                    unsigned* __restrict__ next) {
+                    unsigned* __restrict__ next, size_t made_scratch_off) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ unsigned s_item;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -47,8 +47,12 @@ rbm_mc_batch_kernel(const BatchInst* __restrict__ insts, const uint2* __restrict
         const cplx<float>* Wd = stage_Wd<float>(p, 1, reinterpret_cast<cplx<float>*>(smem_raw));
         const unsigned chain = w.y + warp;
         if(chain < I.a.n_chains) {
-            const MadeSm ms{};
-            mc_chain<float, 1, kBatchU>(p, Wd, I.op, I.with_op, I.a, I.out, chain, lane, false, ms, nullptr);
+            // the instance's learned proposal (if any) read through L1; one H-float scratch
+            // per warp after the largest instance's weights
+            const bool use_made = I.a.made.N != 0 && (I.a.made_on == nullptr || *I.a.made_on != 0);
+            const MadeSm ms = use_made ? made_global(I.a.made) : MadeSm{};
+            float* mh = use_made ? reinterpret_cast<float*>(smem_raw + made_scratch_off) + warp * I.a.made.H : nullptr;
+            mc_chain<float, 1, kBatchU>(p, Wd, I.op, I.with_op, I.a, I.out, chain, lane, use_made, ms, mh);
         }
         __syncthreads();  // before the next item restages the weights
     }
@@ -88,6 +92,7 @@ struct ann_batch_impl {
     std::vector<uint2> host_items;
     DevBuf insts, items, counter;
     size_t smem = 0;
+    size_t made_off = 0;   // byte offset of the per-warp learned-proposal scratch in shared memory
     bool table_valid = false;
     bool table_inits = false;  // the table draws fresh configurations (first call / non-persistent)
     std::vector<cudaStream_t> streams;
@@ -120,6 +125,7 @@ void batch_table(ann_batch_impl& b) {
     b.host_insts.assign(n, BatchInst{});
     std::vector<double> cost(n);
     size_t max_wd = 0;
+    unsigned max_made_h = 0;
     for(size_t i = 0; i < n; i++) {
         ann_psi_impl& psi = *b.psis[i];
         ann_ens_impl& ens = *b.enss[i];
@@ -149,6 +155,15 @@ void batch_table(ann_batch_impl& b) {
         a.made = MadeDev{};
         a.indep_per_sample = 0;
         a.made_on = nullptr;
+        a.made_smem = 0;
+        if(ens.made && ens.indep_per_sample > 0) {
+            if(ens.made->N != psi.N) throw Error(ANN_ERR_INVALID, "learned proposal size differs from psi.N");
+            if(ens.made->H > 256) throw Error(ANN_ERR_INVALID, "learned proposals in the sampler need H <= 256");
+            a.made = made_view(*ens.made);
+            a.indep_per_sample = ens.indep_per_sample;
+            a.made_on = ens.made_on.as<int>();
+            max_made_h = std::max(max_made_h, ens.made->H);
+        }
         SampleTargets tg{&ens.rows, nullptr, 0, true};
         if(b.tdvps[i]) tg = tdvp_prepare(*b.tdvps[i], psi, ens);
         const size_t rows = (size_t)spc * ens.n_chains;
@@ -166,7 +181,8 @@ void batch_table(ann_batch_impl& b) {
         o.ldO = tg.ldO;
         o.status = status_word();
         max_wd = std::max(max_wd, (size_t)psi.N * psi.Mpad * sizeof(cplx<float>));
-        cost[i] = (double)ens.n_chains * (ens.num_sweeps + (a.do_init ? ens.num_therm : 0)) * psi.N * psi.M;
+        cost[i] = (double)ens.n_chains * (ens.num_sweeps + (a.do_init ? ens.num_therm : 0) + a.indep_per_sample) *
+                  psi.N * psi.M;
         b.table_inits = b.table_inits || a.do_init;
     }
     std::vector<size_t> order(n);
@@ -178,7 +194,8 @@ void batch_table(ann_batch_impl& b) {
     upload(b.insts, b.host_insts.data(), b.host_insts.size() * sizeof(BatchInst));
     upload(b.items, b.host_items.data(), b.host_items.size() * sizeof(uint2));
     b.counter.ensure(sizeof(unsigned));
-    b.smem = (max_wd + 15) & ~(size_t)15;
+    b.made_off = (max_wd + 15) & ~(size_t)15;
+    b.smem = b.made_off + (size_t)kBatchWarps * max_made_h * sizeof(float);
     if(b.smem > 200 * 1024) throw Error(ANN_ERR_INVALID, "instance weights exceed shared memory");
     ANN_CUDA(cudaFuncSetAttribute(rbm_mc_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::max<size_t>(b.smem, 1024)));
@@ -203,8 +220,17 @@ void batch_sample(ann_batch_impl& b, cudaStream_t st) {
     const unsigned n_items = (unsigned)b.host_items.size();
     const unsigned grid = std::min<unsigned>(n_items, (unsigned)sms * 2);
     rbm_mc_batch_kernel<<<grid, kBatchWarps * 32, std::max<size_t>(b.smem, 16), st>>>(
-        b.insts.as<BatchInst>(), b.items.as<uint2>(), n_items, b.counter.as<unsigned>());
+        b.insts.as<BatchInst>(), b.items.as<uint2>(), n_items, b.counter.as<unsigned>(), b.made_off);
     check_launch("rbm_mc_batch_kernel");
+    for(size_t i = 0; i < b.enss.size(); i++) {
+        ann_ens_impl& e = *b.enss[i];
+        if(e.made && e.indep_per_sample > 0) {
+            made_drop_rule_kernel<<<1, 1, 0, st>>>(e.acc_rej.as<unsigned long long>(), e.made_min_acceptance,
+                                                   e.made_on.as<int>());
+            check_launch("made_drop_rule_kernel");
+        }
+        if(e.hist_cap) hist_append(e, e.rows.conf.as<uint64_t>(), e.rows.n, st);  // the proposal's training data
+    }
     for(auto* e : b.enss) e->chains_valid = true;
     if(b.table_inits && !capturing(st)) b.table_valid = false;  // next call continues the chains
 }

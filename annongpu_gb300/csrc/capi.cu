@@ -186,17 +186,18 @@ void run_ensemble(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, c
     } else {
         deep_run(psi, op, ens, t, st);
     }
-    if(ens.hist_cap) {
-        // append the configurations of this pass to the ring buffer; the write position is
-        // a device counter, so replays of a captured step keep advancing it
-        const size_t n = t.rows->n;
-        hist_append_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
-            t.rows->conf.as<uint64_t>(), n, ens.hist.as<uint64_t>(), ens.hist_cap, ens.hist_posd.as<unsigned long long>());
-        check_launch("hist_append_kernel");
-        hist_advance_kernel<<<1, 1, 0, st>>>(ens.hist_posd.as<unsigned long long>(), n);
-        check_launch("hist_advance_kernel");
-        ens.hist_len = std::min(ens.hist_cap, ens.hist_len + n);  // rows valid once written (host bound)
-    }
+    if(ens.hist_cap) hist_append(ens, t.rows->conf.as<uint64_t>(), t.rows->n, st);
+}
+
+// appends the configurations of a pass (n rows of conf) to the ring buffer; the write
+// position is a device counter, so replays of a captured step keep advancing it
+void hist_append(ann_ens_impl& ens, const uint64_t* conf, size_t n, cudaStream_t st) {
+    hist_append_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+        conf, n, ens.hist.as<uint64_t>(), ens.hist_cap, ens.hist_posd.as<unsigned long long>());
+    check_launch("hist_append_kernel");
+    hist_advance_kernel<<<1, 1, 0, st>>>(ens.hist_posd.as<unsigned long long>(), n);
+    check_launch("hist_advance_kernel");
+    ens.hist_len = std::min(ens.hist_cap, ens.hist_len + n);  // rows valid once written (host bound)
 }
 
 void run_confs(ann_psi_impl& psi, const ann_op_impl* op, const uint64_t* confs, size_t n, Rows& rows, void* O,

@@ -50,7 +50,8 @@ struct CnnDev {
     unsigned nbr_off[kCnnMaxLayers];
     unsigned tab_len;        // entries of nbr (= inv)
     unsigned x0max, x1max;   // capacity of the changed-site lists (layer 0, layer 1)
-    cplx<T>* slab;           // per resident warp: z0 [ch0 N] | z1 [ch1 N] | work A [ch0 N] | work B [ch1 N]
+    cplx<T>* slab;           // per resident warp: z0 [ch0 N] | z1 [ch1 N] | f0(z0) [ch0 N] | f1(z1) [ch1 N] |
+                             // work A [ch0 N] | work B [ch1 N]
     size_t slab_len;         // complex entries per warp
 };
 
@@ -64,12 +65,15 @@ struct CnnCtx {
     // this warp's slab (global)
     cplx<T>* z0;     // ch0 x N pre-activations of the current configuration
     cplx<T>* z1;     // ch1 x N (two layers)
+    cplx<T>* a0;     // ch0 x N f0(z0), kept with z0 (each changed entry costs one activation)
+    cplx<T>* f1;     // ch1 x N f1(z1)
     cplx<T>* bufA;   // ch0 x N work buffer (activations, deltas)
     cplx<T>* bufB;   // ch1 x N work buffer
     // this warp's move lists (shared)
     cplx<T>* da0;    // x0max x ch0: f0(z0 new) - f0(z0 old) on the changed layer-0 sites
     cplx<T>* z0n;    // x0max x ch0: new z0 there
     cplx<T>* z1n;    // x1max x ch1: new z1 on the changed layer-1 sites
+    cplx<T>* df1;    // x1max x ch1: f1(z1 new) - f1(z1 old) there
     uint8_t* pos0;   // kCnnMaxSites: position of a site in list0, 0xFF if absent
     uint8_t* mark;   // kCnnMaxSites
     uint8_t* list0;  // x0max changed layer-0 sites
@@ -122,7 +126,7 @@ __device__ __forceinline__ cplx<T> scaled_lp(const CnnDev<T>& p, cplx<T> acc) {
     return mk<T>((T)(p.ff * (double)acc.re) + p.lp.re, (T)(p.ff * (double)acc.im) + p.lp.im);
 }
 
-// Full forward pass of s into the warp's slab (z0, z1; layer-0 activations left in bufA);
+// Full forward pass of s into the warp's slab (pre-activations z0, z1 and activations f0, f1);
 // returns log psi in every lane.
 template<typename T>
 __device__ cplx<T> cnn_forward_state(const CnnCtx<T>& c, const Conf<2>& s, int lane) {
@@ -133,16 +137,18 @@ __device__ cplx<T> cnn_forward_state(const CnnCtx<T>& c, const Conf<2>& s, int l
         const cplx<T> z = z0_of(c, s, ch, x);
         c.z0[e] = z;
         const cplx<T> f = act_f(z, p.act, 0);
+        c.a0[e] = f;
         if(p.L == 1) acc += f;
-        else c.bufA[e] = f;
     }
     __syncwarp();
     if(p.L > 1) {
         for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) {
             const unsigned d = e / p.N, x = e % p.N;
-            const cplx<T> z = z1_of(c, c.bufA, d, x);
+            const cplx<T> z = z1_of(c, c.a0, d, x);
             c.z1[e] = z;
-            acc += act_f(z, p.act, 1);
+            const cplx<T> f = act_f(z, p.act, 1);
+            c.f1[e] = f;
+            acc += f;
         }
         __syncwarp();
     }
@@ -223,11 +229,11 @@ __device__ cplx<T> cnn_delta(CnnCtx<T>& c, const Conf<2>& s, const unsigned* F, 
             dz.re += m * wr[k].re;
             dz.im += m * wr[k].im;
         }
-        const cplx<T> zo = c.z0[ch * N + x], zn = zo + dz;
+        const cplx<T> zn = c.z0[ch * N + x] + dz;
         c.z0n[e] = zn;
-        const cplx<T> df = act_f(zn, p.act, 0) - act_f(zo, p.act, 0);
+        const cplx<T> df = act_f(zn, p.act, 0) - c.a0[ch * N + x];
+        c.da0[e] = df;
         if(p.L == 1) acc += df;
-        else c.da0[e] = df;
     }
     c.n1 = 0;
     if(p.L > 1) {
@@ -248,9 +254,11 @@ __device__ cplx<T> cnn_delta(CnnCtx<T>& c, const Conf<2>& s, const unsigned* F, 
                 const cplx<T>* da = c.da0 + u * C0;
                 for(unsigned ci = 0; ci < C0; ci++) cmac(dz, wr[ci * cstride + k], da[ci]);
             }
-            const cplx<T> zo = c.z1[d * N + x], zn = zo + dz;
+            const cplx<T> zn = c.z1[d * N + x] + dz;
             c.z1n[e] = zn;
-            acc += act_f(zn, p.act, 1) - act_f(zo, p.act, 1);
+            const cplx<T> df = act_f(zn, p.act, 1) - c.f1[d * N + x];
+            c.df1[e] = df;
+            acc += df;
         }
     }
     __syncwarp();
@@ -265,10 +273,17 @@ __device__ cplx<T> cnn_delta(CnnCtx<T>& c, const Conf<2>& s, const unsigned* F, 
 template<typename T>
 __device__ void cnn_commit(const CnnCtx<T>& c, int lane) {
     const CnnDev<T>& p = *c.p;
-    for(unsigned e = lane; e < c.n0 * p.ch[0]; e += 32) c.z0[(e % p.ch[0]) * p.N + c.list0[e / p.ch[0]]] = c.z0n[e];
+    for(unsigned e = lane; e < c.n0 * p.ch[0]; e += 32) {
+        const unsigned q = (e % p.ch[0]) * p.N + c.list0[e / p.ch[0]];
+        c.z0[q] = c.z0n[e];
+        c.a0[q] += c.da0[e];  // f0(z0 new) up to one rounding: samples recompute it exactly
+    }
     if(p.L > 1)
-        for(unsigned e = lane; e < c.n1 * p.ch[1]; e += 32)
-            c.z1[(e % p.ch[1]) * p.N + c.list1[e / p.ch[1]]] = c.z1n[e];
+        for(unsigned e = lane; e < c.n1 * p.ch[1]; e += 32) {
+            const unsigned q = (e % p.ch[1]) * p.N + c.list1[e / p.ch[1]];
+            c.z1[q] = c.z1n[e];
+            c.f1[q] += c.df1[e];
+        }
     __syncwarp();
 }
 
@@ -282,7 +297,6 @@ __device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T
         for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) c.bufA[e] = ff * act_df(c.z0[e], p.act, 0);
         __syncwarp();
     } else {
-        for(unsigned e = lane; e < p.ch[0] * p.N; e += 32) c.bufA[e] = act_f(c.z0[e], p.act, 0);
         for(unsigned e = lane; e < p.ch[1] * p.N; e += 32) c.bufB[e] = ff * act_df(c.z1[e], p.act, 1);
         __syncwarp();
         // layer-1 parameters: O[(ci, d), cls, k] = sum_{x: cls(x)=cls} delta1_d(x) a0_ci(x + k)
@@ -295,7 +309,7 @@ __device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T
             const unsigned ci = link / p.ch[1], d = link % p.ch[1];
             cplx<T> o = mk<T>(T(0), T(0));
             const cplx<T>* dl = c.bufB + d * p.N;
-            const cplx<T>* ac = c.bufA + ci * p.N;
+            const cplx<T>* ac = c.a0 + ci * p.N;
             for(unsigned x = 0; x < p.N; x++) {
                 if(c.cls[x] != cl) continue;
                 cmac(o, dl[x], ac[nb[x * p.vol[1] + k]]);
@@ -313,7 +327,6 @@ __device__ void cnn_O_row(const CnnCtx<T>& c, const Conf<2>& s, int lane, cplx<T
                     const unsigned x = iv[k];
                     cmac(g, wgt(c, 1, ci, d, c.cls[x], k), c.bufB[d * p.N + x]);
                 }
-            // bufA[e] (the activation a0) is read by no other lane from here on
             c.bufA[e] = g * act_df(c.z0[e], p.act, 0);
         }
         __syncwarp();
@@ -397,7 +410,7 @@ __device__ void cnn_process_sample(CnnCtx<T>& c, const OpDev* op, const Conf<2>&
 
 __host__ __device__ inline size_t cnn_warp_smem(unsigned x0max, unsigned x1max, unsigned ch0, unsigned ch1,
                                                 size_t elem) {
-    const size_t cplx_bytes = ((size_t)2 * x0max * ch0 + (size_t)x1max * ch1) * elem;
+    const size_t cplx_bytes = ((size_t)2 * x0max * ch0 + (size_t)2 * x1max * ch1) * elem;
     const size_t byte_bytes = 2 * kCnnMaxSites + x0max + x1max;
     return (cplx_bytes + byte_bytes + 15) & ~(size_t)15;
 }
@@ -426,7 +439,8 @@ __device__ CnnCtx<T> cnn_stage(const CnnDev<T>& p, unsigned char* smem) {
     c.da0 = reinterpret_cast<cplx<T>*>(q);
     c.z0n = c.da0 + (size_t)p.x0max * p.ch[0];
     c.z1n = c.z0n + (size_t)p.x0max * p.ch[0];
-    uint8_t* b = reinterpret_cast<uint8_t*>(c.z1n + (size_t)p.x1max * ch1);
+    c.df1 = c.z1n + (size_t)p.x1max * ch1;
+    uint8_t* b = reinterpret_cast<uint8_t*>(c.df1 + (size_t)p.x1max * ch1);
     c.pos0 = b;
     c.mark = b + kCnnMaxSites;
     c.list0 = b + 2 * kCnnMaxSites;
@@ -440,7 +454,9 @@ __device__ CnnCtx<T> cnn_stage(const CnnDev<T>& p, unsigned char* smem) {
     cplx<T>* slab = p.slab + (size_t)(blockIdx.x * (blockDim.x >> 5) + warp) * p.slab_len;
     c.z0 = slab;
     c.z1 = c.z0 + (size_t)p.ch[0] * p.N;
-    c.bufA = c.z1 + (size_t)ch1 * p.N;
+    c.a0 = c.z1 + (size_t)ch1 * p.N;
+    c.f1 = c.a0 + (size_t)p.ch[0] * p.N;
+    c.bufA = c.f1 + (size_t)ch1 * p.N;
     c.bufB = c.bufA + (size_t)p.ch[0] * p.N;
     c.w = w;
     c.nbr = nb;
@@ -568,7 +584,7 @@ CnnDev<T> cnn_view(const ann_psi_impl& psi) {
     p.cls = meta + 4 * tab;
     p.x0max = psi.cnn_x0;
     p.x1max = p.L > 1 ? psi.cnn_x1 : 0u;
-    p.slab_len = (size_t)2 * (p.ch[0] + (p.L > 1 ? p.ch[1] : 0u)) * p.N;
+    p.slab_len = (size_t)3 * (p.ch[0] + (p.L > 1 ? p.ch[1] : 0u)) * p.N;
     return p;
 }
 
@@ -582,7 +598,7 @@ size_t cnn_smem(const CnnDev<T>& p, int warps) {
 template<typename T>
 int cnn_warps(const CnnDev<T>& p) {
     int w = 8;
-    while(w > 1 && cnn_smem(p, w) > 100 * 1024) w >>= 1;
+    while(w > 1 && cnn_smem(p, w) > 112 * 1024) w >>= 1;
     if(cnn_smem(p, w) > 220 * 1024) throw Error(ANN_ERR_INVALID, "PsiCNN too large for shared memory");
     return w;
 }

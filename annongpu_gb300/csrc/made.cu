@@ -184,15 +184,17 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     p[i] -= a.lr * (mm / a.c1) / (sqrtf(vv / a.c2) + a.eps);
 }
 
-// BF16 transposed copies: W1t[i][k] = W1[k][i], W2t[k][j] = W2[j][k]
+// BF16 copies: W1t[i][k] = W1[k][i], W2t[k][j] = W2[j][k], W2b[j][k] = W2[j][k]
 __global__ void refresh_bf16_kernel(const float* __restrict__ W1, const float* __restrict__ W2, unsigned N, unsigned H,
-                                    __nv_bfloat16* __restrict__ W1t, __nv_bfloat16* __restrict__ W2t) {
+                                    __nv_bfloat16* __restrict__ W1t, __nv_bfloat16* __restrict__ W2t,
+                                    __nv_bfloat16* __restrict__ W2b) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if(idx >= (size_t)N * H) return;
     const unsigned i = (unsigned)(idx / H), k = (unsigned)(idx % H);
     W1t[idx] = __float2bfloat16_rn(W1[(size_t)k * N + i]);
     const unsigned kk = (unsigned)(idx / N), j = (unsigned)(idx % N);
     W2t[idx] = __float2bfloat16_rn(W2[(size_t)j * H + kk]);
+    W2b[idx] = __float2bfloat16_rn(W2[idx]);
 }
 
 __global__ void __launch_bounds__(256) made_logq_kernel(MadeDev m, const uint64_t* __restrict__ confs, size_t n,
@@ -253,6 +255,7 @@ MadeDev made_view(const ann_made_impl& m) {
     d.b1 = m.b1.as<float>();
     d.W2t = m.W2t.as<__nv_bfloat16>();
     d.b2 = m.b2.as<float>();
+    d.W2 = m.W2b.as<__nv_bfloat16>();
     return d;
 }
 
@@ -260,7 +263,8 @@ void made_refresh(ann_made_impl& m, cudaStream_t st) {
     const size_t nh = (size_t)m.N * m.H;
     refresh_bf16_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, st>>>(m.W1.as<float>(), m.W2.as<float>(), m.N, m.H,
                                                                         m.W1t.as<__nv_bfloat16>(),
-                                                                        m.W2t.as<__nv_bfloat16>());
+                                                                        m.W2t.as<__nv_bfloat16>(),
+                                                                        m.W2b.as<__nv_bfloat16>());
     check_launch("refresh_bf16_kernel");
 }
 
@@ -296,6 +300,7 @@ void made_init(ann_made_impl& m, uint64_t seed) {
     }
     m.W1t.ensure(nh * 2);
     m.W2t.ensure(nh * 2);
+    m.W2b.ensure(nh * 2);
     m.adam_t = 0;
     made_refresh(m, nullptr);
     ANN_CUDA(cudaDeviceSynchronize());

@@ -58,6 +58,12 @@ __device__ inline MadeSm made_stage(const MadeDev& m, unsigned char* smem) {
     return s;
 }
 
+// the weights as stored in global memory (read through L1: for samplers whose local
+// sweeps outweigh the learned moves, so shared memory is left to occupancy)
+__device__ __forceinline__ MadeSm made_global(const MadeDev& m) {
+    return MadeSm{m.N, m.H, m.W1t, m.b1, m.W2, m.b2};
+}
+
 __device__ __forceinline__ float softplusf(float z) {
     return z > 0.f ? z + log1pf(expf(-z)) : log1pf(expf(z));
 }

@@ -469,8 +469,13 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
     float* mh = nullptr;
     if(use_made) {
         unsigned char* mbase = smem_raw + (w_smem ? (((size_t)p.N * p.Mpad * sizeof(cplx<T>) + 15) & ~(size_t)15) : 0);
-        ms = made_stage(a.made, mbase);
-        mh = reinterpret_cast<float*>(mbase + made_smem_bytes(a.made.N, a.made.H)) + (threadIdx.x >> 5) * a.made.H;
+        if(a.made_smem) {
+            ms = made_stage(a.made, mbase);
+            mbase += made_smem_bytes(a.made.N, a.made.H);
+        } else {
+            ms = made_global(a.made);
+        }
+        mh = reinterpret_cast<float*>(mbase) + (threadIdx.x >> 5) * a.made.H;
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;

@@ -135,6 +135,7 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     a.made = MadeDev{};
     a.indep_per_sample = 0;
     a.made_on = nullptr;
+    a.made_smem = 0;
     // the learned moves are launched whenever a proposal is set; the device flag (the drop
     // rule) decides in the kernel whether they run
     const bool learned = ens.made && ens.indep_per_sample > 0 && !a.tape_site;
@@ -145,6 +146,10 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
         a.made = made_view(*ens.made);
         a.indep_per_sample = ens.indep_per_sample;
         a.made_on = ens.made_on.as<int>();
+        // the proposal's weights in shared memory when its moves are a large part of the
+        // work (each costs about one sweep); read through L1 when the local sweeps dominate,
+        // so shared memory is left to occupancy
+        a.made_smem = 4 * ens.indep_per_sample >= ens.num_sweeps ? 1 : 0;
     }
     if(a.tape_site) {
         // replay starts from the recorded initial configurations every call
@@ -159,7 +164,8 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     // chains (warps) per CTA: the autotuned choice for this shape, else the default
     int wpb = tuning_get(key_mc_wpb(psi, ens), warps_per_block<T>(0));
     if(wpb < 1 || wpb > 8) wpb = warps_per_block<T>(0);
-    const size_t made_bytes = learned ? made_smem_bytes(ens.made->N, ens.made->H) + (size_t)wpb * ens.made->H * 4 : 0;
+    const size_t made_bytes =
+        learned ? (a.made_smem ? made_smem_bytes(ens.made->N, ens.made->H) : 0) + (size_t)wpb * ens.made->H * 4 : 0;
     // W staged in shared memory when it fits, unless the tuning table prefers reading it
     // through L1 (fewer bytes of shared memory per CTA, more CTAs per SM)
     const int w_smem = (wb + made_bytes <= kMaxSmemWd && tuning_get(key_mc_wsmem(psi, ens), 1)) ? 1 : 0;

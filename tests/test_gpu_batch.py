@@ -91,3 +91,43 @@ def test_batched_sr_steps_equal_single_steps_and_graph():
     torch.cuda.synchronize()
     for (p1, *_), (p2, *_) in zip(inst, ref):
         np.testing.assert_array_equal(p1.params, p2.params)
+
+
+def test_batched_learned_proposals_equal_single_chains():
+    """Instances with a learned MADE proposal each (two independence moves per sample after
+    the local sweeps) in the one persistent launch: every batched chain, its learned-move
+    acceptance and the history ring the proposal trains on are the same as the instance
+    sampled alone."""
+    def with_proposals(inst):
+        mades = []
+        for k, (psi, op, mc, _, _) in enumerate(inst):
+            made = ann.MADE(psi.N, 64, seed=50 + k)
+            mc.set_proposal(made, indep_per_sample=2, min_acceptance=0.0)
+            mc.set_history(4 * mc.num_markov_chains)
+            mades.append(made)
+        return mades
+
+    inst = build()
+    m1 = with_proposals(inst)
+    batch = ann.Batch([x[0] for x in inst], [x[1] for x in inst], [x[2] for x in inst])
+    ref = build()
+    m2 = with_proposals(ref)
+    for rep in range(2):
+        batch.sample()
+        for psi2, op2, mc2, _, _ in ref:
+            ann.ExpectationValue()(op2, psi2, mc2)
+        for (psi, op, mc, _, _), (psi2, op2, mc2, _, _) in zip(inst, ref):
+            c1, l1, el1 = mc.samples()
+            c2, l2, el2 = mc2.samples()
+            np.testing.assert_array_equal(c1, c2)
+            np.testing.assert_array_equal(el1, el2)
+            mc.refresh_stats()
+            mc2.refresh_stats()
+            assert mc.proposal_acceptance == mc2.proposal_acceptance
+            assert mc.proposal_acceptance > 0.0
+    # the rings hold the same configurations: training on them gives the same weights
+    for (made1, made2), (_, _, mc, _, _), (_, _, mc2, _, _) in zip(zip(m1, m2), inst, ref):
+        made1.train_on_samples(mc, steps=4, batch=256, lr=1e-3)
+        made2.train_on_samples(mc2, steps=4, batch=256, lr=1e-3)
+        for x, y in zip(made1.params, made2.params):
+            np.testing.assert_array_equal(x, y)

@@ -353,3 +353,54 @@ def test_tensor_core_S_monte_carlo_rows(oracle):
     scale = np.abs(ref["S"]).max()
     assert np.abs(S_tc - ref["S"]).max() / scale < 1e-2
     np.testing.assert_allclose(td.F_vector, ref["F"], rtol=1e-4, atol=1e-5 * np.abs(ref["F"]).max())
+
+
+def test_exp_sigma_z_matches_oracle(oracle):
+    """ExpectationValue.exp_sigma_z (ExpectationValue.cu.template:52-81): sum over the
+    exact-summation weights |psi(s)|^2 of exp(sum_n c_n <s|P_n|P_n s>), the per-string
+    matrix elements from the oracle's Pauli algebra (pinned to the reference's KATs)."""
+    N, M = 8, 16
+    c = Case("deep", N, M, None, seed=77)
+    H = ann.transverse_field_ising_1d(N, 0.7) + 0.3 * ann.sigma_y(1) * ann.sigma_y(2) + 0.2 * ann.sigma_z(3)
+    es = ann.ExactSummationSpins(N)
+    got = ann.ExpectationValue().exp_sigma_z(ann.Operator(H), c.gpu, es)
+    w = np.abs(ann.psi_vector(c.gpu, es)) ** 2
+    want = 0j
+    for s in range(1 << N):
+        a = sum(complex(coef) * oracle.pauli_apply(ka, kb, s, N)[0] for (ka, kb), coef in H)
+        want += w[s] * np.exp(a)
+    np.testing.assert_allclose(got, want, rtol=1e-10)
+
+
+@pytest.mark.parametrize("mode,shift,S_tol,delta_tol", [("bf16", 1e-3, 2e-2, 5e-2), ("bf16_split", 1e-4, 2e-4, 5e-3)])
+def test_tensor_core_S_many_waves_against_fp64(mode, shift, S_tol, delta_tol):
+    """Tensor-core S at Np = 4224 (33 parameter blocks of 128: 561 tiles, several waves of
+    the S kernel) from 8192 Monte Carlo samples, against a full FP64 evaluation of the same
+    samples (complex128 O rows, FP64 HERK), and the SR update delta = (S + shift)^{-1} F
+    against the FP64 Cholesky solve of the FP64 S: relative Frobenius error of S and relative
+    error of delta within the stated bounds (BF16 at shift 1e-3, hi+lo split at 1e-4)."""
+    N, M = 64, 64
+    rng = np.random.default_rng(17)
+    cc = lambda *s: 0.05 * (rng.standard_normal(s) + 1j * rng.standard_normal(s))  # noqa: E731
+    a, b, W = cc(N), cc(M), cc(N, M)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    psi64 = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp64")
+    assert psi.num_params == 4224
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    n = 8192
+    mc = ann.MonteCarloSpins(n, 4, 16, n, True, seed=5, persistent=True)
+    td = ann.TDVP(psi.num_params, s_mode=mode, solver="mixed")
+    td.eval(op, psi, mc)
+    S, F = td.S_matrix, td.F_vector
+    d = td.solve(shift)
+    conf, _, _ = mc.samples()
+    replay = ann.MonteCarloSpins(n, 0, 0, n, True, persistent=True)
+    replay.set_tape(conf[:, 0], np.zeros((n, 1), np.uint32), np.zeros((n, 1)))
+    t64 = ann.TDVP(psi.num_params, s_mode="fp32", solver="fp64")
+    t64.eval(op, psi64, replay)
+    S64, F64 = t64.S_matrix, t64.F_vector
+    d64 = t64.solve(shift)
+    rel = lambda x, y: np.linalg.norm(x - y) / np.linalg.norm(y)  # noqa: E731
+    assert rel(F, F64) < 1e-5, rel(F, F64)
+    assert rel(S, S64) < S_tol, rel(S, S64)
+    assert rel(d, d64) < delta_tol, rel(d, d64)
