@@ -372,13 +372,19 @@ def test_exp_sigma_z_matches_oracle(oracle):
     np.testing.assert_allclose(got, want, rtol=1e-10)
 
 
-@pytest.mark.parametrize("mode,shift,S_tol,delta_tol", [("bf16", 1e-3, 2e-2, 5e-2), ("bf16_split", 1e-4, 2e-4, 5e-3)])
+@pytest.mark.parametrize("mode,shift,S_tol,delta_tol", [("bf16", 1e-3, 2e-2, 0.2), ("bf16_split", 1e-4, 2e-4, 0.12)])
 def test_tensor_core_S_many_waves_against_fp64(mode, shift, S_tol, delta_tol):
     """Tensor-core S at Np = 4224 (33 parameter blocks of 128: 561 tiles, several waves of
     the S kernel) from 8192 Monte Carlo samples, against a full FP64 evaluation of the same
     samples (complex128 O rows, FP64 HERK), and the SR update delta = (S + shift)^{-1} F
-    against the FP64 Cholesky solve of the FP64 S: relative Frobenius error of S and relative
-    error of delta within the stated bounds (BF16 at shift 1e-3, hi+lo split at 1e-4)."""
+    against the FP64 Cholesky solve of the FP64 S.
+
+    Bounds: relative Frobenius error of S (2e-2 BF16, 2e-4 hi+lo split). The update is
+    checked by its backward error: delta solves (S64 + shift) delta = F64 up to exactly the
+    perturbation (S - S64) delta - (F - F64) (the mixed solve adds nothing of its own), and
+    its forward error is that perturbation amplified by cond(S64 + shift), about 1e3-1e4 for
+    this random-init, nearly rank-deficient S: measured 0.083 (BF16, shift 1e-3) and 0.057
+    (hi+lo, shift 1e-4), bounded here at 0.2 and 0.12."""
     N, M = 64, 64
     rng = np.random.default_rng(17)
     cc = lambda *s: 0.05 * (rng.standard_normal(s) + 1j * rng.standard_normal(s))  # noqa: E731
@@ -403,4 +409,8 @@ def test_tensor_core_S_many_waves_against_fp64(mode, shift, S_tol, delta_tol):
     rel = lambda x, y: np.linalg.norm(x - y) / np.linalg.norm(y)  # noqa: E731
     assert rel(F, F64) < 1e-5, rel(F, F64)
     assert rel(S, S64) < S_tol, rel(S, S64)
+    nF = np.linalg.norm(F64)
+    backward = np.linalg.norm(S64 @ d + shift * d - F64) / nF
+    explained = np.linalg.norm((S - S64) @ d - (F - F64)) / nF
+    assert abs(backward - explained) <= 1e-9 + 1e-6 * explained, (backward, explained)
     assert rel(d, d64) < delta_tol, rel(d, d64)
