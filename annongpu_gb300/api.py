@@ -1272,7 +1272,7 @@ def activation_function(z, layer=0, activation="poly") -> complex:
 # ----------------------------------------------------------------------------------
 # autotuner (tuning.cu; this project's addition)
 _KNOBS = {0: "rbm_mc.wpb", 1: "stats.slab", 2: "chol.update", 3: "rbm_mc.wsmem", 4: "chol.reserve",
-          5: "chol.pair"}
+          5: "chol.pair", 6: "rbm_mc.team"}
 
 
 def autotune(operator, psi, ensemble, tdvp, diag_shift=1e-3, stream=None):

@@ -159,7 +159,27 @@ __host__ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
 }
 
 // ---------------------------------------------------------------------------------
-// warp reductions (xor butterflies leave the bit-identical sum in every lane)
+// FP32 <-> FP64 conversions off the FP64 pipe
+// Exact FP32 -> FP64 widening in integer arithmetic (sign, exponent rebias 127 -> 1023,
+// mantissa shifted to 52 bits; subnormals renormalised; infinities and NaNs kept).
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    uint64_t bits;
+    if(e != 0u && e != 0xFFu) {
+        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    } else if(e == 0xFFu) {
+        bits = sign | (0x7FFull << 52) | ((uint64_t)m << 29);
+    } else if(m == 0u) {
+        bits = sign;
+    } else {
+        const uint32_t p = 31u - __clz(m);  // top set bit: value = 1.f * 2^(p - 149)
+        bits = sign | ((uint64_t)(p + 874u) << 52) | ((uint64_t)(m ^ (1u << p)) << (52u - p));
+    }
+    return __longlong_as_double((long long)bits);
+}
+
 // Round-to-nearest-even FP64 -> FP32 in integer arithmetic (subnormal results rounded
 // at their own precision, overflow to infinity, NaN kept as NaN): the same value as
 // cvt.rn.f32.f64, without the FP64 pipe, which runs at 1/64 of the FP32 rate on GB300.
@@ -193,6 +213,8 @@ __device__ __forceinline__ float narrow(double d) {
     return __uint_as_float(r | sign);
 }
 
+// ---------------------------------------------------------------------------------
+// warp reductions (xor butterflies leave the bit-identical sum in every lane)
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -206,6 +228,45 @@ __device__ __forceinline__ double warp_sum(double v) {
 template<typename T>
 __device__ __forceinline__ cplx<T> warp_sum(cplx<T> v) {
     return {warp_sum(v.re), warp_sum(v.im)};
+}
+
+// Teams of TL lanes (32: a whole warp; 16: half a warp) that run one Markov chain each.
+// A half-warp team reproduces a whole-warp team's sums bit for bit: team lane l stands
+// for the warp lanes l and l + 16 ("virtual lanes", kVirt<TL> = 32 / TL of them), keeps one
+// partial per virtual lane in that warp lane's order of terms, and adds the two partials
+// (the warp's first butterfly level, xor 16) before its own butterfly (xor 8 ... 1).
+template<int TL>
+constexpr int kVirt = 32 / TL;
+
+template<int TL>
+__device__ __forceinline__ unsigned team_mask() {
+    static_assert(TL == 32 || TL == 16, "teams of 32 or 16 lanes");
+    return TL == 32 ? 0xffffffffu : (0xffffu << ((threadIdx.x & 31u) & 16u));
+}
+template<int TL>
+__device__ __forceinline__ float team_sum(float v) {
+    const unsigned m = team_mask<TL>();
+#pragma unroll
+    for(int o = TL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o);
+    return v;
+}
+template<int TL>
+__device__ __forceinline__ double team_sum(double v) {
+    const unsigned m = team_mask<TL>();
+#pragma unroll
+    for(int o = TL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o);
+    return v;
+}
+template<int TL, typename T>
+__device__ __forceinline__ cplx<T> team_sum(cplx<T> v) {
+    return {team_sum<TL>(v.re), team_sum<TL>(v.im)};
+}
+// sum over the team of per-virtual-lane partials part[0 .. kVirt<TL>)
+template<int TL, typename V>
+__device__ __forceinline__ V team_total(const V* part) {
+    V v = part[0];
+    if constexpr(TL == 16) v += part[1];
+    return team_sum<TL>(v);
 }
 
 // Pauli-sum operator grouped by flip mask. A string's matrix element on |s> is

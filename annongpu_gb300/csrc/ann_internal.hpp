@@ -167,6 +167,12 @@ struct ann_tdvp_impl {
     DevBuf Obar, F, Osum;       // Np complex128
     DevBuf partial;             // reduction scratch
     DevBuf S;                   // Np x Np complex128
+    // S from the tensor-core HERK holds FP32 sums: with the mixed or FP32 solver it is kept
+    // in complex64 (half the bytes for the HERK's stores, the FP32 copy and every residual
+    // of the refinement); the complex128 copy is formed only when something reads it
+    DevBuf S32;                 // Np x Np complex64
+    bool S_in32 = false;        // the last S is in S32
+    bool S64_fresh = false;     // S (complex128) holds the last S
     DevBuf L;                   // Cholesky factor (lower), Np x Np complex128
     DevBuf rhs, delta, resid;   // Np complex128
     DevBuf tmp64;               // Np complex128: intermediate of the FP64 triangular solves
@@ -178,6 +184,7 @@ struct ann_tdvp_impl {
     double ir_tol = 1e-12;
     bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state
+    DevBuf xs32;                // double-float split of the iterate (residual from a complex64 S)
     int chol_tc = 1;            // FP32 Cholesky trailing update: 1 tcgen05 (split TF32), 0 FP32 SIMT
     int chol_form = 0;          // ANN_CHOL_FORM_* of the last FP32 factorisation
     bool chol_tc_set = false;   // chosen explicitly (ann_tdvp_set_chol_update): the tuning table is not read
@@ -258,6 +265,8 @@ void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want
 
 // FP64 Cholesky SR solve (cholesky.cu)
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
+// the last S in complex128 (widened from S32 on first use after an evaluation that kept it there)
+const cplx<double>* S64(ann_tdvp_impl& td, cudaStream_t st);
 // mixed-precision SR solve (cholesky_mixed.cu); out4 = {solves, first and last
 // relative FP64 residual, stalled}
 void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double tol, bool pivots_to_status,
@@ -290,6 +299,7 @@ int tuning_get(const std::string& key, int dflt);
 void tuning_set(const std::string& key, int value);
 std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens);
+std::string key_mc_team(const ann_psi_impl& psi, const ann_ens_impl& ens);
 std::string key_slab(size_t rows, unsigned Np);
 std::string key_chol_update(unsigned n);
 std::string key_chol_reserve(unsigned n);

@@ -6,6 +6,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include <cuda_profiler_api.h>
 
@@ -1216,12 +1217,20 @@ void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want
               t.Obar.as<cplx<double>>(), t.F.as<cplx<double>>(), t.stats.as<Stats>(), nullptr, t.partial, st);
     mark(2, st);
     if(want_S) {
-        t.S.ensure((size_t)psi.Np * psi.Np * 16);
-        if(t.s_mode == ANN_S_FP32 || psi.precision == 1)
+        const size_t nn = (size_t)psi.Np * psi.Np;
+        if(t.s_mode == ANN_S_FP32 || psi.precision == 1) {
+            t.S.ensure(nn * 16);
+            t.S_in32 = false;
             herk_simt(t.O.p, psi.precision, rows, ld, psi.Np, tw, w0, t.Obar.as<cplx<double>>(),
                       t.stats.as<Stats>(), t.S.as<cplx<double>>(), st);
-        else
+        } else {
+            // FP32 sums: complex64 storage when the solver reads FP32
+            t.S_in32 = t.solver != ANN_SOLVER_FP64;
+            if(t.S_in32) t.S32.ensure(nn * 8);
+            else t.S.ensure(nn * 16);
             herk_tc(t, tw, w0, t.s_mode == ANN_S_BF16_SPLIT, st);
+        }
+        t.S64_fresh = !t.S_in32;
         t.have_S = true;
     }
     mark(3, st);
@@ -1254,7 +1263,15 @@ int ann_tdvp_get_S(ann_tdvp* t, double* out) {
         need(t && out && t->have_S, "S not evaluated");
         ANN_CUDA(cudaDeviceSynchronize());
         check_status();
-        ANN_CUDA(cudaMemcpy(out, t->S.p, (size_t)t->Np * t->Np * 16, cudaMemcpyDeviceToHost));
+        const size_t nn = (size_t)t->Np * t->Np;
+        if(t->S_in32 && !t->S64_fresh) {
+            // complex64 values, widened exactly on the host
+            std::vector<float> s32(2 * nn);
+            ANN_CUDA(cudaMemcpy(s32.data(), t->S32.p, nn * 8, cudaMemcpyDeviceToHost));
+            for(size_t k = 0; k < 2 * nn; k++) out[k] = (double)s32[k];
+        } else {
+            ANN_CUDA(cudaMemcpy(out, t->S.p, nn * 16, cudaMemcpyDeviceToHost));
+        }
     });
 }
 int ann_tdvp_get_F(ann_tdvp* t, double* out) {

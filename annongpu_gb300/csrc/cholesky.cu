@@ -309,6 +309,26 @@ void ensure_side_stream(ann_tdvp_impl& td) {
     for(auto& e : td.side_ev) ANN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 }
 
+namespace {
+__global__ void widen_S_kernel(const float2* __restrict__ s32, double2* __restrict__ s, size_t nn) {
+    for(size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = s32[k];
+        s[k] = make_double2(widen(v.x), widen(v.y));
+    }
+}
+}  // namespace
+
+const cplx<double>* S64(ann_tdvp_impl& td, cudaStream_t st) {
+    if(td.S_in32 && !td.S64_fresh) {
+        const size_t nn = (size_t)td.Np * td.Np;
+        td.S.ensure(nn * 16);
+        widen_S_kernel<<<152 * 8, 256, 0, st>>>(td.S32.as<float2>(), td.S.as<double2>(), nn);
+        check_launch("widen_S_kernel");
+        td.S64_fresh = true;
+    }
+    return td.S.as<cplx<double>>();
+}
+
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st) {
     const unsigned n = td.Np;
     const size_t nn = (size_t)n * n;
@@ -321,7 +341,7 @@ void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status, cudaStream_t st
     zc* x = td.delta.as<zc>();
     zc* r = td.resid.as<zc>();
     double* info = reinterpret_cast<double*>(r + 2 * n);
-    const zc* S = td.S.as<zc>();
+    const zc* S = S64(td, st);
     const zc* F = td.F.as<zc>();
     copy_shift_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(S, A, n, shift);
     check_launch("copy_shift_kernel");

@@ -9,6 +9,8 @@
 //      and every later triangular solve multiply by it instead of substituting.
 //   3. x = 0, r = F; repeat: c = (L L^H)^{-1} r in FP32, x += c in FP64,
 //      r = F - (S + shift I) x in FP64, until ||r|| / ||F|| <= tol or max_iter.
+//      When S holds FP32 values in complex64 (the tensor-core HERK's sums), S x is
+//      formed on the FP32 pipe in double-float arithmetic (below) and r in FP64.
 //
 // The iteration is classical mixed-precision iterative refinement (Wilkinson;
 // Moler 1967; analysed by Higham, "Accuracy and Stability of Numerical
@@ -37,31 +39,37 @@ using zc = cplx<double>;
 
 // lower triangle of S + shift I in complex64, row-major n x n. CTA b converts rows b and
 // n - 1 - b (n + 1 entries together, so every CTA has the same work).
-__global__ void __launch_bounds__(256) cvt_shift_kernel(const zc* __restrict__ S, cf* __restrict__ A, unsigned n,
+__device__ __forceinline__ zc to_zc(zc v) { return v; }
+__device__ __forceinline__ zc to_zc(cf v) { return mk(widen(v.re), widen(v.im)); }
+
+template<typename TS>
+__global__ void __launch_bounds__(256) cvt_shift_kernel(const TS* __restrict__ S, cf* __restrict__ A, unsigned n,
                                                         double shift) {
     const unsigned rows[2] = {blockIdx.x, n - 1u - blockIdx.x};
     for(int h = 0; h < 2; h++) {
         const unsigned i = rows[h];
         if(h == 1 && i == rows[0]) break;
-        const zc* Si = S + (size_t)i * n;
+        const TS* Si = S + (size_t)i * n;
         cf* Ai = A + (size_t)i * n;
         unsigned j = threadIdx.x;
-        // four 16-byte loads in flight per thread
+        // four loads in flight per thread; off the diagonal a complex64 S is copied as is
+        // (narrow(widen(v)) == v), the diagonal gets the shift in FP64 and one rounding
         for(; j + 768u <= i; j += 1024u) {
-            zc v[4];
+            TS v[4];
 #pragma unroll
             for(int q = 0; q < 4; q++) v[q] = Si[j + 256u * q];
 #pragma unroll
             for(int q = 0; q < 4; q++) {
                 const unsigned jj = j + 256u * q;
-                if(jj == i) v[q].re += shift;
-                Ai[jj] = mk(narrow(v[q].re), narrow(v[q].im));
+                zc w = to_zc(v[q]);
+                if(jj == i) w.re += shift;
+                Ai[jj] = mk(narrow(w.re), narrow(w.im));
             }
         }
         for(; j <= i; j += 256u) {
-            zc v = Si[j];
-            if(j == i) v.re += shift;
-            Ai[j] = mk(narrow(v.re), narrow(v.im));
+            zc w = to_zc(Si[j]);
+            if(j == i) w.re += shift;
+            Ai[j] = mk(narrow(w.re), narrow(w.im));
         }
     }
 }
@@ -594,11 +602,21 @@ __global__ void ir_init_kernel(const zc* __restrict__ F, zc* __restrict__ x, zc*
     }
 }
 
-// x += c (FP64), then c is recomputed from the new residual by ir_residual_kernel
-__global__ void ir_axpy_kernel(zc* __restrict__ x, const cf* __restrict__ c, unsigned n, const IrState* st) {
+// x += c (FP64), then c is recomputed from the new residual by ir_residual_kernel. With
+// xs, x is also split for the double-float residual: xs[i] = (hi, lo) of Re and Im, hi =
+// fl32(x), lo = fl32(x - hi), so x = hi + lo to 2^-48 relative.
+__global__ void ir_axpy_kernel(zc* __restrict__ x, const cf* __restrict__ c, unsigned n, const IrState* st,
+                               float4* __restrict__ xs) {
     if(st->done) return;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i < n) x[i] += cvt<double>(c[i]);
+    if(i < n) {
+        const zc v = x[i] + cvt<double>(c[i]);
+        x[i] = v;
+        if(xs) {
+            const float rh = narrow(v.re), ih = narrow(v.im);
+            xs[i] = make_float4(rh, narrow(v.re - widen(rh)), ih, narrow(v.im - widen(ih)));
+        }
+    }
 }
 
 // r = F - (S + shift I) x in FP64 (one warp per row), c = (complex64) r, and per-CTA
@@ -634,6 +652,110 @@ __global__ void __launch_bounds__(256) ir_residual_kernel(const zc* __restrict__
                 c[i] = cvt<float>(ri);
                 rr = norm2(ri);
                 ff = norm2(F[i]);
+            }
+        }
+    }
+    if(lane == 0) { sh[0][warp] = rr; sh[1][warp] = ff; }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for(int w = 0; w < 8; w++) { a += sh[0][w]; b += sh[1][w]; }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+
+// ---- double-float arithmetic (pairs hi + lo of FP32 values; Dekker 1971, Knuth's
+// TwoSum): S x for an S of FP32 entries on the FP32 pipe. Every operation is an explicit
+// round-to-nearest intrinsic, so no multiply-add is contracted into the error terms.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (h, l) += s (xh + xl): s xh exactly as p + pe (pe = fma(s, xh, -p)), s xl rounded once
+__device__ __forceinline__ void df_mac(float& h, float& l, float s, float xh, float xl) {
+    const float p = __fmul_rn(s, xh);
+    const float pe = __fmaf_rn(s, xh, -p);
+    float t, e;
+    two_sum(h, p, t, e);
+    h = t;
+    l = __fadd_rn(l, __fadd_rn(e, __fmaf_rn(s, xl, pe)));
+}
+// back to |l| <= ulp(h) / 2 (Fast2Sum; |l| << |h| here)
+__device__ __forceinline__ void df_norm(float& h, float& l) {
+    const float s = __fadd_rn(h, l);
+    l = __fsub_rn(l, __fsub_rn(s, h));
+    h = s;
+}
+__device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
+    float s, e;
+    two_sum(h, h2, s, e);
+    h = s;
+    l = __fadd_rn(__fadd_rn(l, l2), e);
+    df_norm(h, l);
+}
+__device__ __forceinline__ void df_warp_sum(float& h, float& l) {
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+        df_add(h, l, h2, l2);
+    }
+}
+
+constexpr unsigned kRes32Rows = 16;  // rows per CTA of ir_residual32_kernel (two per warp)
+
+// r = F - (S + shift I) x for S in complex64 holding FP32 values (the tensor-core HERK's
+// sums): S x in double-float from x's split xs (each product s xh exact, s xl rounded
+// once, sums by TwoSum with renormalisation after every term: about 2^-48 relative per
+// term, against 2^-53 for FP64 arithmetic), then F - S x - shift x in FP64. GB300's FP64
+// pipe (1/64 of the FP32 rate) would bound the FP64 product at ~0.5 ms for Np = 8384;
+// here the S rows stream at HBM rate. One warp per two rows (each xs load serves both).
+__global__ void __launch_bounds__(256) ir_residual32_kernel(const cf* __restrict__ S, unsigned n, double shift,
+                                                            const zc* __restrict__ x, const float4* __restrict__ xs,
+                                                            const zc* __restrict__ F, zc* __restrict__ r,
+                                                            cf* __restrict__ c, double* __restrict__ part,
+                                                            const IrState* st) {
+    __shared__ double sh[2][8];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double rr = 0.0, ff = 0.0;
+    if(!st->done) {
+        const size_t i0 = (size_t)blockIdx.x * kRes32Rows + 2 * warp;
+        if(i0 < n) {
+            const bool two = i0 + 1 < n;
+            const cf* S0 = S + i0 * n;
+            const cf* S1 = S + (two ? i0 + 1 : i0) * n;
+            // [row][re, im] accumulators
+            float h[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, l[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 4
+            for(unsigned j = lane; j < n; j += 32) {
+                const float4 xv = xs[j];
+                const cf s[2] = {S0[j], S1[j]};
+#pragma unroll
+                for(int q = 0; q < 2; q++) {
+                    df_mac(h[q][0], l[q][0], s[q].re, xv.x, xv.y);   // Re s Re x
+                    df_mac(h[q][0], l[q][0], -s[q].im, xv.z, xv.w);  // - Im s Im x
+                    df_mac(h[q][1], l[q][1], s[q].re, xv.z, xv.w);   // Re s Im x
+                    df_mac(h[q][1], l[q][1], s[q].im, xv.x, xv.y);   // Im s Re x
+                    df_norm(h[q][0], l[q][0]);
+                    df_norm(h[q][1], l[q][1]);
+                }
+            }
+#pragma unroll
+            for(int q = 0; q < 2; q++) {
+                df_warp_sum(h[q][0], l[q][0]);
+                df_warp_sum(h[q][1], l[q][1]);
+            }
+            if(lane == 0) {
+                for(int q = 0; q < (two ? 2 : 1); q++) {
+                    const size_t i = i0 + q;
+                    const zc acc = mk(widen(h[q][0]) + widen(l[q][0]), widen(h[q][1]) + widen(l[q][1]));
+                    const zc ri = F[i] - acc - shift * x[i];
+                    r[i] = ri;
+                    c[i] = cvt<float>(ri);
+                    rr += norm2(ri);
+                    ff += norm2(F[i]);
+                }
             }
         }
     }
@@ -828,7 +950,10 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     td.delta.ensure(n * sizeof(zc));
     td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
     td.c32.ensure((size_t)n * sizeof(cf));
-    const unsigned res_blocks = (n + 7) / 8;
+    // S in complex64 (FP32 values): double-float residual on the FP32 pipe; else FP64
+    const bool s32 = td.S_in32;
+    if(s32) td.xs32.ensure((size_t)n * sizeof(float4));
+    const unsigned res_blocks = s32 ? (n + kRes32Rows - 1) / kRes32Rows : (n + 7) / 8;
     static_assert(sizeof(IrState) % 16 == 0, "the solve's tagged blocks need 16-byte alignment");
     td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double) + kSolveSyncHead +
                  2 * (size_t)nblk * NB * sizeof(ulonglong2));
@@ -841,7 +966,9 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     IrState* irs = td.ir.as<IrState>();
     double* part = reinterpret_cast<double*>(irs + 1);
     int* sync = reinterpret_cast<int*>(part + 2 * (size_t)res_blocks);
-    const zc* S = td.S.as<zc>();
+    const zc* S = s32 ? nullptr : td.S.as<zc>();
+    const cf* S32 = s32 ? td.S32.as<cf>() : nullptr;
+    float4* xs = s32 ? td.xs32.as<float4>() : nullptr;
     const zc* F = td.F.as<zc>();
 
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -849,7 +976,8 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     const int report = cs != cudaStreamCaptureStatusNone;
     ir_init_kernel<<<(n + 255) / 256, 256, 0, st>>>(F, x, r, c, n, irs);
     check_launch("ir_init_kernel");
-    cvt_shift_kernel<<<(n + 1) / 2, 256, 0, st>>>(S, A, n, shift);
+    if(s32) cvt_shift_kernel<cf><<<(n + 1) / 2, 256, 0, st>>>(S32, A, n, shift);
+    else cvt_shift_kernel<zc><<<(n + 1) / 2, 256, 0, st>>>(S, A, n, shift);
     check_launch("cvt_shift_kernel");
     // FP32 pivot failures are recorded in the refinement state (they end in a stall and
     // the FP64 fallback), or, with no refinement to fall back from, in the status word
@@ -858,10 +986,15 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     solve_mark(1, st);
     for(unsigned it = 0; it < max_iter; it++) {
         solve32(A, Dinv, DinvH, n, c, irs, sync, status, st);
-        ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs);
+        ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs, xs);
         check_launch("ir_axpy_kernel");
-        ir_residual_kernel<<<res_blocks, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs);
-        check_launch("ir_residual_kernel");
+        if(s32) {
+            ir_residual32_kernel<<<res_blocks, 256, 0, st>>>(S32, n, shift, x, xs, F, r, c, part, irs);
+            check_launch("ir_residual32_kernel");
+        } else {
+            ir_residual_kernel<<<res_blocks, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs);
+            check_launch("ir_residual_kernel");
+        }
         ir_check_kernel<<<1, 1024, 0, st>>>(part, res_blocks, tol, it + 1 == max_iter, irs, report, status);
         check_launch("ir_check_kernel");
     }

@@ -50,29 +50,10 @@ struct HerkArgs {
     unsigned lo_offset;     // column of the lo copy in XT
     const cplx<double>* Obar;
     const Stats* stats;
-    cplx<double>* S;
+    cplx<double>* S;        // S in complex128 (integer-widened FP32 sums) ...
+    cplx<float>* S32;       // ... or, when non-null, in complex64 (the mixed / FP32 solvers read it)
     unsigned* status;
 };
-
-// Exact FP32 -> FP64 widening in integer arithmetic (sign, exponent rebias 127 -> 1023,
-// mantissa shifted to 52 bits; subnormals renormalised; infinities and NaNs kept).
-__device__ __forceinline__ double widen(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint64_t sign = (uint64_t)(u >> 31) << 63;
-    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
-    uint64_t bits;
-    if(e != 0u && e != 0xFFu) {
-        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
-    } else if(e == 0xFFu) {
-        bits = sign | (0x7FFull << 52) | ((uint64_t)m << 29);
-    } else if(m == 0u) {
-        bits = sign;
-    } else {
-        const uint32_t p = 31u - __clz(m);  // top set bit: value = 1.f * 2^(p - 149)
-        bits = sign | ((uint64_t)(p + 874u) << 52) | ((uint64_t)(m ^ (1u << p)) << (52u - p));
-    }
-    return __longlong_as_double((long long)bits);
-}
 
 __device__ __forceinline__ void store_widened(cplx<double>* p, float re, float im) {
     *reinterpret_cast<double2*>(p) = make_double2(widen(re), widen(im));
@@ -202,8 +183,13 @@ herk_tc_kernel(const __grid_constant__ CUtensorMap tmap, HerkArgs a) {
                 vr = fmaf(-ok_c.im, ob.im, vr);
                 vi = fmaf(ok_c.re, ob.im, vi);
                 vi = fmaf(ok_c.im, ob.re, vi);
-                store_widened(a.S + (size_t)k * a.Np + l, vr, vi);
-                if(I != J) store_widened(a.S + (size_t)l * a.Np + k, vr, -vi);
+                if(a.S32) {
+                    a.S32[(size_t)k * a.Np + l] = mk(vr, vi);
+                    if(I != J) a.S32[(size_t)l * a.Np + k] = mk(vr, -vi);
+                } else {
+                    store_widened(a.S + (size_t)k * a.Np + l, vr, vi);
+                    if(I != J) store_widened(a.S + (size_t)l * a.Np + k, vr, -vi);
+                }
             }
         }
     } else if(warp == 0 && lane == 0) {
@@ -326,7 +312,8 @@ void herk_tc(ann_tdvp_impl& td, const double* wts, double w0, bool split, cudaSt
     a.lo_offset = (unsigned)ns_pad;
     a.Obar = td.Obar.as<cplx<double>>();
     a.stats = td.stats.as<Stats>();
-    a.S = td.S.as<cplx<double>>();
+    a.S = td.S_in32 ? nullptr : td.S.as<cplx<double>>();
+    a.S32 = td.S_in32 ? td.S32.as<cplx<float>>() : nullptr;
     a.status = status_word();
     static bool attr = false;
     if(!attr) {

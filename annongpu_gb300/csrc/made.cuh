@@ -73,53 +73,65 @@ __device__ __forceinline__ float xbit(const Conf<NW>& s, unsigned i) {
     return spin_bit(s, i) ? 1.f : 0.f;
 }
 
-// log q(s), warp-cooperative; h is a per-warp scratch of H floats
-template<int NW>
+// log q(s), cooperative over a team of TL lanes (lane: the lane within the team; the sums
+// per virtual lane, as in the sampler, so any team gives the whole warp's value); h is a
+// per-team scratch of H floats
+template<int NW, int TL = 32>
 __device__ float made_logq(const MadeSm& m, const Conf<NW>& s, float* h, int lane) {
-    for(unsigned k = lane; k < m.H; k += 32) {
+    const unsigned mask = team_mask<TL>();
+    for(unsigned k = lane; k < m.H; k += TL) {
         float pre = m.b1[k];
         for(unsigned i = 0; i < m.N; i++)
             if(spin_bit(s, i)) pre += __bfloat162float(m.W1t[i * m.H + k]);
         h[k] = fmaxf(pre, 0.f);
     }
-    __syncwarp();
+    __syncwarp(mask);
     // logit j: lanes split the hidden units (consecutive W2[j][k]), butterfly sum
     float acc = 0.f;
     for(unsigned j = 0; j < m.N; j++) {
-        float part = 0.f;
-        for(unsigned k = lane; k < m.H; k += 32) part = fmaf(__bfloat162float(m.W2[j * m.H + k]), h[k], part);
-        const float l = m.b2[j] + warp_sum(part);
+        float part[kVirt<TL>];
+#pragma unroll
+        for(int v = 0; v < kVirt<TL>; v++) {
+            part[v] = 0.f;
+            for(unsigned k = lane + v * TL; k < m.H; k += 32)
+                part[v] = fmaf(__bfloat162float(m.W2[j * m.H + k]), h[k], part[v]);
+        }
+        const float l = m.b2[j] + team_total<TL>(part);
         acc -= spin_bit(s, j) ? softplusf(-l) : softplusf(l);
     }
-    __syncwarp();
+    __syncwarp(mask);
     return acc;
 }
 
 // Draws s ~ q autoregressively; uniforms from Philox counters (c0, c1, c2, 3 + 4 b),
 // word j % 4 of block b = j / 4, u_j = (word >> 8) 2^-24; x_j = 1 iff u_j < sigmoid(l_j).
-// Lane k keeps the pre-activations of hidden units k, k+32, ... in registers.
-template<int NW, int HU>
+// Team lane k keeps the pre-activations of hidden units k, k+TL, ... in registers; the
+// team's lanes hold the uniforms of 4 TL spins (N <= 4 TL).
+template<int NW, int HU, int TL = 32>
 __device__ float made_sample(const MadeSm& m, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2,
                              Conf<NW>& s, int lane) {
+    const unsigned mask = team_mask<TL>();
     const u32x4 rr = philox4x32_10(k0, k1, u32x4{c0, c1, c2, 3u + 4u * (uint32_t)lane});
     float pre[HU];
 #pragma unroll
     for(int u = 0; u < HU; u++) {
-        const unsigned k = u * 32 + lane;
+        const unsigned k = u * TL + lane;
         pre[u] = k < m.H ? m.b1[k] : 0.f;
     }
     for(int w = 0; w < NW; w++) s.w[w] = 0;
     float logq = 0.f;
     for(unsigned j = 0; j < m.N; j++) {
-        float part = 0.f;
+        float part[kVirt<TL>];
+#pragma unroll
+        for(int v = 0; v < kVirt<TL>; v++) part[v] = 0.f;
 #pragma unroll
         for(int u = 0; u < HU; u++) {
-            const unsigned k = u * 32 + lane;
-            if(k < m.H) part = fmaf(__bfloat162float(m.W2[j * m.H + k]), fmaxf(pre[u], 0.f), part);
+            const unsigned k = u * TL + lane;
+            if(k < m.H) part[u % kVirt<TL>] = fmaf(__bfloat162float(m.W2[j * m.H + k]), fmaxf(pre[u], 0.f), part[u % kVirt<TL>]);
         }
-        const float l = m.b2[j] + warp_sum(part);
+        const float l = m.b2[j] + team_total<TL>(part);
         const uint32_t word_src = (j & 3u) == 0 ? rr.x : (j & 3u) == 1 ? rr.y : (j & 3u) == 2 ? rr.z : rr.w;
-        const uint32_t word = __shfl_sync(0xffffffffu, word_src, j >> 2);
+        const uint32_t word = __shfl_sync(mask, word_src, j >> 2, TL);
         const float uj = __uint2float_rz(word >> 8) * 0x1.0p-24f;
         const float p = 1.f / (1.f + expf(-l));
         const bool up = uj < p;
@@ -128,7 +140,7 @@ __device__ float made_sample(const MadeSm& m, uint32_t k0, uint32_t k1, uint32_t
             s.w[j >> 6] |= (uint64_t)1 << (j & 63u);
 #pragma unroll
             for(int u = 0; u < HU; u++) {
-                const unsigned k = u * 32 + lane;
+                const unsigned k = u * TL + lane;
                 if(k < m.H) pre[u] += __bfloat162float(m.W1t[j * m.H + k]);
             }
         }

@@ -1,5 +1,6 @@
-// RBM-family wavefunctions on the GPU: one warp per Markov chain (or per enumerated
-// configuration), hidden-unit angles held in registers and updated incrementally.
+// RBM-family wavefunctions on the GPU: one warp or half-warp per Markov chain (one warp
+// per enumerated configuration), hidden-unit angles held in registers and updated
+// incrementally.
 //
 // Covers the reference's PsiRBM (include/quantum_state/PsiRBM.hpp:69-176) and
 // PsiDeep with one hidden layer (include/quantum_state/PsiDeep.hpp:138-445): both
@@ -17,12 +18,20 @@ namespace ann {
 
 constexpr int kWarpsPerBlock = 8;
 
-// Wavefunction as the kernels see it. Unit j of the padded width Mpad = 32 * U
-// lives in lane j % 32, register slot j / 32.
+// A team of TL lanes runs one chain: TL = 32 (a whole warp) or 16 (half a warp, two chains
+// per warp: fewer shuffle levels per proposal and twice the independent units per lane).
+// Below, `lane` is the lane within the team; unit j of the padded width lives in team lane
+// j % TL, register slot j / TL. Slot u of a half-warp team belongs to virtual lane u % 2
+// (unit u * 16 + l is unit (u / 2) * 32 + l + 16 (u % 2)), so every sum below, taken per
+// virtual lane and combined by team_total, equals the whole-warp sum bit for bit: the
+// choice of team changes speed, not chains.
+
+// Wavefunction as the kernels see it. Unit j of the padded width Mpad lives in lane
+// j % TL of the chain's team, register slot j / TL (Mpad = TL * U).
 template<typename T>
 struct RbmDev {
     unsigned N, M, Mpad, C, Np;
-    unsigned Uact;       // register slots in use (Mpad / 32 <= U)
+    unsigned Uact;       // register slots in use (Mpad / TL <= U)
     int layout;          // 0: params = W (PsiRBM), 1: params = [a | b | W] (PsiDeep)
     int a_in_log_psi;    // 1: log psi includes a.s
     int act;             // Activation
@@ -35,7 +44,7 @@ struct RbmDev {
     int fw_real;         // every final weight is real: Re(fw f) = Re fw Re f
 };
 
-// Per lane: the angles of units lane, lane + 32, ... and the real parts of their
+// Per lane: the angles of units lane, lane + TL, ... and the real parts of their
 // log-psi terms. A Metropolis decision needs only Re(log psi' - log psi), so proposals
 // evaluate the real part of the activation alone; the complex terms are formed when a
 // sample is taken.
@@ -61,24 +70,24 @@ __device__ __forceinline__ T act_f_re(cplx<T> z, int act) {
     return w.re + T(0.5) * flog(norm2(mk<T>(T(1) + e.re, e.im))) - T(0.69314718055994530942);
 }
 
-// Re(fw_j f(z)) of unit j = u * 32 + lane (complex final weights are read from memory)
-template<typename T, int U>
+// Re(fw_j f(z)) of unit j = u * TL + lane (complex final weights are read from memory)
+template<typename T, int U, int TL = 32>
 __device__ __forceinline__ T fw_f_re(const RbmDev<T>& p, const Lane<T, U>& L, int u, int lane, cplx<T> z) {
     if(p.fw_real) return L.fwr[u] * act_f_re(z, p.act);
-    const cplx<T> fw = p.fw[u * 32 + lane];
+    const cplx<T> fw = p.fw[u * TL + lane];
     const cplx<T> f = act_f(z, p.act, 0);
     return fw.re * f.re - fw.im * f.im;
 }
 
 // theta_j = b_j + sum_i s_i Wd[i][j] from scratch
-template<typename T, int NW, int U>
+template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
                                           const Conf<NW>& s, Lane<T, U>& L, int lane) {
 #pragma unroll
     for(int u = 0; u < U; u++) {
         const bool on = (unsigned)u < p.Uact;
-        L.th[u] = on ? p.b[u * 32 + lane] : mk<T>(T(0), T(0));
-        L.fwr[u] = on ? p.fw[u * 32 + lane].re : T(0);
+        L.th[u] = on ? p.b[u * TL + lane] : mk<T>(T(0), T(0));
+        L.fwr[u] = on ? p.fw[u * TL + lane].re : T(0);
     }
     for(unsigned i = 0; i < p.N; i++) {
         const T si = spin_bit(s, i) ? T(1) : T(-1);
@@ -86,26 +95,26 @@ __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __r
 #pragma unroll
         for(int u = 0; u < U; u++) {
             if((unsigned)u >= p.Uact) break;
-            const cplx<T> w = row[u * 32];
+            const cplx<T> w = row[u * TL];
             L.th[u].re += si * w.re;
             L.th[u].im += si * w.im;
         }
     }
 #pragma unroll
-    for(int u = 0; u < U; u++) L.fr[u] = (unsigned)u < p.Uact ? fw_f_re(p, L, u, lane, L.th[u]) : T(0);
+    for(int u = 0; u < U; u++) L.fr[u] = (unsigned)u < p.Uact ? fw_f_re<T, U, TL>(p, L, u, lane, L.th[u]) : T(0);
 }
 
 // complex terms fw_j f(theta_j) of the lane's units (sample time)
-template<typename T, int U>
+template<typename T, int U, int TL = 32>
 __device__ __forceinline__ void lane_terms(const RbmDev<T>& p, const Lane<T, U>& L, int lane, cplx<T>* ft) {
 #pragma unroll
     for(int u = 0; u < U; u++)
-        ft[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
+        ft[u] = (unsigned)u < p.Uact ? p.fw[u * TL + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
 }
 
-// Re(log psi(s') - log psi(s)) summed over the warp for the flip of `sites`; leaves the
+// Re(log psi(s') - log psi(s)) summed over the team for the flip of `sites`; leaves the
 // angle changes in dth and the new real terms in fnew for an accepted move
-template<typename T, int NW, int U>
+template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ T delta_re(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const Conf<NW>& s,
                                       const Lane<T, U>& L, int lane, const uint16_t* sites, unsigned nsites,
                                       cplx<T>* dth, T* fnew) {
@@ -119,27 +128,29 @@ __device__ __forceinline__ T delta_re(const RbmDev<T>& p, const cplx<T>* __restr
 #pragma unroll
         for(int u = 0; u < U; u++) {
             if((unsigned)u >= p.Uact) break;
-            const cplx<T> w = row[u * 32];
+            const cplx<T> w = row[u * TL];
             dth[u].re += m2s * w.re;
             dth[u].im += m2s * w.im;
         }
         if(p.a_in_log_psi) dvis += m2s * p.a[i].re;
     }
-    T d = T(0);
+    T d[kVirt<TL>];
+#pragma unroll
+    for(int k = 0; k < kVirt<TL>; k++) d[k] = T(0);
 #pragma unroll
     for(int u = 0; u < U; u++) {
         if((unsigned)u >= p.Uact) {
             fnew[u] = T(0);
             continue;
         }
-        fnew[u] = fw_f_re(p, L, u, lane, L.th[u] + dth[u]);
-        d += fnew[u] - L.fr[u];
+        fnew[u] = fw_f_re<T, U, TL>(p, L, u, lane, L.th[u] + dth[u]);
+        d[u % kVirt<TL>] += fnew[u] - L.fr[u];
     }
-    return warp_sum(d) + dvis;
+    return team_total<TL>(d) + dvis;
 }
 
-// sum over the warp of fw_j (f(theta_j + dtheta_j) - f(theta_j)) for the sites in `sites`
-template<typename T, int NW, int U>
+// sum over the team of fw_j (f(theta_j + dtheta_j) - f(theta_j)) for the sites in `sites`
+template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
                                                  const Conf<NW>& s, const Lane<T, U>& L, const cplx<T>* ft,
                                                  int lane, const uint16_t* sites, unsigned nsites,
@@ -154,43 +165,49 @@ __device__ __forceinline__ cplx<T> delta_log_psi(const RbmDev<T>& p, const cplx<
 #pragma unroll
         for(int u = 0; u < U; u++) {
             if((unsigned)u >= p.Uact) break;
-            const cplx<T> w = row[u * 32];
+            const cplx<T> w = row[u * TL];
             dth[u].re += m2s * w.re;
             dth[u].im += m2s * w.im;
         }
         if(p.a_in_log_psi) dvis += m2s * p.a[i];
     }
-    cplx<T> d = mk<T>(T(0), T(0));
+    cplx<T> d[kVirt<TL>];
+#pragma unroll
+    for(int k = 0; k < kVirt<TL>; k++) d[k] = mk<T>(T(0), T(0));
 #pragma unroll
     for(int u = 0; u < U; u++) {
         if((unsigned)u >= p.Uact) {
             fnew[u] = mk<T>(T(0), T(0));
             continue;
         }
-        fnew[u] = p.fw[u * 32 + lane] * act_f(L.th[u] + dth[u], p.act, 0);
-        d += fnew[u] - ft[u];
+        fnew[u] = p.fw[u * TL + lane] * act_f(L.th[u] + dth[u], p.act, 0);
+        d[u % kVirt<TL>] += fnew[u] - ft[u];
     }
-    d = warp_sum(d);
-    return d + dvis;
+    return team_total<TL>(d) + dvis;
 }
 
 // local energy of configuration s (Operator.hpp:86-121 semantics)
-template<typename T, int NW, int U>
+template<typename T, int NW, int U, int TL = 32>
 __device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op,
                                      const Conf<NW>& s, const Lane<T, U>& L, const cplx<T>* ft, int lane) {
     // arithmetic in the kernel precision T (coefficients are stored in FP64 and
     // rounded once); the FP64 pipe is reserved for the final conversion
     // diagonal strings, split over lanes
-    T dre = T(0), dim = T(0);
-    for(unsigned n = lane; n < op.n_diag; n += 32) {
-        int neg = 0;
+    T dre[kVirt<TL>], dim[kVirt<TL>];
 #pragma unroll
-        for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.diag_mask[n * op.nw + w]);
-        const T c_re = diag_coeff<T>(op)[2 * n], c_im = diag_coeff<T>(op)[2 * n + 1];
-        dre += (neg & 1) ? -c_re : c_re;
-        dim += (neg & 1) ? -c_im : c_im;
+    for(int k = 0; k < kVirt<TL>; k++) {
+        dre[k] = T(0);
+        dim[k] = T(0);
+        for(unsigned n = lane + k * TL; n < op.n_diag; n += 32) {
+            int neg = 0;
+#pragma unroll
+            for(int w = 0; w < NW; w++) neg += __popcll((~s.w[w]) & op.diag_mask[n * op.nw + w]);
+            const T c_re = diag_coeff<T>(op)[2 * n], c_im = diag_coeff<T>(op)[2 * n + 1];
+            dre[k] += (neg & 1) ? -c_re : c_re;
+            dim[k] += (neg & 1) ? -c_im : c_im;
+        }
     }
-    cplx<T> e = mk<T>(warp_sum(dre), warp_sum(dim));
+    cplx<T> e = mk<T>(team_total<TL>(dre), team_total<TL>(dim));
     cplx<T> dth[U], fnew[U];
     for(unsigned g = 0; g < op.n_groups; g++) {
         // summed matrix element of the group first: when it vanishes (e.g. XX + YY on
@@ -206,28 +223,32 @@ __device__ cplx<double> local_energy(const RbmDev<T>& p, const cplx<T>* __restri
         }
         if(cg.re == T(0) && cg.im == T(0)) continue;
         const unsigned sb = op.grp_site_begin[g], se = op.grp_site_begin[g + 1];
-        const cplx<T> d = delta_log_psi<T, NW, U>(p, Wd, s, L, ft, lane, op.grp_sites + sb, se - sb, dth, fnew);
+        const cplx<T> d = delta_log_psi<T, NW, U, TL>(p, Wd, s, L, ft, lane, op.grp_sites + sb, se - sb, dth, fnew);
         e += cg * cexp(d);
     }
     return cvt<double>(e);
 }
 
 // log psi, local energy, O_k row and sample bookkeeping for one configuration
-template<typename T, int NW, int U>
+template<typename T, int NW, int U, int TL = 32>
 __device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev* op,
                                const Conf<NW>& s, const Lane<T, U>& L, int lane, size_t row,
                                const SampleOut& out, bool exact_weight) {
     cplx<T> ft[U];
-    lane_terms<T, U>(p, L, lane, ft);
-    cplx<T> lsum = mk<T>(T(0), T(0));
+    lane_terms<T, U, TL>(p, L, lane, ft);
+    cplx<T> lpart[kVirt<TL>];
 #pragma unroll
-    for(int u = 0; u < U; u++) lsum += ft[u];
+    for(int k = 0; k < kVirt<TL>; k++) lpart[k] = mk<T>(T(0), T(0));
+#pragma unroll
+    for(int u = 0; u < U; u++) lpart[u % kVirt<TL>] += ft[u];
     if(p.a_in_log_psi)
-        for(unsigned i = lane; i < p.N; i += 32) lsum += (spin_bit(s, i) ? T(1) : T(-1)) * p.a[i];
-    lsum = warp_sum(lsum);
+#pragma unroll
+        for(int k = 0; k < kVirt<TL>; k++)
+            for(unsigned i = lane + k * TL; i < p.N; i += 32) lpart[k] += (spin_bit(s, i) ? T(1) : T(-1)) * p.a[i];
+    const cplx<T> lsum = team_total<TL>(lpart);
     const cplx<double> lpsi = cvt<double>(lsum) + cvt<double>(p.lp);
     cplx<double> e = mk<double>(0.0, 0.0);
-    if(op) e = local_energy<T, NW, U>(p, Wd, *op, s, L, ft, lane);
+    if(op) e = local_energy<T, NW, U, TL>(p, Wd, *op, s, L, ft, lane);
     if(lane == 0) {
         for(int w = 0; w < kMaxWords; w++) out.conf[row * kMaxWords + w] = w < NW ? s.w[w] : 0;
         out.log_psi[row] = lpsi;
@@ -241,13 +262,13 @@ __device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ W
         cplx<T> g[U];
 #pragma unroll
         for(int u = 0; u < U; u++)
-            g[u] = (unsigned)u < p.Uact ? p.fw[u * 32 + lane] * act_df(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
+            g[u] = (unsigned)u < p.Uact ? p.fw[u * TL + lane] * act_df(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
         unsigned off = 0;
         if(p.layout == 1) {
-            for(unsigned i = lane; i < p.N; i += 32) O[i] = mk<T>(spin_bit(s, i) ? T(1) : T(-1), T(0));
+            for(unsigned i = lane; i < p.N; i += TL) O[i] = mk<T>(spin_bit(s, i) ? T(1) : T(-1), T(0));
 #pragma unroll
             for(int u = 0; u < U; u++) {
-                const unsigned j = u * 32 + lane;
+                const unsigned j = u * TL + lane;
                 if(j < p.M) O[p.N + j] = g[u];
             }
             off = p.N + p.M;
@@ -257,7 +278,7 @@ __device__ void process_sample(const RbmDev<T>& p, const cplx<T>* __restrict__ W
             cplx<T>* orow = O + off + (size_t)c * p.M;
 #pragma unroll
             for(int u = 0; u < U; u++) {
-                const unsigned j = u * 32 + lane;
+                const unsigned j = u * TL + lane;
                 if(j < p.M) orow[j] = spin_bit(s, cr[j]) ? g[u] : -g[u];
             }
         }
@@ -279,7 +300,7 @@ __device__ __forceinline__ const cplx<T>* stage_Wd(const RbmDev<T>& p, int w_sme
 
 // One chain: thermalisation (when drawing fresh configurations), then per sample
 // the local sweeps, the learned independence moves, and the sample bookkeeping.
-template<typename T, int NW, int U>
+template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const OpDev& op, int with_op,
                          const McArgs& a, const SampleOut& out, unsigned chain, int lane, bool use_made,
                          const MadeSm& ms, float* mh) {
@@ -323,9 +344,10 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
     }
 
     Lane<T, U> L;
-    recompute<T, NW, U>(p, Wd, s, L, lane);
+    recompute<T, NW, U, TL>(p, Wd, s, L, lane);
     unsigned long long n_acc = 0, n_rej = 0, m_acc = 0, m_rej = 0;
-    // Philox words for the 32 counters [rr_base, rr_base + 32), one per lane
+    const unsigned mask = team_mask<TL>();
+    // Philox words for the TL counters [rr_base, rr_base + TL), one per team lane
     uint64_t rr_base = 0;
     bool rr_valid = false;
     u32x4 rr = {0, 0, 0, 0};
@@ -344,17 +366,17 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
             if(sizeof(T) == 4) uf = (float)u;
             tape_pos++;
         } else {
-            if(!rr_valid || t - rr_base >= 32u) {
+            if(!rr_valid || t - rr_base >= (unsigned)TL) {
                 rr_valid = true;
                 rr_base = t;
                 const uint64_t tl = t + lane;
                 rr = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tl, (uint32_t)(tl >> 32), chain, 0u});
             }
             const unsigned k = (unsigned)(t - rr_base);
-            const uint32_t r0 = __shfl_sync(0xffffffffu, rr.x, k);
-            const uint32_t r1 = __shfl_sync(0xffffffffu, rr.y, k);
-            const uint32_t r2 = __shfl_sync(0xffffffffu, rr.z, k);
-            const uint32_t r3 = __shfl_sync(0xffffffffu, rr.w, k);
+            const uint32_t r0 = __shfl_sync(mask, rr.x, k, TL);
+            const uint32_t r1 = __shfl_sync(mask, rr.y, k, TL);
+            const uint32_t r2 = __shfl_sync(mask, rr.z, k, TL);
+            const uint32_t r3 = __shfl_sync(mask, rr.w, k, TL);
             t++;
             i = mulhi32(r0, N);
             if(a.move_kind == 1) {
@@ -376,7 +398,7 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
             sites[1] = (uint16_t)j;
             ns = 2;
         }
-        const T d = delta_re<T, NW, U>(p, Wd, s, L, lane, sites, ns, dth, fnew);
+        const T d = delta_re<T, NW, U, TL>(p, Wd, s, L, lane, sites, ns, dth, fnew);
         const T ratio = fexp(T(2) * d);
         // MonteCarlo.hpp:158-160: accept if ratio > 1 or u <= ratio; u < 1 makes
         // the first clause redundant.
@@ -399,22 +421,27 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
     auto propose_learned = [&]() {
         const uint64_t tq = t++;
         Conf<NW> s2;
-        const float lq2 = made_sample<NW, 8>(ms, a.k0, a.k1, (uint32_t)tq, (uint32_t)(tq >> 32), chain, s2, lane);
+        const float lq2 = made_sample<NW, 256 / TL, TL>(ms, a.k0, a.k1, (uint32_t)tq, (uint32_t)(tq >> 32), chain, s2,
+                                                        lane);
         if(lq_stale) {
-            lq_cur = made_logq(ms, s, mh, lane);
+            lq_cur = made_logq<NW, TL>(ms, s, mh, lane);
             lq_stale = false;
         }
         Lane<T, U> L2;
-        recompute<T, NW, U>(p, Wd, s2, L2, lane);
-        T d = T(0);
+        recompute<T, NW, U, TL>(p, Wd, s2, L2, lane);
+        T dp[kVirt<TL>];
 #pragma unroll
-        for(int q = 0; q < U; q++) d += L2.fr[q] - L.fr[q];
+        for(int k = 0; k < kVirt<TL>; k++) dp[k] = T(0);
+#pragma unroll
+        for(int q = 0; q < U; q++) dp[q % kVirt<TL>] += L2.fr[q] - L.fr[q];
         if(p.a_in_log_psi)
-            for(unsigned i = lane; i < p.N; i += 32) {
-                const int b1 = spin_bit(s2, i), b0 = spin_bit(s, i);
-                if(b1 != b0) d += (b1 ? T(2) : T(-2)) * p.a[i].re;
-            }
-        d = warp_sum(d);
+#pragma unroll
+            for(int k = 0; k < kVirt<TL>; k++)
+                for(unsigned i = lane + k * TL; i < p.N; i += 32) {
+                    const int b1 = spin_bit(s2, i), b0 = spin_bit(s, i);
+                    if(b1 != b0) dp[k] += (b1 ? T(2) : T(-2)) * p.a[i].re;
+                }
+        const T d = team_total<TL>(dp);
         const u32x4 r = philox4x32_10(a.k0, a.k1, u32x4{(uint32_t)tq, (uint32_t)(tq >> 32), chain, 0u});
         const float lr = 2.f * (float)d + lq_cur - lq2;
         const float uf = __uint2float_rz(r.w >> 8) * 0x1.0p-24f;
@@ -434,9 +461,9 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
         for(unsigned k = 0; k < a.num_sweeps * N; k++) propose();
         if(use_made)
             for(unsigned k = 0; k < a.indep_per_sample; k++) propose_learned();
-        recompute<T, NW, U>(p, Wd, s, L, lane);  // removes accumulated rounding of the increments
-        process_sample<T, NW, U>(p, Wd, with_op ? &op : nullptr, s, L, lane,
-                                 (size_t)st * a.n_chains + chain, out, false);
+        recompute<T, NW, U, TL>(p, Wd, s, L, lane);  // removes accumulated rounding of the increments
+        process_sample<T, NW, U, TL>(p, Wd, with_op ? &op : nullptr, s, L, lane,
+                                     (size_t)st * a.n_chains + chain, out, false);
     }
     if(lane == 0) {
         if(!tape) {
@@ -454,15 +481,16 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
 
 
 // ---------------------------------------------------------------------------------
-// Metropolis sampler: one warp per chain.
+// Metropolis sampler: one team of TL lanes per chain (32 / TL chains per warp).
 // complex64 chains with up to 128 hidden units: registers capped for three 8-warp CTAs per
-// SM (the sampler is latency-bound; the cap costs a few spilled words to L1)
-template<typename T, int NW, int U>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 && U <= 4) ? 3 : 1)
+// SM with whole-warp teams, two with half-warp teams (twice the units per lane; the
+// sampler is latency-bound, the cap costs a few spilled words to L1)
+template<typename T, int NW, int U, int TL>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && U * TL <= 128) ? (TL == 32 ? 3 : 2) : 1)
 rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w_smem) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const cplx<T>* Wd = stage_Wd<T>(p, w_smem, reinterpret_cast<cplx<T>*>(smem_raw));
-    // learned-proposal weights after Wd, then one H-float scratch per warp; the drop rule
+    // learned-proposal weights after Wd, then one H-float scratch per team; the drop rule
     // switches the moves off through a device flag (graph replays see it change)
     const bool use_made = a.made.N != 0 && (a.made_on == nullptr || *a.made_on != 0);
     MadeSm ms{};
@@ -475,15 +503,15 @@ rbm_mc_kernel(RbmDev<T> p, OpDev op, int with_op, McArgs a, SampleOut out, int w
         } else {
             ms = made_global(a.made);
         }
-        mh = reinterpret_cast<float*>(mbase) + (threadIdx.x >> 5) * a.made.H;
+        mh = reinterpret_cast<float*>(mbase) + (threadIdx.x / TL) * a.made.H;  // one H-float scratch per team
         __syncthreads();
     }
-    const int lane = threadIdx.x & 31;
-    const unsigned chain = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & (TL - 1);
+    const unsigned chain = blockIdx.x * (blockDim.x / TL) + threadIdx.x / TL;
     if(chain >= a.n_chains) return;
     RbmDev<T> q = p;
-    q.Uact = U;  // the padded width is exactly 32 U here: the per-slot guards fold away
-    mc_chain<T, NW, U>(q, Wd, op, with_op, a, out, chain, lane, use_made, ms, mh);
+    q.Uact = U;  // the padded width is exactly TL U here: the per-slot guards fold away
+    mc_chain<T, NW, U, TL>(q, Wd, op, with_op, a, out, chain, lane, use_made, ms, mh);
 }
 
 // Drop rule of the learned proposal, on the device after each sampling pass: the flag

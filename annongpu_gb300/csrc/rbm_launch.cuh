@@ -161,22 +161,49 @@ void rbm_mc_T(ann_psi_impl& psi, const ann_op_impl* op, ann_ens_impl& ens, const
     OpDev ov{};
     if(op) ov = op->view();
     const size_t wb = wd_bytes<T>(psi);
-    // chains (warps) per CTA: the autotuned choice for this shape, else the default
+    // warps per CTA: the autotuned choice for this shape, else the default
     int wpb = tuning_get(key_mc_wpb(psi, ens), warps_per_block<T>(0));
     if(wpb < 1 || wpb > 8) wpb = warps_per_block<T>(0);
-    const size_t made_bytes =
-        learned ? (a.made_smem ? made_smem_bytes(ens.made->N, ens.made->H) : 0) + (size_t)wpb * ens.made->H * 4 : 0;
+    // lanes per chain: half-warp teams (two chains per warp, 2 U hidden units per lane)
+    // for complex64 chains up to 128 hidden units, when the tuning table chose them; the
+    // learned moves then draw their uniforms from 16 lanes (N <= 64)
+    const bool team_ok = sizeof(T) == 4 && psi.Mpad <= 128 && (!learned || psi.N <= 64);
+    const int team = team_ok && tuning_get(key_mc_team(psi, ens), 32) == 16 ? 16 : 32;
+    const unsigned chains_per_cta = (unsigned)wpb * (32u / team);
+    const size_t made_bytes = learned ? (a.made_smem ? made_smem_bytes(ens.made->N, ens.made->H) : 0) +
+                                            (size_t)chains_per_cta * ens.made->H * 4
+                                      : 0;
     // W staged in shared memory when it fits, unless the tuning table prefers reading it
     // through L1 (fewer bytes of shared memory per CTA, more CTAs per SM)
     const int w_smem = (wb + made_bytes <= kMaxSmemWd && tuning_get(key_mc_wsmem(psi, ens), 1)) ? 1 : 0;
     const size_t smem = (w_smem ? ((wb + 15) & ~(size_t)15) : 0) + made_bytes;
     if(smem > 220 * 1024) throw Error(ANN_ERR_INVALID, "learned proposal too large for shared memory");
-    const unsigned grid = (ens.n_chains + wpb - 1) / wpb;
-    ANN_DISPATCH_NW_U(psi.NW, psi.U, {
-        auto k = rbm_mc_kernel<T, NWc, Uc>;
-        set_smem(k, smem);
-        k<<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out, w_smem);
-    });
+    const unsigned grid = (ens.n_chains + chains_per_cta - 1) / chains_per_cta;
+    if(team == 16) {
+        if constexpr(sizeof(T) == 4) {
+            // U of the half-warp kernel = Mpad / 16 (2, 4 or 8)
+            auto go = [&](auto k) {
+                set_smem(k, smem);
+                k<<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out, w_smem);
+            };
+            const int u16 = (int)psi.Mpad / 16;
+            if(psi.NW == 1) {
+                if(u16 == 2) go(rbm_mc_kernel<T, 1, 2, 16>);
+                else if(u16 == 4) go(rbm_mc_kernel<T, 1, 4, 16>);
+                else go(rbm_mc_kernel<T, 1, 8, 16>);
+            } else {
+                if(u16 == 2) go(rbm_mc_kernel<T, 2, 2, 16>);
+                else if(u16 == 4) go(rbm_mc_kernel<T, 2, 4, 16>);
+                else go(rbm_mc_kernel<T, 2, 8, 16>);
+            }
+        }
+    } else {
+        ANN_DISPATCH_NW_U(psi.NW, psi.U, {
+            auto k = rbm_mc_kernel<T, NWc, Uc, 32>;
+            set_smem(k, smem);
+            k<<<grid, wpb * 32, smem, st>>>(p, ov, op ? 1 : 0, a, out, w_smem);
+        });
+    }
     check_launch("rbm_mc_kernel");
     if(learned) {
         made_drop_rule_kernel<<<1, 1, 0, st>>>(ens.acc_rej.as<unsigned long long>(), ens.made_min_acceptance,

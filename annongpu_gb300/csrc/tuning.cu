@@ -7,6 +7,8 @@
 // repeats) and keeping the fastest:
 //   rbm_mc.wpb      warps (chains) per CTA of the Metropolis sampler: 2, 4, 8
 //   rbm_mc.wsmem    sampler weights W staged in shared memory (1) or read through L1 (0)
+//   rbm_mc.team     lanes per chain of the complex64 sampler: 32 (one chain per warp) or
+//                   16 (two chains per warp, twice the hidden units per lane; Mpad <= 128)
 //   stats.slab      rows per FP32 slab of the <O> / F reductions: 128, 256, 512
 //   chol.update     trailing update of the FP32 Cholesky: 128 x 128 tcgen05 tiles
 //                   (split TF32) or 64 x 64 FP32 SIMT tiles
@@ -89,6 +91,11 @@ std::string key_mc_wpb(const ann_psi_impl& psi, const ann_ens_impl& ens) {
 std::string key_mc_wsmem(const ann_psi_impl& psi, const ann_ens_impl& ens) {
     std::string k = key_mc_wpb(psi, ens);
     return "rbm_mc.wsmem" + k.substr(k.find('/'));
+}
+
+std::string key_mc_team(const ann_psi_impl& psi, const ann_ens_impl& ens) {
+    std::string k = key_mc_wpb(psi, ens);
+    return "rbm_mc.team" + k.substr(k.find('/'));
 }
 
 std::string key_slab(size_t rows, unsigned Np) {
@@ -198,6 +205,20 @@ int ann_autotune(ann_tdvp* t, ann_op* op, ann_psi* psi, ann_ens* ens, double dia
         try {
             // sampler launch shape (RBM family, Monte Carlo)
             if(psi->kind == 0 && e2->kind == 1) {
+                // lanes per chain first (at the default CTA size), when the shape allows half warps
+                if(psi->precision == 0 && psi->Mpad <= 128) {
+                    const std::string kt = key_mc_team(*psi, *e2);
+                    double best_t_ms = 1e300;
+                    int best_t = 32;
+                    for(int tl : {32, 16}) {
+                        tuning_set(kt, tl);
+                        const SampleTargets tg = tdvp_prepare(*t, *psi, *e2);
+                        const double ms = time_ms([&] { run_ensemble(*psi, op, *e2, tg, st); }, 3, st);
+                        record(6, tl, ms);
+                        if(ms < best_t_ms) { best_t_ms = ms; best_t = tl; }
+                    }
+                    tuning_set(kt, best_t);
+                }
                 const std::string key = key_mc_wpb(*psi, *e2);
                 double best = 1e300;
                 int best_w = 8;

@@ -738,6 +738,30 @@ def hsd_timing(ann, f, st):
             "note": "host-synchronous calls (the gradient returns to the host), 64-sweep sampling included"}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the precision step's kernels
+# from one capture of this workload at full size with those one-pass metrics:
+#   python bench.py --form precision --steps 1 --warmup 1 --train-steps 3 --no-cpu --no-legs \
+#       --save-tuning tuning.json
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
+#       --clock-control none --profile-from-start off --csv --log-file traffic.csv \
+#       python bench.py --form precision --steps 1 --warmup 1 --train-steps 3 --no-cpu --no-legs \
+#       --tuning tuning.json --profile-window
+# sampler: one launch (half-warp chains, O rows 1.10 GB written); S: one herk_tc launch
+# (complex64 S); factorisation: its 129 tcgen05 update launches (10.36 GB) and the panel
+# kernels potrf32 / trsm32 / herk32 (0.58 GB), per factorisation.
+TRAFFIC_BYTES = {"sampler": 1.0579e9, "herk_tc": 6.4534e9, "factorisation": 1.0937e10}
+TRAFFIC_SRC = "DRAM bytes per launch from one full-size ncu capture of this workload (one-pass metrics)"
+
+
+def sampler_kernel_name(ann):
+    """The sampler instance the tuning table selects for the 8x8 shape (whole- or
+    half-warp chains)."""
+    team = next((v for k, v in ann.tuning_table().items()
+                 if f"/rbm_mc.team/N{N_SITES}.M{M_HIDDEN}." in k and k.endswith("made1")), 32)
+    return ("rbm_mc_kernel<float,1,8,16> (half-warp chains; sampling + E_loc + O rows)" if team == 16 else
+            "rbm_mc_kernel<float,1,4,32> (sampling + E_loc + O rows)")
+
+
 def roofline_objects(f, ms, phase, pk, pk_kind):
     """The dominant kernel of the precision step (the sampler at 64 sweeps) and the other
     two large kernel groups, each with its algorithmic work per launch."""
@@ -745,10 +769,12 @@ def roofline_objects(f, ms, phase, pk, pk_kind):
     props = Ns * (SWEEPS * N_SITES)
     simt_peak = fp32_simt_peak_tflops()
     flops_sampler = 34.0 * M_HIDDEN * props  # 34 M flops per proposal (the 64-sweep part alone)
-    sampler = {"bound": "fp32_simt", "kernel": "rbm_mc_kernel<float,1,4> (sampling + E_loc + O rows)",
+    sampler = {"bound": "fp32_simt", "kernel": sampler_kernel_name(f.ann),
                "achieved": flops_sampler / (phase[0] * 1e-3) / 1e12, "peak": simt_peak, "unit": "TFLOP/s",
                "frac": flops_sampler / (phase[0] * 1e-3) / 1e12 / simt_peak, "ms": phase[0],
-               "traffic": None,
+               "traffic": TRAFFIC_BYTES["sampler"],
+               "dram_gbs": TRAFFIC_BYTES["sampler"] / (phase[0] * 1e-3) / 1e9,
+               "traffic_source": TRAFFIC_SRC,
                "work": f"34*M flops per single-flip proposal x {props} proposals per step (16384 chains x 64 "
                        "sweeps x 64 sites); E_loc and the O-row writes (1.1 GB) are not credited",
                "peak_kind": "nominal FP32 FMA rate (SMs x 128 lanes x 2 flops x max SM clock): "
@@ -756,7 +782,8 @@ def roofline_objects(f, ms, phase, pk, pk_kind):
     flops_S = 4.0 * Np * (Np + 1) * Ns
     herk = {"bound": "tensor", "kernel": "herk_tc_kernel (S = O_c^H O_c, tcgen05 BF16)",
             "achieved": flops_S / (phase[2] * 1e-3) / 1e12, "peak": pk.get("bf16_tflops", 1900.0),
-            "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst", "ms": phase[2], "traffic": None,
+            "unit": "TFLOP/s", "peak_kind": pk_kind + " bf16 burst", "ms": phase[2],
+            "traffic": TRAFFIC_BYTES["herk_tc"], "traffic_source": TRAFFIC_SRC,
             "work": "4*Np*(Np+1)*Ns real flops per step (over the S phase: operand prep + kernel)"}
     herk["frac"] = herk["achieved"] / herk["peak"]
     out = {"roofline": sampler, "roofline_herk": herk}
@@ -767,7 +794,9 @@ def roofline_objects(f, ms, phase, pk, pk_kind):
             "bound": "tensor", "kernel": "FP32 Cholesky factorisation (tcgen05 split-TF32 trailing updates + "
                                         "potrf32/trsm32 panel path)",
             "achieved": chol, "peak": peak, "unit": "TFLOP/s", "frac": chol / peak, "ms": f.t_factor_ms,
-            "traffic": None, "update_form": f.tdvp.solver_info.get("update_form"),
+            "traffic": TRAFFIC_BYTES["factorisation"],
+            "traffic_source": "DRAM bytes per factorisation (all its launches) from one full-size ncu capture",
+            "update_form": f.tdvp.solver_info.get("update_form"),
             "peak_kind": pk_kind + " bf16 burst (no credit for the three split products)",
             "work": "(4/3)*Np^3 real flops per factorisation (CUDA events around it)"}
     return out

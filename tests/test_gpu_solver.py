@@ -139,3 +139,52 @@ def test_mixed_solver_graph_replay_equals_eager():
     st.synchronize()
     assert not t1.solver_info["fell_back"] and t2.solver_info["residual_last"] <= 1e-12
     np.testing.assert_array_equal(p1.params, p2.params)
+
+
+def test_complex64_S_store_keeps_values_and_solutions():
+    """With the tensor-core S and the mixed solver, S is kept in complex64 (its values are
+    FP32 sums) and the refinement's residual is formed in double-float arithmetic on the
+    FP32 pipe. The same chains evaluated for the FP64 solver (S kept in complex128) give a
+    bit-identical S and F; the mixed solve from the complex64 S agrees with the mixed
+    solve from the complex128 S (FP64 residual) and with the FP64 Cholesky solve to the
+    refinement's bound, and its residual checked on the host in FP64 is <= 2e-12; the FP64
+    solve of the widened complex64 S equals the one of the complex128 S bit for bit, and a
+    stalled refinement falls back to exactly that solve."""
+    N, M = 32, 64  # Np = 2144
+    rng = np.random.default_rng(21)
+    a, b, W = cplx(rng, N, 0.01), cplx(rng, M, 0.01), cplx(rng, (N, M), 0.01)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(4096, 2, 8, 4096, True, seed=17, persistent=True)
+    t32 = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    t32.eval(op, psi, mc)  # thermalises the persistent chains
+    conf0, ctr0 = mc.get_chains()
+    mc.set_chains(conf0, ctr0)
+    t32.eval(op, psi, mc)
+    t64 = ann.TDVP(psi.num_params, s_mode="bf16", solver="fp64")
+    mc.set_chains(conf0, ctr0)
+    t64.eval(op, psi, mc)
+    S, F = t64.S_matrix, t64.F_vector
+    assert np.array_equal(t32.S_matrix, S) and np.array_equal(t32.F_vector, F)
+    shift = 1e-3
+    d32 = t32.solve(shift)
+    info = t32.solver_info
+    assert not info["fell_back"] and info["residual_last"] <= 1e-12, info
+    r = F - (S @ d32 + shift * d32)
+    assert np.linalg.norm(r) <= 2e-12 * np.linalg.norm(F)
+    t64.set_solver("mixed", 6, 1e-12)
+    d64 = t64.solve(shift)
+    scale = np.abs(d64).max()
+    np.testing.assert_allclose(d32, d64, rtol=1e-9, atol=1e-10 * scale)
+    t64.set_solver("fp64")
+    dref = t64.solve(shift)
+    np.testing.assert_allclose(d32, dref, rtol=1e-8, atol=1e-9 * scale)
+    t32.set_solver("fp64")
+    np.testing.assert_array_equal(t32.solve(shift), dref)
+    # a fresh complex64 S (the complex128 copy stale) and a refinement that cannot converge
+    t32.set_solver("mixed", 1, 1e-15)
+    mc.set_chains(conf0, ctr0)
+    t32.eval(op, psi, mc)
+    d_fb = t32.solve(shift)
+    assert t32.solver_info["fell_back"]
+    np.testing.assert_array_equal(d_fb, dref)
