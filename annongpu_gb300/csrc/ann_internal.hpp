@@ -150,10 +150,15 @@ struct ann_made_impl {
     DevBuf W1, b1, W2, b2;            // FP32 master weights (W1: H x N, W2: N x H)
     DevBuf W1t, W2t;                  // BF16 transposed copies read by the kernels
     DevBuf W2b;                       // BF16 copy of W2 as stored (N x H): read through L1 by the samplers
+    // BF16 operands of the tensor-core training GEMMs (rows zero-padded to 64-value multiples):
+    // W1 as stored (H x N64), W2 as stored (N x H64), W2^T (H x N64)
+    DevBuf W1g, W2g, W2Tg;
     DevBuf deg;                       // hidden-unit degrees (u16)
     DevBuf mW1, vW1, mb1, vb1, mW2, vW2, mb2, vb2;  // Adam moments
     DevBuf gW1, gb1, gW2, gb2;        // gradients
     DevBuf X, pre, hbuf, l, dl, dh, row_loss;       // training scratch
+    // BF16 hi / lo splits of the training step's activations and gradients (GEMM operands)
+    DevBuf Xg, XTg, hs, hTs, dls, dlTs, dhTs;
     DevBuf kpart;                                   // split-K partial tiles of the weight gradients
 };
 
@@ -264,6 +269,30 @@ SampleTargets tdvp_prepare(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& en
 void tdvp_post(ann_tdvp_impl& t, ann_psi_impl& psi, ann_ens_impl& ens, bool want_S, cudaStream_t st);
 
 // FP64 Cholesky SR solve (cholesky.cu)
+// BF16 tensor-core GEMM of the MADE training step (made_tc.cu):
+//   C (M x N, FP32) = sum over segments s of A[:, aoff_s : aoff_s + K] . B[:, boff_s : boff_s + K]^T
+// A (a_rows x a_cols) and B (b_rows x b_cols) BF16 row-major; K and the offsets multiples of 64;
+// with splits > 1 the K range is split over CTAs and the partial tiles summed in order.
+struct MadeGemm {
+    const void* A;
+    unsigned a_rows, a_cols;
+    const void* B;
+    unsigned b_rows, b_cols;
+    unsigned M, N, K, nseg;
+    int aoff[3], boff[3];
+    float* C;
+    size_t ldc;
+    const float* bias;     // per output column, or null
+    const float* aux;      // C = 0 where aux[m * ldc + n] <= 0, or null
+    unsigned splits;
+};
+void made_gemm(const MadeGemm& g, DevBuf& scratch, cudaStream_t st);
+// BF16 hi (and lo) of an FP32 R x C matrix into a zero-padded rows x cols block: row-major
+// (dst[r][c], lo at column lo_off + c) or transposed (dst[c][r], lo at lo_off + r)
+void made_split_rows(const float* src, unsigned R, unsigned C, size_t lds, void* dst, size_t ldd, unsigned rows,
+                     unsigned cols, unsigned lo_off, bool with_lo, cudaStream_t st);
+void made_split_cols(const float* src, unsigned R, unsigned C, size_t lds, void* dst, size_t ldd, unsigned rows,
+                     unsigned cols, unsigned lo_off, bool with_lo, cudaStream_t st);
 void sr_solve(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
 // the last S in complex128 (widened from S32 on first use after an evaluation that kept it there)
 const cplx<double>* S64(ann_tdvp_impl& td, cudaStream_t st);

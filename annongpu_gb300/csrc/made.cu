@@ -8,8 +8,12 @@
 //   dW1 = dh^T X, db1 = sum dh
 //   Adam (Kingma & Ba 2015) on the FP32 master weights, masked gradients, then the
 //   BF16 transposed copies the samplers read are refreshed.
-// The GEMMs are small (B <= 4096, N <= 128, H <= 512) and run on a tiled SIMT kernel.
+// The GEMMs run on the tensor cores (made_tc.cu: tcgen05 BF16 MMAs with FP32 accumulation
+// in tensor memory); FP32 activations and gradients enter as BF16 hi + lo pairs, the
+// weights as the BF16 copies the samplers read.
+#include <algorithm>
 #include <cmath>
+#include <initializer_list>
 #include <random>
 
 #include "ann_internal.hpp"
@@ -19,80 +23,8 @@ namespace ann {
 
 namespace {
 
-// C[m][n] = alpha * sum_k A(m,k) B(k,n) (+ bias[n]) (* [aux[m][n] > 0]);
-// A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn]
-template<typename TB>
-__global__ void __launch_bounds__(256)
-sgemm_kernel(unsigned Mm, unsigned Nn, unsigned K, const float* __restrict__ A, size_t sam, size_t sak,
-             const TB* __restrict__ B, size_t sbk, size_t sbn, float* __restrict__ C, size_t ldc, float alpha,
-             const float* __restrict__ bias, const float* __restrict__ aux, unsigned kchunk = 0) {
-    __shared__ float As[16][64];
-    __shared__ float Bs[16][64];
-    const unsigned m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-    if(kchunk) {
-        // split K: this CTA sums k in [z kchunk, (z + 1) kchunk) into partial tile z
-        const unsigned k0 = blockIdx.z * kchunk;
-        K = min(K - k0, kchunk);
-        A += (size_t)k0 * sak;
-        B += (size_t)k0 * sbk;
-        C += (size_t)blockIdx.z * Mm * ldc;
-    }
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    float acc[4][4] = {};
-    for(unsigned k0 = 0; k0 < K; k0 += 16) {
-        __syncthreads();
-        for(int q = threadIdx.x; q < 16 * 64; q += 256) {
-            const int kk = q / 64, r = q % 64;
-            const unsigned k = k0 + kk;
-            As[kk][r] = (m0 + r < Mm && k < K) ? A[(size_t)(m0 + r) * sam + (size_t)k * sak] : 0.f;
-            float bv = 0.f;
-            if(n0 + r < Nn && k < K) {
-                if constexpr(sizeof(TB) == 2) bv = __bfloat162float(B[(size_t)k * sbk + (size_t)(n0 + r) * sbn]);
-                else bv = B[(size_t)k * sbk + (size_t)(n0 + r) * sbn];
-            }
-            Bs[kk][r] = bv;
-        }
-        __syncthreads();
-#pragma unroll
-        for(int kk = 0; kk < 16; kk++) {
-            float a[4], b[4];
-#pragma unroll
-            for(int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
-#pragma unroll
-            for(int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-            for(int i = 0; i < 4; i++)
-#pragma unroll
-                for(int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-    }
-#pragma unroll
-    for(int i = 0; i < 4; i++) {
-        const unsigned m = m0 + ty + 16 * i;
-        if(m >= Mm) continue;
-#pragma unroll
-        for(int j = 0; j < 4; j++) {
-            const unsigned n = n0 + tx + 16 * j;
-            if(n >= Nn) continue;
-            float v = alpha * acc[i][j];
-            if(bias) v += bias[n];
-            if(aux && !(aux[(size_t)m * ldc + n] > 0.f)) v = 0.f;
-            C[(size_t)m * ldc + n] = v;
-        }
-    }
-}
-
-template<typename TB>
-void sgemm(unsigned Mm, unsigned Nn, unsigned K, const float* A, size_t sam, size_t sak, const TB* B, size_t sbk,
-           size_t sbn, float* C, size_t ldc, float alpha, const float* bias, const float* aux, cudaStream_t st) {
-    dim3 grid((Nn + 63) / 64, (Mm + 63) / 64);
-    sgemm_kernel<TB><<<grid, 256, 0, st>>>(Mm, Nn, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, bias, aux);
-    check_launch("sgemm_kernel");
-}
-
-// C = sum over K split into chunks of kSplitK: grid.z chunks write partial tiles to
-// P[z] (Mm x Nn), split_reduce_kernel adds them in chunk order (deterministic). For
-// the weight gradients, whose outputs are small (N x H) and whose K is the batch.
+// column sums over slabs of kSplitK rows; split_reduce_kernel adds the slabs in order
+// (deterministic)
 constexpr unsigned kSplitK = 128;
 
 __global__ void split_reduce_kernel(const float* __restrict__ P, unsigned splits, size_t mn, float* __restrict__ C) {
@@ -103,20 +35,30 @@ __global__ void split_reduce_kernel(const float* __restrict__ P, unsigned splits
     C[i] = acc;
 }
 
-template<typename TB>
-void sgemm_splitk(unsigned Mm, unsigned Nn, unsigned K, const float* A, size_t sam, size_t sak, const TB* B,
-                  size_t sbk, size_t sbn, float* C, DevBuf& scratch, cudaStream_t st) {
-    const unsigned splits = (K + kSplitK - 1) / kSplitK;
-    const size_t mn = (size_t)Mm * Nn;
-    scratch.ensure(splits * mn * sizeof(float));
-    float* P = scratch.as<float>();
-    dim3 grid((Nn + 63) / 64, (Mm + 63) / 64, splits);
-    sgemm_kernel<TB><<<grid, 256, 0, st>>>(Mm, Nn, K, A, sam, sak, B, sbk, sbn, P, Nn, 1.f, nullptr, nullptr,
-                                           kSplitK);
-    check_launch("sgemm_kernel");
-    split_reduce_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(P, splits, mn, C);
-    check_launch("split_reduce_kernel");
+// GEMM operand extents: K (columns) padded to 64 values; rows to a whole number of tiles
+// (128-row A tiles, B tiles of 64, 128 or 256 rows), the padding zero
+__host__ __device__ inline unsigned pad64(unsigned x) { return (x + 63u) & ~63u; }
+__host__ __device__ inline unsigned prow(unsigned x) { return x <= 128u ? 128u : (x + 255u) & ~255u; }
+
+// BF16 operands of the training GEMMs: W1g[k][i] = W1[k][i] (prow(H) x N64),
+// W2g[j][k] = W2[j][k] (prow(N) x H64), W2Tg[k][j] = W2[j][k] (prow(H) x N64)
+__global__ void refresh_gemm_kernel(const float* __restrict__ W1, const float* __restrict__ W2, unsigned N, unsigned H,
+                                    __nv_bfloat16* __restrict__ W1g, __nv_bfloat16* __restrict__ W2g,
+                                    __nv_bfloat16* __restrict__ W2Tg) {
+    const unsigned N64 = pad64(N), H64 = pad64(H);
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if(idx < (size_t)prow(H) * N64) {
+        const unsigned k = (unsigned)(idx / N64), j = (unsigned)(idx % N64);
+        const bool in = k < H && j < N;
+        W1g[idx] = __float2bfloat16_rn(in ? W1[(size_t)k * N + j] : 0.f);
+        W2Tg[idx] = __float2bfloat16_rn(in ? W2[(size_t)j * H + k] : 0.f);
+    }
+    if(idx < (size_t)prow(N) * H64) {
+        const unsigned j = (unsigned)(idx / H64), k = (unsigned)(idx % H64);
+        W2g[idx] = __float2bfloat16_rn(j < N && k < H ? W2[(size_t)j * H + k] : 0.f);
+    }
 }
+
 
 __global__ void bits_kernel(const uint64_t* __restrict__ confs, unsigned B, unsigned N, float* __restrict__ X) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -266,6 +208,15 @@ void made_refresh(ann_made_impl& m, cudaStream_t st) {
                                                                         m.W2t.as<__nv_bfloat16>(),
                                                                         m.W2b.as<__nv_bfloat16>());
     check_launch("refresh_bf16_kernel");
+    const size_t ng = std::max((size_t)prow(m.H) * pad64(m.N), (size_t)prow(m.N) * pad64(m.H));
+    m.W1g.ensure((size_t)prow(m.H) * pad64(m.N) * 2);
+    m.W2Tg.ensure((size_t)prow(m.H) * pad64(m.N) * 2);
+    m.W2g.ensure((size_t)prow(m.N) * pad64(m.H) * 2);
+    refresh_gemm_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(m.W1.as<float>(), m.W2.as<float>(), m.N, m.H,
+                                                                        m.W1g.as<__nv_bfloat16>(),
+                                                                        m.W2g.as<__nv_bfloat16>(),
+                                                                        m.W2Tg.as<__nv_bfloat16>());
+    check_launch("refresh_gemm_kernel");
 }
 
 void made_init(ann_made_impl& m, uint64_t seed) {
@@ -318,6 +269,8 @@ void colsum(const float* X, unsigned M, unsigned Nn, float* out, DevBuf& scratch
 
 void made_gradient(ann_made_impl& m, const uint64_t* confs, unsigned B, double* loss_dev, cudaStream_t st) {
     const unsigned N = m.N, H = m.H;
+    const unsigned N64 = pad64(N), H64 = pad64(H), B64 = pad64(B);
+    const unsigned Br = prow(B), Nr = prow(N), Hr = prow(H);
     m.X.ensure((size_t)B * N * 4);
     m.pre.ensure((size_t)B * H * 4);
     m.hbuf.ensure((size_t)B * H * 4);
@@ -325,33 +278,74 @@ void made_gradient(ann_made_impl& m, const uint64_t* confs, unsigned B, double* 
     m.dl.ensure((size_t)B * N * 4);
     m.dh.ensure((size_t)B * H * 4);
     m.row_loss.ensure((size_t)B * 4);
+    m.Xg.ensure((size_t)Br * N64 * 2);
+    m.XTg.ensure((size_t)Nr * B64 * 2);
+    m.hs.ensure((size_t)Br * 2 * H64 * 2);
+    m.hTs.ensure((size_t)Hr * 2 * B64 * 2);
+    m.dls.ensure((size_t)Br * 2 * N64 * 2);
+    m.dlTs.ensure((size_t)Nr * 2 * B64 * 2);
+    m.dhTs.ensure((size_t)Hr * 2 * B64 * 2);
     float* X = m.X.as<float>();
     float* pre = m.pre.as<float>();
     float* h = m.hbuf.as<float>();
     float* l = m.l.as<float>();
     float* dl = m.dl.as<float>();
     float* dh = m.dh.as<float>();
-    const auto* W1t = m.W1t.as<__nv_bfloat16>();
-    const auto* W2t = m.W2t.as<__nv_bfloat16>();
+    // weight gradients: K = the batch, split over CTAs in chunks of >= 4 K steps
+    const unsigned splits = std::max(1u, std::min(16u, B64 / 256u));
+    auto gemm = [&](const void* A, unsigned ar, unsigned ac, const void* Bm, unsigned br, unsigned bc, unsigned M,
+                    unsigned Nn, unsigned K, std::initializer_list<int> ao, std::initializer_list<int> bo, float* C,
+                    size_t ldc, const float* bias, const float* aux, unsigned sp) {
+        MadeGemm g{};
+        g.A = A;
+        g.a_rows = ar;
+        g.a_cols = ac;
+        g.B = Bm;
+        g.b_rows = br;
+        g.b_cols = bc;
+        g.M = M;
+        g.N = Nn;
+        g.K = K;
+        g.nseg = (unsigned)ao.size();
+        int s = 0;
+        for(int v : ao) g.aoff[s++] = v;
+        s = 0;
+        for(int v : bo) g.boff[s++] = v;
+        g.C = C;
+        g.ldc = ldc;
+        g.bias = bias;
+        g.aux = aux;
+        g.splits = sp;
+        made_gemm(g, m.kpart, st);
+    };
     bits_kernel<<<(unsigned)(((size_t)B * N + 255) / 256), 256, 0, st>>>(confs, B, N, X);
     check_launch("bits_kernel");
-    // pre[b][k] = sum_i X[b][i] W1t[i][k] + b1[k]
-    sgemm<__nv_bfloat16>(B, H, N, X, N, 1, W1t, H, 1, pre, H, 1.f, m.b1.as<float>(), nullptr, st);
+    made_split_rows(X, B, N, N, m.Xg.p, N64, Br, N64, 0, false, st);   // X (exact in BF16)
+    made_split_cols(X, B, N, N, m.XTg.p, B64, Nr, B64, 0, false, st);  // X^T
+    // pre[b][k] = sum_i X[b][i] W1[k][i] + b1[k]
+    gemm(m.Xg.p, Br, N64, m.W1g.p, Hr, N64, B, H, N64, {0}, {0}, pre, H, m.b1.as<float>(), nullptr, 1);
     relu_kernel<<<(unsigned)(((size_t)B * H + 255) / 256), 256, 0, st>>>(pre, h, (size_t)B * H);
     check_launch("relu_kernel");
-    // l[b][j] = sum_k h[b][k] W2t[k][j] + b2[j]
-    sgemm<__nv_bfloat16>(B, N, H, h, H, 1, W2t, N, 1, l, N, 1.f, m.b2.as<float>(), nullptr, st);
+    made_split_rows(h, B, H, H, m.hs.p, 2 * H64, Br, H64, H64, true, st);   // [h | h_lo]
+    made_split_cols(h, B, H, H, m.hTs.p, 2 * B64, Hr, B64, B64, true, st);  // [h^T | lo]
+    // l[b][j] = sum_k h[b][k] W2[j][k] + b2[j]   (hi.W2 + lo.W2)
+    gemm(m.hs.p, Br, 2 * H64, m.W2g.p, Nr, H64, B, N, H64, {0, (int)H64}, {0, 0}, l, N, m.b2.as<float>(), nullptr, 1);
     dlogits_kernel<<<(B + 7) / 8, 256, 0, st>>>(l, X, B, N, dl, m.row_loss.as<float>());
     check_launch("dlogits_kernel");
     loss_sum_kernel<<<1, 256, 0, st>>>(m.row_loss.as<float>(), B, loss_dev);
     check_launch("loss_sum_kernel");
-    // dW2[j][k] = sum_b dl[b][j] h[b][k]
-    sgemm_splitk<float>(N, H, B, dl, 1, N, h, H, 1, m.gW2.as<float>(), m.kpart, st);
+    made_split_rows(dl, B, N, N, m.dls.p, 2 * N64, Br, N64, N64, true, st);   // [dl | lo]
+    made_split_cols(dl, B, N, N, m.dlTs.p, 2 * B64, Nr, B64, B64, true, st);  // [dl^T | lo]
+    // dW2[j][k] = sum_b dl[b][j] h[b][k]   (hi.hi + lo.hi + hi.lo)
+    gemm(m.dlTs.p, Nr, 2 * B64, m.hTs.p, Hr, 2 * B64, N, H, B64, {0, (int)B64, 0}, {0, 0, (int)B64},
+         m.gW2.as<float>(), H, nullptr, nullptr, splits);
     colsum(dl, B, N, m.gb2.as<float>(), m.kpart, st);
-    // dh[b][k] = sum_j dl[b][j] W2t[k][j] * [pre > 0]   (the weights the forward pass used)
-    sgemm<__nv_bfloat16>(B, H, N, dl, N, 1, W2t, 1, N, dh, H, 1.f, nullptr, pre, st);
-    // dW1[k][i] = sum_b dh[b][k] X[b][i]
-    sgemm_splitk<float>(H, N, B, dh, 1, H, X, N, 1, m.gW1.as<float>(), m.kpart, st);
+    // dh[b][k] = sum_j dl[b][j] W2[j][k] * [pre > 0]   (the weights the forward pass used)
+    gemm(m.dls.p, Br, 2 * N64, m.W2Tg.p, Hr, N64, B, H, N64, {0, (int)N64}, {0, 0}, dh, H, nullptr, pre, 1);
+    made_split_cols(dh, B, H, H, m.dhTs.p, 2 * B64, Hr, B64, B64, true, st);  // [dh^T | lo]
+    // dW1[k][i] = sum_b dh[b][k] X[b][i]   (hi.X + lo.X)
+    gemm(m.dhTs.p, Hr, 2 * B64, m.XTg.p, Nr, B64, H, N, B64, {0, (int)B64}, {0, 0}, m.gW1.as<float>(), N, nullptr,
+         nullptr, splits);
     colsum(dh, B, H, m.gb1.as<float>(), m.kpart, st);
 }
 

@@ -1071,6 +1071,24 @@ def run_profile_case_sampler():
     print("profile case (sampler): E/N =", td.E_local / N_SITES)
 
 
+def run_profile_case_made():
+    """Small case for ncu captures of the proposal's training GEMMs: N = 64, H = 256 (the
+    alpha = 4 workload's proposal), batches of 4096 configurations, 8 Adam steps (each one
+    forward and backward pass: five tcgen05 GEMMs)."""
+    import torch
+    import annongpu_gb300 as ann
+    rng = np.random.default_rng(SEED)
+    m = ann.MADE(64, 256, seed=SEED)
+    confs = rng.integers(0, 2 ** 63, size=(8192, 2), dtype=np.uint64)
+    confs[:, 1] = 0
+    m.train(confs, steps=2, batch=4096, lr=1e-3)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = m.train(confs, steps=8, batch=4096, lr=1e-3)
+    torch.cuda.synchronize()
+    print(f"profile case (proposal training): 8 steps in {1e3 * (time.perf_counter() - t0):.2f} ms, loss {loss:.4f}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1083,8 +1101,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="headline only: skip the FP64 checks and other workloads")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
-    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "sampler"],
-                    help="SR solver of the small profile case; 'sampler': the sampler case")
+    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "sampler", "made"],
+                    help="SR solver of the small profile case; 'sampler': the sampler case; 'made': the "
+                         "proposal's training")
     ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
     ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
     ap.add_argument("--profile-window", action="store_true",
@@ -1095,6 +1114,8 @@ def main():
     if args.profile_case:
         if args.profile_solver == "sampler":
             run_profile_case_sampler()
+        elif args.profile_solver == "made":
+            run_profile_case_made()
         else:
             run_profile_case(args.profile_solver)
         return
