@@ -184,6 +184,8 @@ _SIGS = {
     "ann_made_train": ([P, P, U, U, U, D, P, P], I),
     "ann_made_train_on_samples": ([P, P, U, U, D, P, P], I),
     "ann_get_solve_times": ([P], I),
+    "ann_set_factor_trace": ([I], I),
+    "ann_get_factor_trace": ([P, U, P], I),
     "ann_get_phase_times": ([P], I),
 }
 

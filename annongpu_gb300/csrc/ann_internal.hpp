@@ -317,6 +317,9 @@ void ensure_side_stream(ann_tdvp_impl& td);
 void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
 // CUDA-event marks around the FP32 factorisation when phase timing is on (capi.cu)
 void solve_mark(int i, cudaStream_t st);
+// tagged events of the FP32 Cholesky's timeline (ann_set_factor_trace); reset per factorisation
+void factor_mark(int tag, cudaStream_t st);
+void factor_trace_reset();
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
 
 unsigned* status_word();

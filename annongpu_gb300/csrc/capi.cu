@@ -238,6 +238,30 @@ void solve_mark(int i, cudaStream_t st) {
     g_sev_used[i] = true;
 }
 
+// event timeline of the FP32 Cholesky (tagged events on its main and look-ahead streams)
+namespace {
+std::vector<std::pair<int, cudaEvent_t>> g_fev;
+size_t g_fev_used = 0;
+bool g_ftrace = false;
+}  // namespace
+
+void factor_trace_reset() { g_fev_used = 0; }
+
+void factor_mark(int tag, cudaStream_t st) {
+    if(!g_ftrace) return;
+    cudaStreamCaptureStatus cs;
+    ANN_CUDA(cudaStreamIsCapturing(st, &cs));
+    if(cs != cudaStreamCaptureStatusNone) return;
+    if(g_fev_used == g_fev.size()) {
+        cudaEvent_t e;
+        ANN_CUDA(cudaEventCreate(&e));
+        g_fev.push_back({tag, e});
+    }
+    g_fev[g_fev_used].first = tag;
+    ANN_CUDA(cudaEventRecord(g_fev[g_fev_used].second, st));
+    g_fev_used++;
+}
+
 }  // namespace ann
 
 using namespace ann;
@@ -1434,6 +1458,29 @@ int ann_get_solve_times(float* ms1) {
         if(g_sev_used[0] && g_sev_used[1]) {
             ANN_CUDA(cudaEventSynchronize(g_sev[1]));
             ANN_CUDA(cudaEventElapsedTime(&ms1[0], g_sev[0], g_sev[1]));
+        }
+    });
+}
+
+int ann_set_factor_trace(int enable) {
+    return guard([&] {
+        g_ftrace = enable != 0;
+        g_fev_used = 0;
+    });
+}
+
+int ann_get_factor_trace(double* out, unsigned cap, unsigned* n) {
+    return guard([&] {
+        need(n, "null argument");
+        *n = (unsigned)g_fev_used;
+        if(!g_fev_used || !out) return;
+        ANN_CUDA(cudaEventSynchronize(g_fev[g_fev_used - 1].second));
+        for(size_t k = 0; k < g_fev_used && k < cap; k++) {
+            float ms = 0.f;
+            ANN_CUDA(cudaEventSynchronize(g_fev[k].second));
+            ANN_CUDA(cudaEventElapsedTime(&ms, g_fev[0].second, g_fev[k].second));
+            out[2 * k] = g_fev[k].first;
+            out[2 * k + 1] = ms;
         }
     });
 }

@@ -81,15 +81,28 @@ __global__ void __launch_bounds__(256) cvt_shift_kernel(const TS* __restrict__ S
 // one row per lane: lanes 0-15 of every warp hold the 16 diagonal rows (each warp
 // factorises them redundantly, so no warp waits on another) and lanes 16-31 hold 16 of
 // the rows below. Column j of the panel is then
-//   l_jj = sqrt(a_jj), l_rj = a_rj / l_jj, a_rc -= l_rj conj(l_cj) (c = j+1..15),
-// with l_cj broadcast by shuffle from lane c. The 16-column trailing update of the rest
-// of the block runs on all threads in 2 x 2 register tiles; two barriers per panel.
+//   l_jj = a_jj rsqrt(a_jj), l_rj = a_rj rsqrt(a_jj), a_rc -= l_rj conj(l_cj) (c = j+1..15),
+// with l_cj broadcast by shuffle from lane c. Every lane applies every column update
+// (the entries above the diagonal of the panel block are never read back), so the
+// updates of one column carry no branch and overlap; the chain per column is one
+// shuffle, the reciprocal square root, one shuffle and one complex multiply-add. The
+// 16-column trailing update of the rest of the block runs on all threads in 2 x 2
+// register tiles; two barriers per panel.
 constexpr int kPotrfThreads = 256;
 constexpr int kPw = 16;  // panel width
+constexpr unsigned kNoPrev = 0xFFFFFFFFu;
+// dynamic shared memory of potrf32_kernel (two 64 x 65 complex blocks) and trsm32_kernel (one)
+constexpr size_t kPotrfSmem = 2 * NB * (NB + 1) * sizeof(cf);
+constexpr size_t kTrsmSmem = NB * (NB + 1) * sizeof(cf);
 
+// With prev != kNoPrev the block first receives the rank-64 update of the panel at columns
+// prev (the first panel of a pair: a_rc -= sum_k l_rk conj(l_ck) over its 64 columns),
+// which the pair form applies here and in trsm32_kernel instead of a separate launch.
 __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
-                                                                unsigned* status) {
-    __shared__ cf a[NB][NB + 1];
+                                                                unsigned* status, unsigned prev) {
+    extern __shared__ float4 panel_smem[];
+    cf (*a)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(panel_smem);
+    cf (*w)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(reinterpret_cast<cf*>(panel_smem) + NB * (NB + 1));
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     {
@@ -104,8 +117,47 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__
             const unsigned t = tid + q * kPotrfThreads;
             a[t / NB][t % NB] = v[q];
         }
+        if(prev != kNoPrev) {
+#pragma unroll
+            for(int q = 0; q < NB * NB / kPotrfThreads; q++) {
+                const unsigned t = tid + q * kPotrfThreads, r = t / NB, k = t % NB;
+                w[r][k] = r < nb ? A[(size_t)(kb + r) * n + prev + k] : mk(0.f, 0.f);
+            }
+        }
     }
     __syncthreads();
+    if(prev != kNoPrev) {
+        // a_rc -= sum_k w_rk conj(w_ck) on the lower triangle, in 4 x 4 register tiles
+        // (rows 4 ty .. 4 ty + 3, columns 4 tx .. 4 tx + 3; tiles above the diagonal idle)
+        const unsigned tx = tid & 15u, ty = tid >> 4;
+        if(tx <= ty) {
+            cf acc[4][4];
+#pragma unroll
+            for(int i = 0; i < 4; i++)
+#pragma unroll
+                for(int j = 0; j < 4; j++) acc[i][j] = mk(0.f, 0.f);
+#pragma unroll 4
+            for(int k = 0; k < NB; k++) {
+                cf wr[4], wc[4];
+#pragma unroll
+                for(int i = 0; i < 4; i++) wr[i] = w[4 * ty + i][k];
+#pragma unroll
+                for(int j = 0; j < 4; j++) wc[j] = w[4 * tx + j][k];
+#pragma unroll
+                for(int i = 0; i < 4; i++)
+#pragma unroll
+                    for(int j = 0; j < 4; j++) cmac_conj(acc[i][j], wc[j], wr[i]);  // += w_rk conj(w_ck)
+            }
+#pragma unroll
+            for(int i = 0; i < 4; i++)
+#pragma unroll
+                for(int j = 0; j < 4; j++) {
+                    const unsigned r = 4 * ty + i, c = 4 * tx + j;
+                    if(c <= r) a[r][c] = a[r][c] - acc[i][j];
+                }
+        }
+        __syncthreads();
+    }
 #pragma unroll 1
     for(unsigned kk = 0; kk < NB; kk += kPw) {
         const unsigned below = NB - kk - kPw;                       // rows under the panel's diagonal block
@@ -125,16 +177,16 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__
                     if(tid == 0) atomicOr(status, kStatusNotPosDef);
                     d = 1.f;
                 }
-                const float s = sqrtf(d), inv = __frcp_rn(s);
-                if(diag && lane == (unsigned)j) x[j] = mk(s, 0.f);
-                else x[j] = inv * x[j];
+                const float inv = rsqrtf(d), s = d * inv;
+                x[j] = (diag && lane == (unsigned)j) ? mk(s, 0.f) : inv * x[j];
+                const cf nx = -x[j];
 #pragma unroll
                 for(int c = 1; c < kPw; c++) {  // constant bounds, so that both loops unroll
                     if(c <= j) continue;
                     cf l;
                     l.re = __shfl_sync(0xffffffffu, x[j].re, c);
                     l.im = __shfl_sync(0xffffffffu, x[j].im, c);
-                    if(!diag || lane >= (unsigned)c) cmac_conj(x[c], l, -x[j]);  // -= l_rj conj(l_cj)
+                    cmac_conj(x[c], l, nx);  // -= l_rj conj(l_cj)
                 }
             }
             if(live && (!diag || warp == 0)) {
@@ -257,9 +309,59 @@ __device__ __forceinline__ void put_tf32(const PtDst& d, size_t i, unsigned p, c
     im[lo + p] = tf32_round(v.im - hi);
 }
 
-__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb, PtDst pt) {
-    __shared__ cf Lt[NB][NB + 1];
+__global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigned n, unsigned kb, PtDst pt,
+                                                     unsigned prev) {
+    // one 64 x 65 buffer: first W (the previous panel's factor rows of this block, for the
+    // pending update), then L_kk transposed; 33 KB per CTA keeps six CTAs per SM
+    extern __shared__ float4 panel_smem[];
+    cf (*Lt)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(panel_smem);
+    cf (*W)[NB + 1] = Lt;
     __shared__ float inv_d[NB];
+    const unsigned nbk = min((unsigned)NB, n - kb);
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t row0 = (size_t)kb + NB + (size_t)blockIdx.x * kTrsmRows;
+    // each warp solves its two rows (warp, warp + 8) side by side: two independent chains
+    static_assert(kTrsmRows == 16, "two rows per warp of eight");
+    const size_t ra = row0 + warp, rb = row0 + warp + 8;
+    const bool has_a = ra < n, has_b = rb < n;
+    cf* Xa = A + (has_a ? ra : kb) * n + kb;
+    cf* Xb = A + (has_b ? rb : (has_a ? ra : kb)) * n + kb;
+    cf a0 = mk(0.f, 0.f), a1 = a0, b0 = a0, b1 = a0;
+    if(has_a) {
+        a0 = Xa[lane];
+        a1 = Xa[lane + 32];
+        b0 = Xb[lane];
+        b1 = Xb[lane + 32];
+    }
+    if(prev != kNoPrev) {
+        for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+            const unsigned q = t / NB, c = t % NB;
+            W[q][c] = q < nbk ? A[(size_t)(kb + q) * n + prev + c] : mk(0.f, 0.f);
+        }
+        __syncthreads();
+    }
+    if(prev != kNoPrev && has_a) {
+        // the previous panel's rank-64 update of these rows: x_q -= sum_k p_k conj(W[q][k]),
+        // p = the row's factor entries in that panel, broadcast from lane k % 32
+        const cf* Pa = A + ra * n + prev;
+        const cf* Pb = A + (has_b ? rb : ra) * n + prev;
+        const cf pa0 = Pa[lane], pa1 = Pa[lane + 32], pb0 = Pb[lane], pb1 = Pb[lane + 32];
+#pragma unroll 8
+        for(int k = 0; k < NB; k++) {
+            const cf sa = k < 32 ? pa0 : pa1, sb = k < 32 ? pb0 : pb1;
+            cf pa, pb;
+            pa.re = __shfl_sync(0xffffffffu, sa.re, k & 31);
+            pa.im = __shfl_sync(0xffffffffu, sa.im, k & 31);
+            pb.re = __shfl_sync(0xffffffffu, sb.re, k & 31);
+            pb.im = __shfl_sync(0xffffffffu, sb.im, k & 31);
+            const cf w0 = W[lane][k], w1 = W[lane + 32][k];
+            cmac_conj(a0, w0, -pa);  // -= p_k conj(W[q][k])
+            cmac_conj(a1, w1, -pa);
+            cmac_conj(b0, w0, -pb);
+            cmac_conj(b1, w1, -pb);
+        }
+    }
+    if(prev != kNoPrev) __syncthreads();  // W is read; the buffer takes L_kk next
     for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
         const unsigned q = t / NB, c = t % NB;  // element (q, c) of L_kk
         Lt[c][q] = c <= q ? A[(size_t)(kb + q) * n + kb + c] : mk(0.f, 0.f);
@@ -267,16 +369,8 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
     __syncthreads();
     if(threadIdx.x < NB) inv_d[threadIdx.x] = 1.f / Lt[threadIdx.x][threadIdx.x].re;
     __syncthreads();
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t row0 = (size_t)kb + NB + (size_t)blockIdx.x * kTrsmRows;
-    // each warp solves its two rows (warp, warp + 8) side by side: two independent chains
-    static_assert(kTrsmRows == 16, "two rows per warp of eight");
-    const size_t ra = row0 + warp, rb = row0 + warp + 8;
-    if(ra >= n) return;
-    const bool has_b = rb < n;
-    cf* Xa = A + ra * n + kb;
-    cf* Xb = A + (has_b ? rb : ra) * n + kb;
-    cf a0 = Xa[lane], a1 = Xa[lane + 32], b0 = Xb[lane], b1 = Xb[lane + 32];
+    if(!has_a) return;
+#pragma unroll 8
     for(unsigned c = 0; c < 32; c++) {
         cf xa, xb;
         xa.re = __shfl_sync(0xffffffffu, a0.re, c);
@@ -287,16 +381,17 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
         xa = id * xa;
         xb = id * xb;
         const cf l0 = Lt[c][lane], l1 = Lt[c][lane + 32];
-        if(lane == c) {
-            a0 = xa;
-            b0 = xb;
-        } else if(lane > c) {
-            cmac_conj(a0, l0, -xa);  // -= x_c conj(L_qc)
-            cmac_conj(b0, l0, -xb);
-        }
+        // lane c takes x_c, lanes above subtract x_c conj(L_qc), lanes below keep their
+        // finished values: selects, not branches, so consecutive columns overlap
+        cf ua = a0, ub = b0;
+        cmac_conj(ua, l0, -xa);
+        cmac_conj(ub, l0, -xb);
+        a0 = lane == c ? xa : (lane > c ? ua : a0);
+        b0 = lane == c ? xb : (lane > c ? ub : b0);
         cmac_conj(a1, l1, -xa);
         cmac_conj(b1, l1, -xb);
     }
+#pragma unroll 8
     for(unsigned c = 32; c < NB; c++) {
         cf xa, xb;
         xa.re = __shfl_sync(0xffffffffu, a1.re, c - 32);
@@ -307,13 +402,11 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
         xa = id * xa;
         xb = id * xb;
         const cf l1 = Lt[c][lane + 32];
-        if(lane + 32 == c) {
-            a1 = xa;
-            b1 = xb;
-        } else if(lane + 32 > c) {
-            cmac_conj(a1, l1, -xa);
-            cmac_conj(b1, l1, -xb);
-        }
+        cf ua = a1, ub = b1;
+        cmac_conj(ua, l1, -xa);
+        cmac_conj(ub, l1, -xb);
+        a1 = lane + 32 == c ? xa : (lane + 32 > c ? ua : a1);
+        b1 = lane + 32 == c ? xb : (lane + 32 > c ? ub : b1);
     }
     Xa[lane] = a0;
     Xa[lane + 32] = a1;
@@ -801,28 +894,31 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
 }
 
 // diagonal block, then the rows below it (and, for the tensor-core update, its operand)
-void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, PtDst pt, cudaStream_t st) {
-    potrf32_kernel<<<1, kPotrfThreads, 0, st>>>(A, n, kb, status);
+// (prev: a pending rank-64 update from the panel at those columns, applied first)
+void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, PtDst pt, cudaStream_t st, unsigned prev = kNoPrev) {
+    potrf32_kernel<<<1, kPotrfThreads, kPotrfSmem, st>>>(A, n, kb, status, prev);
     check_launch("potrf32_kernel");
+    factor_mark(110, st);
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned below = n - kb - nb;
     if(below) {
-        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, 0, st>>>(A, n, kb, pt);
+        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, kTrsmSmem, st>>>(A, n, kb, pt, prev);
         check_launch("trsm32_kernel");
     }
 }
 
-// the panel pair at columns pb .. pb + 127: panel pb, its rank-64 update of the second
-// panel's 64 columns (FP32 SIMT, rows below pb + 64), then the second panel. The rows
-// from pb + 128 on of both panels go to PT (pair layout: K = 128, rows [hi | lo] of 256
-// floats) for the pair's tensor-core update of the rest.
+// the panel pair at columns pb .. pb + 127: panel pb, then the second panel, whose
+// diagonal block (potrf32) and rows below (trsm32) first apply the first panel's rank-64
+// update of the second panel's 64 columns. The rows from pb + 128 on of both panels go to
+// PT (pair layout: K = 128, rows [hi | lo] of 256 floats) for the pair's tensor-core update
+// of the rest.
 void panel_pair32(cf* A, unsigned n, unsigned pb, unsigned* status, float* PT, cudaStream_t st) {
+    factor_mark(100, st);
     panel32(A, n, pb, status, PtDst{PT, pb + 2 * NB, 0, 4 * NB}, st);
+    factor_mark(101, st);
     if(n - pb <= (unsigned)NB) return;
-    const unsigned below = n - pb - NB;
-    herk32_kernel<<<(below + UT - 1) / UT, 256, 2 * NB * (UT + 1) * sizeof(cf), st>>>(A, n, pb, NB, 1);
-    check_launch("herk32_kernel");
-    panel32(A, n, pb + NB, status, PtDst{PT, pb + 2 * NB, NB, 4 * NB}, st);
+    panel32(A, n, pb + NB, status, PtDst{PT, pb + 2 * NB, NB, 4 * NB}, st, pb);
+    factor_mark(103, st);
 }
 
 void set_smem_attrs() {
@@ -832,6 +928,7 @@ void set_smem_attrs() {
                                   2 * NB * (NB + 1) * (int)sizeof(cf)));
     ANN_CUDA(cudaFuncSetAttribute(herk32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   2 * NB * (UT + 1) * (int)sizeof(cf)));
+    ANN_CUDA(cudaFuncSetAttribute(potrf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPotrfSmem));
     done = true;
 }
 
@@ -850,6 +947,7 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
     const bool pair = tc && td.chol_reduce && tuning_get(key_chol_pair(n), 1) != 0;
+    factor_trace_reset();
     td.chol_form = pair ? ANN_CHOL_FORM_TC_PAIR : (tc ? ANN_CHOL_FORM_TC_PANEL : ANN_CHOL_FORM_SIMT);
     if(pair) {
         // Panel pairs (128 columns): the tensor-core update of the rest is one rank-128
@@ -860,13 +958,17 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
         auto ppt = [&](unsigned pb) { return chol_update_tc_pair_operand(td, (pb / (2 * NB)) & 1u); };
         panel_pair32(A, n, 0, status, ppt(0), st);
         for(unsigned pb = 0; pb + 2 * NB < n; pb += 2 * NB) {
+            factor_mark(200, st);
             chol_update_tc_pair(td, A, n, pb, true, status, st);
+            factor_mark(201, st);
             ANN_CUDA(cudaEventRecord(td.side_ev[0], st));
             ANN_CUDA(cudaStreamWaitEvent(td.side, td.side_ev[0], 0));
             panel_pair32(A, n, pb + 2 * NB, status, ppt(pb + 2 * NB), td.side);
             ANN_CUDA(cudaEventRecord(td.side_ev[1], td.side));
             chol_update_tc_pair(td, A, n, pb, false, status, st);
+            factor_mark(202, st);
             ANN_CUDA(cudaStreamWaitEvent(st, td.side_ev[1], 0));
+            factor_mark(203, st);
         }
         diag_inv_kernel<<<(n + NB - 1) / NB, 1024, 2 * NB * (NB + 1) * sizeof(cf), st>>>(A, n, Dinv, DinvH);
         check_launch("diag_inv_kernel");

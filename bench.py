@@ -842,6 +842,9 @@ def run_ours(args):
     Np, Ns = f.Np, N_CHAINS
     energy = f.energy_check()
     summary = {name: form_summary(r[0], r[1], r[2], r[4]) for name, r in results.items()}
+    timeline = None
+    if f.tdvp.solver_info.get("update_form") == "tensor core, rank 128 per panel pair":
+        timeline = factor_timeline(ann, f.tdvp)  # one more solve of the last S, outside the timed steps
 
     # end to end through the public API: parameters from pinned host memory in, the
     # step's energy out, every step
@@ -871,7 +874,7 @@ def run_ours(args):
         "energy_per_site": energy["energy_per_site"], "energy_check": energy,
         "phase_ms": summary[f.name]["phase_ms"],
         "phase_note": "CUDA-event phases of eager steps (the headline times graph replays)",
-        "solver": info, "train_seconds": t_train,
+        "solver": info, "factorisation_timeline": timeline, "train_seconds": t_train,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": Np * 16,
                 "d2h_bytes_per_step": 16, "ms_per_step": ms_e2e_w},
@@ -1071,6 +1074,60 @@ def run_profile_case_sampler():
     print("profile case (sampler): E/N =", td.E_local / N_SITES)
 
 
+def factor_timeline(ann, td, shift=SHIFT):
+    """Event timeline of one FP32 factorisation (pair form): per panel pair the tile-column
+    update that precedes it, the look-ahead stream's panel kernels and the rest of the
+    tensor-core update beside them, in microseconds."""
+    import ctypes as ct
+    ann._lib.call("ann_set_factor_trace", 1)
+    td.solve(shift)
+    out = np.zeros(2 * 8192)
+    n = ct.c_uint(0)
+    ann._lib.call("ann_get_factor_trace", ann._lib.ptr(out), 8192, ct.byref(n))
+    ann._lib.call("ann_set_factor_trace", 0)
+    ev = out[: 2 * n.value].reshape(-1, 2)
+    tags, t = ev[:, 0].astype(int), ev[:, 1] * 1e3
+    starts = [i for i, g in enumerate(tags) if g == 200]
+    rows = []
+    for k, i0 in enumerate(starts):
+        seg = list(zip(tags[i0: starts[k + 1] if k + 1 < len(starts) else len(tags)],
+                       t[i0: starts[k + 1] if k + 1 < len(starts) else len(tags)]))
+        d, p110 = {}, []
+        for g, tt in seg:
+            (p110.append(tt) if g == 110 else d.__setitem__(g, tt))
+        if 103 not in d or len(p110) < 2:
+            continue
+        rows.append({"tile_column_update": d[201] - d[200], "stream_hand_off": d[100] - d[201],
+                     "potrf_1": p110[0] - d[100], "trsm_1": d[101] - p110[0], "potrf_2": p110[1] - d[101],
+                     "trsm_2": d[103] - p110[1], "panel_pair": d[103] - d[100], "rest_of_update": d[202] - d[201],
+                     "iteration": d[203] - d[200]})
+    keys = list(rows[0]) if rows else []
+    return {"pairs": len(rows), "total_ms": float(t.max() / 1e3) if len(t) else None,
+            "sum_us": {k: float(sum(r[k] for r in rows)) for k in keys},
+            "first_pair_us": {k: round(rows[0][k], 1) for k in keys} if rows else None,
+            "last_pair_us": {k: round(rows[-1][k], 1) for k in keys} if rows else None,
+            "panel_bound_pairs": int(sum(r["panel_pair"] + r["stream_hand_off"] > r["rest_of_update"] for r in rows))}
+
+
+def run_profile_case_factor():
+    """The 8x8 workload's S (Np = 8384, BF16, 16384 samples of the random-init RBM), the
+    mixed solve autotuned, then the event timeline of one FP32 factorisation."""
+    import annongpu_gb300 as ann
+    a, b, W = init_params(np.random.default_rng(SEED))
+    op = ann.Operator(ann.transverse_field_ising_2d(L, L, h=H_FIELD))
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    mc = ann.MonteCarloLoop(N_CHAINS, 8, THERM, N_CHAINS, True, seed=3, persistent=True)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    td.eval(op, psi, mc)
+    ann.autotune(op, psi, mc, td, SHIFT)
+    td.eval(op, psi, mc)
+    for _ in range(3):
+        td.solve(SHIFT)
+    print(json.dumps({"factorisation_timeline": factor_timeline(ann, td),
+                      "tuning": {k: v for k, v in ann.tuning_table().items() if "chol" in k},
+                      "solver": td.solver_info}))
+
+
 def run_profile_case_made():
     """Small case for ncu captures of the proposal's training GEMMs: N = 64, H = 256 (the
     alpha = 4 workload's proposal), batches of 4096 configurations, 8 Adam steps (each one
@@ -1101,9 +1158,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="headline only: skip the FP64 checks and other workloads")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
-    ap.add_argument("--profile-solver", default="fp64", choices=["fp64", "mixed", "fp32", "sampler", "made"],
+    ap.add_argument("--profile-solver", default="fp64",
+                    choices=["fp64", "mixed", "fp32", "sampler", "made", "factor-trace"],
                     help="SR solver of the small profile case; 'sampler': the sampler case; 'made': the "
-                         "proposal's training")
+                         "proposal's training; 'factor-trace': event timeline of the 8x8 factorisation")
     ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
     ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
     ap.add_argument("--profile-window", action="store_true",
@@ -1116,6 +1174,8 @@ def main():
             run_profile_case_sampler()
         elif args.profile_solver == "made":
             run_profile_case_made()
+        elif args.profile_solver == "factor-trace":
+            run_profile_case_factor()
         else:
             run_profile_case(args.profile_solver)
         return
