@@ -1059,11 +1059,14 @@ def run_profile_case(solver="fp64"):
     print("profile case: E/N =", td.E_local / 32)
 
 
-def run_profile_case_sampler():
+def run_profile_case_sampler(team=32):
     """Small case for ncu captures of the sampler: the 8x8 workload's shapes (N = 64,
     M = 128, h = 3.04) with 4096 chains (O rows 275 MB), 8 sweeps between samples, two
-    sampling passes with E_loc and O rows (TDVP evaluations, BF16 S)."""
+    sampling passes with E_loc and O rows (TDVP evaluations, BF16 S); chains of `team`
+    lanes (32: one per warp, 16: two per warp)."""
+    import torch
     import annongpu_gb300 as ann
+    ann.set_tuning({f"dev{torch.cuda.current_device()}/rbm_mc.team/N{N_SITES}.M{M_HIDDEN}.U4.P0.made0": team})
     a, b, W = init_params(np.random.default_rng(SEED))
     op = ann.Operator(ann.transverse_field_ising_2d(L, L, h=H_FIELD))
     psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
@@ -1159,8 +1162,9 @@ def main():
     ap.add_argument("--no-legs", action="store_true", help="headline only: skip the FP64 checks and other workloads")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu capture case and exit")
     ap.add_argument("--profile-solver", default="fp64",
-                    choices=["fp64", "mixed", "fp32", "sampler", "made", "factor-trace"],
-                    help="SR solver of the small profile case; 'sampler': the sampler case; 'made': the "
+                    choices=["fp64", "mixed", "fp32", "sampler", "sampler16", "made", "factor-trace"],
+                    help="SR solver of the small profile case; 'sampler' / 'sampler16': the sampler case "
+                         "(whole- / half-warp chains); 'made': the "
                          "proposal's training; 'factor-trace': event timeline of the 8x8 factorisation")
     ap.add_argument("--tuning", default=None, help="load this tuning table (from --save-tuning) instead of autotuning")
     ap.add_argument("--save-tuning", default=None, help="save the tuning table after the run")
@@ -1170,8 +1174,8 @@ def main():
     if args.warmup < 1 or args.steps < 1:
         ap.error("--steps and --warmup must be at least 1")
     if args.profile_case:
-        if args.profile_solver == "sampler":
-            run_profile_case_sampler()
+        if args.profile_solver in ("sampler", "sampler16"):
+            run_profile_case_sampler(16 if args.profile_solver == "sampler16" else 32)
         elif args.profile_solver == "made":
             run_profile_case_made()
         elif args.profile_solver == "factor-trace":
