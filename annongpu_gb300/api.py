@@ -794,7 +794,7 @@ class TDVP(_Handle):
 
     _destroy = "ann_tdvp_destroy"
 
-    def __init__(self, num_params, gpu=True, *, s_mode="fp32", solver="fp64", max_iter=6, tol=1e-12,
+    def __init__(self, num_params, gpu=True, *, s_mode="fp32", solver="fp64", max_iter=10, tol=1e-12,
                  stream=None):
         _Handle.__init__(self)
         self.num_params = int(num_params)
@@ -805,7 +805,7 @@ class TDVP(_Handle):
         self.s_mode = s_mode
         self.set_solver(solver, max_iter, tol)
 
-    def set_solver(self, solver="fp64", max_iter=6, tol=1e-12):
+    def set_solver(self, solver="fp64", max_iter=10, tol=1e-12):
         """SR solver: "fp64" (FP64 Cholesky + one refinement step), "mixed" (FP32
         Cholesky + refinement with FP64 residuals until ||r||/||F|| <= tol, at most
         max_iter FP32 solves; a stalled eager solve is redone in FP64) or "fp32" (one

@@ -185,7 +185,7 @@ struct ann_tdvp_impl {
     // (FP32 Cholesky + FP64 refinement to ir_tol, at most ir_max solves) or
     // ANN_SOLVER_FP32 (one FP32 Cholesky solve, no refinement)
     int solver = ANN_SOLVER_FP64;
-    unsigned ir_max = 6;
+    unsigned ir_max = 10;
     double ir_tol = 1e-12;
     bool fell_back = false;     // the last mixed solve stalled and the FP64 solve replaced it
     DevBuf L32, Dinv32, c32, ir;  // FP32 factor, inverted diagonal blocks, FP32 vectors, refinement state

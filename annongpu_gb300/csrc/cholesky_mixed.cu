@@ -10,7 +10,8 @@
 //   3. x = 0, r = F; repeat: c = (L L^H)^{-1} r in FP32, x += c in FP64,
 //      r = F - (S + shift I) x in FP64, until ||r|| / ||F|| <= tol or max_iter.
 //      When S holds FP32 values in complex64 (the tensor-core HERK's sums), S x is
-//      formed on the FP32 pipe in double-float arithmetic (below) and r in FP64.
+//      formed on the FP32 pipe in double-float arithmetic (below) until ||r|| / ||F||
+//      falls to 1e-10, then in FP64 (whose 53 bits the last steps need).
 //
 // The iteration is classical mixed-precision iterative refinement (Wilkinson;
 // Moler 1967; analysed by Higham, "Accuracy and Stability of Numerical
@@ -714,29 +715,42 @@ __global__ void ir_axpy_kernel(zc* __restrict__ x, const cf* __restrict__ c, uns
 
 // r = F - (S + shift I) x in FP64 (one warp per row), c = (complex64) r, and per-CTA
 // partial sums of |r|^2 and |F|^2 for the convergence test
-__global__ void __launch_bounds__(256) ir_residual_kernel(const zc* __restrict__ S, unsigned n, double shift,
+// The refinement of a complex64 S switches residuals: double-float (ir_residual32_kernel)
+// while ||r|| / ||F|| is above kFp64Below, FP64 (this kernel) from there on, where the
+// double-float floor (about 2^-48 of sum |s x| per term, against 2^-53 in FP64) would
+// otherwise decide whether the tolerance is reached. Both are launched every iteration;
+// each reads the state and the one not due writes zero partials.
+constexpr double kFp64Below = 1e-10;
+
+__device__ __forceinline__ bool fp64_residual_due(const IrState* st, int always) {
+    return always || (st->last >= 0.0 && st->last <= kFp64Below);
+}
+
+template<typename TS>
+__global__ void __launch_bounds__(256) ir_residual_kernel(const TS* __restrict__ S, unsigned n, double shift,
                                                           const zc* __restrict__ x, const zc* __restrict__ F,
                                                           zc* __restrict__ r, cf* __restrict__ c,
-                                                          double* __restrict__ part, const IrState* st) {
+                                                          double* __restrict__ part, const IrState* st,
+                                                          int always) {
     __shared__ double sh[2][8];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double rr = 0.0, ff = 0.0;
-    if(!st->done) {
+    if(!st->done && fp64_residual_due(st, always)) {
         const size_t i = (size_t)blockIdx.x * 8 + warp;
         if(i < n) {
-            const zc* Si = S + i * n;
-            // four independent accumulators: four 16-byte loads in flight per lane
+            const TS* Si = S + i * n;
+            // four independent accumulators: four loads in flight per lane
             zc a0 = mk(0.0, 0.0), a1 = a0, a2 = a0, a3 = a0;
             unsigned j = lane;
             for(; j + 96 < n; j += 128) {
-                const zc s0 = Si[j], s1 = Si[j + 32], s2 = Si[j + 64], s3 = Si[j + 96];
+                const zc s0 = to_zc(Si[j]), s1 = to_zc(Si[j + 32]), s2 = to_zc(Si[j + 64]), s3 = to_zc(Si[j + 96]);
                 const zc x0 = x[j], x1 = x[j + 32], x2 = x[j + 64], x3 = x[j + 96];
                 cmac(a0, s0, x0);
                 cmac(a1, s1, x1);
                 cmac(a2, s2, x2);
                 cmac(a3, s3, x3);
             }
-            for(; j < n; j += 32) cmac(a0, Si[j], x[j]);
+            for(; j < n; j += 32) cmac(a0, to_zc(Si[j]), x[j]);
             zc acc = (a0 + a1) + (a2 + a3);
             acc = warp_sum(acc);
             if(lane == 0) {
@@ -781,29 +795,18 @@ __device__ __forceinline__ void df_norm(float& h, float& l) {
     l = __fsub_rn(l, __fsub_rn(s, h));
     h = s;
 }
-__device__ __forceinline__ void df_add(float& h, float& l, float h2, float l2) {
-    float s, e;
-    two_sum(h, h2, s, e);
-    h = s;
-    l = __fadd_rn(__fadd_rn(l, l2), e);
-    df_norm(h, l);
-}
-__device__ __forceinline__ void df_warp_sum(float& h, float& l) {
-#pragma unroll
-    for(int o = 16; o > 0; o >>= 1) {
-        const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
-        df_add(h, l, h2, l2);
-    }
-}
-
 constexpr unsigned kRes32Rows = 16;  // rows per CTA of ir_residual32_kernel (two per warp)
+constexpr unsigned kResBlock = 16;   // terms per lane in one double-float block of ir_residual32_kernel
 
 // r = F - (S + shift I) x for S in complex64 holding FP32 values (the tensor-core HERK's
-// sums): S x in double-float from x's split xs (each product s xh exact, s xl rounded
-// once, sums by TwoSum with renormalisation after every term: about 2^-48 relative per
-// term, against 2^-53 for FP64 arithmetic), then F - S x - shift x in FP64. GB300's FP64
-// pipe (1/64 of the FP32 rate) would bound the FP64 product at ~0.5 ms for Np = 8384;
-// here the S rows stream at HBM rate. One warp per two rows (each xs load serves both).
+// sums): S x from x's split xs, each product s xh exact, s xl rounded once, summed by
+// TwoSum with renormalisation after every term (about 2^-48 relative) over blocks of 16
+// terms per lane; the block sums go into FP64 accumulators, so the error is 2^-48 of a
+// block's partial sum plus FP64 rounding of the running sum, not 2^-48 of a running sum
+// that cancellation may leave far larger than the residual; then F - S x - shift x in FP64.
+// GB300's FP64 pipe (1/64 of the FP32 rate) would bound an FP64 product at ~0.5 ms for
+// Np = 8384; here the FP64 work is two adds per 16 terms. One warp per two rows (each xs
+// load serves both).
 __global__ void __launch_bounds__(256) ir_residual32_kernel(const cf* __restrict__ S, unsigned n, double shift,
                                                             const zc* __restrict__ x, const float4* __restrict__ xs,
                                                             const zc* __restrict__ F, zc* __restrict__ r,
@@ -812,37 +815,49 @@ __global__ void __launch_bounds__(256) ir_residual32_kernel(const cf* __restrict
     __shared__ double sh[2][8];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double rr = 0.0, ff = 0.0;
-    if(!st->done) {
+    if(!st->done && !fp64_residual_due(st, 0)) {
         const size_t i0 = (size_t)blockIdx.x * kRes32Rows + 2 * warp;
         if(i0 < n) {
             const bool two = i0 + 1 < n;
             const cf* S0 = S + i0 * n;
             const cf* S1 = S + (two ? i0 + 1 : i0) * n;
-            // [row][re, im] accumulators
-            float h[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, l[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+            // [row][re, im]: double-float partials over blocks of kResBlock terms, each block
+            // added to an FP64 accumulator (h + l is exact in FP64): the running sum keeps
+            // FP64 precision whatever its size, the double-float error stays relative to one
+            // block's partial
+            double acc_d[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+            for(unsigned j0 = lane; j0 < n; j0 += 32 * kResBlock) {
+                float h[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, l[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll 4
-            for(unsigned j = lane; j < n; j += 32) {
-                const float4 xv = xs[j];
-                const cf s[2] = {S0[j], S1[j]};
+                for(unsigned jj = 0; jj < kResBlock; jj++) {
+                    const unsigned j = j0 + 32 * jj;
+                    if(j >= n) break;
+                    const float4 xv = xs[j];
+                    const cf s[2] = {S0[j], S1[j]};
 #pragma unroll
-                for(int q = 0; q < 2; q++) {
-                    df_mac(h[q][0], l[q][0], s[q].re, xv.x, xv.y);   // Re s Re x
-                    df_mac(h[q][0], l[q][0], -s[q].im, xv.z, xv.w);  // - Im s Im x
-                    df_mac(h[q][1], l[q][1], s[q].re, xv.z, xv.w);   // Re s Im x
-                    df_mac(h[q][1], l[q][1], s[q].im, xv.x, xv.y);   // Im s Re x
-                    df_norm(h[q][0], l[q][0]);
-                    df_norm(h[q][1], l[q][1]);
+                    for(int q = 0; q < 2; q++) {
+                        df_mac(h[q][0], l[q][0], s[q].re, xv.x, xv.y);   // Re s Re x
+                        df_mac(h[q][0], l[q][0], -s[q].im, xv.z, xv.w);  // - Im s Im x
+                        df_mac(h[q][1], l[q][1], s[q].re, xv.z, xv.w);   // Re s Im x
+                        df_mac(h[q][1], l[q][1], s[q].im, xv.x, xv.y);   // Im s Re x
+                        df_norm(h[q][0], l[q][0]);
+                        df_norm(h[q][1], l[q][1]);
+                    }
                 }
+#pragma unroll
+                for(int q = 0; q < 2; q++)
+#pragma unroll
+                    for(int k = 0; k < 2; k++) acc_d[q][k] += widen(h[q][k]) + widen(l[q][k]);
             }
 #pragma unroll
             for(int q = 0; q < 2; q++) {
-                df_warp_sum(h[q][0], l[q][0]);
-                df_warp_sum(h[q][1], l[q][1]);
+                acc_d[q][0] = warp_sum(acc_d[q][0]);
+                acc_d[q][1] = warp_sum(acc_d[q][1]);
             }
             if(lane == 0) {
                 for(int q = 0; q < (two ? 2 : 1); q++) {
                     const size_t i = i0 + q;
-                    const zc acc = mk(widen(h[q][0]) + widen(l[q][0]), widen(h[q][1]) + widen(l[q][1]));
+                    const zc acc = mk(acc_d[q][0], acc_d[q][1]);
                     const zc ri = F[i] - acc - shift * x[i];
                     r[i] = ri;
                     c[i] = cvt<float>(ri);
@@ -870,7 +885,7 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
     if(st->done) return;
     __shared__ double sh[2][32];
     double a = 0.0, b = 0.0;
-    for(unsigned k = threadIdx.x; k < n_part; k += blockDim.x) {
+    for(unsigned k = threadIdx.x; k < n_part; k += blockDim.x) {  // the residual kernel not due wrote zeros
         a += part[2 * k];
         b += part[2 * k + 1];
     }
@@ -1052,10 +1067,13 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
     td.delta.ensure(n * sizeof(zc));
     td.resid.ensure(2 * n * sizeof(zc) + 2 * sizeof(double));
     td.c32.ensure((size_t)n * sizeof(cf));
-    // S in complex64 (FP32 values): double-float residual on the FP32 pipe; else FP64
+    // S in complex64 (FP32 values): double-float residuals on the FP32 pipe until the
+    // residual nears the tolerance, then FP64 ones; a complex128 S: FP64 residuals. The two
+    // kernels keep their partial sums in separate ranges of `part` (FP64 first).
     const bool s32 = td.S_in32;
     if(s32) td.xs32.ensure((size_t)n * sizeof(float4));
-    const unsigned res_blocks = s32 ? (n + kRes32Rows - 1) / kRes32Rows : (n + 7) / 8;
+    const unsigned res64 = (n + 7) / 8, res32 = s32 ? (n + kRes32Rows - 1) / kRes32Rows : 0u;
+    const unsigned res_blocks = res64 + res32;
     static_assert(sizeof(IrState) % 16 == 0, "the solve's tagged blocks need 16-byte alignment");
     td.ir.ensure(sizeof(IrState) + 2 * (size_t)res_blocks * sizeof(double) + kSolveSyncHead +
                  2 * (size_t)nblk * NB * sizeof(ulonglong2));
@@ -1091,12 +1109,13 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
         ir_axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, c, n, irs, xs);
         check_launch("ir_axpy_kernel");
         if(s32) {
-            ir_residual32_kernel<<<res_blocks, 256, 0, st>>>(S32, n, shift, x, xs, F, r, c, part, irs);
+            ir_residual32_kernel<<<res32, 256, 0, st>>>(S32, n, shift, x, xs, F, r, c, part + 2 * (size_t)res64, irs);
             check_launch("ir_residual32_kernel");
+            ir_residual_kernel<cf><<<res64, 256, 0, st>>>(S32, n, shift, x, F, r, c, part, irs, 0);
         } else {
-            ir_residual_kernel<<<res_blocks, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs);
-            check_launch("ir_residual_kernel");
+            ir_residual_kernel<zc><<<res64, 256, 0, st>>>(S, n, shift, x, F, r, c, part, irs, 1);
         }
+        check_launch("ir_residual_kernel");
         ir_check_kernel<<<1, 1024, 0, st>>>(part, res_blocks, tol, it + 1 == max_iter, irs, report, status);
         check_launch("ir_check_kernel");
     }

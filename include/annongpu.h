@@ -302,8 +302,9 @@ int ann_force_vector_noalloc(const void* O_rows, size_t n_rows, size_t ld, unsig
    ANN_SOLVER_FP64: FP64 Cholesky of S + shift I on the GPU, two triangular solves and
      one step of iterative refinement (the default).
    ANN_SOLVER_MIXED: FP32 Cholesky of S + shift I, then iterative refinement with the
-     residual F - (S + shift I) x formed in FP64 against the FP64 S, until
-     ||r|| / ||F|| <= tol or max_iter FP32 solves; converges to the FP64 answer when
+     residual F - (S + shift I) x formed against S (FP64 arithmetic, or double-float
+     arithmetic with FP64 accumulation when S is held in complex64), until
+     ||r|| / ||F|| <= tol or max_iter FP32 solves (default 10); converges to the FP64 answer when
      cond(S + shift I) * 6e-8 < 1. An eager solve that does not converge (or whose FP32
      factorisation meets a non-positive pivot) is redone with ANN_SOLVER_FP64; inside a
      captured graph it raises ANN_ERR_NUMERIC at the next status check instead.
