@@ -765,9 +765,9 @@ def hsd_timing(ann, f, st):
 #       python bench.py --form precision --steps 1 --warmup 1 --train-steps 3 --no-cpu --no-legs \
 #       --tuning tuning.json --profile-window
 # sampler: one launch (half-warp chains, O rows 1.10 GB written); S: one herk_tc launch
-# (complex64 S); factorisation: its 129 tcgen05 update launches (10.36 GB) and the panel
-# kernels potrf32 / trsm32 / herk32 (0.58 GB), per factorisation.
-TRAFFIC_BYTES = {"sampler": 1.0579e9, "herk_tc": 6.4534e9, "factorisation": 1.0937e10}
+# (complex64 S); factorisation: its 129 tcgen05 update launches (10.37 GB) and the panel
+# kernels potrf32 / trsm32 (0.44 GB), per factorisation.
+TRAFFIC_BYTES = {"sampler": 1.0583e9, "herk_tc": 6.4523e9, "factorisation": 1.0811e10}
 TRAFFIC_SRC = "DRAM bytes per launch from one full-size ncu capture of this workload (one-pass metrics)"
 
 

@@ -188,3 +188,42 @@ def test_complex64_S_store_keeps_values_and_solutions():
     d_fb = t32.solve(shift)
     assert t32.solver_info["fell_back"]
     np.testing.assert_array_equal(d_fb, dref)
+
+
+def test_factorisation_event_timeline():
+    """ann_set_factor_trace records the tagged events of the FP32 factorisation (pair form:
+    per panel pair a tile-column update on the main stream, the look-ahead panel kernels);
+    the times are ordered per stream and the trace is off again afterwards."""
+    import ctypes as ct
+    N, M = 32, 64  # Np = 2144: 34 panels of 64 (the last of 32 columns) in 17 pairs
+    rng = np.random.default_rng(4)
+    a, b, W = cplx(rng, N, 0.01), cplx(rng, M, 0.01), cplx(rng, (N, M), 0.01)
+    psi = ann.PsiRBM(W, 1.0, 0.0, True, a=a, b=b, precision="fp32")
+    op = ann.Operator(ann.transverse_field_ising_1d(N, 1.0))
+    mc = ann.MonteCarloLoop(4096, 2, 8, 4096, True, seed=23)
+    td = ann.TDVP(psi.num_params, s_mode="bf16", solver="mixed")
+    td.chol_update = "tc"
+    td.eval(op, psi, mc)
+    td.solve(1e-3)
+    if td.solver_info["update_form"] != "tensor core, rank 128 per panel pair":
+        pytest.skip("the tuning table chose another update form")
+    ann._lib.call("ann_set_factor_trace", 1)
+    td.solve(1e-3)
+    out = np.zeros(2 * 4096)
+    n = ct.c_uint(0)
+    ann._lib.call("ann_get_factor_trace", ann._lib.ptr(out), 4096, ct.byref(n))
+    ann._lib.call("ann_set_factor_trace", 0)
+    ev = out[: 2 * n.value].reshape(-1, 2)
+    tags, t = ev[:, 0].astype(int), ev[:, 1]
+    n_p = psi.num_params
+    pairs, panels = (n_p + 127) // 128, (n_p + 63) // 64
+    assert (tags == 200).sum() == pairs - 1 and (tags == 203).sum() == pairs - 1
+    assert (tags == 100).sum() == pairs and (tags == 101).sum() == pairs
+    assert (tags == 110).sum() == panels and (tags == 103).sum() == panels - pairs
+    for main in (t[np.isin(tags, [200, 201, 202, 203])], t[np.isin(tags, [100, 110, 101, 103])]):
+        assert (np.diff(main) >= -1e-3).all()  # each stream's events in order (ms, event resolution)
+    assert t.max() > 0
+    # off: the next factorisation records nothing new
+    td.solve(1e-3)
+    ann._lib.call("ann_get_factor_trace", None, 0, ct.byref(n))
+    assert n.value == 0
