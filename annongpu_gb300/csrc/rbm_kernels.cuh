@@ -79,6 +79,68 @@ __device__ __forceinline__ T fw_f_re(const RbmDev<T>& p, const Lane<T, U>& L, in
     return fw.re * f.re - fw.im * f.im;
 }
 
+// ---- two-wide FP32 unit work (sm_100+ packed FP32 instructions) ----
+// For complex64 chains with the polynomial activation and real final weights (PsiRBM),
+// proposals and recompute() evaluate the units two values per instruction: angle changes
+// and new angles as (re, im) of one unit, the activation's real part as (slot u, slot
+// u + 1). Each component of a two-wide instruction rounds as the scalar instruction does,
+// and every step below is an explicit round-to-nearest operation, so the results do not
+// depend on the team width or on the compiler's contraction choices.
+__device__ __forceinline__ float2 as_f2(cplx<float> c) { return make_float2(c.re, c.im); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// a += b; a += s b with s = +-1 (exact product): one instruction for complex64
+template<typename T>
+__device__ __forceinline__ void add_to(cplx<T>& a, cplx<T> b) { a += b; }
+__device__ __forceinline__ void add_to(cplx<float>& a, cplx<float> b) {
+    const float2 r = __fadd2_rn(as_f2(a), as_f2(b));
+    a = mk(r.x, r.y);
+}
+template<typename T>
+__device__ __forceinline__ void add_signed(cplx<T>& a, T s, cplx<T> b) {
+    a.re += s * b.re;
+    a.im += s * b.im;
+}
+__device__ __forceinline__ void add_signed(cplx<float>& a, float s, cplx<float> b) {
+    const float2 r = __ffma2_rn(dup2(s), as_f2(b), as_f2(a));
+    a = mk(r.x, r.y);
+}
+
+// Re f(z) of the polynomial f = z^2/2 - z^4/12 + z^6/45 for two units, from P = Re z^2 =
+// x^2 - y^2 and q = x y: Re z^4 = P^2 - 4 q^2, Re z^6 = P (P^2 - 12 q^2), so
+// Re f = P/2 - P^2/12 + q^2/3 + (P/45) (P^2 - 12 q^2).
+__device__ __forceinline__ float2 poly_re2(float2 z0, float2 z1) {
+    const float2 s0 = __fmul2_rn(z0, z0), s1 = __fmul2_rn(z1, z1);
+    const float2 P = make_float2(__fsub_rn(s0.x, s0.y), __fsub_rn(s1.x, s1.y));
+    const float2 q = make_float2(__fmul_rn(z0.x, z0.y), __fmul_rn(z1.x, z1.y));
+    const float2 A = __fmul2_rn(P, P), b = __fmul2_rn(q, q);
+    const float2 c = __ffma2_rn(b, dup2(-12.f), A);
+    const float2 t = __ffma2_rn(A, dup2(-1.f / 12.f), __fmul2_rn(b, dup2(1.f / 3.f)));
+    const float2 h = __ffma2_rn(P, dup2(0.5f), t);
+    return __ffma2_rn(__fmul2_rn(P, dup2(1.f / 45.f)), c, h);
+}
+
+// the packed path applies (complex64, polynomial activation, real final weights)
+template<typename T>
+__device__ __forceinline__ bool packed_units(const RbmDev<T>& p) {
+    if constexpr(sizeof(T) == 4) return p.act == kPoly && p.fw_real;
+    else return false;
+}
+
+// L.fr of every slot from L.th and L.fwr, two slots per step (slots past Uact hold
+// th = 0 and fwr = 0, so their terms are 0)
+template<int U>
+__device__ __forceinline__ void lane_fr2(Lane<float, U>& L) {
+#pragma unroll
+    for(int u = 0; u < U; u += 2) {
+        const float2 z1 = u + 1 < U ? as_f2(L.th[u + 1]) : make_float2(0.f, 0.f);
+        const float2 fw = make_float2(L.fwr[u], u + 1 < U ? L.fwr[u + 1] : 0.f);
+        const float2 f = __fmul2_rn(fw, poly_re2(as_f2(L.th[u]), z1));
+        L.fr[u] = f.x;
+        if(u + 1 < U) L.fr[u + 1] = f.y;
+    }
+}
+
 // theta_j = b_j + sum_i s_i Wd[i][j] from scratch
 template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd,
@@ -95,9 +157,13 @@ __device__ __forceinline__ void recompute(const RbmDev<T>& p, const cplx<T>* __r
 #pragma unroll
         for(int u = 0; u < U; u++) {
             if((unsigned)u >= p.Uact) break;
-            const cplx<T> w = row[u * TL];
-            L.th[u].re += si * w.re;
-            L.th[u].im += si * w.im;
+            add_signed(L.th[u], si, row[u * TL]);
+        }
+    }
+    if constexpr(sizeof(T) == 4) {
+        if(packed_units(p)) {
+            lane_fr2<U>(L);
+            return;
         }
     }
 #pragma unroll
@@ -112,12 +178,73 @@ __device__ __forceinline__ void lane_terms(const RbmDev<T>& p, const Lane<T, U>&
         ft[u] = (unsigned)u < p.Uact ? p.fw[u * TL + lane] * act_f(L.th[u], p.act, 0) : mk<T>(T(0), T(0));
 }
 
+// delta_re below on the two-wide path. The per-virtual-lane sums keep the scalar order:
+// slot u of a half-warp team belongs to virtual lane u % 2, so the pair (u, u + 1) adds
+// into (d[0], d[1]) in one instruction; a whole-warp team adds its slots one by one.
+template<int NW, int U, int TL>
+__device__ __forceinline__ float delta_re2(const RbmDev<float>& p, const cplx<float>* __restrict__ Wd,
+                                           const Conf<NW>& s, const Lane<float, U>& L, int lane,
+                                           const uint16_t* sites, unsigned nsites, cplx<float>* dth, float* fnew) {
+    float2 dt[U];
+#pragma unroll
+    for(int u = 0; u < U; u++) dt[u] = make_float2(0.f, 0.f);
+    float dvis = 0.f;
+    for(unsigned q = 0; q < nsites; q++) {
+        const unsigned i = sites[q];
+        const float m2s = spin_bit(s, i) ? -2.f : 2.f;  // s'_i - s_i
+        const float2 m2 = dup2(m2s);
+        const cplx<float>* row = Wd + (size_t)i * p.Mpad + lane;
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            if((unsigned)u >= p.Uact) break;
+            dt[u] = __ffma2_rn(m2, as_f2(row[u * TL]), dt[u]);  // m2s w is exact
+        }
+        if(p.a_in_log_psi) dvis += m2s * p.a[i].re;
+    }
+    float d[kVirt<TL>];
+    float2 dd = make_float2(0.f, 0.f);  // (d[0], d[1]) of a half-warp team
+    d[0] = 0.f;
+#pragma unroll
+    for(int u = 0; u < U; u += 2) {
+        if((unsigned)u >= p.Uact) {
+            fnew[u] = 0.f;
+            if(u + 1 < U) fnew[u + 1] = 0.f;
+            continue;
+        }
+        // a slot past Uact has th = dt = 0 and fwr = fr = 0: its difference is +0
+        const float2 z0 = __fadd2_rn(as_f2(L.th[u]), dt[u]);
+        const float2 z1 = u + 1 < U ? __fadd2_rn(as_f2(L.th[u + 1]), dt[u + 1]) : make_float2(0.f, 0.f);
+        const float2 fw = make_float2(L.fwr[u], u + 1 < U ? L.fwr[u + 1] : 0.f);
+        const float2 f = __fmul2_rn(fw, poly_re2(z0, z1));
+        const float2 fr = make_float2(L.fr[u], u + 1 < U ? L.fr[u + 1] : 0.f);
+        const float2 df = __ffma2_rn(fr, dup2(-1.f), f);  // f - fr, rounded once
+        fnew[u] = f.x;
+        if(u + 1 < U) fnew[u + 1] = f.y;
+        if constexpr(kVirt<TL> == 2) {
+            dd = __fadd2_rn(dd, df);
+        } else {
+            d[0] += df.x;
+            if(u + 1 < U) d[0] += df.y;
+        }
+    }
+    if constexpr(kVirt<TL> == 2) {
+        d[0] = dd.x;
+        d[kVirt<TL> - 1] = dd.y;
+    }
+#pragma unroll
+    for(int u = 0; u < U; u++) dth[u] = mk(dt[u].x, dt[u].y);
+    return team_total<TL>(d) + dvis;
+}
+
 // Re(log psi(s') - log psi(s)) summed over the team for the flip of `sites`; leaves the
 // angle changes in dth and the new real terms in fnew for an accepted move
 template<typename T, int NW, int U, int TL = 32>
 __device__ __forceinline__ T delta_re(const RbmDev<T>& p, const cplx<T>* __restrict__ Wd, const Conf<NW>& s,
                                       const Lane<T, U>& L, int lane, const uint16_t* sites, unsigned nsites,
                                       cplx<T>* dth, T* fnew) {
+    if constexpr(sizeof(T) == 4) {
+        if(packed_units(p)) return delta_re2<NW, U, TL>(p, Wd, s, L, lane, sites, nsites, dth, fnew);
+    }
 #pragma unroll
     for(int u = 0; u < U; u++) dth[u] = mk<T>(T(0), T(0));
     T dvis = T(0);
@@ -407,7 +534,7 @@ __device__ __forceinline__ void mc_chain(const RbmDev<T>& p, const cplx<T>* __re
         const bool accept = sizeof(T) == 4 ? (uf <= (float)ratio) : (u <= (double)ratio);
         if(accept) {
 #pragma unroll
-            for(int q = 0; q < U; q++) { L.th[q] += dth[q]; L.fr[q] = fnew[q]; }
+            for(int q = 0; q < U; q++) { add_to(L.th[q], dth[q]); L.fr[q] = fnew[q]; }
             for(unsigned q = 0; q < ns; q++) flip(s, sites[q]);
             n_acc++;
             lq_stale = true;
