@@ -317,8 +317,10 @@ void ensure_side_stream(ann_tdvp_impl& td);
 void sr_solve_any(ann_tdvp_impl& td, double shift, unsigned* status_dev, cudaStream_t st);
 // CUDA-event marks around the FP32 factorisation when phase timing is on (capi.cu)
 void solve_mark(int i, cudaStream_t st);
-// tagged events of the FP32 Cholesky's timeline (ann_set_factor_trace); reset per factorisation
-void factor_mark(int tag, cudaStream_t st);
+// tagged events of the FP32 Cholesky's timeline (ann_set_factor_trace); reset per factorisation.
+// A mark of level 2 sits between two panel kernels and turns their programmatic launch
+// into a plain one, so it is recorded only at trace level 2
+void factor_mark(int tag, cudaStream_t st, int level = 1);
 void factor_trace_reset();
 void sr_update(ann_psi_impl& psi, const cplx<double>* delta, double lr, cudaStream_t st);
 

@@ -242,13 +242,13 @@ void solve_mark(int i, cudaStream_t st) {
 namespace {
 std::vector<std::pair<int, cudaEvent_t>> g_fev;
 size_t g_fev_used = 0;
-bool g_ftrace = false;
+int g_ftrace = 0;  // 0 off, 1 panel-pair marks, 2 also the marks between the panel kernels
 }  // namespace
 
 void factor_trace_reset() { g_fev_used = 0; }
 
-void factor_mark(int tag, cudaStream_t st) {
-    if(!g_ftrace) return;
+void factor_mark(int tag, cudaStream_t st, int level) {
+    if(g_ftrace < level) return;
     cudaStreamCaptureStatus cs;
     ANN_CUDA(cudaStreamIsCapturing(st, &cs));
     if(cs != cudaStreamCaptureStatusNone) return;
@@ -1464,7 +1464,8 @@ int ann_get_solve_times(float* ms1) {
 
 int ann_set_factor_trace(int enable) {
     return guard([&] {
-        g_ftrace = enable != 0;
+        need(enable >= 0 && enable <= 2, "factor trace level 0, 1 or 2");
+        g_ftrace = enable;
         g_fev_used = 0;
     });
 }

@@ -96,9 +96,22 @@ constexpr unsigned kNoPrev = 0xFFFFFFFFu;
 constexpr size_t kPotrfSmem = 2 * NB * (NB + 1) * sizeof(cf);
 constexpr size_t kTrsmSmem = NB * (NB + 1) * sizeof(cf);
 
+// The panel kernels run as programmatic dependent launches (sm_90+ griddepcontrol): a
+// kernel launched with cudaLaunchAttributeProgrammaticStreamSerialization may start while
+// the kernel before it on the stream still runs, and loads what does not depend on that
+// kernel (its own rows, the pending update of the panel pair) in the meantime. pdl_wait()
+// returns once the kernel before has completed and its writes are visible (at once for a
+// kernel launched without the attribute); pdl_trigger() lets the next kernel start.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // With prev != kNoPrev the block first receives the rank-64 update of the panel at columns
 // prev (the first panel of a pair: a_rc -= sum_k l_rk conj(l_ck) over its 64 columns),
 // which the pair form applies here and in trsm32_kernel instead of a separate launch.
+// The diagonal block is read before pdl_wait() (nothing before this kernel on its stream
+// writes it: the panel at prev writes only its own columns); the rows at prev after it.
+// The trigger follows the wait, so a kernel started by it finds the kernel before this
+// one completed as well.
 __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__ A, unsigned n, unsigned kb,
                                                                 unsigned* status, unsigned prev) {
     extern __shared__ float4 panel_smem[];
@@ -118,6 +131,8 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__
             const unsigned t = tid + q * kPotrfThreads;
             a[t / NB][t % NB] = v[q];
         }
+        pdl_wait();
+        pdl_trigger();
         if(prev != kNoPrev) {
 #pragma unroll
             for(int q = 0; q < NB * NB / kPotrfThreads; q++) {
@@ -318,6 +333,10 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
     cf (*Lt)[NB + 1] = reinterpret_cast<cf (*)[NB + 1]>(panel_smem);
     cf (*W)[NB + 1] = Lt;
     __shared__ float inv_d[NB];
+    // Started as a programmatic dependent launch after potrf32_kernel of this panel: the
+    // rows and the pending update (the pair's first panel, completed before the potrf32
+    // launch that started this kernel released it) are read before pdl_wait(), L_kk after.
+    pdl_trigger();
     const unsigned nbk = min((unsigned)NB, n - kb);
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t row0 = (size_t)kb + NB + (size_t)blockIdx.x * kTrsmRows;
@@ -363,6 +382,7 @@ __global__ void __launch_bounds__(256) trsm32_kernel(cf* __restrict__ A, unsigne
         }
     }
     if(prev != kNoPrev) __syncthreads();  // W is read; the buffer takes L_kk next
+    pdl_wait();
     for(unsigned t = threadIdx.x; t < NB * NB; t += blockDim.x) {
         const unsigned q = t / NB, c = t % NB;  // element (q, c) of L_kk
         Lt[c][q] = c <= q ? A[(size_t)(kb + q) * n + kb + c] : mk(0.f, 0.f);
@@ -910,14 +930,34 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
 
 // diagonal block, then the rows below it (and, for the tensor-core update, its operand)
 // (prev: a pending rank-64 update from the panel at those columns, applied first)
+// a launch that may start before the kernel ahead of it on the stream has completed (the
+// kernel waits for it with pdl_wait())
+template<typename... P, typename... Args>
+void launch_pdl(void (*kernel)(P...), unsigned grid, unsigned block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ANN_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+}
+
 void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, PtDst pt, cudaStream_t st, unsigned prev = kNoPrev) {
-    potrf32_kernel<<<1, kPotrfThreads, kPotrfSmem, st>>>(A, n, kb, status, prev);
+    // the first panel of a pair waits for the update before it in full (a plain launch);
+    // the second starts under the first panel's row solve
+    if(prev == kNoPrev) potrf32_kernel<<<1, kPotrfThreads, kPotrfSmem, st>>>(A, n, kb, status, prev);
+    else launch_pdl(potrf32_kernel, 1, kPotrfThreads, kPotrfSmem, st, A, n, kb, status, prev);
     check_launch("potrf32_kernel");
-    factor_mark(110, st);
+    factor_mark(110, st, 2);
     const unsigned nb = min((unsigned)NB, n - kb);
     const unsigned below = n - kb - nb;
     if(below) {
-        trsm32_kernel<<<(below + kTrsmRows - 1) / kTrsmRows, 256, kTrsmSmem, st>>>(A, n, kb, pt, prev);
+        launch_pdl(trsm32_kernel, (below + kTrsmRows - 1) / kTrsmRows, 256, kTrsmSmem, st, A, n, kb, pt, prev);
         check_launch("trsm32_kernel");
     }
 }
@@ -930,7 +970,7 @@ void panel32(cf* A, unsigned n, unsigned kb, unsigned* status, PtDst pt, cudaStr
 void panel_pair32(cf* A, unsigned n, unsigned pb, unsigned* status, float* PT, cudaStream_t st) {
     factor_mark(100, st);
     panel32(A, n, pb, status, PtDst{PT, pb + 2 * NB, 0, 4 * NB}, st);
-    factor_mark(101, st);
+    factor_mark(101, st, 2);
     if(n - pb <= (unsigned)NB) return;
     panel32(A, n, pb + NB, status, PtDst{PT, pb + 2 * NB, NB, 4 * NB}, st, pb);
     factor_mark(103, st);

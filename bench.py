@@ -1095,12 +1095,14 @@ def run_profile_case_sampler(team=32):
     print("profile case (sampler): E/N =", td.E_local / N_SITES)
 
 
-def factor_timeline(ann, td, shift=SHIFT):
+def factor_timeline(ann, td, shift=SHIFT, level=1):
     """Event timeline of one FP32 factorisation (pair form): per panel pair the tile-column
     update that precedes it, the look-ahead stream's panel kernels and the rest of the
-    tensor-core update beside them, in microseconds."""
+    tensor-core update beside them, in microseconds. Level 2 also splits the panel pair into
+    its four kernels; its extra events make those kernels run one after the other instead of
+    as programmatic dependent launches."""
     import ctypes as ct
-    ann._lib.call("ann_set_factor_trace", 1)
+    ann._lib.call("ann_set_factor_trace", level)
     td.solve(shift)
     out = np.zeros(2 * 8192)
     n = ct.c_uint(0)
@@ -1116,12 +1118,14 @@ def factor_timeline(ann, td, shift=SHIFT):
         d, p110 = {}, []
         for g, tt in seg:
             (p110.append(tt) if g == 110 else d.__setitem__(g, tt))
-        if 103 not in d or len(p110) < 2:
+        if 103 not in d or (level == 2 and len(p110) < 2):
             continue
-        rows.append({"tile_column_update": d[201] - d[200], "stream_hand_off": d[100] - d[201],
-                     "potrf_1": p110[0] - d[100], "trsm_1": d[101] - p110[0], "potrf_2": p110[1] - d[101],
-                     "trsm_2": d[103] - p110[1], "panel_pair": d[103] - d[100], "rest_of_update": d[202] - d[201],
-                     "iteration": d[203] - d[200]})
+        row = {"tile_column_update": d[201] - d[200], "stream_hand_off": d[100] - d[201]}
+        if level == 2:
+            row.update({"potrf_1": p110[0] - d[100], "trsm_1": d[101] - p110[0], "potrf_2": p110[1] - d[101],
+                        "trsm_2": d[103] - p110[1]})
+        row.update({"panel_pair": d[103] - d[100], "rest_of_update": d[202] - d[201], "iteration": d[203] - d[200]})
+        rows.append(row)
     keys = list(rows[0]) if rows else []
     return {"pairs": len(rows), "total_ms": float(t.max() / 1e3) if len(t) else None,
             "sum_us": {k: float(sum(r[k] for r in rows)) for k in keys},
@@ -1145,6 +1149,7 @@ def run_profile_case_factor():
     for _ in range(3):
         td.solve(SHIFT)
     print(json.dumps({"factorisation_timeline": factor_timeline(ann, td),
+                      "factorisation_timeline_kernels": factor_timeline(ann, td, level=2),
                       "tuning": {k: v for k, v in ann.tuning_table().items() if "chol" in k},
                       "solver": td.solver_info}))
 

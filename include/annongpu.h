@@ -486,12 +486,14 @@ int ann_get_phase_times(float* ms5);
    last mixed / FP32 SR solve (-1 if none was timed) */
 int ann_get_solve_times(float* ms1);
 /* event timeline of the FP32 Cholesky factorisation (this project's diagnostic): with the
-   trace on, every mixed / FP32 factorisation outside graph capture records tagged CUDA
-   events; ann_get_factor_trace writes (tag, ms since the first event) pairs of the last
-   one. Tags: 200 / 201 tile-column update of the next panel pair start / end, 202 rest of
-   the trailing update done, 203 main stream joined with the look-ahead stream (main
-   stream); 100 panel pair start, 110 after each diagonal-block factorisation, 101 after
-   the first panel, 103 after the second (look-ahead stream). */
+   trace on (enable 1 or 2), every mixed / FP32 factorisation outside graph capture records
+   tagged CUDA events; ann_get_factor_trace writes (tag, ms since the first event) pairs of
+   the last one. Tags: 200 / 201 tile-column update of the next panel pair start / end, 202
+   rest of the trailing update done, 203 main stream joined with the look-ahead stream (main
+   stream); 100 panel pair start, 103 panel pair done (look-ahead stream). Level 2 adds 110
+   after each diagonal-block factorisation and 101 after the first panel of a pair; those
+   events sit between panel kernels that otherwise start early as programmatic dependent
+   launches, so level 2 times the panel kernels one after the other. */
 int ann_set_factor_trace(int enable);
 int ann_get_factor_trace(double* out, unsigned cap, unsigned* n);
 

@@ -207,22 +207,26 @@ def test_factorisation_event_timeline():
     td.solve(1e-3)
     if td.solver_info["update_form"] != "tensor core, rank 128 per panel pair":
         pytest.skip("the tuning table chose another update form")
-    ann._lib.call("ann_set_factor_trace", 1)
-    td.solve(1e-3)
-    out = np.zeros(2 * 4096)
-    n = ct.c_uint(0)
-    ann._lib.call("ann_get_factor_trace", ann._lib.ptr(out), 4096, ct.byref(n))
-    ann._lib.call("ann_set_factor_trace", 0)
-    ev = out[: 2 * n.value].reshape(-1, 2)
-    tags, t = ev[:, 0].astype(int), ev[:, 1]
     n_p = psi.num_params
     pairs, panels = (n_p + 127) // 128, (n_p + 63) // 64
-    assert (tags == 200).sum() == pairs - 1 and (tags == 203).sum() == pairs - 1
-    assert (tags == 100).sum() == pairs and (tags == 101).sum() == pairs
-    assert (tags == 110).sum() == panels and (tags == 103).sum() == panels - pairs
-    for main in (t[np.isin(tags, [200, 201, 202, 203])], t[np.isin(tags, [100, 110, 101, 103])]):
-        assert (np.diff(main) >= -1e-3).all()  # each stream's events in order (ms, event resolution)
-    assert t.max() > 0
+    x0 = td.solve(1e-3)
+    n = ct.c_uint(0)
+    for level in (1, 2):  # 1: panel pairs; 2: also between the panel kernels
+        ann._lib.call("ann_set_factor_trace", level)
+        x = td.solve(1e-3)
+        out = np.zeros(2 * 4096)
+        ann._lib.call("ann_get_factor_trace", ann._lib.ptr(out), 4096, ct.byref(n))
+        ann._lib.call("ann_set_factor_trace", 0)
+        np.testing.assert_array_equal(x, x0)  # the trace changes timing, not results
+        ev = out[: 2 * n.value].reshape(-1, 2)
+        tags, t = ev[:, 0].astype(int), ev[:, 1]
+        assert (tags == 200).sum() == pairs - 1 and (tags == 203).sum() == pairs - 1
+        assert (tags == 100).sum() == pairs and (tags == 103).sum() == panels - pairs
+        assert (tags == 101).sum() == (pairs if level == 2 else 0)
+        assert (tags == 110).sum() == (panels if level == 2 else 0)
+        for main in (t[np.isin(tags, [200, 201, 202, 203])], t[np.isin(tags, [100, 110, 101, 103])]):
+            assert (np.diff(main) >= -1e-3).all()  # each stream's events in order (ms, event resolution)
+        assert t.max() > 0
     # off: the next factorisation records nothing new
     td.solve(1e-3)
     ann._lib.call("ann_get_factor_trace", None, 0, ct.byref(n))
