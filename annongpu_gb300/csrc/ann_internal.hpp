@@ -302,7 +302,7 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
                     unsigned* status_dev, cudaStream_t st);
 void mixed_solve_info(const ann_tdvp_impl& td, double* out4, cudaStream_t st);
 // tensor-core trailing update of the FP32 Cholesky (chol_update_tc.cu)
-void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n);
+void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n, cudaStream_t st);
 bool chol_update_tc_bind(ann_tdvp_impl& td, cplx<float>* A, unsigned n);
 // operand buffer 0 / 1 (panel k uses k % 2), written by the panel solve
 float* chol_update_tc_operand(ann_tdvp_impl& td, unsigned buf);

@@ -77,6 +77,7 @@ unsigned* status_word() {
     unsigned* p = nullptr;
     ANN_CUDA(cudaMalloc(&p, sizeof(unsigned)));
     ANN_CUDA(cudaMemset(p, 0, sizeof(unsigned)));
+    ANN_CUDA(cudaDeviceSynchronize());
     g_status[dev] = p;
     return p;
 }
@@ -321,6 +322,7 @@ void check_status() {
     ANN_CUDA(cudaMemcpy(&v, p, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if(v) {
         ANN_CUDA(cudaMemset(p, 0, sizeof(unsigned)));
+        ANN_CUDA(cudaDeviceSynchronize());  // cleared before later kernels on other streams raise flags
         std::string m = "device status:";
         if(v & kStatusNonFinite) m += " non-finite value in log psi / local energy;";
         if(v & kStatusNotPosDef) m += " S + shift is not positive definite;";
@@ -402,6 +404,7 @@ int ann_status(unsigned* out) {
         unsigned* p = status_word();
         ANN_CUDA(cudaMemcpy(out, p, sizeof(unsigned), cudaMemcpyDeviceToHost));
         ANN_CUDA(cudaMemset(p, 0, sizeof(unsigned)));
+        ANN_CUDA(cudaDeviceSynchronize());
     });
 }
 
@@ -742,6 +745,9 @@ int ann_ens_create_mc(const ann_mc_desc* d, ann_ens** out) {
             ANN_CUDA(cudaMemset(e->chain_counter.p, 0, e->chain_counter.bytes));
             e->acc_rej.ensure(4 * sizeof(unsigned long long));
             ANN_CUDA(cudaMemset(e->acc_rej.p, 0, 4 * sizeof(unsigned long long)));
+            // the clears run on the legacy default stream, which does not order with the
+            // non-blocking streams the ensemble is used on: complete them here
+            ANN_CUDA(cudaDeviceSynchronize());
         } catch(...) {
             delete e;
             throw;
@@ -838,6 +844,7 @@ int ann_ens_set_history(ann_ens* e, unsigned capacity) {
             e->hist.ensure((size_t)capacity * kMaxWords * sizeof(uint64_t));
             e->hist_posd.ensure(sizeof(unsigned long long));
             ANN_CUDA(cudaMemset(e->hist_posd.p, 0, sizeof(unsigned long long)));
+            ANN_CUDA(cudaDeviceSynchronize());  // before any non-blocking stream appends
         }
     });
 }

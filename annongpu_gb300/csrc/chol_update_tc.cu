@@ -482,11 +482,13 @@ static void encode_pt(unsigned char* map, unsigned char* base, size_t bytes, uns
     if(r != CUDA_SUCCESS) throw Error(ANN_ERR_CUDA, "cuTensorMapEncodeTiled failed (Cholesky panel operand)");
 }
 
-void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n) {
+// (the clear is ordered on the solve's stream: a plain cudaMemset goes to the legacy default
+// stream, which does not order with the non-blocking streams the solves run on)
+void chol_update_tc_prepare(ann_tdvp_impl& td, unsigned n, cudaStream_t st) {
     const size_t b1 = pt_bytes_w(n, kPanel), b2 = pt_bytes_w(n, 2 * kPanel);
     if(td.chol_pt.bytes >= 2 * b2 && td.chol_pt_n == n) return;
     td.chol_pt.ensure(2 * b2);
-    ANN_CUDA(cudaMemset(td.chol_pt.p, 0, 2 * b2));
+    ANN_CUDA(cudaMemsetAsync(td.chol_pt.p, 0, 2 * b2, st));
     td.chol_pt_n = n;
     for(int b = 0; b < 2; b++) {
         encode_pt(td.chol_map[b], td.chol_pt.as<unsigned char>() + b * b1, b1, kPanel);

@@ -928,6 +928,20 @@ __global__ void ir_check_kernel(const double* __restrict__ part, unsigned n_part
     }
 }
 
+// Inside a CUDA graph there is no host-side FP64 fallback: a refinement that ends with a
+// non-finite residual or one above kKeepBelow leaves delta = 0 (the SR update then changes
+// nothing) instead of a step that would corrupt the parameters; ir_check_kernel has raised
+// kStatusSolveStalled for it. The flags of the FP32 factorisation (a non-positive pivot, a
+// wait that gave up), which an eager solve answers with the FP64 fallback, go to the status
+// word as well.
+constexpr double kKeepBelow = 1e-3;
+
+__global__ void ir_guard_kernel(zc* __restrict__ x, unsigned n, const IrState* st, unsigned* status) {
+    if(blockIdx.x == 0 && threadIdx.x == 0 && st->notpd) atomicOr(status, st->notpd);
+    if(st->last <= kKeepBelow) return;  // also false for NaN
+    for(unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = mk(0.0, 0.0);
+}
+
 // diagonal block, then the rows below it (and, for the tensor-core update, its operand)
 // (prev: a pending rank-64 update from the panel at those columns, applied first)
 // a launch that may start before the kernel ahead of it on the stream has completed (the
@@ -997,7 +1011,7 @@ void cholesky32(ann_tdvp_impl& td, cf* A, unsigned n, cf* Dinv, cf* DinvH, unsig
     // an explicit choice, else the autotuned one for this size, else the default
     const bool tc = td.chol_tc_set ? td.chol_tc != 0 : tuning_get(key_chol_update(n), td.chol_tc) != 0;
     if(tc) {
-        chol_update_tc_prepare(td, n);
+        chol_update_tc_prepare(td, n, st);
         chol_update_tc_bind(td, A, n);
     }
     const size_t herk_smem = 2 * NB * (UT + 1) * sizeof(cf);
@@ -1158,6 +1172,10 @@ void sr_solve_mixed(ann_tdvp_impl& td, double shift, unsigned max_iter, double t
         check_launch("ir_residual_kernel");
         ir_check_kernel<<<1, 1024, 0, st>>>(part, res_blocks, tol, it + 1 == max_iter, irs, report, status);
         check_launch("ir_check_kernel");
+    }
+    if(report && !pivots_to_status) {
+        ir_guard_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, irs, status);
+        check_launch("ir_guard_kernel");
     }
 }
 

@@ -249,6 +249,9 @@ void made_init(ann_made_impl& m, uint64_t seed) {
         b->ensure(N * 4);
         ANN_CUDA(cudaMemset(b->p, 0, N * 4));
     }
+    // the clears run on the legacy default stream, which does not order with the
+    // non-blocking stream the training runs on: complete them here
+    ANN_CUDA(cudaDeviceSynchronize());
     m.W1t.ensure(nh * 2);
     m.W2t.ensure(nh * 2);
     m.W2b.ensure(nh * 2);

@@ -690,12 +690,6 @@ def batched_instances(ann, st, steps):
     batch.capture_sr_step(SHIFT, LR, st)  # runs one eager step first
     batch.launch_sr_step(st)
     ms_batched = timed(lambda: batch.launch_sr_step(st), steps)
-    # the same step with the mixed-precision solve per instance (FP32 Cholesky on the tensor
-    # cores + FP64 refinement to ||r|| / ||F|| <= 1e-12), for comparison
-    for _, _, _, td in inst:
-        td.set_solver("mixed", 10, 1e-12)
-    batch.capture_sr_step(SHIFT, LR, st)
-    ms_batched_mixed = timed(lambda: batch.launch_sr_step(st), steps)
     batch.sample()
     E = batch.energies()
     acc = []
@@ -714,6 +708,27 @@ def batched_instances(ann, st, steps):
             checks.append({"L": L, "alpha": al, "h": round(h, 4), "E_mc": float(E[k].real), "E_exact": float(e_ex),
                            "abs_diff_per_site": float(abs(E[k].real - e_ex) / L),
                            "diff_in_se": float(abs(E[k].real - e_ex) / se)})
+    # the same step with the mixed-precision solve per instance (FP32 Cholesky on the tensor
+    # cores + FP64 refinement to ||r|| / ||F|| <= 1e-12), for comparison. Inside the graph a
+    # refinement that fails (an instance whose S + shift is too ill-conditioned for the FP32
+    # factor) has no FP64 fallback: it raises the stall flag and leaves that instance's step
+    # at zero; the comparison then records the instances instead of a time.
+    import ctypes as ct
+    for _, _, _, td in inst:
+        td.set_solver("mixed", 10, 1e-12)
+    try:
+        batch.capture_sr_step(SHIFT, LR, st)
+        ms_batched_mixed = timed(lambda: batch.launch_sr_step(st), steps)
+        word = ct.c_uint(0)
+        ann._lib.call("ann_status", ct.byref(word))  # reads and clears the device status word
+        if word.value:
+            raise RuntimeError(f"device status 0x{word.value:x} after the mixed-solver graph steps")
+    except Exception as e:  # noqa: BLE001 (the status word names the failure)
+        failed = [{"instance": k, "L": specs[k][0], "alpha": specs[k][2], "num_params": nps[k],
+                   "chains": chains[k], **td.solver_info}
+                  for k, (_, _, _, td) in enumerate(inst) if td.solver_info["fell_back"]]
+        ms_batched_mixed = {"error": f"{type(e).__name__}: {e}", "instances_not_converged": failed}
+        ann._lib.lib.ann_status(ct.byref(ct.c_uint(0)))  # clear what is left of the status word
     del batch, inst, mades
     torch.cuda.empty_cache()
     seq = [make(k) for k in range(N_INST)]

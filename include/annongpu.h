@@ -307,7 +307,9 @@ int ann_force_vector_noalloc(const void* O_rows, size_t n_rows, size_t ld, unsig
      ||r|| / ||F|| <= tol or max_iter FP32 solves (default 10); converges to the FP64 answer when
      cond(S + shift I) * 6e-8 < 1. An eager solve that does not converge (or whose FP32
      factorisation meets a non-positive pivot) is redone with ANN_SOLVER_FP64; inside a
-     captured graph it raises ANN_ERR_NUMERIC at the next status check instead.
+     captured graph it raises ANN_ERR_NUMERIC at the next status check instead, and a
+     solution whose final ||r|| / ||F|| is not finite or above 1e-3 is replaced by zero, so
+     the graph's SR update leaves the parameters unchanged.
    ANN_SOLVER_FP32: the FP32 factorisation and one FP32 solve, no refinement; its FP64
      residual is still measured and reported by ann_tdvp_solver_info.
    max_iter and tol apply to ANN_SOLVER_MIXED. */
