@@ -93,6 +93,37 @@ def test_batched_sr_steps_equal_single_steps_and_graph():
         np.testing.assert_array_equal(p1.params, p2.params)
 
 
+def test_batched_mixed_solver_steps_equal_single_steps():
+    """The same with the mixed-precision solver (FP32 tcgen05 Cholesky + refinement) on every
+    instance: the batch runs those solves one instance after another, and each instance's
+    parameters after eager and graph-replayed batched steps equal its single-instance steps."""
+    import torch
+    inst = build(tdvp=True)
+    ref = build(tdvp=True)
+    for x in inst + ref:
+        x[3].set_solver("mixed", 10, 1e-12)
+    st = torch.cuda.Stream()
+    batch = ann.Batch([x[0] for x in inst], [x[1] for x in inst], [x[2] for x in inst], [x[3] for x in inst],
+                      stream=st)
+    batch.sr_step(1e-3, 0.02)
+    for psi, op, mc, td, _ in ref:
+        td.sr_step(op, psi, mc, 1e-3, 0.02)
+    st.synchronize()
+    torch.cuda.synchronize()
+    for (p1, *_), (p2, *_) in zip(inst, ref):
+        np.testing.assert_array_equal(p1.params, p2.params)
+    batch.capture_sr_step(1e-3, 0.02, st)  # one eager step, then the capture
+    batch.launch_sr_step(st)
+    for psi, op, mc, td, _ in ref:
+        for _ in range(2):
+            td.sr_step(op, psi, mc, 1e-3, 0.02)
+    st.synchronize()
+    torch.cuda.synchronize()
+    for (p1, *_, t1, _), (p2, *_, t2, _) in zip(inst, ref):
+        assert t1.solver_info["residual_last"] <= 1e-12 and not t2.solver_info["fell_back"]
+        np.testing.assert_array_equal(p1.params, p2.params)
+
+
 def test_batched_learned_proposals_equal_single_chains():
     """Instances with a learned MADE proposal each (two independence moves per sample after
     the local sweeps) in the one persistent launch: every batched chain and its learned-move
