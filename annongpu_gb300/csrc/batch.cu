@@ -248,26 +248,17 @@ void batch_streams(ann_batch_impl& b) {
     ANN_CUDA(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
 }
 
-// per-instance reductions, S, solve and update, spread over the stream pool. With an
-// FP32 (mixed-precision or plain) solver on any instance the instances run one after the
-// other on the pool's first stream (each factorisation still overlaps its look-ahead panel
-// stream with its trailing update): when the FP32 solves of several instances ran
-// concurrently in one graph, some replays gave an instance a wrong FP32 factor (a first
-// residual 30x the usual, or a non-positive pivot), which the same instances never showed
-// one after the other; the cause is not found, so those solves are not run side by side.
+// per-instance reductions, S, solve and update, spread over the stream pool
 void batch_sr(ann_batch_impl& b, double shift, double lr, cudaStream_t st) {
     batch_streams(b);
-    bool fp32_solves = false;
-    for(const ann_tdvp_impl* t : b.tdvps) fp32_solves |= t->solver != ANN_SOLVER_FP64;
-    const size_t n_streams = fp32_solves ? 1 : b.streams.size();
     ANN_CUDA(cudaEventRecord(b.fork, st));
-    for(size_t k = 0; k < n_streams; k++) ANN_CUDA(cudaStreamWaitEvent(b.streams[k], b.fork, 0));
+    for(auto s : b.streams) ANN_CUDA(cudaStreamWaitEvent(s, b.fork, 0));
     // longest first onto the least-loaded stream; the estimated cost (us) of an instance
     // is its solve: a latency-bound chain of Np / 64 panels plus the (4/3) Np^3 update
     // work, and the S product over its rows
     const size_t n = b.psis.size();
     std::vector<size_t> order(n);
-    std::vector<double> cost(n), load(n_streams, 0.0);
+    std::vector<double> cost(n), load(b.streams.size(), 0.0);
     for(size_t i = 0; i < n; i++) {
         const double np = b.psis[i]->Np, ns = (double)b.enss[i]->num_steps();
         cost[i] = np / 64.0 * 40.0 + (4.0 / 3.0) * np * np * np / 5e7 + 4.0 * np * np * ns / 1e9;
@@ -283,7 +274,7 @@ void batch_sr(ann_batch_impl& b, double shift, double lr, cudaStream_t st) {
         sr_solve_any(t, shift, status_word(), s);
         sr_update(*b.psis[i], t.delta.as<cplx<double>>(), lr, s);
     }
-    for(size_t k = 0; k < n_streams; k++) {
+    for(size_t k = 0; k < b.streams.size(); k++) {
         ANN_CUDA(cudaEventRecord(b.done[k], b.streams[k]));
         ANN_CUDA(cudaStreamWaitEvent(st, b.done[k], 0));
     }

@@ -178,14 +178,16 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf32_kernel(cf* __restrict__
     for(unsigned kk = 0; kk < NB; kk += kPw) {
         const unsigned below = NB - kk - kPw;                       // rows under the panel's diagonal block
         const unsigned nwp = below ? (below + kPw - 1) / kPw : 1u;  // warps on the panel
-        if(warp < nwp) {
-            // lane < 16: diagonal row kk + lane; lane >= 16: row kk + 16 + 16 warp + lane - 16
-            const bool diag = lane < kPw;
-            const unsigned r = diag ? kk + lane : kk + kPw + warp * kPw + (lane - kPw);
-            const bool live = r < NB;
-            cf x[kPw];
+        // lane < 16: diagonal row kk + lane; lane >= 16: row kk + 16 + 16 warp + lane - 16
+        const bool diag = lane < kPw;
+        const unsigned r = diag ? kk + lane : kk + kPw + warp * kPw + (lane - kPw);
+        const bool live = warp < nwp && r < NB;
+        cf x[kPw];
 #pragma unroll
-            for(int c = 0; c < kPw; c++) x[c] = live ? a[r][kk + c] : mk(0.f, 0.f);
+        for(int c = 0; c < kPw; c++) x[c] = live ? a[r][kk + c] : mk(0.f, 0.f);
+        // every warp holds its copy of the diagonal rows before warp 0 writes them back
+        __syncthreads();
+        if(warp < nwp) {
 #pragma unroll
             for(int j = 0; j < kPw; j++) {
                 float d = __shfl_sync(0xffffffffu, x[j].re, j);

@@ -458,8 +458,7 @@ int ann_made_train_on_samples(ann_made* m, const ann_ens* ens, unsigned steps, u
  * Hamiltonian per call): n (psi, op, Monte Carlo ensemble, TDVP) tuples; complex64
  * RBM-family wavefunctions with N <= 64 and M <= 256, single-flip ensembles. One
  * persistent launch samples every instance (device work queue, largest first);
- * the per-instance S, FP64 Cholesky solves and updates run on a stream pool (one
- * stream, instance after instance, when any instance's TDVP uses an FP32 solver).
+ * the per-instance S, Cholesky solves and updates run on a stream pool.
  * ------------------------------------------------------------------------------ */
 int ann_batch_create(unsigned n, ann_psi** psis, ann_op** ops, ann_ens** enss, ann_tdvp** tdvps, ann_batch** out);
 int ann_batch_destroy(ann_batch* b);
