@@ -48,3 +48,16 @@ def test_error_reporting_without_device(lib):
     rc = lib.ann_ens_create_exact(40, ct.byref(out))
     assert rc == 1
     assert b"exact summation" in lib.ann_last_error()
+
+
+def test_factor_trace_levels_without_device(lib):
+    """ann_set_factor_trace takes 0 (off), 1 (panel pairs) or 2 (also between the panel
+    kernels); anything else is rejected before any device work."""
+    lib.ann_last_error.restype = ct.c_char_p
+    for level in (0, 1, 2, 0):
+        assert lib.ann_set_factor_trace(level) == 0
+    assert lib.ann_set_factor_trace(3) == 1
+    assert b"factor trace level" in lib.ann_last_error()
+    assert lib.ann_set_factor_trace(-1) == 1
+    n = ct.c_uint(7)
+    assert lib.ann_get_factor_trace(None, 0, ct.byref(n)) == 0 and n.value == 0
