@@ -319,3 +319,18 @@ def test_hsd_exact_matches_reference(oracle, form, nu):
     close(d, g[f"{tag}_dist"][0])
     close(d, g[f"{tag}_dist"][1])
     close(grad, g[f"{tag}_grad"], rtol=1e-9, atol=1e-12)
+
+
+def test_polynomial_real_part_rearrangement(oracle):
+    """The complex64 sampler evaluates the real part of the reference's polynomial activation
+    (first layer) as Re f = P/2 - P^2/12 + q^2/3 + (P/45)(P^2 - 12 q^2) with P = x^2 - y^2,
+    q = x y (two units per two-wide FP32 instruction). In FP64 the rearrangement equals Re of
+    the oracle's activation, which the reference's known-answer values pin."""
+    rng = np.random.default_rng(5)
+    zs = list(load("kats.npz")["z"]) + list(0.8 * (rng.standard_normal(64) + 1j * rng.standard_normal(64)))
+    for z in zs:
+        f, _ = oracle.activation(complex(z), 0)
+        x, y = z.real, z.imag
+        P, q = x * x - y * y, x * y
+        re = P / 2 - P * P / 12 + q * q / 3 + (P / 45) * (P * P - 12 * q * q)
+        close(re, np.real(f), rtol=1e-13, atol=1e-15)
